@@ -1,0 +1,298 @@
+"""Python access to the two CPU oracles.  TEST INFRASTRUCTURE ONLY.
+
+* ``Restatement`` -- the plain-C restatement in oracle/pbs_oracle.c (built into
+  oracle/_build/liboracle.so).  It needs nothing from the reference and runs anywhere.
+* ``Reference``   -- the reference's own sources compiled against the stand-ins in
+  oracle/shim (oracle/_ref/libyatfhe_ref_t{32,56}.so, built by ``make ref`` only where the
+  reference tree exists).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs import
+this module; the shipped package (yatfhe_gb300/) does not.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF_TREE = Path(os.environ.get("YATFHE_REFERENCE", "/root/reference"))
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def _ptr(a: np.ndarray, typ):
+    return a.ctypes.data_as(typ)
+
+
+def build_restatement() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    return HERE / "_build" / "liboracle.so"
+
+
+def reference_available() -> bool:
+    return (REF_TREE / "yatfhe" / "src" / "bootstrapping.cpp").exists() or all(
+        (HERE / "_ref" / f"libyatfhe_ref_t{t}.so").exists() for t in (32, 56))
+
+
+def build_reference() -> None:
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={REF_TREE}"], check=True)
+
+
+class _CParams(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_int) for f in
+                "n N k radix_bits l l_approx ks_radix_bits ks_level lwe_noise_b rlwe_noise_b torus_base torus_bits".split()]
+
+
+def _cparams(p) -> _CParams:
+    return _CParams(*(int(getattr(p, f)) for f, _ in _CParams._fields_))
+
+
+class _Common:
+    """Shared numpy-facing helpers; subclasses bind ``_call(name, *args)``."""
+
+    p = None
+
+    def _alloc_lwe(self, count):
+        return np.zeros((count, self.p.n + 1), np.int32)
+
+    def encrypt(self, mu) -> np.ndarray:
+        mu = np.ascontiguousarray(mu, np.int64)
+        out = self._alloc_lwe(len(mu))
+        self._call("encrypt", _ptr(mu, _i64p), len(mu), _ptr(out, _i32p))
+        return out
+
+    def decrypt(self, lwe, base: int) -> np.ndarray:
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        out = np.zeros(len(lwe), np.int32)
+        self._call("decrypt", _ptr(lwe, _i32p), len(lwe), base, _ptr(out, _i32p))
+        return out
+
+    def keys(self):
+        s = np.zeros(self.p.n, np.int32)
+        z = np.zeros(self.p.k * self.p.N, np.int32)
+        self._call("get_keys" if self.prefix == "po_" else "export_keys", _ptr(s, _i32p), _ptr(z, _i32p))
+        return s, z
+
+    def ksk(self) -> np.ndarray:
+        out = np.zeros(self.p.ksk_words if hasattr(self.p, "ksk_words") else
+                       self.p.k * self.p.N * self.p.ks_level * (self.p.n + 1), np.int32)
+        self._call("get_ksk" if self.prefix == "po_" else "export_ksk", _ptr(out, _i32p))
+        return out
+
+    def bsk_ntt(self) -> np.ndarray:
+        p = self.p
+        out = np.zeros(p.n * p.l_approx * (p.k + 1) ** 2 * p.N, np.uint64)
+        self._call("get_bsk_ntt" if self.prefix == "po_" else "export_bsk_ntt", _ptr(out, _u64p))
+        return out
+
+    def test_polynomial(self, kind: int, modP: int) -> np.ndarray:
+        v = np.zeros(self.p.N, np.int64)
+        self._call("test_polynomial", kind, modP, _ptr(v, _i64p))
+        return v
+
+    def modswitch(self, lwe) -> np.ndarray:
+        lwe = np.ascontiguousarray(lwe, np.int32)
+        out = np.zeros(self.p.n + 1, np.int32)
+        self._call("modswitch", _ptr(lwe, _i32p), _ptr(out, _i32p))
+        return out
+
+    def decompose(self, poly, levels: int) -> np.ndarray:
+        poly = np.ascontiguousarray(poly, np.int64)
+        out = np.zeros((levels, len(poly)), np.int64)
+        if self.prefix == "po_":
+            self._call("decompose", _ptr(poly, _i64p), levels, _ptr(out, _i64p))
+        else:
+            self._call("decompose", _ptr(poly, _i64p), len(poly), levels, _ptr(out, _i64p))
+        return out
+
+    def decompose_ks(self, value: int) -> np.ndarray:
+        out = np.zeros(self.p.ks_level, np.int64)
+        self._call("decompose_ks", ctypes.c_int64(int(value)), _ptr(out, _i64p))
+        return out
+
+    def ntt_forward(self, poly) -> np.ndarray:
+        poly = np.ascontiguousarray(poly, np.int64)
+        out = np.zeros(self.p.N, np.uint64)
+        self._call("ntt_forward", _ptr(poly, _i64p), _ptr(out, _u64p))
+        return out
+
+    def ntt_inverse(self, ntt) -> np.ndarray:
+        ntt = np.ascontiguousarray(ntt, np.uint64)
+        out = np.zeros(self.p.N, np.int64)
+        self._call("ntt_inverse", _ptr(ntt, _u64p), _ptr(out, _i64p))
+        return out
+
+    def external_product(self, trlwe, i: int) -> np.ndarray:
+        trlwe = np.ascontiguousarray(trlwe, np.int64)
+        out = np.zeros_like(trlwe)
+        self._call("external_product", _ptr(trlwe, _i64p), i, _ptr(out, _i64p))
+        return out
+
+    def extract(self, acc) -> np.ndarray:
+        acc = np.ascontiguousarray(acc, np.int64)
+        out = np.zeros(self.p.k * self.p.N + 1, np.int32)
+        self._call("extract", _ptr(acc, _i64p), _ptr(out, _i32p))
+        return out
+
+    def keyswitch(self, lwe_big) -> np.ndarray:
+        lwe_big = np.ascontiguousarray(lwe_big, np.int32)
+        out = np.zeros(self.p.n + 1, np.int32)
+        self._call("keyswitch", _ptr(lwe_big, _i32p), _ptr(out, _i32p))
+        return out
+
+    def blind_rotate_trace(self, lwe, v, checkpoints):
+        lwe = np.ascontiguousarray(lwe, np.int32)
+        v = np.ascontiguousarray(v, np.int64)
+        cps = np.ascontiguousarray(sorted(checkpoints), np.int32)
+        stride = (self.p.k + 1) * self.p.N
+        out = np.zeros((len(cps), stride), np.int64)
+        final = np.zeros(stride, np.int64)
+        self._call("blind_rotate_trace", _ptr(lwe, _i32p), _ptr(v, _i64p),
+                   cps.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(cps), _ptr(out, _i64p),
+                   _ptr(final, _i64p))
+        return out, final
+
+    def pbs(self, lwe, v, threads: int = 1) -> np.ndarray:
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        self._call("pbs", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), threads)
+        return out
+
+
+class Restatement(_Common):
+    """The plain-C oracle for one parameter set."""
+
+    prefix = "po_"
+    _lib = None
+
+    def __init__(self, p):
+        if Restatement._lib is None:
+            so = HERE / "_build" / "liboracle.so"
+            if not so.exists():
+                build_restatement()
+            Restatement._lib = ctypes.CDLL(str(so))
+            Restatement._lib.po_create.restype = ctypes.c_void_p
+            Restatement._lib.po_last_error.restype = ctypes.c_char_p
+            Restatement._lib.po_last_error.argtypes = [ctypes.c_void_p]
+            Restatement._lib.po_destroy.argtypes = [ctypes.c_void_p]
+            Restatement._lib.po_qntt.restype = ctypes.c_uint64
+            Restatement._lib.po_qntt.argtypes = [ctypes.c_void_p]
+        self.p = p
+        cp = _cparams(p)
+        self._h = Restatement._lib.po_create(ctypes.byref(cp))
+        if not self._h:
+            raise ValueError(f"po_create rejected {p}")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and Restatement._lib is not None:
+            Restatement._lib.po_destroy(h)
+            self._h = None
+
+    def _call(self, name, *args):
+        fn = getattr(Restatement._lib, "po_" + name)
+        rc = fn(ctypes.c_void_p(self._h), *args)
+        if rc != 0:
+            raise RuntimeError(f"po_{name}: {Restatement._lib.po_last_error(self._h).decode()}")
+
+    def keygen(self, seed: int) -> None:
+        self._call("keygen", ctypes.c_uint64(seed))
+
+    def set_keys(self, lwe_s, rlwe_s) -> None:
+        a = np.ascontiguousarray(lwe_s, np.int32)
+        b = np.ascontiguousarray(rlwe_s, np.int32)
+        self._call("set_keys", _ptr(a, _i32p), _ptr(b, _i32p))
+
+    def set_ksk(self, ksk) -> None:
+        a = np.ascontiguousarray(ksk, np.int32)
+        self._call("set_ksk", _ptr(a, _i32p))
+
+    def set_bsk_ntt(self, bsk) -> None:
+        a = np.ascontiguousarray(bsk, np.uint64)
+        self._call("set_bsk_ntt", _ptr(a, _u64p))
+
+    def save_bsk_file(self, path) -> None:
+        self._call("save_bsk_file", str(path).encode())
+
+    def load_bsk_file(self, path) -> None:
+        self._call("load_bsk_file", str(path).encode())
+
+    @property
+    def q(self) -> int:
+        return int(Restatement._lib.po_qntt(self._h))
+
+
+class Reference(_Common):
+    """The reference's own code (one process-global parameter set per torus build)."""
+
+    prefix = "ref_"
+    _libs: dict = {}
+
+    def __init__(self, p):
+        t = p.torus_bits
+        if t not in Reference._libs:
+            so = HERE / "_ref" / f"libyatfhe_ref_t{t}.so"
+            if not so.exists():
+                build_reference()
+            lib = ctypes.CDLL(str(so))
+            lib.ref_last_error.restype = ctypes.c_char_p
+            lib.ref_ntt_root.restype = ctypes.c_uint64
+            Reference._libs[t] = lib
+        self.lib = Reference._libs[t]
+        self.p = p
+        cp = _CParams(*(int(getattr(p, f)) for f, _ in _CParams._fields_))
+        if self.lib.ref_setup(ctypes.byref(cp)) != 0:
+            raise RuntimeError(self.lib.ref_last_error().decode())
+
+    def _call(self, name, *args):
+        rc = getattr(self.lib, "ref_" + name)(*args)
+        if rc != 0:
+            raise RuntimeError(f"ref_{name}: {self.lib.ref_last_error().decode()}")
+
+    def keygen(self, seed: int) -> None:
+        self._call("keygen", ctypes.c_uint64(seed))
+
+    def save_bsk_file(self, path) -> None:
+        self._call("save_bsk", str(path).encode())
+
+    def load_bsk_file(self, path) -> None:
+        self._call("load_bsk", str(path).encode())
+
+    def set_keys(self, lwe_s, rlwe_s) -> None:
+        a = np.ascontiguousarray(lwe_s, np.int32)
+        b = np.ascontiguousarray(rlwe_s, np.int32)
+        self._call("import_keys", _ptr(a, _i32p), _ptr(b, _i32p))
+
+    def set_ksk(self, ksk) -> None:
+        a = np.ascontiguousarray(ksk, np.int32)
+        self._call("import_ksk", _ptr(a, _i32p))
+
+    def rotate(self, poly, a: int, minus_one: bool) -> np.ndarray:
+        poly = np.ascontiguousarray(poly, np.int64)
+        out = np.zeros_like(poly)
+        self._call("rotate", _ptr(poly, _i64p), len(poly), a, int(minus_one), _ptr(out, _i64p))
+        return out
+
+    def pbs_pool(self, lwe, v) -> np.ndarray:
+        """One reference-ThreadPool task per ciphertext (throughput form)."""
+        return self.pbs(lwe, v, threads=1)
+
+    def ntt_root(self) -> int:
+        return int(self.lib.ref_ntt_root())
+
+
+def _restatement_rotate(self, poly, a: int, minus_one: bool) -> np.ndarray:
+    poly = np.ascontiguousarray(poly, np.int64)
+    out = np.zeros_like(poly)
+    self._call("rotate", _ptr(poly, _i64p), a, int(minus_one), _ptr(out, _i64p))
+    return out
+
+
+Restatement.rotate = _restatement_rotate

@@ -1,0 +1,824 @@
+/*
+ * pbs_oracle.c -- plain-C restatement of the reference's GINX/MP21 programmable
+ * bootstrap and of the seeded key generation that feeds it.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker: tests/, __graft_entry__.smoke() and the
+ * cpu_baseline leg of bench.py may call it; the shipped library (yatfhe_gb300/) never
+ * links, loads or runs it.  Every function cites the reference source it restates
+ * (paths relative to the reference project).  Torus values are carried in int64 and
+ * brought back to the torus width T with sext(), which reproduces both the reference's
+ * int32 wrap arithmetic (TORUS32) and its longModPow2 reductions (TORUS56).
+ */
+#define _GNU_SOURCE
+#include "pbs_oracle.h"
+
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ntt_q.h"
+
+/* yatfhe/include/yatfhe/torus.h:151,157 */
+#define Q_49P_T32 562941363486721ULL
+#define Q_61P_T56 1945555039024054273ULL
+
+/* ------------------------------------------------------------------ helpers */
+
+/* longModPow2 (yatfhe/include/yatfhe/numeric.h:69-71): sign-extend the low `bits` bits. */
+static inline int64_t sext(int64_t x, int bits) {
+    const int sh = 64 - bits;
+    return (int64_t)((uint64_t)x << sh) >> sh;
+}
+
+/* ------------------------------------------------------------------ RNG */
+
+/*
+ * ChaCha20 (RFC 8439 sec. 2.3) keyed as oracle/shim/seeded_csprng.cpp keys the
+ * reference's ChaCha20Rng: key = (seed_lo, seed_hi, 0 x 6), counter 0, nonce (stream, 0).
+ */
+typedef struct {
+    uint32_t state[16];
+    uint32_t block[16];
+    int pos;
+} po_rng;
+
+static inline uint32_t rotl32(uint32_t x, int n) { return (x << n) | (x >> (32 - n)); }
+
+#define QR(a, b, c, d)                                                                  \
+    do {                                                                                \
+        x[a] += x[b]; x[d] ^= x[a]; x[d] = rotl32(x[d], 16);                            \
+        x[c] += x[d]; x[b] ^= x[c]; x[b] = rotl32(x[b], 12);                            \
+        x[a] += x[b]; x[d] ^= x[a]; x[d] = rotl32(x[d], 8);                             \
+        x[c] += x[d]; x[b] ^= x[c]; x[b] = rotl32(x[b], 7);                             \
+    } while (0)
+
+static void rng_seed(po_rng* r, uint64_t seed, uint32_t stream) {
+    static const uint32_t sigma[4] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u};
+    for (int i = 0; i < 4; i++) r->state[i] = sigma[i];
+    r->state[4] = (uint32_t)seed;
+    r->state[5] = (uint32_t)(seed >> 32);
+    for (int i = 6; i < 12; i++) r->state[i] = 0;
+    r->state[12] = 0;
+    r->state[13] = 0;
+    r->state[14] = stream;
+    r->state[15] = 0;
+    r->pos = 16;
+}
+
+static void rng_refill(po_rng* r) {
+    uint32_t x[16];
+    memcpy(x, r->state, sizeof(x));
+    for (int i = 0; i < 10; i++) {
+        QR(0, 4, 8, 12); QR(1, 5, 9, 13); QR(2, 6, 10, 14); QR(3, 7, 11, 15);
+        QR(0, 5, 10, 15); QR(1, 6, 11, 12); QR(2, 7, 8, 13); QR(3, 4, 9, 14);
+    }
+    for (int i = 0; i < 16; i++) r->block[i] = x[i] + r->state[i];
+    if (++r->state[12] == 0) ++r->state[13];
+    r->pos = 0;
+}
+
+static inline uint32_t rng_next(po_rng* r) {
+    if (r->pos == 16) rng_refill(r);
+    return r->block[r->pos++];
+}
+
+/*
+ * std::uniform_int_distribution as libstdc++ (GCC 13) implements it for a generator
+ * whose outputs span exactly 32 bits: ranges below 2^32 are "downscaled" with Lemire's
+ * nearly-divisionless multiply-and-reject in 64-bit arithmetic; a range of exactly 2^32
+ * takes one draw; wider ranges are "upscaled" by drawing the high part recursively and
+ * one more word for the low part, rejecting overflow.  Both the int32 and the uint64
+ * instantiations the reference uses reduce to this on the unsigned difference b - a.
+ */
+static uint32_t rng_nd32(po_rng* r, uint32_t range) {
+    uint64_t product = (uint64_t)rng_next(r) * range;
+    uint32_t low = (uint32_t)product;
+    if (low < range) {
+        uint32_t threshold = (uint32_t)(-range) % range;
+        while (low < threshold) {
+            product = (uint64_t)rng_next(r) * range;
+            low = (uint32_t)product;
+        }
+    }
+    return (uint32_t)(product >> 32);
+}
+
+static uint64_t rng_urange(po_rng* r, uint64_t urange) {
+    if (urange < 0xFFFFFFFFull) return rng_nd32(r, (uint32_t)(urange + 1));
+    if (urange == 0xFFFFFFFFull) return rng_next(r);
+    uint64_t ret, tmp;
+    do {
+        tmp = (uint64_t)0x100000000ull * rng_urange(r, urange >> 32);
+        ret = tmp + rng_next(r);
+    } while (ret > urange || ret < tmp);
+    return ret;
+}
+
+/* uniform over [a, b] for signed bounds (the two's-complement wrap is the library's). */
+static inline int64_t rng_uniform_i64(po_rng* r, int64_t a, int64_t b) {
+    return (int64_t)(rng_urange(r, (uint64_t)b - (uint64_t)a) + (uint64_t)a);
+}
+
+/* binaryDistrib(rng) (yatfhe/src/numeric.cpp:11) */
+static inline int rng_binary(po_rng* r) { return (int)rng_urange(r, 1); }
+
+/* genTUniformNoise (yatfhe/src/numeric.cpp:47-55) */
+static int64_t rng_tuniform(po_rng* r, int b) {
+    const int bits = b + 2;
+    const uint64_t mask = bits >= 64 ? UINT64_MAX : ((uint64_t)1 << bits) - 1;
+    uint64_t cand = rng_urange(r, mask);
+    uint64_t low = cand & 1;
+    cand = (cand >> 1) + low;
+    return (int64_t)cand - ((int64_t)1 << b);
+}
+
+/* ------------------------------------------------------------------ context */
+
+struct po_ctx {
+    po_params p;
+    int T;               /* torus bits */
+    int L;               /* key / decomposition levels = l_approx */
+    uint64_t q;          /* qNtt */
+    nq_plan plan;
+    po_rng rng;
+    int have_rng;
+    int32_t* lwe_s;      /* n */
+    int32_t* rlwe_s;     /* k*N */
+    uint64_t* rlwe_s_ntt;/* k*N */
+    uint64_t* bsk;       /* [n][L][k+1][k+1][N] */
+    int32_t* ksk;        /* [k*N][t][n+1] */
+    char err[256];
+};
+
+static int fail(po_ctx* c, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+    return -1;
+}
+
+const char* po_last_error(po_ctx* c) { return c->err; }
+uint64_t po_qntt(po_ctx* c) { return c->q; }
+
+static size_t bsk_words(const po_ctx* c) {
+    const size_t k1 = (size_t)c->p.k + 1;
+    return (size_t)c->p.n * c->L * k1 * k1 * c->p.N;
+}
+static size_t ksk_words(const po_ctx* c) {
+    return (size_t)c->p.k * c->p.N * c->p.ks_level * (c->p.n + 1);
+}
+
+po_ctx* po_create(const po_params* p) {
+    if (p->torus_bits != 32 && p->torus_bits != 56) return NULL;
+    po_ctx* c = (po_ctx*)calloc(1, sizeof(po_ctx));
+    if (!c) return NULL;
+    c->p = *p;
+    c->T = p->torus_bits;
+    c->L = p->l_approx;
+    c->q = c->T == 32 ? Q_49P_T32 : Q_61P_T56;
+    if (nq_plan_init(&c->plan, (uint32_t)p->N, c->q) != 0) {
+        free(c);
+        return NULL;
+    }
+    c->lwe_s = (int32_t*)calloc((size_t)p->n, sizeof(int32_t));
+    c->rlwe_s = (int32_t*)calloc((size_t)p->k * p->N, sizeof(int32_t));
+    c->rlwe_s_ntt = (uint64_t*)calloc((size_t)p->k * p->N, sizeof(uint64_t));
+    c->bsk = (uint64_t*)calloc(bsk_words(c), sizeof(uint64_t));
+    c->ksk = (int32_t*)calloc(ksk_words(c), sizeof(int32_t));
+    if (!c->lwe_s || !c->rlwe_s || !c->rlwe_s_ntt || !c->bsk || !c->ksk) {
+        po_destroy(c);
+        return NULL;
+    }
+    return c;
+}
+
+void po_destroy(po_ctx* c) {
+    if (!c) return;
+    nq_plan_free(&c->plan);
+    free(c->lwe_s);
+    free(c->rlwe_s);
+    free(c->rlwe_s_ntt);
+    free(c->bsk);
+    free(c->ksk);
+    free(c);
+}
+
+/* ------------------------------------------------------------------ ring helpers */
+
+/* applyNtt (yatfhe/include/yatfhe/ntt_hexl.h:34-44): lift v < 0 to v + q, forward NTT. */
+static void ntt_from_torus(const po_ctx* c, uint64_t* out, const int64_t* in) {
+    const int N = c->p.N;
+    for (int j = 0; j < N; j++) out[j] = in[j] < 0 ? (uint64_t)in[j] + c->q : (uint64_t)in[j];
+    nq_forward(&c->plan, out);
+}
+
+/* applyIntt (yatfhe/src/ntt_hexl.cpp:153-175): inverse NTT, centre at (q+1)/2, reduce to T bits. */
+static void intt_to_torus(const po_ctx* c, int64_t* out, uint64_t* in_scratch) {
+    const int N = c->p.N;
+    const uint64_t half = (c->q + 1) >> 1;
+    nq_inverse(&c->plan, in_scratch);
+    for (int j = 0; j < N; j++) {
+        uint64_t r = in_scratch[j];
+        uint64_t centred = r >= half ? r - c->q : r;
+        out[j] = sext((int64_t)centred, c->T);
+    }
+}
+
+static inline uint64_t addmod(uint64_t a, uint64_t b, uint64_t q) {
+    uint64_t s = a + b;
+    return s >= q ? s - q : s;
+}
+
+/* validateRotator (yatfhe/src/polynomial.cpp:22-29) */
+static void validate_rotator(int* aTrue, int* isWrap, int a, int N) {
+    int t = a % (2 * N);
+    if (t < 0) t += 2 * N;
+    *isWrap = t < N ? 1 : -1;
+    *aTrue = t < N ? t : t - N;
+}
+
+/* rotateTorusPolynomial (yatfhe/src/polynomial.cpp:184-193) and
+ * rotateTorusPolynomialMinusOne (:213-238): out = X^a in, or X^a in - in. */
+static void rotate_poly(const po_ctx* c, int64_t* out, const int64_t* in, int a, int minus_one) {
+    const int N = c->p.N;
+    int aTrue, isWrap;
+    validate_rotator(&aTrue, &isWrap, a, N);
+    for (int i = 0; i < N; i++) {
+        int64_t r = i < aTrue ? -in[i - aTrue + N] * isWrap : in[i - aTrue] * isWrap;
+        out[i] = minus_one ? sext(r - in[i], c->T) : sext(r, c->T);
+    }
+}
+
+/*
+ * zeroMeanDigits (yatfhe/include/yatfhe/gadget_decomposition.h:76-95): signed balanced
+ * digits of the top levels*radixBits bits of a widthBits-wide value, rounded half away
+ * from zero, emitted from the least significant level up with a carry; ties go up when
+ * the top bit of the next window is set.  digits[level], level 0 most significant.
+ */
+static void zero_mean_digits(uint64_t u, int levels, int radixBits, int widthBits, int64_t* digits) {
+    const uint64_t wmask = widthBits >= 64 ? UINT64_MAX : (((uint64_t)1 << widthBits) - 1);
+    u &= wmask;
+    const int negative = (int)((u >> (widthBits - 1)) & 1);
+    const int dropped = widthBits - levels * radixBits;
+    const uint64_t bias = dropped > 0 ? (uint64_t)1 << (dropped - 1) : 0;
+    const uint64_t m = (negative ? (0 - u) & wmask : u) + bias;
+    const int64_t B = (int64_t)1 << radixBits, halfB = B >> 1;
+    int64_t carry = 0;
+    for (int level = levels - 1; level >= 0; --level) {
+        const int shift = widthBits - (level + 1) * radixBits;
+        const int64_t window = (int64_t)((m >> shift) & (uint64_t)(B - 1));
+        const int64_t digit = window + carry;
+        const int64_t tie = level > 0 ? (int64_t)((m >> (shift + 2 * radixBits - 1)) & 1) : 0;
+        carry = (digit > halfB) | ((digit == halfB) & tie);
+        const int64_t bal = carry ? digit - B : digit;
+        digits[level] = negative ? -bal : bal;
+    }
+}
+
+/* modSwitchFromTorusGeneral (yatfhe/src/numeric.cpp:189-208), downscaling branch with a
+ * power-of-two target: round half away from zero, then sign-extend. */
+static int64_t modswitch_down(int64_t x, int fromBits, int toBits) {
+    const int64_t scale = (int64_t)1 << (fromBits - toBits);
+    const int64_t real = x >= 0 ? (x + scale / 2) / scale : (x - scale / 2) / scale;
+    return sext(real, toBits);
+}
+
+static int log2i(int x) {
+    int r = 0;
+    while ((1 << r) < x) r++;
+    return r;
+}
+
+/* ------------------------------------------------------------------ key generation */
+
+/* NTT-domain RLWE encryption: initTrlweMultiSampleSimple / initTrlweSingleSampleSimple
+ * (yatfhe/src/trlwe.cpp:24-46) then symEncTrlweNttSimple (:58-60).  `mu` holds the N
+ * torus plaintext coefficients; out = [a_0..a_{k-1}, b] NTT polys. */
+static void enc_trlwe_ntt(po_ctx* c, uint64_t* out, const int64_t* mu, int64_t* tmpT) {
+    const int N = c->p.N, k = c->p.k;
+    const uint64_t q = c->q;
+    uint64_t* b = out + (size_t)k * N;
+    for (int j = 0; j < N; j++) tmpT[j] = sext(mu[j] + rng_tuniform(&c->rng, c->p.rlwe_noise_b), c->T);
+    ntt_from_torus(c, b, tmpT);
+    for (int r = 0; r < k; r++)
+        for (int j = 0; j < N; j++) out[(size_t)r * N + j] = rng_urange(&c->rng, q - 1);
+    for (int r = 0; r < k; r++)
+        for (int j = 0; j < N; j++)
+            b[j] = addmod(b[j], nq_mulmod(&c->plan.br, out[(size_t)r * N + j], c->rlwe_s_ntt[(size_t)r * N + j]), q);
+}
+
+/* symEncTlwe (yatfhe/src/tlwe.cpp:21-31) with addTUniformNoise (numeric.cpp:57-60) and
+ * addTorus / longModP mod LWE_Q = 2^32 (numeric.h:53-66,163-177). */
+static void enc_tlwe(po_ctx* c, int32_t* out, int64_t message, const int32_t* s, int n) {
+    int64_t tmp = 0;
+    for (int i = 0; i < n; i++) {
+        int64_t a = rng_uniform_i64(&c->rng, -((int64_t)1 << 31), ((int64_t)1 << 31) - 1);
+        out[i] = (int32_t)a;
+        if (s[i]) tmp += a * s[i];
+    }
+    int64_t muE = sext(message + rng_tuniform(&c->rng, c->p.lwe_noise_b), 32);
+    out[n] = (int32_t)sext(muE + sext(tmp, 32), 32);
+}
+
+/*
+ * Keys from a seed, in the order oracle/ref_capi.cpp:ref_keygen draws them on one RNG
+ * stream: genTlweKey (yatfhe/src/tlwe.cpp:10-18), genTrlweKey (yatfhe/src/trlwe.cpp:70-81),
+ * encryptTrgswMPNtt(bsk[i], s_i, pos 0) for i = 0..n-1 (yatfhe/src/trgsw.cpp:36-51, the
+ * per-i body of genBootstrappingKeyMP, bootstrapping.cpp:150-174), genTlweKeySwitchingKey
+ * (yatfhe/src/keyswitching.cpp:19-29).
+ */
+int po_keygen(po_ctx* c, uint64_t seed) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, T = c->T;
+    const int k1 = k + 1;
+    rng_seed(&c->rng, seed, 0);
+    c->have_rng = 1;
+    for (int i = 0; i < n; i++) c->lwe_s[i] = rng_binary(&c->rng);
+    int64_t* tmpT = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    int64_t* muPoly = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    uint64_t* muNtt = (uint64_t*)calloc((size_t)N, sizeof(uint64_t));
+    int64_t* zeroPoly = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    if (!tmpT || !muPoly || !muNtt || !zeroPoly) {
+        free(tmpT); free(muPoly); free(muNtt); free(zeroPoly);
+        return fail(c, "po_keygen: out of memory");
+    }
+    for (int r = 0; r < k; r++) {
+        for (int j = 0; j < N; j++) c->rlwe_s[(size_t)r * N + j] = rng_binary(&c->rng);
+        for (int j = 0; j < N; j++) tmpT[j] = c->rlwe_s[(size_t)r * N + j];
+        ntt_from_torus(c, c->rlwe_s_ntt + (size_t)r * N, tmpT);
+    }
+    const size_t rowWords = (size_t)k1 * N;           /* one RLWE sample */
+    const size_t lvlWords = (size_t)k1 * rowWords;    /* c[lvl][0..k-1] + cPrime[lvl] */
+    for (int i = 0; i < n; i++) {
+        const int64_t mu = c->lwe_s[i];
+        memset(muPoly, 0, sizeof(int64_t) * N);
+        for (int lvl = 0; lvl < L; lvl++) {
+            uint64_t* g = c->bsk + ((size_t)i * L + lvl) * lvlWords;
+            muPoly[0] = sext(mu << (T - (lvl + 1) * c->p.radix_bits), T);
+            ntt_from_torus(c, muNtt, muPoly);
+            /* cPrime[lvl] = RLWE(mu * g_lvl) */
+            enc_trlwe_ntt(c, g + (size_t)k * rowWords, muPoly, tmpT);
+            /* c[lvl][r] = RLWE(0) with a[r] += NTT(mu * g_lvl) */
+            for (int r = 0; r < k; r++) {
+                uint64_t* row = g + (size_t)r * rowWords;
+                enc_trlwe_ntt(c, row, zeroPoly, tmpT);
+                for (int j = 0; j < N; j++) row[(size_t)r * N + j] = addmod(row[(size_t)r * N + j], muNtt[j], c->q);
+            }
+        }
+    }
+    /* key switching key: ksk[i][j] = LWE_s(s'_i * 2^(32 - (j+1) ksRadix)) */
+    const int kN = k * N, t = c->p.ks_level, nb = n + 1;
+    for (int i = 0; i < kN; i++) {
+        for (int j = 0; j < t; j++) {
+            const int sh = 32 - (j + 1) * c->p.ks_radix_bits;
+            const int64_t m = sext((int64_t)c->rlwe_s[i] << sh, T);
+            enc_tlwe(c, c->ksk + ((size_t)i * t + j) * nb, m, c->lwe_s, n);
+        }
+    }
+    free(tmpT);
+    free(muPoly);
+    free(muNtt);
+    free(zeroPoly);
+    return 0;
+}
+
+int po_encrypt(po_ctx* c, const int64_t* mu, int count, int32_t* out) {
+    if (!c->have_rng) return fail(c, "po_encrypt: no RNG stream (run po_keygen first)");
+    const int n = c->p.n;
+    for (int i = 0; i < count; i++) enc_tlwe(c, out + (size_t)i * (n + 1), mu[i], c->lwe_s, n);
+    return 0;
+}
+
+/* symDecTlweToInt (yatfhe/src/tlwe.cpp:44-53) with roundTorusGeneralError (numeric.cpp:95-98)
+ * and modSwitchToTorusGeneral (numeric.cpp:182-187), all mod LWE_Q = 2^32. */
+static int64_t int_mod_p(int64_t a, int64_t p) {
+    int64_t b = a % p;
+    if (b > (p - 1) / 2) b -= p;
+    else if (b < -p / 2) b += p;
+    return b;
+}
+
+static int64_t modswitch_general(int64_t x, int64_t newMod) {
+    const int64_t torusQ = (int64_t)1 << 32;
+    const int64_t scale = torusQ / newMod;
+    const int64_t real = x >= 0 ? (x + scale / 2) / scale : (x - scale / 2) / scale;
+    /* longModP: pow2 -> sign-extend, else centred remainder */
+    if ((newMod & (newMod - 1)) == 0) return sext(real, log2i((int)newMod));
+    return int_mod_p(real, newMod);
+}
+
+int po_decrypt(po_ctx* c, const int32_t* in, int count, int base, int32_t* out) {
+    const int n = c->p.n;
+    for (int ci = 0; ci < count; ci++) {
+        const int32_t* x = in + (size_t)ci * (n + 1);
+        int64_t tmp = 0;
+        for (int i = 0; i < n; i++)
+            if (c->lwe_s[i]) tmp += (int64_t)x[i] * c->lwe_s[i];
+        int64_t phase = sext((int64_t)x[n] - sext(tmp, 32), 32);
+        int64_t t = modswitch_general(phase, base);
+        int64_t rounded = int_mod_p(t, base) * (((int64_t)1 << 32) / base);
+        out[ci] = (int32_t)modswitch_general(sext(rounded, 32), base);
+    }
+    return 0;
+}
+
+int po_get_keys(po_ctx* c, int32_t* lwe_s, int32_t* rlwe_s) {
+    memcpy(lwe_s, c->lwe_s, sizeof(int32_t) * c->p.n);
+    memcpy(rlwe_s, c->rlwe_s, sizeof(int32_t) * c->p.k * c->p.N);
+    return 0;
+}
+
+int po_set_keys(po_ctx* c, const int32_t* lwe_s, const int32_t* rlwe_s) {
+    const int N = c->p.N;
+    memcpy(c->lwe_s, lwe_s, sizeof(int32_t) * c->p.n);
+    memcpy(c->rlwe_s, rlwe_s, sizeof(int32_t) * c->p.k * N);
+    int64_t* tmp = (int64_t*)malloc(sizeof(int64_t) * N);
+    if (!tmp) return fail(c, "po_set_keys: out of memory");
+    for (int r = 0; r < c->p.k; r++) {
+        for (int j = 0; j < N; j++) tmp[j] = rlwe_s[(size_t)r * N + j];
+        ntt_from_torus(c, c->rlwe_s_ntt + (size_t)r * N, tmp);
+    }
+    free(tmp);
+    return 0;
+}
+
+int po_get_ksk(po_ctx* c, int32_t* out) { memcpy(out, c->ksk, sizeof(int32_t) * ksk_words(c)); return 0; }
+int po_set_ksk(po_ctx* c, const int32_t* in) { memcpy(c->ksk, in, sizeof(int32_t) * ksk_words(c)); return 0; }
+int po_get_bsk_ntt(po_ctx* c, uint64_t* out) { memcpy(out, c->bsk, sizeof(uint64_t) * bsk_words(c)); return 0; }
+int po_set_bsk_ntt(po_ctx* c, const uint64_t* in) { memcpy(c->bsk, in, sizeof(uint64_t) * bsk_words(c)); return 0; }
+
+/* ------------------------------------------------------------------ BSK file */
+
+/*
+ * serializeBskMP / deserializeBskMP (yatfhe/src/ya_serializer.cpp:276-303) with the
+ * nested serializers for TrgswMPDft (:176-218), TrlweDft (:76-98) and NttPolynomial
+ * (:21-30): native-endian PODs, int = 4 bytes, bool = 1 byte.
+ */
+static int wr(FILE* f, const void* p, size_t n) { return fwrite(p, 1, n, f) == n ? 0 : -1; }
+static int rd(FILE* f, void* p, size_t n) { return fread(p, 1, n, f) == n ? 0 : -1; }
+
+static int wr_trlwe_dft(FILE* f, const uint64_t* rows, int k, int N) {
+    int32_t kk = k;
+    uint8_t init = 1;
+    int32_t NN = N, asz = k;
+    int e = 0;
+    e |= wr(f, &kk, 4);
+    e |= wr(f, &init, 1);
+    e |= wr(f, &NN, 4);
+    e |= wr(f, rows + (size_t)k * N, sizeof(uint64_t) * N); /* b */
+    e |= wr(f, &asz, 4);
+    for (int r = 0; r < k; r++) {
+        e |= wr(f, &NN, 4);
+        e |= wr(f, rows + (size_t)r * N, sizeof(uint64_t) * N);
+    }
+    return e;
+}
+
+static int rd_expect_i32(FILE* f, int32_t want) {
+    int32_t v;
+    if (rd(f, &v, 4)) return -1;
+    return v == want ? 0 : -1;
+}
+
+static int rd_trlwe_dft(FILE* f, uint64_t* rows, int k, int N) {
+    uint8_t init;
+    if (rd_expect_i32(f, k) || rd(f, &init, 1) || init != 1) return -1;
+    if (rd_expect_i32(f, N) || rd(f, rows + (size_t)k * N, sizeof(uint64_t) * N)) return -1;
+    if (rd_expect_i32(f, k)) return -1;
+    for (int r = 0; r < k; r++)
+        if (rd_expect_i32(f, N) || rd(f, rows + (size_t)r * N, sizeof(uint64_t) * N)) return -1;
+    return 0;
+}
+
+int po_save_bsk_file(po_ctx* c, const char* path) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, "po_save_bsk_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L;
+    const size_t rowWords = (size_t)(k + 1) * N, lvlWords = (size_t)(k + 1) * rowWords;
+    int e = 0;
+    for (int i = 0; i < n; i++) {
+        int32_t l = L, kk = k;
+        uint8_t half = 0;
+        e |= wr(f, &l, 4);
+        e |= wr(f, &kk, 4);
+        e |= wr(f, &half, 1);
+        e |= wr(f, &l, 4);
+        for (int lvl = 0; lvl < L; lvl++) {
+            e |= wr(f, &kk, 4);
+            for (int r = 0; r < k; r++)
+                e |= wr_trlwe_dft(f, c->bsk + ((size_t)i * L + lvl) * lvlWords + r * rowWords, k, N);
+        }
+        e |= wr(f, &l, 4);
+        for (int lvl = 0; lvl < L; lvl++)
+            e |= wr_trlwe_dft(f, c->bsk + ((size_t)i * L + lvl) * lvlWords + (size_t)k * rowWords, k, N);
+    }
+    int32_t nn = n, group = 1;
+    uint8_t half = 0;
+    e |= wr(f, &nn, 4);
+    e |= wr(f, &group, 4);
+    e |= wr(f, &half, 1);
+    if (fclose(f) != 0) e = -1;
+    return e ? fail(c, "po_save_bsk_file: write failed") : 0;
+}
+
+int po_load_bsk_file(po_ctx* c, const char* path) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(c, "po_load_bsk_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L;
+    const size_t rowWords = (size_t)(k + 1) * N, lvlWords = (size_t)(k + 1) * rowWords;
+    int e = 0;
+    for (int i = 0; i < n && !e; i++) {
+        uint8_t half;
+        e |= rd_expect_i32(f, L) | rd_expect_i32(f, k) | rd(f, &half, 1);
+        if (e || half) { e = -1; break; }
+        e |= rd_expect_i32(f, L);
+        for (int lvl = 0; lvl < L && !e; lvl++) {
+            e |= rd_expect_i32(f, k);
+            for (int r = 0; r < k && !e; r++)
+                e |= rd_trlwe_dft(f, c->bsk + ((size_t)i * L + lvl) * lvlWords + r * rowWords, k, N);
+        }
+        e |= rd_expect_i32(f, L);
+        for (int lvl = 0; lvl < L && !e; lvl++)
+            e |= rd_trlwe_dft(f, c->bsk + ((size_t)i * L + lvl) * lvlWords + (size_t)k * rowWords, k, N);
+    }
+    if (!e) e |= rd_expect_i32(f, n);
+    fclose(f);
+    return e ? fail(c, "po_load_bsk_file: %s is not a GINX key for these parameters", path) : 0;
+}
+
+/* ------------------------------------------------------------------ small pieces */
+
+/* generateTestPolynomial (kind 0) / generateTestPolynomialFR (kind 1)
+ * (yatfhe/src/polynomial.cpp:75-107) with modQ = 2N; slot values via
+ * modSwitchToTorus32 (numeric.cpp:210-214) with TORUS_Q = 2^T. */
+int po_test_polynomial(po_ctx* c, int kind, int modP, int64_t* v) {
+    const int N = c->p.N, modQ = 2 * N;
+    const int box = modQ / modP, half = box / 2, hh = half / 2;
+    const int width = kind == 0 ? box : half;
+    const int neg = kind == 0 ? half : hh;
+    const int64_t scale = ((int64_t)1 << c->T) / modP;
+    int64_t* t = (int64_t*)malloc(sizeof(int64_t) * N);
+    if (!t) return fail(c, "po_test_polynomial: out of memory");
+    for (int i = 0; i < N; i++) t[i] = sext(int_mod_p(i / width, modP) * scale, c->T);
+    for (int i = 0; i < neg; i++) t[i] = sext(-t[i], c->T);
+    for (int i = 0; i < N; i++) v[i] = t[(i + neg) % N]; /* std::rotate left by neg */
+    free(t);
+    return 0;
+}
+
+/* rescaleTlweToNewMod (yatfhe/src/tlwe.cpp:75-81) into mod 2N. */
+int po_modswitch(po_ctx* c, const int32_t* in, int32_t* out) {
+    const int n = c->p.n, bits = log2i(2 * c->p.N);
+    for (int i = 0; i <= n; i++) out[i] = (int32_t)modswitch_down(in[i], 32, bits);
+    return 0;
+}
+
+int po_rotate(po_ctx* c, const int64_t* in, int a, int minus_one, int64_t* out) {
+    rotate_poly(c, out, in, a, minus_one);
+    return 0;
+}
+
+/* decomposeRow (yatfhe/include/yatfhe/gadget_decomposition.h:190-236); out = [level][N]. */
+int po_decompose(po_ctx* c, const int64_t* in, int levels, int64_t* out) {
+    const int N = c->p.N;
+    if (levels * c->p.radix_bits > c->T) return fail(c, "po_decompose: l * radixBits exceeds the torus width");
+    int64_t d[64];
+    for (int j = 0; j < N; j++) {
+        zero_mean_digits((uint64_t)in[j], levels, c->p.radix_bits, c->T, d);
+        for (int l = 0; l < levels; l++) out[(size_t)l * N + j] = d[l];
+    }
+    return 0;
+}
+
+/* signedGadgetDecompositionKs (yatfhe/src/gadget_decomposition.cpp:53-56). */
+int po_decompose_ks(po_ctx* c, int64_t value, int64_t* out) {
+    zero_mean_digits((uint64_t)value, c->p.ks_level, c->p.ks_radix_bits, 32, out);
+    return 0;
+}
+
+int po_ntt_forward(po_ctx* c, const int64_t* in, uint64_t* out) {
+    ntt_from_torus(c, out, in);
+    return 0;
+}
+
+int po_ntt_inverse(po_ctx* c, const uint64_t* in, int64_t* out) {
+    uint64_t* t = (uint64_t*)malloc(sizeof(uint64_t) * c->p.N);
+    if (!t) return fail(c, "po_ntt_inverse: out of memory");
+    memcpy(t, in, sizeof(uint64_t) * c->p.N);
+    intt_to_torus(c, out, t);
+    free(t);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ external product */
+
+typedef struct {
+    int64_t* digits;   /* L x N */
+    uint64_t* dntt;    /* N */
+    uint64_t* acc;     /* (k+1) x N, NTT domain */
+    int64_t* tmp;      /* (k+1) x N, torus */
+    int64_t* dg;       /* per-value digit scratch, L */
+} ep_scratch;
+
+static int ep_alloc(const po_ctx* c, ep_scratch* s) {
+    const int N = c->p.N, k1 = c->p.k + 1;
+    s->digits = (int64_t*)malloc(sizeof(int64_t) * (size_t)c->L * N);
+    s->dntt = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    s->acc = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)k1 * N);
+    s->tmp = (int64_t*)malloc(sizeof(int64_t) * (size_t)k1 * N);
+    s->dg = (int64_t*)malloc(sizeof(int64_t) * (size_t)(c->L > 0 ? c->L : 1));
+    return (s->digits && s->dntt && s->acc && s->tmp && s->dg) ? 0 : -1;
+}
+
+static void ep_free(ep_scratch* s) {
+    free(s->digits); free(s->dntt); free(s->acc); free(s->tmp); free(s->dg);
+}
+
+/*
+ * externalProductTrgswMPNttImpl (yatfhe/src/trgsw.cpp:712-767): decompose every input
+ * poly into L levels (gadgetDecomposeTrlwe, yatfhe/src/trlwe.cpp:185-198), NTT each
+ * digit poly, multiply-accumulate against the key rows -- a-digits against c[lvl][r],
+ * b-digits against cPrime[lvl] (:737-744) -- sum all levels mod q, inverse NTT (:761-766).
+ * The NTT-domain sum is a sum mod q, so accumulating every (level, row) product into one
+ * accumulator gives the same residues as the reference's per-level partials.
+ * in/out = [a_0..a_{k-1}, b], may alias.
+ */
+static void external_product(const po_ctx* c, ep_scratch* s, const uint64_t* key, const int64_t* in, int64_t* out) {
+    const int N = c->p.N, k = c->p.k, k1 = k + 1, L = c->L;
+    const uint64_t q = c->q;
+    const nq_barrett* br = &c->plan.br;
+    const size_t rowWords = (size_t)k1 * N, lvlWords = (size_t)k1 * rowWords;
+    memset(s->acc, 0, sizeof(uint64_t) * rowWords);
+    for (int r = 0; r < k1; r++) {
+        const int64_t* poly = in + (size_t)r * N;
+        for (int j = 0; j < N; j++) {
+            zero_mean_digits((uint64_t)poly[j], L, c->p.radix_bits, c->T, s->dg);
+            for (int lvl = 0; lvl < L; lvl++) s->digits[(size_t)lvl * N + j] = s->dg[lvl];
+        }
+        for (int lvl = 0; lvl < L; lvl++) {
+            ntt_from_torus(c, s->dntt, s->digits + (size_t)lvl * N);
+            const uint64_t* keyRow = key + (size_t)lvl * lvlWords + (size_t)r * rowWords;
+            for (int o = 0; o < k1; o++) {
+                const uint64_t* kp = keyRow + (size_t)o * N;
+                uint64_t* ap = s->acc + (size_t)o * N;
+                for (int j = 0; j < N; j++) ap[j] = addmod(ap[j], nq_mulmod(br, s->dntt[j], kp[j]), q);
+            }
+        }
+    }
+    for (int o = 0; o < k1; o++) intt_to_torus(c, out + (size_t)o * N, s->acc + (size_t)o * N);
+}
+
+int po_external_product(po_ctx* c, const int64_t* in, int i, int64_t* out) {
+    ep_scratch s;
+    if (ep_alloc(c, &s)) { ep_free(&s); return fail(c, "po_external_product: out of memory"); }
+    const size_t k1 = (size_t)c->p.k + 1;
+    external_product(c, &s, c->bsk + (size_t)i * c->L * k1 * k1 * c->p.N, in, out);
+    ep_free(&s);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ blind rotation */
+
+/* genNoiselessTrlweSample (yatfhe/src/trlwe.cpp:175-182) + the binary branch of
+ * blindRotateMP21Ntt (yatfhe/src/blind_rotate.cpp:1556-1563):
+ *   for i < n: if a_i != 0: acc += ExtProd(BSK_i, X^{a_i} acc - acc). */
+static void blind_rotate(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc,
+                         const int* checkpoints, int ncheck, int64_t* acc_out) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, k1 = k + 1;
+    const size_t stride = (size_t)k1 * N;
+    const size_t keyWords = (size_t)c->L * k1 * k1 * N;
+    memset(acc, 0, sizeof(int64_t) * (size_t)k * N);
+    rotate_poly(c, acc + (size_t)k * N, v, -scaled[n], 0);
+    int cp = 0;
+    for (int i = 0; i < n; i++) {
+        const int a = scaled[i];
+        if (a != 0) {
+            for (int r = 0; r < k1; r++) rotate_poly(c, s->tmp + (size_t)r * N, acc + (size_t)r * N, a, 1);
+            external_product(c, s, c->bsk + (size_t)i * keyWords, s->tmp, s->tmp);
+            for (size_t j = 0; j < stride; j++) acc[j] = sext(acc[j] + s->tmp[j], c->T);
+        }
+        while (cp < ncheck && checkpoints[cp] == i) {
+            memcpy(acc_out + (size_t)cp * stride, acc, sizeof(int64_t) * stride);
+            cp++;
+        }
+    }
+}
+
+/* extractTlweFromTrlwe(out, acc, 0) (yatfhe/src/trlwe.cpp:240-250): a'[r N + j] =
+ * j == 0 ? a_r[0] : -a_r[N - j], b' = b[0], each rescaled 2^T -> 2^32 (numeric.cpp:189-208). */
+static void extract(const po_ctx* c, const int64_t* acc, int32_t* out) {
+    const int N = c->p.N, k = c->p.k, T = c->T;
+    for (int r = 0; r < k; r++)
+        for (int j = 0; j < N; j++) {
+            int64_t x = j == 0 ? acc[(size_t)r * N] : sext(-acc[(size_t)r * N + N - j], T);
+            out[(size_t)r * N + j] = (int32_t)modswitch_down(x, T, 32);
+        }
+    out[(size_t)k * N] = (int32_t)modswitch_down(acc[(size_t)k * N], T, 32);
+}
+
+/* switchKeyForTlwe (yatfhe/src/keyswitching.cpp:48-72): int64 sums of digit * ksk word,
+ * zero digits skipped, results reduced mod 2^32. */
+static void keyswitch(const po_ctx* c, const int32_t* in, int32_t* out, int64_t* delta) {
+    const int n = c->p.n, kN = c->p.k * c->p.N, t = c->p.ks_level, nb = n + 1;
+    int64_t d[64];
+    memset(delta, 0, sizeof(int64_t) * nb);
+    for (int i = 0; i < kN; i++) {
+        zero_mean_digits((uint64_t)(int64_t)in[i], t, c->p.ks_radix_bits, 32, d);
+        for (int j = 0; j < t; j++) {
+            const int64_t coef = d[j];
+            if (!coef) continue;
+            const int32_t* row = c->ksk + ((size_t)i * t + j) * nb;
+            for (int x = 0; x < nb; x++) delta[x] += coef * row[x];
+        }
+    }
+    for (int x = 0; x < n; x++) out[x] = (int32_t)sext(-delta[x], 32);
+    out[n] = (int32_t)sext((int64_t)in[kN] - delta[n], 32);
+}
+
+int po_extract(po_ctx* c, const int64_t* acc, int32_t* out) {
+    extract(c, acc, out);
+    return 0;
+}
+
+int po_keyswitch(po_ctx* c, const int32_t* in, int32_t* out) {
+    int64_t* delta = (int64_t*)malloc(sizeof(int64_t) * (c->p.n + 1));
+    if (!delta) return fail(c, "po_keyswitch: out of memory");
+    keyswitch(c, in, out, delta);
+    free(delta);
+    return 0;
+}
+
+int po_blind_rotate_trace(po_ctx* c, const int32_t* in, const int64_t* v, const int* checkpoints, int ncheck,
+                          int64_t* acc_out, int64_t* acc_final) {
+    ep_scratch s;
+    if (ep_alloc(c, &s)) { ep_free(&s); return fail(c, "po_blind_rotate_trace: out of memory"); }
+    int32_t* scaled = (int32_t*)malloc(sizeof(int32_t) * (c->p.n + 1));
+    if (!scaled) { ep_free(&s); return fail(c, "po_blind_rotate_trace: out of memory"); }
+    po_modswitch(c, in, scaled);
+    blind_rotate(c, &s, scaled, v, acc_final, checkpoints, ncheck, acc_out);
+    free(scaled);
+    ep_free(&s);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ full bootstrap */
+
+typedef struct {
+    po_ctx* c;
+    const int32_t* in;
+    const int64_t* v;
+    int32_t* out;
+    int begin, end;
+    int rc;
+} pbs_job;
+
+/* functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:71-80). */
+static void* pbs_worker(void* arg) {
+    pbs_job* j = (pbs_job*)arg;
+    po_ctx* c = j->c;
+    const int n = c->p.n, N = c->p.N, k = c->p.k, nb = n + 1;
+    ep_scratch s;
+    int32_t* scaled = (int32_t*)malloc(sizeof(int32_t) * nb);
+    int64_t* acc = (int64_t*)malloc(sizeof(int64_t) * (size_t)(k + 1) * N);
+    int32_t* ext = (int32_t*)malloc(sizeof(int32_t) * ((size_t)k * N + 1));
+    int64_t* delta = (int64_t*)malloc(sizeof(int64_t) * nb);
+    if (ep_alloc(c, &s) || !scaled || !acc || !ext || !delta) {
+        j->rc = -1;
+    } else {
+        for (int i = j->begin; i < j->end; i++) {
+            po_modswitch(c, j->in + (size_t)i * nb, scaled);
+            blind_rotate(c, &s, scaled, j->v, acc, NULL, 0, NULL);
+            extract(c, acc, ext);
+            keyswitch(c, ext, j->out + (size_t)i * nb, delta);
+        }
+        j->rc = 0;
+    }
+    ep_free(&s);
+    free(scaled); free(acc); free(ext); free(delta);
+    return NULL;
+}
+
+int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > count) threads = count > 0 ? count : 1;
+    pbs_job* jobs = (pbs_job*)calloc((size_t)threads, sizeof(pbs_job));
+    pthread_t* tids = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    if (!jobs || !tids) { free(jobs); free(tids); return fail(c, "po_pbs: out of memory"); }
+    int rc = 0;
+    for (int t = 0; t < threads; t++) {
+        jobs[t].c = c; jobs[t].in = in; jobs[t].v = v; jobs[t].out = out;
+        jobs[t].begin = (int)((long long)count * t / threads);
+        jobs[t].end = (int)((long long)count * (t + 1) / threads);
+        if (threads == 1) pbs_worker(&jobs[t]);
+        else if (pthread_create(&tids[t], NULL, pbs_worker, &jobs[t]) != 0) { jobs[t].rc = -1; tids[t] = 0; }
+    }
+    if (threads > 1)
+        for (int t = 0; t < threads; t++)
+            if (tids[t]) pthread_join(tids[t], NULL);
+    for (int t = 0; t < threads; t++) rc |= jobs[t].rc;
+    free(jobs);
+    free(tids);
+    return rc ? fail(c, "po_pbs: worker failed") : 0;
+}

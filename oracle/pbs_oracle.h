@@ -1,0 +1,64 @@
+/*
+ * pbs_oracle.h -- plain-C restatement of the reference's TFHE programmable bootstrap
+ * path (GINX / MP21), used as the correctness oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the CPU-baseline leg
+ * of bench.py call it as the checker; the shipped library never links it.
+ *
+ * Conventions: torus values are int64 sign-extended from the torus width T (32 or 56);
+ * LWE ciphertexts are int32 words [a_0 .. a_{n-1}, b] (mod 2^32);
+ * NTT-domain key words are uint64 residues mod qNtt in the convention of ntt_q.h.
+ */
+#ifndef YATFHE_ORACLE_PBS_ORACLE_H
+#define YATFHE_ORACLE_PBS_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int n, N, k, radix_bits, l, l_approx, ks_radix_bits, ks_level, lwe_noise_b, rlwe_noise_b, torus_base;
+    int torus_bits; /* 32 or 56 */
+} po_params;
+
+typedef struct po_ctx po_ctx;
+
+po_ctx* po_create(const po_params* p);
+void po_destroy(po_ctx* c);
+const char* po_last_error(po_ctx* c);
+uint64_t po_qntt(po_ctx* c);
+
+int po_keygen(po_ctx* c, uint64_t seed);
+int po_encrypt(po_ctx* c, const int64_t* mu, int count, int32_t* out);
+int po_decrypt(po_ctx* c, const int32_t* in, int count, int base, int32_t* out);
+
+int po_get_keys(po_ctx* c, int32_t* lwe_s, int32_t* rlwe_s);
+int po_set_keys(po_ctx* c, const int32_t* lwe_s, const int32_t* rlwe_s);
+int po_get_ksk(po_ctx* c, int32_t* out);
+int po_set_ksk(po_ctx* c, const int32_t* in);
+int po_get_bsk_ntt(po_ctx* c, uint64_t* out);
+int po_set_bsk_ntt(po_ctx* c, const uint64_t* in);
+int po_save_bsk_file(po_ctx* c, const char* path);
+int po_load_bsk_file(po_ctx* c, const char* path);
+
+int po_test_polynomial(po_ctx* c, int kind, int modP, int64_t* v);
+int po_modswitch(po_ctx* c, const int32_t* in, int32_t* out);
+int po_rotate(po_ctx* c, const int64_t* in, int a, int minus_one, int64_t* out);
+int po_decompose(po_ctx* c, const int64_t* in, int levels, int64_t* out);
+int po_decompose_ks(po_ctx* c, int64_t value, int64_t* out);
+int po_ntt_forward(po_ctx* c, const int64_t* in, uint64_t* out);
+int po_ntt_inverse(po_ctx* c, const uint64_t* in, int64_t* out);
+int po_external_product(po_ctx* c, const int64_t* in, int i, int64_t* out);
+int po_extract(po_ctx* c, const int64_t* acc, int32_t* out);
+int po_keyswitch(po_ctx* c, const int32_t* in, int32_t* out);
+int po_blind_rotate_trace(po_ctx* c, const int32_t* in, const int64_t* v, const int* checkpoints, int ncheck,
+                          int64_t* acc_out, int64_t* acc_final);
+int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YATFHE_ORACLE_PBS_ORACLE_H */
