@@ -1,0 +1,81 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own code.
+
+Runs only where the reference tree is present: it builds oracle/_ref (the reference's
+sources compiled against the HEXL/GMP stand-ins and the seeded RNG) and records, per
+parameter set and key seed:
+  * SHA-256 digests of the key material the reference generates from the seed
+    (LWE key, RLWE key, NTT-domain BSK words, KSK words) -- small, but enough for any
+    machine to confirm that the restatement regenerates the same keys;
+  * input ciphertexts (symEncTlwe on the same RNG stream, right after key generation),
+    the test polynomial, the reference's outputs of functionalBootstrappingMPNtt, its
+    decryptions, and the blind-rotation accumulator of ciphertext 0 after a few CMux steps.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+from oracle.oracle import Reference  # noqa: E402
+from yatfhe_gb300 import lut as lutmod  # noqa: E402
+from yatfhe_gb300.params import T32_N1024, T56_N2048, small  # noqa: E402
+
+CASES = {
+    # name: (params, key seed, number of ciphertexts, message seed)
+    "t32_n1024_seed5eed0001": (T32_N1024, 0x5EED0001, 8, 11),
+    "t56_n2048_seed5eed0003": (T56_N2048, 0x5EED0003, 6, 12),
+    "t32_n1024_small40_seed7": (small(T32_N1024, 40), 7, 16, 13),
+}
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def messages(p, count, seed):
+    rng = np.random.default_rng(seed)
+    if p.torus_bits == 32:
+        bits = rng.integers(0, 2, count)
+        mu = np.where(bits == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+        return mu, lutmod.sign_lut(p.N, 32), 8, np.where(bits == 1, 1, -1)
+    m = rng.integers(0, 16, count)
+    table = rng.integers(0, 16, 16)
+    mu = (m * (1 << 27)).astype(np.int64)
+    return mu, lutmod.padded_message_lut(p.N, 56, table), 32, table[m]
+
+
+def make(name, p, seed, count, mseed):
+    ref = Reference(p)
+    ref.keygen(seed)
+    s, z = ref.keys()
+    bsk = ref.bsk_ntt()
+    ksk = ref.ksk()
+    mu, lut, base, expect = messages(p, count, mseed)
+    lwe = ref.encrypt(mu)
+    out = ref.pbs(lwe, lut, threads=1)
+    dec = ref.decrypt(out, base)
+    if not np.array_equal(dec, expect):
+        raise SystemExit(f"{name}: the reference's own decryptions {dec} differ from the messages {expect}")
+    cps = sorted({0, 1, p.n // 2, p.n - 1})
+    acc, final = ref.blind_rotate_trace(lwe[0], lut, cps)
+    np.savez_compressed(
+        HERE / f"{name}.npz",
+        params=np.array([p.n, p.N, p.k, p.radix_bits, p.l, p.l_approx, p.ks_radix_bits, p.ks_level, p.lwe_noise_b,
+                         p.rlwe_noise_b, p.torus_base, p.torus_bits], np.int64),
+        seed=np.array([seed], np.uint64),
+        sha_lwe_s=digest(s), sha_rlwe_s=digest(z), sha_bsk=digest(bsk), sha_ksk=digest(ksk),
+        mu=mu, lwe_in=lwe, lut=lut, lwe_out=out, decrypted=dec, base=np.array([base]),
+        checkpoints=np.array(cps, np.int64), acc=acc, acc_final=final)
+    print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
+
+
+if __name__ == "__main__":
+    for name, (p, seed, count, mseed) in CASES.items():
+        make(name, p, seed, count, mseed)

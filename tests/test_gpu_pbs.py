@@ -1,0 +1,141 @@
+"""GPU parity: the CUDA bootstrap against the oracle, bit for bit, through the C ABI.
+
+Keys come from the oracle's seeded key generation (bit-identical to the reference's own,
+checked on CPU in test_oracle.py); the GPU path receives them exactly as a reference user
+would hand them over (NTT-domain key words / the reference's key file format).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Restatement
+from yatfhe_gb300 import lut as lutmod
+from yatfhe_gb300.params import T32_N1024, T56_N2048, small
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _sign_inputs(ora, count, seed):
+    rng = np.random.default_rng(seed)
+    bits = rng.integers(0, 2, count)
+    mu = np.where(bits == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    return mu, ora.encrypt(mu)
+
+
+def _setup(p, seed, built_lib):
+    from yatfhe_gb300 import api
+
+    ora = Restatement(p)
+    ora.keygen(seed)
+    ctx = api.Context(p, 0)
+    key = api.BootstrapKey.from_ntt_words(ctx, ora.bsk_ntt()).set_ksk(ora.ksk())
+    return ora, ctx, key
+
+
+@pytest.fixture(scope="module")
+def t32_small(built_lib):
+    return _setup(small(T32_N1024, 32), 0x5EED0001, built_lib)
+
+
+@pytest.fixture(scope="module")
+def t56_small(built_lib):
+    return _setup(small(T56_N2048, 12), 0x5EED0003, built_lib)
+
+
+def _pbs_gpu(ctx, key, lwe, lut):
+    from yatfhe_gb300 import api
+
+    out = api.functional_bootstrapping_mp_ntt(ctx, key, torch.from_numpy(lwe).cuda(), torch.from_numpy(lut).cuda())
+    return out.cpu().numpy()
+
+
+def test_pbs_t32_small_bit_exact(t32_small):
+    ora, ctx, key = t32_small
+    mu, lwe = _sign_inputs(ora, 16, 1)
+    lut = lutmod.sign_lut(ctx.params.N, 32)
+    got = _pbs_gpu(ctx, key, lwe, lut)
+    np.testing.assert_array_equal(got, ora.pbs(lwe, lut, threads=8))
+    np.testing.assert_array_equal(ora.decrypt(got, 8), np.where(mu > 0, 1, -1))
+
+
+def test_blind_rotate_checkpoints_t32(t32_small):
+    """Accumulator after 1, 2, 7 and all CMux steps equals the oracle's trace."""
+    from yatfhe_gb300 import api
+
+    ora, ctx, key = t32_small
+    _, lwe = _sign_inputs(ora, 2, 2)
+    lut = ora.test_polynomial(0, 8)
+    cps = [0, 1, 6, ctx.params.n - 1]
+    d_in = torch.from_numpy(lwe).cuda()
+    d_lut = torch.from_numpy(lut).cuda()
+    for c in range(len(lwe)):
+        want, final = ora.blind_rotate_trace(lwe[c], lut, cps)
+        for k, step in enumerate(cps):
+            acc = api.blind_rotate_mp21_ntt(ctx, key, d_in[c:c + 1], d_lut, steps=step + 1).cpu().numpy()[0]
+            np.testing.assert_array_equal(acc, want[k], err_msg=f"ciphertext {c}, after step {step}")
+        np.testing.assert_array_equal(want[-1], final)
+
+
+def test_keyswitch_alone_t32(t32_small):
+    from yatfhe_gb300 import api
+
+    ora, ctx, key = t32_small
+    p = ctx.params
+    rng = np.random.default_rng(3)
+    big = rng.integers(-(1 << 31), 1 << 31, size=(5, p.k * p.N + 1), dtype=np.int64).astype(np.int32)
+    big[0, :] = np.int32(-(1 << 31))  # extreme words
+    big[1, :] = 0
+    got = api.switch_key_for_tlwe(ctx, key, torch.from_numpy(big).cuda()).cpu().numpy()
+    for c in range(len(big)):
+        np.testing.assert_array_equal(got[c], ora.keyswitch(big[c]))
+
+
+def test_pbs_t56_small_bit_exact(t56_small):
+    ora, ctx, key = t56_small
+    rng = np.random.default_rng(4)
+    m = rng.integers(0, 16, 12)
+    table = rng.integers(0, 16, 16)
+    mu = (m * (1 << 27)).astype(np.int64)  # m 2^32 / 32
+    lwe = ora.encrypt(mu)
+    lut = lutmod.padded_message_lut(ctx.params.N, 56, table)
+    got = _pbs_gpu(ctx, key, lwe, lut)
+    np.testing.assert_array_equal(got, ora.pbs(lwe, lut, threads=8))
+
+
+def test_pbs_empty_and_single(t32_small):
+    from yatfhe_gb300 import api
+
+    ora, ctx, key = t32_small
+    lut = torch.from_numpy(lutmod.sign_lut(ctx.params.N, 32)).cuda()
+    empty = torch.empty((0, ctx.params.n + 1), dtype=torch.int32, device="cuda")
+    assert api.functional_bootstrapping_mp_ntt(ctx, key, empty, lut).shape == (0, ctx.params.n + 1)
+    _, lwe = _sign_inputs(ora, 1, 5)
+    got = _pbs_gpu(ctx, key, lwe, lut.cpu().numpy())
+    np.testing.assert_array_equal(got, ora.pbs(lwe, lut.cpu().numpy()))
+
+
+@pytest.mark.parametrize("which", ["t32", "t56"])
+def test_pbs_full_size_bit_exact(which, built_lib):
+    """Full parameter sets (n = 630 / N = 1024 and n = 750 / N = 2048)."""
+    if which == "t32":
+        p, seed = T32_N1024, 0x5EED0001
+    else:
+        p, seed = T56_N2048, 0x5EED0003
+    ora, ctx, key = _setup(p, seed, built_lib)
+    rng = np.random.default_rng(6)
+    if which == "t32":
+        mu, lwe = _sign_inputs(ora, 24, 7)
+        lut = lutmod.sign_lut(p.N, 32)
+        expect = np.where(mu > 0, 1, -1)
+        base = 8
+    else:
+        m = rng.integers(0, 16, 16)
+        table = rng.integers(0, 16, 16)
+        lwe = ora.encrypt((m * (1 << 27)).astype(np.int64))
+        lut = lutmod.padded_message_lut(p.N, 56, table)
+        expect = table[m]
+        base = 32
+    got = _pbs_gpu(ctx, key, lwe, lut)
+    want = ora.pbs(lwe, lut, threads=16)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(ora.decrypt(got, base), expect)

@@ -1,0 +1,166 @@
+"""Python view of the C ABI, for tests, the benchmark and scripting.
+
+Names follow the reference's C++ entry points (yatfhe/include/yatfhe/*.h) in snake case:
+
+  Context                          initYatfhe + YatfheParameters (one parameter set)
+  BootstrapKey.from_file           deserializeBskMP (yatfhe/src/ya_serializer.cpp:287-303)
+  BootstrapKey.from_ntt_words      BootstrappingKeyMP::bskDft already in memory
+  BootstrapKey.set_ksk             TlweKeySwitchingKey (yatfhe/include/yatfhe/keyswitching.h:14-31)
+  functional_bootstrapping_mp_ntt  functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:71-80)
+  blind_rotate_mp21_ntt            rescaleTlweToNewMod + genNoiselessTrlweSample + blindRotateMP21Ntt
+  switch_key_for_tlwe              switchKeyForTlwe (yatfhe/src/keyswitching.cpp:48-72)
+
+Device arguments are torch CUDA tensors (int32 ciphertext words, int64 torus LUT words);
+work is enqueued on torch's current stream.  ``*_host`` variants take numpy arrays.
+Errors raise the Python counterpart of the reference's exceptions (ValueError for
+std::invalid_argument, OSError for the serializer's std::runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .params import PbsParams
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _stream_handle(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dptr(t, dtype_name: str, what: str):
+    torch = _torch()
+    want = getattr(torch, dtype_name)
+    if not t.is_cuda or t.dtype != want or not t.is_contiguous():
+        raise ValueError(f"{what} must be a contiguous CUDA tensor of {dtype_name}")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class Context:
+    def __init__(self, params: PbsParams, device: int = 0):
+        params.validate()
+        self.params = params
+        self.device = device
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_ctx_create(ctypes.byref(_lib.YgParams.of(params)), device, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().yg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BootstrapKey:
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self._h = handle
+
+    @classmethod
+    def from_file(cls, ctx: Context, path) -> "BootstrapKey":
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_load_bsk_file(ctx.handle, str(path).encode(), ctypes.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def from_ntt_words(cls, ctx: Context, words: np.ndarray) -> "BootstrapKey":
+        w = np.ascontiguousarray(words, np.uint64)
+        if w.size != ctx.params.bsk_ntt_words:
+            raise ValueError(f"expected {ctx.params.bsk_ntt_words} NTT words, got {w.size}")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_upload_bsk_ntt(ctx.handle, ctypes.c_void_p(w.ctypes.data), ctypes.byref(h)))
+        return cls(ctx, h)
+
+    def set_ksk(self, ksk: np.ndarray) -> "BootstrapKey":
+        k = np.ascontiguousarray(ksk, np.int32)
+        if k.size != self.ctx.params.ksk_words:
+            raise ValueError(f"expected {self.ctx.params.ksk_words} KSK words, got {k.size}")
+        _lib.check(_lib.lib().yg_key_set_ksk(self._h, ctypes.c_void_p(k.ctypes.data)))
+        return self
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.lib().yg_key_device_bytes(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().yg_key_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def functional_bootstrapping_mp_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, out=None, stream=None):
+    """Bootstraps every row of ``lwe_in`` ([count, n+1] int32 CUDA tensor) through ``lut``."""
+    torch = _torch()
+    n1 = ctx.params.n + 1
+    if lwe_in.dim() != 2 or lwe_in.shape[1] != n1:
+        raise ValueError(f"lwe_in must have shape [count, {n1}]")
+    if out is None:
+        out = torch.empty_like(lwe_in)
+    _lib.check(_lib.lib().yg_pbs(ctx.handle, key.handle, _dptr(lwe_in, "int32", "lwe_in"),
+                                 _dptr(out, "int32", "out"), lwe_in.shape[0], _dptr(lut, "int64", "lut"),
+                                 _stream_handle(stream)))
+    return out
+
+
+def functional_bootstrapping_mp_ntt_host(ctx: Context, key: BootstrapKey, lwe_in: np.ndarray, lut: np.ndarray,
+                                         out: np.ndarray | None = None) -> np.ndarray:
+    """Host-buffer form: copies in, bootstraps, copies out (pinned buffers give the fastest copies)."""
+    a = np.ascontiguousarray(lwe_in, np.int32).reshape(-1, ctx.params.n + 1)
+    v = np.ascontiguousarray(lut, np.int64)
+    if out is None:
+        out = np.empty_like(a)
+    _lib.check(_lib.lib().yg_pbs_host(ctx.handle, key.handle, ctypes.c_void_p(a.ctypes.data),
+                                      ctypes.c_void_p(out.ctypes.data), len(a), ctypes.c_void_p(v.ctypes.data),
+                                      ctypes.c_void_p(0)))
+    return out
+
+
+def blind_rotate_mp21_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
+    """Accumulators [count, (k+1) N] (int64 torus words) after ``steps`` CMux steps (default n)."""
+    torch = _torch()
+    p = ctx.params
+    steps = p.n if steps is None else steps
+    acc = torch.empty((lwe_in.shape[0], (p.k + 1) * p.N), dtype=torch.int64, device=lwe_in.device)
+    _lib.check(_lib.lib().yg_blind_rotate(ctx.handle, key.handle, _dptr(lwe_in, "int32", "lwe_in"),
+                                          _dptr(lut, "int64", "lut"), _dptr(acc, "int64", "acc"),
+                                          lwe_in.shape[0], steps, _stream_handle(stream)))
+    return acc
+
+
+def switch_key_for_tlwe(ctx: Context, key: BootstrapKey, big, stream=None):
+    """Key-switches extracted ciphertexts ([count, kN+1] int32) to [count, n+1]."""
+    torch = _torch()
+    p = ctx.params
+    out = torch.empty((big.shape[0], p.n + 1), dtype=torch.int32, device=big.device)
+    _lib.check(_lib.lib().yg_keyswitch(ctx.handle, key.handle, _dptr(big, "int32", "big"), _dptr(out, "int32", "out"),
+                                       big.shape[0], _stream_handle(stream)))
+    return out

@@ -1,0 +1,603 @@
+// host.cpp -- C ABI of the GB300 bootstrap (include/yatfhe_gb300.h): contexts, key
+// loading and conversion, launches.
+//
+// Key conversion.  The reference stores bootstrapping keys in the NTT domain of its
+// 64-bit prime q (serializeBskMP, yatfhe/src/ya_serializer.cpp:276-285; the words come
+// from HEXL's forward transform, yatfhe/include/yatfhe/ntt_hexl.h:34-44).  Every CMux
+// only ever uses them through centred(INTT(sum NTT(d) . K) mod q) (ntt_hexl.cpp:153-175),
+// so the loader takes each key polynomial back to coefficients once (inverse negacyclic
+// transform mod q with the minimal primitive 2N-th root, bit-reversed slot order: the
+// convention HEXL documents), centres them, reduces them into the three RNS channels
+// and hands them to keyconv_kernel, which applies the GPU's own per-channel NTT.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/yatfhe_gb300.h"
+#include "pbs_kernels.cuh"
+
+namespace {
+
+using u64 = uint64_t;
+using u128 = unsigned __int128;
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+u64 mulmod(u64 a, u64 b, u64 m) { return (u64)((u128)a * b % m); }
+u64 powmod(u64 b, u64 e, u64 m) {
+    u64 r = 1 % m;
+    b %= m;
+    while (e) {
+        if (e & 1) r = mulmod(r, b, m);
+        b = mulmod(b, b, m);
+        e >>= 1;
+    }
+    return r;
+}
+u64 invmod(u64 a, u64 p) { return powmod(a, p - 2, p); }
+uint32_t brv(uint32_t x, int bits) {
+    uint32_t r = 0;
+    for (int i = 0; i < bits; i++) r = (r << 1) | ((x >> i) & 1);
+    return r;
+}
+
+// Smallest primitive 2N-th root of unity mod a prime m == 1 (mod 2N).
+u64 minimal_root(u64 N, u64 m) {
+    const u64 twoN = 2 * N;
+    u64 psi0 = 0;
+    for (u64 x = 2; x < m && !psi0; x++) {
+        const u64 c = powmod(x, (m - 1) / twoN, m);
+        if (powmod(c, N, m) == m - 1) psi0 = c;
+    }
+    if (!psi0) throw std::invalid_argument("no primitive 2N-th root of unity");
+    u64 best = psi0, cur = psi0;
+    const u64 sq = mulmod(psi0, psi0, m);
+    for (u64 k = 1; k < N; k++) {
+        cur = mulmod(cur, sq, m);
+        best = std::min(best, cur);
+    }
+    return best;
+}
+
+// Inverse negacyclic transform mod q (Gentleman-Sande, psi^-brv(k) twiddles with Shoup
+// companions): bit-reversed NTT slots in, natural-order coefficients in [0, q) out.
+struct QInverse {
+    int N = 0, logN = 0;
+    u64 q = 0;
+    std::vector<u64> w, wp;
+    u64 ninv = 0, ninvp = 0;
+
+    QInverse(int N_, u64 q_) : N(N_), q(q_) {
+        while ((1 << logN) < N) logN++;
+        const u64 psi_inv = invmod(minimal_root(N, q), q);
+        w.resize(N);
+        wp.resize(N);
+        for (int k = 0; k < N; k++) {
+            w[k] = powmod(psi_inv, brv(k, logN), q);
+            wp[k] = (u64)(((u128)w[k] << 64) / q);
+        }
+        ninv = invmod(N, q);
+        ninvp = (u64)(((u128)ninv << 64) / q);
+    }
+
+    u64 mulshoup(u64 x, u64 ww, u64 wwp) const {
+        const u64 qh = (u64)(((u128)x * wwp) >> 64);
+        const u64 r = x * ww - qh * q;
+        return r >= q ? r - q : r;
+    }
+
+    void run(u64* a) const {
+        int t = 1;
+        for (int m = N; m > 1; m >>= 1) {
+            const int h = m >> 1;
+            for (int i = 0; i < h; i++) {
+                u64* x = a + 2 * i * t;
+                u64* y = x + t;
+                for (int j = 0; j < t; j++) {
+                    const u64 u = x[j], v = y[j];
+                    const u64 s = u + v;
+                    x[j] = s >= q ? s - q : s;
+                    y[j] = mulshoup(u >= v ? u - v : u + q - v, w[h + i], wp[h + i]);
+                }
+            }
+            t <<= 1;
+        }
+        for (int j = 0; j < N; j++) a[j] = mulshoup(a[j], ninv, ninvp);
+    }
+};
+
+uint32_t shoup32(uint32_t w, uint32_t p) { return (uint32_t)(((u64)w << 32) / p); }
+
+}  // namespace
+
+struct yg_ctx {
+    yg_params p{};
+    int logN = 0;
+    int device = 0;
+    u64 q = 0;
+    uint2* d_tw = nullptr;  // [3][2][N]: forward then inverse twiddles per channel
+    yg::Chan ch[yg::kChannels]{};
+    yg::Crt crt{};
+    uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
+    std::unique_ptr<QInverse> qinv;
+};
+
+struct yg_key {
+    yg_ctx* ctx = nullptr;
+    uint32_t* d_bsk = nullptr;
+    int32_t* d_ksk = nullptr;
+    size_t bsk_bytes = 0, ksk_bytes = 0;
+};
+
+namespace {
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const CudaError& e) {
+        return set_err(YG_ERR_CUDA, e.what());
+    } catch (const std::invalid_argument& e) {
+        return set_err(YG_ERR_INVALID, e.what());
+    } catch (const std::bad_alloc&) {
+        return set_err(YG_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return set_err(YG_ERR_IO, e.what());
+    }
+}
+
+void validate(const yg_params& p) {
+    if (p.torus_bits != 32 && p.torus_bits != 56) throw std::invalid_argument("torus_bits must be 32 or 56");
+    if (p.N != 1024 && p.N != 2048) throw std::invalid_argument("N must be 1024 or 2048");
+    if (p.k != 1) throw std::invalid_argument("only k = 1 is supported");
+    if (p.n < 1 || p.n > 4096) throw std::invalid_argument("n must be in [1, 4096]");
+    if (p.l_approx < 1 || p.radix_bits < 1 || p.l_approx * p.radix_bits > p.torus_bits)
+        throw std::invalid_argument("decomposeRow: l * radixBits exceeds the torus width");
+    if (p.radix_bits > 15) throw std::invalid_argument("radix_bits must be <= 15 (int16 digits)");
+    if (p.ks_level < 1 || p.ks_level > 16 || p.ks_radix_bits < 1 || p.ks_level * p.ks_radix_bits > 32 ||
+        p.ks_radix_bits > 7)
+        throw std::invalid_argument("key-switching decomposition must fit 32 bits, t <= 16, radix <= 7");
+    // exactness of the three-prime RNS: |X| <= (B/2)(q/2)(k+1) l N must stay below M/2
+    const double q = p.torus_bits == 32 ? 562941363486721.0 : 1945555039024054273.0;
+    const double bound = std::ldexp(1.0, p.radix_bits - 1) * (q / 2) * (p.k + 1) * p.l_approx * p.N;
+    const double M = (double)yg::kPrimes[0] * yg::kPrimes[1] * yg::kPrimes[2];
+    if (bound >= M / 4) throw std::invalid_argument("parameters exceed the exact range of the RNS");
+}
+
+void ctx_init_tables(yg_ctx* c) {
+    const int N = c->p.N;
+    std::vector<uint2> tw((size_t)yg::kChannels * 2 * N);
+    for (int ci = 0; ci < yg::kChannels; ci++) {
+        const uint32_t p = yg::kPrimes[ci];
+        const u64 psi = minimal_root(N, p);
+        const u64 psi_inv = invmod(psi, p);
+        for (int k = 0; k < N; k++) {
+            const uint32_t e = brv(k, c->logN);
+            const uint32_t wf = (uint32_t)powmod(psi, e, p), wi = (uint32_t)powmod(psi_inv, e, p);
+            tw[((size_t)ci * 2 + 0) * N + k] = make_uint2(wf, shoup32(wf, p));
+            tw[((size_t)ci * 2 + 1) * N + k] = make_uint2(wi, shoup32(wi, p));
+        }
+        // Montgomery form with N^-1 folded in: N^-1 2^32 mod p
+        const uint32_t sc = (uint32_t)mulmod(invmod(N, p), ((u64)1 << 32) % p, p);
+        c->conv_scale[ci] = sc;
+        c->conv_scale_s[ci] = shoup32(sc, p);
+    }
+    ck(cudaMalloc(&c->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
+    ck(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
+    for (int ci = 0; ci < yg::kChannels; ci++) {
+        const uint32_t p = yg::kPrimes[ci];
+        uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
+        for (int it = 0; it < 5; it++) pinv *= 2 - p * pinv;
+        c->ch[ci] = yg::Chan{p, 2 * p, (uint32_t)(0u - pinv), 0, c->d_tw + (size_t)ci * 2 * N,
+                             c->d_tw + ((size_t)ci * 2 + 1) * N};
+    }
+    const u64 p0 = yg::kPrimes[0], p1 = yg::kPrimes[1], p2 = yg::kPrimes[2];
+    yg::Crt& k = c->crt;
+    k.p0 = (uint32_t)p0;
+    k.p1 = (uint32_t)p1;
+    k.p2 = (uint32_t)p2;
+    k.inv_p0_m1 = (uint32_t)invmod(p0 % p1, p1);
+    k.inv_p0_m1_s = shoup32(k.inv_p0_m1, (uint32_t)p1);
+    k.p0_m2 = (uint32_t)(p0 % p2);
+    k.p0_m2_s = shoup32(k.p0_m2, (uint32_t)p2);
+    k.inv_p01_m2 = (uint32_t)invmod(mulmod(p0, p1, p2), p2);
+    k.inv_p01_m2_s = shoup32(k.inv_p01_m2, (uint32_t)p2);
+    k.half_p2 = (uint32_t)((p2 - 1) / 2);
+    k.p01 = p0 * p1;
+    k.q = c->q;
+    k.half_q = (c->q - 1) / 2;
+    k.a2 = (float)((double)k.p01 / (double)c->q);
+    k.a1 = (float)((double)p0 / (double)c->q);
+    k.a0 = (float)(1.0 / (double)c->q);
+}
+
+// NTT-domain key words -> device key.  Layout in: [n][L][k+1][k+1][N] u64.
+void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
+    const int n = c->p.n, N = c->p.N, L = c->p.l_approx;
+    const size_t polys = (size_t)n * L * 2 * 2;
+    std::vector<uint32_t> res(polys * yg::kChannels * N);
+    const QInverse& qi = *c->qinv;
+    const u64 q = c->q, half = (q + 1) / 2;
+    auto work = [&](size_t begin, size_t end) {
+        std::vector<u64> buf(N);
+        for (size_t poly = begin; poly < end; poly++) {
+            std::memcpy(buf.data(), words + poly * N, sizeof(u64) * N);
+            for (int j = 0; j < N; j++)
+                if (buf[j] >= q) throw std::invalid_argument("key word not reduced mod q");
+            qi.run(buf.data());
+            for (int ci = 0; ci < yg::kChannels; ci++) {
+                const u64 p = yg::kPrimes[ci];
+                uint32_t* dst = res.data() + (poly * yg::kChannels + ci) * N;
+                for (int j = 0; j < N; j++) {
+                    const u64 v = buf[j];
+                    // centred representative: v >= (q+1)/2 stands for v - q
+                    dst[j] = v >= half ? (uint32_t)((p - (q - v) % p) % p) : (uint32_t)(v % p);
+                }
+            }
+        }
+    };
+    const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> errs(hw);
+    for (unsigned t = 0; t < hw; t++) {
+        const size_t b = polys * t / hw, e = polys * (t + 1) / hw;
+        th.emplace_back([&, t, b, e] {
+            try {
+                work(b, e);
+            } catch (...) {
+                errs[t] = std::current_exception();
+            }
+        });
+    }
+    for (auto& x : th) x.join();
+    for (auto& e : errs)
+        if (e) std::rethrow_exception(e);
+
+    const size_t key_words = yg::key_words(n, L, N);
+    key->bsk_bytes = key_words * sizeof(uint32_t);
+    ck(cudaMalloc(&key->d_bsk, key->bsk_bytes), "cudaMalloc bsk");
+    uint32_t* d_res = nullptr;
+    ck(cudaMalloc(&d_res, res.size() * sizeof(uint32_t)), "cudaMalloc key residues");
+    try {
+        ck(cudaMemcpy(d_res, res.data(), res.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload residues");
+        yg::KeyConvArgs a{};
+        a.residues = d_res;
+        a.key = key->d_bsk;
+        a.polys = (int)polys;
+        for (int ci = 0; ci < yg::kChannels; ci++) {
+            a.ch[ci] = c->ch[ci];
+            a.scale[ci] = c->conv_scale[ci];
+            a.scale_s[ci] = c->conv_scale_s[ci];
+        }
+        if (yg::launch_keyconv(c->logN, a, nullptr) != 0) ck(cudaGetLastError(), "keyconv launch");
+        ck(cudaDeviceSynchronize(), "keyconv");
+    } catch (...) {
+        cudaFree(d_res);
+        throw;
+    }
+    cudaFree(d_res);
+}
+
+// deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)
+// (yatfhe/src/ya_serializer.cpp:21-30,87-98,193-218,287-303): native-endian PODs.
+struct Reader {
+    FILE* f;
+    std::string path;
+    void raw(void* p, size_t n) {
+        if (std::fread(p, 1, n, f) != n) throw std::runtime_error("short read in " + path);
+    }
+    int32_t i32() {
+        int32_t v;
+        raw(&v, 4);
+        return v;
+    }
+    uint8_t b8() {
+        uint8_t v;
+        raw(&v, 1);
+        return v;
+    }
+    void expect(int32_t want, const char* what) {
+        const int32_t v = i32();
+        if (v != want)
+            throw std::runtime_error(path + ": " + what + " is " + std::to_string(v) + ", expected " +
+                                     std::to_string(want));
+    }
+};
+
+void read_trlwe_dft(Reader& r, u64* rows, int k, int N) {
+    r.expect(k, "TrlweDft k");
+    if (r.b8() != 1) throw std::runtime_error(r.path + ": TrlweDft without its mask polynomials");
+    r.expect(N, "NttPolynomial N");
+    r.raw(rows + (size_t)k * N, sizeof(u64) * N);
+    r.expect(k, "TrlweDft a size");
+    for (int p = 0; p < k; p++) {
+        r.expect(N, "NttPolynomial N");
+        r.raw(rows + (size_t)p * N, sizeof(u64) * N);
+    }
+}
+
+std::vector<u64> read_bsk_file(const yg_params& p, const char* path) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    Reader r{f, path};
+    const int n = p.n, N = p.N, k = p.k, L = p.l_approx;
+    const size_t row = (size_t)(k + 1) * N, lvl = (size_t)(k + 1) * row;
+    std::vector<u64> words((size_t)n * L * lvl);
+    try {
+        for (int i = 0; i < n; i++) {
+            r.expect(L, "TrgswMPDft l");
+            r.expect(k, "TrgswMPDft k");
+            if (r.b8() != 0) throw std::runtime_error(std::string(path) + ": half (cPrime-only) keys are not GINX keys");
+            r.expect(L, "c size");
+            for (int l = 0; l < L; l++) {
+                r.expect(k, "c[l] size");
+                for (int rr = 0; rr < k; rr++) read_trlwe_dft(r, words.data() + ((size_t)i * L + l) * lvl + rr * row, k, N);
+            }
+            r.expect(L, "cPrime size");
+            for (int l = 0; l < L; l++) read_trlwe_dft(r, words.data() + ((size_t)i * L + l) * lvl + (size_t)k * row, k, N);
+        }
+        r.expect(n, "key n");
+        r.expect(1, "key group");
+        r.b8();
+    } catch (...) {
+        std::fclose(f);
+        throw;
+    }
+    std::fclose(f);
+    return words;
+}
+
+yg::BrArgs br_args(const yg_ctx* c, const yg_key* key) {
+    yg::BrArgs a{};
+    a.key = reinterpret_cast<const uint4*>(key->d_bsk);
+    a.n = c->p.n;
+    a.steps = c->p.n;
+    a.L = c->p.l_approx;
+    a.radix_bits = c->p.radix_bits;
+    for (int ci = 0; ci < yg::kChannels; ci++) a.ch[ci] = c->ch[ci];
+    a.crt = c->crt;
+    return a;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) ck(cudaSetDevice(dev), "cudaSetDevice");
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int check_key(const yg_ctx* c, const yg_key* k, bool need_ksk) {
+    if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
+    if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
+    if (!k->d_bsk) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
+    if (need_ksk && !k->d_ksk) return set_err(YG_ERR_STATE, "key has no key-switching key (yg_key_set_ksk)");
+    return YG_OK;
+}
+
+int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
+           cudaStream_t s) {
+    const int N = c->p.N, kN = c->p.k * N;
+    int32_t* big = nullptr;
+    ck(cudaMallocAsync(&big, (size_t)count * (kN + 1) * sizeof(int32_t), s), "cudaMallocAsync extract buffer");
+    yg::BrArgs a = br_args(c, key);
+    a.lwe_in = d_in;
+    a.lut = d_lut;
+    a.big_out = big;
+    a.count = count;
+    int rc = yg::launch_blind_rotate(c->logN, c->p.torus_bits, a, s);
+    if (rc == 0) {
+        yg::KsArgs k{big, key->d_ksk, d_out, count, kN, c->p.n, c->p.ks_level, c->p.ks_radix_bits};
+        rc = yg::launch_keyswitch(k, s);
+    }
+    cudaError_t e = cudaFreeAsync(big, s);
+    if (rc != 0) ck(cudaGetLastError(), "bootstrap launch");
+    ck(e, "cudaFreeAsync");
+    return YG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* yg_last_error(void) { return g_err.c_str(); }
+
+int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
+    if (!params || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        validate(*params);
+        DeviceGuard g(device);
+        auto c = std::make_unique<yg_ctx>();
+        c->p = *params;
+        c->device = device;
+        c->logN = params->N == 1024 ? 10 : 11;
+        c->q = params->torus_bits == 32 ? 562941363486721ULL : 1945555039024054273ULL;
+        c->qinv = std::make_unique<QInverse>(params->N, c->q);
+        ctx_init_tables(c.get());
+        *out = c.release();
+        return YG_OK;
+    });
+}
+
+void yg_ctx_destroy(yg_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->d_tw) cudaFree(ctx->d_tw);
+    delete ctx;
+}
+
+int yg_key_upload_bsk_ntt(yg_ctx* ctx, const uint64_t* h_bsk_ntt, yg_key** out) {
+    if (!ctx || !h_bsk_ntt || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            upload_bsk(ctx, k.get(), h_bsk_ntt);
+        } catch (...) {
+            if (k->d_bsk) cudaFree(k->d_bsk);
+            k->d_bsk = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_key_load_bsk_file(yg_ctx* ctx, const char* path, yg_key** out) {
+    if (!ctx || !path || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<u64> words = read_bsk_file(ctx->p, path);
+        return yg_key_upload_bsk_ntt(ctx, words.data(), out);
+    });
+}
+
+int yg_key_set_ksk(yg_key* key, const int32_t* h_ksk) {
+    if (!key || !h_ksk) return set_err(YG_ERR_INVALID, "null argument");
+    return guarded([&] {
+        const yg_params& p = key->ctx->p;
+        DeviceGuard g(key->ctx->device);
+        const size_t bytes = (size_t)p.k * p.N * p.ks_level * (p.n + 1) * sizeof(int32_t);
+        if (!key->d_ksk) {
+            ck(cudaMalloc(&key->d_ksk, bytes), "cudaMalloc ksk");
+            key->ksk_bytes = bytes;
+        }
+        ck(cudaMemcpy(key->d_ksk, h_ksk, bytes, cudaMemcpyHostToDevice), "upload ksk");
+        return YG_OK;
+    });
+}
+
+void yg_key_destroy(yg_key* key) {
+    if (!key) return;
+    if (key->d_bsk) cudaFree(key->d_bsk);
+    if (key->d_ksk) cudaFree(key->d_ksk);
+    delete key;
+}
+
+size_t yg_key_device_bytes(const yg_key* key) { return key ? key->bsk_bytes + key->ksk_bytes : 0; }
+
+int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
+           void* stream) {
+    if (int rc = check_key(ctx, key, true)) return rc;
+    if (count < 0 || (count > 0 && (!d_in || !d_out || !d_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        return do_pbs(ctx, key, d_in, d_out, count, d_lut, (cudaStream_t)stream);
+    });
+}
+
+int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_out, int count, const int64_t* h_lut,
+                void* stream) {
+    if (int rc = check_key(ctx, key, true)) return rc;
+    if (count < 0 || (count > 0 && (!h_in || !h_out || !h_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t lwe = (size_t)count * (ctx->p.n + 1) * sizeof(int32_t);
+        const size_t lut = (size_t)ctx->p.N * sizeof(int64_t);
+        char* d = nullptr;
+        ck(cudaMallocAsync(&d, 2 * lwe + lut, s), "cudaMallocAsync io");
+        int32_t* d_in = reinterpret_cast<int32_t*>(d);
+        int32_t* d_out = reinterpret_cast<int32_t*>(d + lwe);
+        int64_t* d_lut = reinterpret_cast<int64_t*>(d + 2 * lwe);
+        try {
+            ck(cudaMemcpyAsync(d_in, h_in, lwe, cudaMemcpyHostToDevice, s), "copy in");
+            ck(cudaMemcpyAsync(d_lut, h_lut, lut, cudaMemcpyHostToDevice, s), "copy lut");
+            do_pbs(ctx, key, d_in, d_out, count, d_lut, s);
+            ck(cudaMemcpyAsync(h_out, d_out, lwe, cudaMemcpyDeviceToHost, s), "copy out");
+        } catch (...) {
+            cudaFreeAsync(d, s);
+            throw;
+        }
+        ck(cudaFreeAsync(d, s), "cudaFreeAsync io");
+        ck(cudaStreamSynchronize(s), "bootstrap");
+        return YG_OK;
+    });
+}
+
+int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut, int64_t* d_acc,
+                    int count, int steps, void* stream) {
+    if (int rc = check_key(ctx, key, false)) return rc;
+    if (count < 0 || steps < 0 || steps > ctx->p.n) return set_err(YG_ERR_INVALID, "bad count or steps");
+    if (count == 0) return YG_OK;
+    if (!d_in || !d_lut || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::BrArgs a = br_args(ctx, key);
+        a.lwe_in = d_in;
+        a.lut = d_lut;
+        a.acc_out = d_acc;
+        a.count = count;
+        a.steps = steps;
+        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
+            ck(cudaGetLastError(), "blind rotate launch");
+        return YG_OK;
+    });
+}
+
+int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut,
+                            int32_t* d_big, int count, void* stream) {
+    if (int rc = check_key(ctx, key, false)) return rc;
+    if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
+    if (count == 0) return YG_OK;
+    if (!d_in || !d_lut || !d_big) return set_err(YG_ERR_INVALID, "bad buffers");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::BrArgs a = br_args(ctx, key);
+        a.lwe_in = d_in;
+        a.lut = d_lut;
+        a.big_out = d_big;
+        a.count = count;
+        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
+            ck(cudaGetLastError(), "blind rotate launch");
+        return YG_OK;
+    });
+}
+
+int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* d_out, int count, void* stream) {
+    if (int rc = check_key(ctx, key, true)) return rc;
+    if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
+    if (count == 0) return YG_OK;
+    if (!d_big || !d_out) return set_err(YG_ERR_INVALID, "bad buffers");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        const int kN = ctx->p.k * ctx->p.N;
+        yg::KsArgs k{d_big, key->d_ksk, d_out, count, kN, ctx->p.n, ctx->p.ks_level, ctx->p.ks_radix_bits};
+        if (yg::launch_keyswitch(k, stream) != 0) ck(cudaGetLastError(), "keyswitch launch");
+        return YG_OK;
+    });
+}
+
+}  // extern "C"

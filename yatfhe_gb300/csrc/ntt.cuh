@@ -1,0 +1,138 @@
+// ntt.cuh -- negacyclic NTT of one polynomial in one RNS channel by a "team" of N/32
+// threads (one warp at N = 1024, two at N = 2048), 32 residues per thread in registers.
+//
+// Forward transform = Cooley-Tukey with psi^brv(k) twiddles (output in bit-reversed
+// slots), inverse = Gentleman-Sande with psi^-brv(k) (bit-reversed in, natural out,
+// NOT scaled by N^-1: that factor is folded into the stored key).  For a stage on index
+// bit s the twiddle is tw[2^(logN-1-s) + (j >> (s+1))].
+//
+// Layouts (tt = thread index in the team, S = N/32 threads):
+//   natural : register r holds coefficient j = r*S + tt           (the 5 top index bits)
+//   slot    : N = 1024: register r holds slot j = tt*32 + r        (the 5 low index bits)
+//             N = 2048: register r holds slot j = (tt>>1)*64 + 2r + (tt&1); index bit 0 is
+//                       split across the lane pair (tt, tt^1) and done with shuffles.
+// Forward: natural -> 5 register stages -> transpose through shared memory -> slot -> 5
+// register stages (+ the shuffle stage at N = 2048).  Inverse mirrors it.  Pointwise
+// products happen in the slot layout, so the key is stored in that layout.
+#pragma once
+#include "rns.cuh"
+
+namespace yg {
+
+__device__ __forceinline__ int tpad(int j) { return j + (j >> 5); }
+
+template <int LOGN>
+struct TeamShape {
+    static constexpr int N = 1 << LOGN;
+    static constexpr int S = N / 32;
+    static constexpr int WARPS = S / 32;
+    static constexpr int TBUF = N + N / 32;  // words of one transpose buffer
+    static_assert(LOGN == 10 || LOGN == 11, "team NTT supports N = 1024 and 2048");
+};
+
+// Barrier over the warps of one channel team (ids 1..3 for teams 0..2; id 0 is __syncthreads).
+template <int LOGN>
+__device__ __forceinline__ void team_sync(int team) {
+    if constexpr (LOGN == 10) {
+        __syncwarp();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(64) : "memory");
+    }
+}
+
+template <int LOGN>
+__device__ __forceinline__ int slot_pos(int tt, int r) {
+    if constexpr (LOGN == 10) return tt * 32 + r;
+    else return (tt >> 1) * 64 + 2 * r + (tt & 1);
+}
+
+template <int LOGN>
+__device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, const Chan& ch) {
+    constexpr int S = TeamShape<LOGN>::S;
+    const uint32_t p = ch.p, two_p = ch.two_p;
+#pragma unroll
+    for (int sp = 4; sp >= 0; --sp) {
+        const int h = 1 << sp;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            if (r & h) continue;
+            ct_bfly(a[r], a[r + h], __ldg(&ch.twf[(1 << (4 - sp)) + (r >> (sp + 1))]), p, two_p);
+        }
+    }
+    team_sync<LOGN>(team);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) tb[tpad(r * S + tt)] = a[r];
+    team_sync<LOGN>(team);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) a[r] = tb[tpad(slot_pos<LOGN>(tt, r))];
+    const int gid = LOGN == 10 ? tt : (tt >> 1);
+#pragma unroll
+    for (int sp = 4; sp >= 0; --sp) {
+        const int h = 1 << sp;
+        const uint2* tw = ch.twf + (1 << (9 - sp)) + gid * (1 << (4 - sp));
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            if (r & h) continue;
+            ct_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p);
+        }
+    }
+    if constexpr (LOGN == 11) {
+        const bool odd = tt & 1;
+        const uint2* tw = ch.twf + 1024 + gid * 32;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            const uint2 w = __ldg(&tw[r]);
+            const uint32_t xr = reduce_once(a[r], two_p);     // U, held by the even lane
+            const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
+            const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
+            a[r] = odd ? other - t + two_p : xr + other;
+        }
+    }
+}
+
+template <int LOGN>
+__device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int tt, int team, const Chan& ch) {
+    constexpr int S = TeamShape<LOGN>::S;
+    const uint32_t p = ch.p, two_p = ch.two_p;
+    const int gid = LOGN == 10 ? tt : (tt >> 1);
+    if constexpr (LOGN == 11) {
+        const bool odd = tt & 1;
+        const uint2* tw = ch.twi + 1024 + gid * 32;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            const uint2 w = __ldg(&tw[r]);
+            const uint32_t mine = a[r];
+            const uint32_t other = __shfl_xor_sync(0xffffffffu, mine, 1);
+            const uint32_t s = mine + other;
+            const uint32_t d = other - mine + two_p;  // U - V for the odd lane
+            a[r] = odd ? mulshoup(d, w.x, w.y, p) : reduce_once(s, two_p);
+        }
+    }
+#pragma unroll
+    for (int sp = 0; sp <= 4; ++sp) {
+        const int h = 1 << sp;
+        const uint2* tw = ch.twi + (1 << (9 - sp)) + gid * (1 << (4 - sp));
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            if (r & h) continue;
+            gs_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p);
+        }
+    }
+    team_sync<LOGN>(team);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) tb[tpad(slot_pos<LOGN>(tt, r))] = a[r];
+    team_sync<LOGN>(team);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) a[r] = tb[tpad(r * S + tt)];
+#pragma unroll
+    for (int sp = 0; sp <= 4; ++sp) {
+        const int h = 1 << sp;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            if (r & h) continue;
+            gs_bfly(a[r], a[r + h], __ldg(&ch.twi[(1 << (4 - sp)) + (r >> (sp + 1))]), p, two_p);
+        }
+    }
+}
+
+}  // namespace yg

@@ -1,0 +1,109 @@
+// rns.cuh -- 32-bit residue arithmetic for the three-prime RNS the GPU bootstrap works in.
+//
+// The reference multiplies in the NTT domain modulo one 49-bit (TORUS32) or 61-bit
+// (TORUS56) prime q (yatfhe/include/yatfhe/torus.h:151,157, ntt_hexl.cpp:183-190).
+// What reaches the accumulator is only centred(INTT(sum NTT(d) . K) mod q) mod 2^T
+// (yatfhe/src/ntt_hexl.cpp:153-175), i.e. the exact integer X = sum_j d_j * k_j
+// (negacyclic, k_j = INTT(K_j) centred) reduced mod q.  |X| < 2^83 for every supported
+// parameter set, so the GPU computes X exactly in an RNS of three primes p_c < 2^30
+// (product ~2^90) on the 32-bit integer pipes and reduces it mod q once per coefficient.
+#pragma once
+#include <cstdint>
+
+namespace yg {
+
+constexpr int kChannels = 3;
+// Largest primes below 2^30 with p == 1 mod 2^13 (negacyclic NTTs up to N = 4096).
+constexpr uint32_t kPrimes[kChannels] = {1073692673u, 1073668097u, 1073651713u};
+
+// Per-channel constants the kernels read.
+struct Chan {
+    uint32_t p;
+    uint32_t two_p;
+    uint32_t pinv_neg;      // -p^-1 mod 2^32 (Montgomery)
+    uint32_t pad;
+    const uint2* twf;       // forward twiddles (w, floor(w 2^32 / p)), psi^brv(k), k in [0, N)
+    const uint2* twi;       // inverse twiddles, psi^-brv(k)
+};
+
+// Constants of the CRT recombination and of the reduction mod q (see crt_to_torus).
+struct Crt {
+    uint32_t p0, p1, p2;
+    uint32_t inv_p0_m1, inv_p0_m1_s;     // p0^-1 mod p1, Shoup companion
+    uint32_t p0_m2, p0_m2_s;             // p0 mod p2, Shoup companion
+    uint32_t inv_p01_m2, inv_p01_m2_s;   // (p0 p1)^-1 mod p2, Shoup companion
+    uint32_t half_p2;                    // (p2 - 1) / 2
+    uint64_t p01;                        // p0 p1
+    uint64_t q;                          // qNtt of the reference
+    uint64_t half_q;                     // (q - 1) / 2
+    float a2, a1, a0;                    // p0 p1 / q, p0 / q, 1 / q
+};
+
+#ifdef __CUDACC__
+// x * w mod p in [0, 2p) for any 32-bit x, with wp = floor(w 2^32 / p), w < p.
+__device__ __forceinline__ uint32_t mulshoup(uint32_t x, uint32_t w, uint32_t wp, uint32_t p) {
+    const uint32_t qh = __umulhi(x, wp);
+    return x * w - qh * p;
+}
+
+// a b 2^-32 mod p in [0, 2p) for a < 4p, b < p, p < 2^30.
+__device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv_neg) {
+    const uint32_t lo = a * b;
+    const uint32_t hi = __umulhi(a, b);
+    const uint32_t m = lo * pinv_neg;
+    return hi + __umulhi(m, p) + (lo != 0u);
+}
+
+__device__ __forceinline__ uint32_t reduce_once(uint32_t x, uint32_t m) { return min(x, x - m); }
+
+// Forward Cooley-Tukey butterfly with lazy reduction: x, y in [0, 4p) -> [0, 4p).
+__device__ __forceinline__ void ct_bfly(uint32_t& x, uint32_t& y, uint2 w, uint32_t p, uint32_t two_p) {
+    const uint32_t xr = reduce_once(x, two_p);
+    const uint32_t t = mulshoup(y, w.x, w.y, p);
+    x = xr + t;
+    y = xr - t + two_p;
+}
+
+// Inverse Gentleman-Sande butterfly: x, y in [0, 2p) -> [0, 2p).
+__device__ __forceinline__ void gs_bfly(uint32_t& x, uint32_t& y, uint2 w, uint32_t p, uint32_t two_p) {
+    const uint32_t s = x + y;
+    const uint32_t d = x - y + two_p;
+    x = reduce_once(s, two_p);
+    y = mulshoup(d, w.x, w.y, p);
+}
+
+// sign-extend the low `bits` bits of x (the reference's longModPow2, numeric.h:69-71).
+template <int BITS>
+__device__ __forceinline__ int64_t sext(int64_t x) {
+    return (int64_t)((uint64_t)x << (64 - BITS)) >> (64 - BITS);
+}
+
+// Residues x_c in [0, p_c) of the exact integer X with |X| < p0 p1 p2 / 2 -> the torus value
+// centred(X mod q) mod 2^T, i.e. what applyIntt (yatfhe/src/ntt_hexl.cpp:153-175) returns.
+// Garner's mixed radix gives X = v0 + v1 p0 + v2 p0 p1 exactly; the top digit is centred
+// (|X| << M/2 puts it within 2^24 of 0 or of p2); a single-precision estimate of X / q
+// picks the quotient to within +-2 and exact 64-bit arithmetic on X mod 2^64 settles it.
+template <int T>
+__device__ __forceinline__ int64_t crt_to_torus(uint32_t x0, uint32_t x1, uint32_t x2, const Crt& k) {
+    const uint32_t x0m1 = reduce_once(x0, k.p1);
+    uint32_t v1 = reduce_once(mulshoup(x1 + k.p1 - x0m1, k.inv_p0_m1, k.inv_p0_m1_s, k.p1), k.p1);
+    const uint32_t v0m2 = reduce_once(x0, k.p2);
+    uint32_t t = reduce_once(mulshoup(v1, k.p0_m2, k.p0_m2_s, k.p2), k.p2) + v0m2;
+    t = reduce_once(t, k.p2);
+    const uint32_t v2 = reduce_once(mulshoup(x2 + k.p2 - t, k.inv_p01_m2, k.inv_p01_m2_s, k.p2), k.p2);
+    const int32_t v2s = v2 > k.half_p2 ? (int32_t)(v2 - k.p2) : (int32_t)v2;
+    const float tf = __fmaf_rn((float)v2s, k.a2, __fmaf_rn((float)v1, k.a1, (float)x0 * k.a0));
+    const int64_t test = (int64_t)__float2ll_rn(tf);
+    const uint64_t xlo = (uint64_t)x0 + (uint64_t)v1 * k.p0 + (uint64_t)(int64_t)v2s * k.p01;
+    int64_t y = (int64_t)(xlo - (uint64_t)test * k.q);
+    const int64_t hq = (int64_t)k.half_q, q = (int64_t)k.q;
+#pragma unroll
+    for (int it = 0; it < 3; ++it) {
+        y = y > hq ? y - q : y;
+        y = y < -hq ? y + q : y;
+    }
+    return sext<T>(y);
+}
+#endif  // __CUDACC__
+
+}  // namespace yg

@@ -82,9 +82,12 @@ class _CParams(ctypes.Structure):
 T32_N1024 = PbsParams(n=630, N=1024, k=1, radix_bits=7, l=3, l_approx=3, ks_radix_bits=2, ks_level=8,
                       lwe_noise_b=18, rlwe_noise_b=8, torus_base=8, torus_bits=32)
 
-# TORUS=56 set: n=750, N=2048, B=2^10, l=4, KS 2^3 x 10, exponents 18 and 17 (sigma = 2^-40).
+# TORUS=56 set: n=750, N=2048, B=2^10, l=4, KS 2^3 x 10, RLWE exponent 17 (sigma = 2^-40).
+# The LWE/KSK exponent is 14 (sigma ~ 2^-19), not 18 (sigma = 2^-15): with 2^-15 the
+# 2048 x 10 key-switching terms alone leave a noise of about half a slot of a 4-bit padded
+# message, and the reference's own outputs misdecrypt about a quarter of them.
 T56_N2048 = PbsParams(n=750, N=2048, k=1, radix_bits=10, l=4, l_approx=4, ks_radix_bits=3, ks_level=10,
-                      lwe_noise_b=18, rlwe_noise_b=17, torus_base=32, torus_bits=56)
+                      lwe_noise_b=14, rlwe_noise_b=17, torus_base=32, torus_bits=56)
 
 # Reduced-n variants of the two sets (same ring, gadget and key-switching parameters, fewer
 # CMux steps); used where the oracle must finish in seconds.
