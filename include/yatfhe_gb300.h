@@ -92,6 +92,16 @@ int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_
 int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut, int64_t* d_acc,
                     int count, int steps, void* stream);
 
+/* blindRotateMP21Ntt with the reference's own signature semantics
+ * (yatfhe/include/yatfhe/blind_rotate.h:69): d_scaled is ScaledTlwe::a ([count][n], values
+ * mod 2N in [-N, N)), d_acc ([count][(k+1) N] int64, a then b) is rotated in place. */
+int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled, int64_t* d_acc, int count,
+                        void* stream);
+
+/* A key object holding only a key-switching key (attach it with yg_key_set_ksk), for
+ * switchKeyForTlwe callers that have no bootstrapping key. */
+int yg_key_create_ksk_only(yg_ctx* ctx, yg_key** out);
+
 /* The first half of functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:75-78):
  * rescale, noiseless sample, blindRotateMP21Ntt, extractTlweFromTrlwe(., ., 0).
  * d_big receives [count][k N + 1] int32 words; yg_keyswitch finishes the bootstrap. */

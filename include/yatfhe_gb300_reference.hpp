@@ -1,0 +1,240 @@
+// yatfhe_gb300_reference.hpp -- the reference library's own C++ bootstrap signatures,
+// implemented on the GB300 C ABI (yatfhe_gb300.h).
+//
+// For programs built against the yatfhe reference headers (yatfhe/include): include this
+// header after them and call yatfhe_gb300::functionalBootstrappingMPNtt & co. with the
+// reference's own types; a `using namespace yatfhe_gb300;` or a qualified call swaps the
+// CPU implementation for the GPU one without touching the surrounding code.  Keys are
+// converted and uploaded on first use and cached per key object (address); call
+// yatfhe_gb300::forgetKeys() after mutating or destroying a key.  Failures throw the
+// exception types the reference throws (std::invalid_argument for bad shapes, and
+// std::runtime_error otherwise).
+//
+// Replaced entry points (reference paths relative to its project):
+//   functionalBootstrappingMPNtt   yatfhe/include/yatfhe/bootstrapping.h:369-370
+//   blindRotateMP21Ntt             yatfhe/include/yatfhe/blind_rotate.h:69
+//   blindRotateJP22Ntt             yatfhe/include/yatfhe/blind_rotate.h:65 (binary keys)
+//   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
+// plus a batched form of the first, which the reference does not have.
+#ifndef YATFHE_GB300_REFERENCE_HPP
+#define YATFHE_GB300_REFERENCE_HPP
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "yatfhe_gb300.h"
+
+namespace yatfhe_gb300 {
+
+namespace detail {
+
+inline void check(int rc) {
+    if (rc == YG_OK) return;
+    const std::string msg = yg_last_error();
+    if (rc == YG_ERR_INVALID) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+}
+
+inline void cuda(cudaError_t e) {
+    if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+}
+
+struct Registry {
+    std::mutex mu;
+    std::map<std::tuple<int, int, int, int, int, int, int, int>, yg_ctx*> ctxs;
+    std::map<const void*, yg_key*> keys;  // BootstrappingKeyMP / bskDft address -> device key
+    std::map<const void*, const void*> ksk_of;
+
+    ~Registry() {
+        for (auto& k : keys) yg_key_destroy(k.second);
+        for (auto& c : ctxs) yg_ctx_destroy(c.second);
+    }
+};
+
+inline Registry& reg() {
+    static Registry r;
+    return r;
+}
+
+inline yg_params params_of(const YatfheParameters& p, int levels) {
+    return yg_params{p.n, p.N, p.k, p.radixBits, levels, p.ksRadixBits, p.ksLevel, p.torusBits};
+}
+
+inline yg_ctx* context(const yg_params& q) {
+    auto& r = reg();
+    auto key = std::make_tuple(q.n, q.N, q.k, q.radix_bits, q.l_approx, q.ks_radix_bits, q.ks_level, q.torus_bits);
+    auto it = r.ctxs.find(key);
+    if (it != r.ctxs.end()) return it->second;
+    yg_ctx* c = nullptr;
+    check(yg_ctx_create(&q, 0, &c));
+    r.ctxs[key] = c;
+    return c;
+}
+
+// BootstrappingKeyMP::bskDft -> [n][l][k+1][k+1][N] words.
+inline std::vector<uint64_t> flatten(const std::vector<std::vector<TrgswMPDft>>& bskDft, int k, int N) {
+    std::vector<uint64_t> w;
+    for (const auto& g : bskDft) {
+        const TrgswMPDft& t = g[0];
+        for (int lvl = 0; lvl < t.l; lvl++)
+            for (int row = 0; row <= k; row++) {
+                const TrlweDft& r = row < k ? t.c[lvl][row] : t.cPrime[lvl];
+                for (int poly = 0; poly <= k; poly++) {
+                    const auto& P = poly < k ? r.a[poly] : r.b;
+                    w.insert(w.end(), P.coeffs.begin(), P.coeffs.begin() + N);
+                }
+            }
+    }
+    return w;
+}
+
+inline yg_key* device_key(yg_ctx* c, const std::vector<std::vector<TrgswMPDft>>& bskDft, const TlweKeySwitchingKey* ksk,
+                          int k, int N) {
+    auto& r = reg();
+    auto it = r.keys.find(&bskDft);
+    yg_key* key = nullptr;
+    if (it == r.keys.end()) {
+        const auto w = flatten(bskDft, k, N);
+        check(yg_key_upload_bsk_ntt(c, w.data(), &key));
+        r.keys[&bskDft] = key;
+    } else {
+        key = it->second;
+    }
+    if (ksk && r.ksk_of[&bskDft] != ksk) {
+        std::vector<int32_t> flat;
+        for (const auto& row : ksk->decomposedKsk)
+            for (const auto& t : row) {
+                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
+                flat.push_back(static_cast<int32_t>(t.b));
+            }
+        check(yg_key_set_ksk(key, flat.data()));
+        r.ksk_of[&bskDft] = ksk;
+    }
+    return key;
+}
+
+template <typename T>
+struct DeviceBuf {
+    T* p = nullptr;
+    explicit DeviceBuf(size_t n) { cuda(cudaMalloc(&p, n * sizeof(T))); }
+    ~DeviceBuf() { cudaFree(p); }
+};
+
+}  // namespace detail
+
+inline void forgetKeys() {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    for (auto& k : r.keys) yg_key_destroy(k.second);
+    r.keys.clear();
+    r.ksk_of.clear();
+}
+
+// Batched functionalBootstrappingMPNtt: out[i] = PBS(in[i]) under one key, one launch.
+inline void functionalBootstrappingMPNttBatch(std::vector<Tlwe>& out, const std::vector<Tlwe>& in,
+                                              const BootstrappingKeyMP& bsk, const TlweKeySwitchingKey& ksk,
+                                              const TorusPolynomial& v, const YatfheParameters& param) {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    const int levels = bsk.bskDft.empty() ? param.lApprox : bsk.bskDft[0][0].l;
+    yg_ctx* c = detail::context(detail::params_of(param, levels));
+    yg_key* key = detail::device_key(c, bsk.bskDft, &ksk, param.k, param.N);
+    const int n = param.n, count = static_cast<int>(in.size());
+    std::vector<int32_t> h_in(static_cast<size_t>(count) * (n + 1)), h_out(h_in.size());
+    for (int i = 0; i < count; i++) {
+        for (int j = 0; j < n; j++) h_in[static_cast<size_t>(i) * (n + 1) + j] = static_cast<int32_t>(in[i].a[j]);
+        h_in[static_cast<size_t>(i) * (n + 1) + n] = static_cast<int32_t>(in[i].b);
+    }
+    std::vector<int64_t> lut(v.coeffs.begin(), v.coeffs.end());
+    detail::check(yg_pbs_host(c, key, h_in.data(), h_out.data(), count, lut.data(), nullptr));
+    out.resize(count, Tlwe(n));
+    for (int i = 0; i < count; i++) {
+        for (int j = 0; j < n; j++) out[i].a[j] = static_cast<LweTorus>(h_out[static_cast<size_t>(i) * (n + 1) + j]);
+        out[i].b = static_cast<LweTorus>(h_out[static_cast<size_t>(i) * (n + 1) + n]);
+    }
+}
+
+inline void functionalBootstrappingMPNtt(Tlwe& out, const Tlwe& input, const BootstrappingKeyMP& bsk,
+                                         const TlweKeySwitchingKey& ksk, const TorusPolynomial& v,
+                                         const YatfheParameters& param) {
+    std::vector<Tlwe> o, i{input};
+    functionalBootstrappingMPNttBatch(o, i, bsk, ksk, v, param);
+    out = o[0];
+}
+
+// blindRotateMP21Ntt: accum (already genNoiselessTrlweSample'd) is rotated in place.
+inline void blindRotateMP21Ntt(Trlwe& accum, const std::vector<std::vector<TrgswMPDft>>& bskDft,
+                               const ScaledTlwe& input, const YatfheParameters& param) {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    yg_ctx* c = detail::context(detail::params_of(param, bskDft[0][0].l));
+    yg_key* key = detail::device_key(c, bskDft, nullptr, param.k, param.N);
+    const int n = param.n, N = param.N, k = param.k;
+    std::vector<int32_t> a(input.a.begin(), input.a.end());
+    std::vector<int64_t> acc(static_cast<size_t>(k + 1) * N);
+    for (int p = 0; p < k; p++)
+        for (int j = 0; j < N; j++) acc[static_cast<size_t>(p) * N + j] = accum.a[p].coeffs[j];
+    for (int j = 0; j < N; j++) acc[static_cast<size_t>(k) * N + j] = accum.b.coeffs[j];
+    detail::DeviceBuf<int32_t> d_a(n);
+    detail::DeviceBuf<int64_t> d_acc(acc.size());
+    detail::cuda(cudaMemcpy(d_a.p, a.data(), a.size() * 4, cudaMemcpyHostToDevice));
+    detail::cuda(cudaMemcpy(d_acc.p, acc.data(), acc.size() * 8, cudaMemcpyHostToDevice));
+    detail::check(yg_blind_rotate_acc(c, key, d_a.p, d_acc.p, 1, nullptr));
+    detail::cuda(cudaMemcpy(acc.data(), d_acc.p, acc.size() * 8, cudaMemcpyDeviceToHost));
+    for (int p = 0; p < k; p++)
+        for (int j = 0; j < N; j++) accum.a[p].coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(p) * N + j]);
+    for (int j = 0; j < N; j++) accum.b.coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(k) * N + j]);
+}
+
+inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,
+                               const YatfheParameters& param) {
+    yatfhe_gb300::blindRotateMP21Ntt(accum, bsk.bskDft, input, param);
+}
+
+inline void switchKeyForTlwe(Tlwe& output, const TlweKeySwitchingKey& ksk, const Tlwe& input,
+                             const YatfheParameters& param) {
+    // the key-switching key alone: attach it to a context-level key slot keyed by its address
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    yg_ctx* c = detail::context(detail::params_of(param, param.lApprox));
+    auto it = r.keys.find(&ksk);
+    yg_key* key = nullptr;
+    if (it == r.keys.end()) {
+        detail::check(yg_key_create_ksk_only(c, &key));
+        r.keys[&ksk] = key;
+    } else {
+        key = it->second;
+    }
+    if (r.ksk_of[&ksk] != &ksk) {
+        std::vector<int32_t> flat;
+        for (const auto& row : ksk.decomposedKsk)
+            for (const auto& t : row) {
+                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
+                flat.push_back(static_cast<int32_t>(t.b));
+            }
+        detail::check(yg_key_set_ksk(key, flat.data()));
+        r.ksk_of[&ksk] = &ksk;
+    }
+    const int kN = param.k * param.N, n = param.n;
+    std::vector<int32_t> big(kN + 1), res(n + 1);
+    for (int j = 0; j < kN; j++) big[j] = static_cast<int32_t>(input.a[j]);
+    big[kN] = static_cast<int32_t>(input.b);
+    detail::DeviceBuf<int32_t> d_big(big.size()), d_out(res.size());
+    detail::cuda(cudaMemcpy(d_big.p, big.data(), big.size() * 4, cudaMemcpyHostToDevice));
+    detail::check(yg_keyswitch(c, key, d_big.p, d_out.p, 1, nullptr));
+    detail::cuda(cudaMemcpy(res.data(), d_out.p, res.size() * 4, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < n; j++) output.a[j] = static_cast<LweTorus>(res[j]);
+    output.b = static_cast<LweTorus>(res[n]);
+}
+
+}  // namespace yatfhe_gb300
+
+#endif  // YATFHE_GB300_REFERENCE_HPP

@@ -1,0 +1,45 @@
+"""The C++ adapter header (include/yatfhe_gb300_reference.hpp) compiles against the
+reference's own headers, i.e. a reference user can call the GPU path with the reference's
+types and signatures.  Compile-only here (no GPU); needs the reference tree."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from oracle import oracle as o
+
+ROOT = Path(__file__).resolve().parents[1]
+REF_INC = o.REF_TREE / "yatfhe" / "include"
+
+SRC = r"""
+#include "yatfhe/bootstrapping.h"
+#include "yatfhe/blind_rotate.h"
+#include "yatfhe/keyswitching.h"
+#include "yatfhe_gb300_reference.hpp"
+
+void use(Tlwe& out, const Tlwe& in, const BootstrappingKeyMP& bsk, const TlweKeySwitchingKey& ksk,
+         const TorusPolynomial& v, const YatfheParameters& p, Trlwe& acc, const ScaledTlwe& s,
+         std::vector<Tlwe>& outs, const std::vector<Tlwe>& ins) {
+    yatfhe_gb300::functionalBootstrappingMPNtt(out, in, bsk, ksk, v, p);
+    yatfhe_gb300::functionalBootstrappingMPNttBatch(outs, ins, bsk, ksk, v, p);
+    yatfhe_gb300::blindRotateMP21Ntt(acc, bsk.bskDft, s, p);
+    yatfhe_gb300::blindRotateJP22Ntt(acc, bsk, s, p);
+    yatfhe_gb300::switchKeyForTlwe(out, ksk, in, p);
+    yatfhe_gb300::forgetKeys();
+}
+"""
+
+
+@pytest.mark.skipif(not REF_INC.exists(), reason="reference headers not present")
+@pytest.mark.parametrize("torus", ["TORUS32", "TORUS56"])
+def test_adapter_compiles_against_reference_headers(tmp_path, torus):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    f = tmp_path / "use.cpp"
+    f.write_text(SRC)
+    cmd = [cxx, "-std=c++17", "-fsyntax-only", f"-D{torus}", f"-I{REF_INC}", f"-I{ROOT / 'oracle' / 'shim'}",
+           f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include", str(f)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

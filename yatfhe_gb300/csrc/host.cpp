@@ -395,10 +395,10 @@ struct DeviceGuard {
     }
 };
 
-int check_key(const yg_ctx* c, const yg_key* k, bool need_ksk) {
+int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk) {
     if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
     if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
-    if (!k->d_bsk) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
+    if (need_bsk && !k->d_bsk) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
     if (need_ksk && !k->d_ksk) return set_err(YG_ERR_STATE, "key has no key-switching key (yg_key_set_ksk)");
     return YG_OK;
 }
@@ -508,7 +508,7 @@ size_t yg_key_device_bytes(const yg_key* key) { return key ? key->bsk_bytes + ke
 
 int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
            void* stream) {
-    if (int rc = check_key(ctx, key, true)) return rc;
+    if (int rc = check_key(ctx, key, true, true)) return rc;
     if (count < 0 || (count > 0 && (!d_in || !d_out || !d_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
     if (count == 0) return YG_OK;
     return guarded([&] {
@@ -519,7 +519,7 @@ int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, 
 
 int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_out, int count, const int64_t* h_lut,
                 void* stream) {
-    if (int rc = check_key(ctx, key, true)) return rc;
+    if (int rc = check_key(ctx, key, true, true)) return rc;
     if (count < 0 || (count > 0 && (!h_in || !h_out || !h_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
     if (count == 0) return YG_OK;
     return guarded([&] {
@@ -549,7 +549,7 @@ int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_
 
 int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut, int64_t* d_acc,
                     int count, int steps, void* stream) {
-    if (int rc = check_key(ctx, key, false)) return rc;
+    if (int rc = check_key(ctx, key, true, false)) return rc;
     if (count < 0 || steps < 0 || steps > ctx->p.n) return set_err(YG_ERR_INVALID, "bad count or steps");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
@@ -569,7 +569,7 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
 
 int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut,
                             int32_t* d_big, int count, void* stream) {
-    if (int rc = check_key(ctx, key, false)) return rc;
+    if (int rc = check_key(ctx, key, true, false)) return rc;
     if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_big) return set_err(YG_ERR_INVALID, "bad buffers");
@@ -586,8 +586,35 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
     });
 }
 
+int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled, int64_t* d_acc, int count,
+                        void* stream) {
+    if (int rc = check_key(ctx, key, true, false)) return rc;
+    if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
+    if (count == 0) return YG_OK;
+    if (!d_scaled || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::BrArgs a = br_args(ctx, key);
+        a.scaled_in = d_scaled;
+        a.acc_in = d_acc;
+        a.acc_out = d_acc;
+        a.count = count;
+        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
+            ck(cudaGetLastError(), "blind rotate launch");
+        return YG_OK;
+    });
+}
+
+int yg_key_create_ksk_only(yg_ctx* ctx, yg_key** out) {
+    if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = new (std::nothrow) yg_key();
+    if (!*out) return set_err(YG_ERR_NOMEM, "host allocation failed");
+    (*out)->ctx = ctx;
+    return YG_OK;
+}
+
 int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* d_out, int count, void* stream) {
-    if (int rc = check_key(ctx, key, true)) return rc;
+    if (int rc = check_key(ctx, key, false, true)) return rc;
     if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
     if (count == 0) return YG_OK;
     if (!d_big || !d_out) return set_err(YG_ERR_INVALID, "bad buffers");

@@ -130,13 +130,21 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) blind_rotate_kernel(co
     const Chan ch = pick_chan(a.ch, team);
     const int L = a.L, n = a.n;
 
-    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81)
-    const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
-    for (int i = tid; i <= n; i += nth) sa[i] = (int16_t)modswitch_down(in[i], 31 - LOGN, LOGN + 1);
+    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81), unless given already scaled
+    if (a.scaled_in) {
+        const int32_t* in = a.scaled_in + (size_t)ct * n;
+        for (int i = tid; i < n; i += nth) sa[i] = (int16_t)in[i];
+    } else {
+        const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+        for (int i = tid; i <= n; i += nth) sa[i] = (int16_t)modswitch_down(in[i], 31 - LOGN, LOGN + 1);
+    }
     __syncthreads();
 
-    // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
-    {
+    if (a.acc_in) {
+        const int64_t* src = a.acc_in + (size_t)ct * 2 * N;
+        for (int idx = tid; idx < 2 * N; idx += nth) acc[idx] = (TorusT)src[idx];
+    } else {
+        // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
         int t2 = -(int)sa[n];
         t2 = ((t2 % (2 * N)) + 2 * N) % (2 * N);
         const bool wrap = t2 >= N;

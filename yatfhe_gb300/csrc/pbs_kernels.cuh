@@ -9,8 +9,10 @@ namespace yg {
 
 // Everything one launch of the blind-rotation kernel needs.
 struct BrArgs {
-    const int32_t* lwe_in;   // [count][n+1]
-    const int64_t* lut;      // [N] torus test polynomial
+    const int32_t* lwe_in;   // [count][n+1], or null when scaled_in is given
+    const int32_t* scaled_in;// [count][n] mask already switched to mod 2N (ScaledTlwe::a), or null
+    const int64_t* lut;      // [N] torus test polynomial, or null when acc_in is given
+    const int64_t* acc_in;   // [count][(k+1) N] starting accumulator, or null
     const uint4* key;        // device BSK, slot layout (see key_slot_words)
     int32_t* big_out;        // [count][k N + 1] extracted LWE, or null
     int64_t* acc_out;        // [count][(k+1) N] accumulator, or null
