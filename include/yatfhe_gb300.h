@@ -86,6 +86,19 @@ int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, 
 int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_out, int count,
                 const int64_t* h_lut, void* stream);
 
+/* No counterpart in the reference.  yg_pbs for callers that cannot let the library
+ * allocate device memory (their memory is owned by their own allocator or budget, or
+ * they reserve everything at start-up): the intermediate ciphertexts live in a fixed
+ * 16 MiB array compiled into the library, resident on every GPU that loads it until the
+ * process exits, instead of a per-call allocation.  At most yg_pbs_noalloc_max_count(ctx)
+ * ciphertexts per call (4092 at N = 1024, 2046 at N = 2048); more is rejected with
+ * YG_ERR_INVALID.  The first call on a device looks up the array's device address, so make
+ * it before any stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int yg_pbs_noalloc(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count,
+                   const int64_t* d_lut, void* stream);
+size_t yg_pbs_noalloc_max_count(const yg_ctx* ctx);
+
 /* rescaleTlweToNewMod + genNoiselessTrlweSample + the first `steps` iterations of
  * blindRotateMP21Ntt (yatfhe/src/blind_rotate.cpp:1538-1565; steps = n is the whole
  * rotation).  d_acc receives [count][(k+1) N] int64 torus words, a then b. */

@@ -44,6 +44,8 @@ _SIGNATURES = {
     "yg_blind_rotate_extract": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "yg_blind_rotate_acc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "yg_key_create_ksk_only": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "yg_pbs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+    "yg_pbs_noalloc_max_count": (ctypes.c_size_t, [_vp]),
     "yg_probe_int32_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
 }
 

@@ -24,27 +24,23 @@
 #include <vector>
 
 #include "../../include/yatfhe_gb300.h"
+#include "internal.hpp"
 #include "pbs_kernels.cuh"
+
+std::string& yg::last_error_slot() {
+    thread_local std::string msg;
+    return msg;
+}
 
 namespace {
 
 using u64 = uint64_t;
 using u128 = unsigned __int128;
-
-thread_local std::string g_err;
-
-int set_err(int code, const std::string& msg) {
-    g_err = msg;
-    return code;
-}
-
-struct CudaError : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-
-void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
-}
+using yg::ck;
+using yg::CudaError;
+using yg::DeviceGuard;
+using yg::guarded;
+using yg::set_err;
 
 u64 mulmod(u64 a, u64 b, u64 m) { return (u64)((u128)a * b % m); }
 u64 powmod(u64 b, u64 e, u64 m) {
@@ -81,6 +77,12 @@ u64 minimal_root(u64 N, u64 m) {
     }
     return best;
 }
+
+uint32_t shoup32(uint32_t w, uint32_t p) { return (uint32_t)(((u64)w << 32) / p); }
+
+}  // namespace
+
+namespace yg {
 
 // Inverse negacyclic transform mod q (Gentleman-Sande, psi^-brv(k) twiddles with Shoup
 // companions): bit-reversed NTT slots in, natural-order coefficients in [0, q) out.
@@ -129,45 +131,11 @@ struct QInverse {
     }
 };
 
-uint32_t shoup32(uint32_t w, uint32_t p) { return (uint32_t)(((u64)w << 32) / p); }
-
-}  // namespace
-
-struct yg_ctx {
-    yg_params p{};
-    int logN = 0;
-    int device = 0;
-    u64 q = 0;
-    uint2* d_tw = nullptr;  // [3][2][N]: forward then inverse twiddles per channel
-    yg::Chan ch[yg::kChannels]{};
-    yg::Crt crt{};
-    uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
-    std::unique_ptr<QInverse> qinv;
-};
-
-struct yg_key {
-    yg_ctx* ctx = nullptr;
-    uint32_t* d_bsk = nullptr;
-    int32_t* d_ksk = nullptr;
-    size_t bsk_bytes = 0, ksk_bytes = 0;
-};
+}  // namespace yg
 
 namespace {
 
-template <typename F>
-int guarded(F&& f) {
-    try {
-        return f();
-    } catch (const CudaError& e) {
-        return set_err(YG_ERR_CUDA, e.what());
-    } catch (const std::invalid_argument& e) {
-        return set_err(YG_ERR_INVALID, e.what());
-    } catch (const std::bad_alloc&) {
-        return set_err(YG_ERR_NOMEM, "host allocation failed");
-    } catch (const std::exception& e) {
-        return set_err(YG_ERR_IO, e.what());
-    }
-}
+using yg::QInverse;
 
 void validate(const yg_params& p) {
     if (p.torus_bits != 32 && p.torus_bits != 56) throw std::invalid_argument("torus_bits must be 32 or 56");
@@ -370,7 +338,9 @@ std::vector<u64> read_bsk_file(const yg_params& p, const char* path) {
     return words;
 }
 
-yg::BrArgs br_args(const yg_ctx* c, const yg_key* key) {
+}  // namespace
+
+yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     yg::BrArgs a{};
     a.key = reinterpret_cast<const uint4*>(key->d_bsk);
     a.n = c->p.n;
@@ -382,26 +352,18 @@ yg::BrArgs br_args(const yg_ctx* c, const yg_key* key) {
     return a;
 }
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) ck(cudaSetDevice(dev), "cudaSetDevice");
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
-int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk) {
+int yg::check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk) {
     if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
     if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
     if (need_bsk && !k->d_bsk) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
     if (need_ksk && !k->d_ksk) return set_err(YG_ERR_STATE, "key has no key-switching key (yg_key_set_ksk)");
     return YG_OK;
 }
+
+namespace {
+
+using yg::br_args;
+using yg::check_key;
 
 int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
            cudaStream_t s) {
@@ -428,7 +390,7 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
 
 extern "C" {
 
-const char* yg_last_error(void) { return g_err.c_str(); }
+const char* yg_last_error(void) { return yg::last_error_slot().c_str(); }
 
 int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
     if (!params || !out) return set_err(YG_ERR_INVALID, "null argument");
@@ -441,7 +403,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
         c->device = device;
         c->logN = params->N == 1024 ? 10 : 11;
         c->q = params->torus_bits == 32 ? 562941363486721ULL : 1945555039024054273ULL;
-        c->qinv = std::make_unique<QInverse>(params->N, c->q);
+        c->qinv = std::make_shared<QInverse>(params->N, c->q);
         ctx_init_tables(c.get());
         *out = c.release();
         return YG_OK;

@@ -1,0 +1,91 @@
+// internal.hpp -- definitions shared by the host-side translation units of the library
+// (context and key objects, error reporting, launch-argument assembly).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/yatfhe_gb300.h"
+#include "pbs_kernels.cuh"
+
+namespace yg {
+
+struct QInverse;
+
+// Message of the last failure on this thread (yg_last_error).
+std::string& last_error_slot();
+
+inline int set_err(int code, const std::string& msg) {
+    last_error_slot() = msg;
+    return code;
+}
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Runs f(), mapping exceptions to the ABI's status codes.
+template <typename F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const CudaError& e) {
+        return set_err(YG_ERR_CUDA, e.what());
+    } catch (const std::invalid_argument& e) {
+        return set_err(YG_ERR_INVALID, e.what());
+    } catch (const std::bad_alloc&) {
+        return set_err(YG_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return set_err(YG_ERR_IO, e.what());
+    }
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) ck(cudaSetDevice(dev), "cudaSetDevice");
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace yg
+
+struct yg_ctx {
+    yg_params p{};
+    int logN = 0;
+    int device = 0;
+    uint64_t q = 0;
+    uint2* d_tw = nullptr;  // [3][2][N]: forward then inverse twiddles per channel
+    yg::Chan ch[yg::kChannels]{};
+    yg::Crt crt{};
+    uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
+    std::shared_ptr<yg::QInverse> qinv;
+};
+
+struct yg_key {
+    yg_ctx* ctx = nullptr;
+    uint32_t* d_bsk = nullptr;
+    int32_t* d_ksk = nullptr;
+    size_t bsk_bytes = 0, ksk_bytes = 0;
+};
+
+namespace yg {
+
+int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk);
+
+// Blind-rotation launch arguments of a context and key (buffers and count left empty).
+BrArgs br_args(const yg_ctx* c, const yg_key* key);
+
+}  // namespace yg
