@@ -76,6 +76,31 @@ def test_blind_rotate_checkpoints_t32(t32_small):
         np.testing.assert_array_equal(want[-1], final)
 
 
+def test_blind_rotate_acc_reference_semantics(t32_small):
+    """yg_blind_rotate_acc = blindRotateMP21Ntt(accum, bsk, scaled, param): a caller-built
+    accumulator and already-switched mask, rotated in place."""
+    import ctypes
+
+    from yatfhe_gb300 import _lib
+
+    ora, ctx, key = t32_small
+    p = ctx.params
+    _, lwe = _sign_inputs(ora, 3, 8)
+    lut = ora.test_polynomial(1, 8)
+    scaled = np.stack([ora.modswitch(c) for c in lwe])
+    acc0 = np.zeros((3, 2 * p.N), np.int64)
+    for c in range(3):
+        acc0[c, p.N:] = ora.rotate(lut, -int(scaled[c, p.n]), False)
+    d_a = torch.from_numpy(np.ascontiguousarray(scaled[:, :p.n])).cuda()
+    d_acc = torch.from_numpy(acc0).cuda()
+    _lib.check(_lib.lib().yg_blind_rotate_acc(ctx.handle, key.handle, ctypes.c_void_p(d_a.data_ptr()),
+                                              ctypes.c_void_p(d_acc.data_ptr()), 3, ctypes.c_void_p(0)))
+    got = d_acc.cpu().numpy()
+    for c in range(3):
+        _, final = ora.blind_rotate_trace(lwe[c], lut, [])
+        np.testing.assert_array_equal(got[c], final)
+
+
 def test_keyswitch_alone_t32(t32_small):
     from yatfhe_gb300 import api
 
