@@ -50,6 +50,9 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-call / batch-size sweep legs")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
+    ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, help="with --per-cta: persistent CTAs per SM (0 = off)")
+    ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
     return ap.parse_args()
 
 
@@ -229,6 +232,13 @@ def main():
     sh = ctypes.c_void_p(stream.cuda_stream)
     d_in = torch.from_numpy(lwe).to(f"cuda:{dev}")
     d_lut = torch.from_numpy(lut).to(f"cuda:{dev}")
+    if args.per_cta:
+        api.set_launch(ctx, args.per_cta, args.ctas_per_sm)
+        tuning = {"choice": {"per_cta": args.per_cta, "ctas_per_sm": args.ctas_per_sm}, "fixed": True}
+    else:
+        from yatfhe_gb300 import autotune
+
+        tuning = autotune.tune(ctx, key, d_lut, use_cache=not args.retune)
     d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
     d_out = torch.empty_like(d_in)
     torch.cuda.synchronize()
@@ -380,6 +390,7 @@ def main():
                                    f"functionalBootstrappingMPNtt on {threads} threads ({cpu_s:.1f} s)"},
         "bit_exact_vs_oracle_sample": bit_exact,
         "key_upload_s": key_upload_s,
+        "launch_shape": tuning,
         "key_device_bytes": key.device_bytes,
     }
     line.update(extras)

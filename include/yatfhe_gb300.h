@@ -125,6 +125,97 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
  * (extractTlweFromTrlwe output), d_out is [count][n + 1]. */
 int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* d_out, int count, void* stream);
 
+/* Batches under many keys (no reference counterpart: the reference bootstraps one
+ * ciphertext per call).  A plan fixes, ahead of time, which key and which test
+ * polynomial each of `count` ciphertexts uses and owns the device tables and the
+ * intermediate buffer; yg_plan_run then only launches kernels (two), so it may be captured
+ * in a CUDA graph and replayed.  h_key_ids / h_lut_ids are host arrays of `count` indices
+ * into keys[] / d_luts[] (NULL: every ciphertext uses entry 0).  Ciphertexts that share a
+ * key should be contiguous: the key switch streams one KSK per run of them.  All keys must
+ * belong to `ctx` and carry a KSK. */
+typedef struct yg_plan yg_plan;
+int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const int32_t* h_key_ids,
+                   const int64_t* const* d_luts, int num_luts, const int32_t* h_lut_ids, int count, yg_plan** out);
+/* Launch shape for this plan: per_cta ciphertexts per blind-rotation CTA (1, 2 or 4;
+ * 0 = the context's setting) and grid CTAs (0 = enough for the batch; fewer = persistent
+ * CTAs that loop over it). */
+int yg_plan_set_launch(yg_plan* plan, int per_cta, int grid);
+int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream);
+void yg_plan_destroy(yg_plan* plan);
+/* Blind-rotation CTAs of per_cta ciphertexts each that fit on one SM (0: none fits). */
+int yg_ctas_per_sm(yg_ctx* ctx, int per_cta, int* out);
+/* Launch shape of every bootstrap on this context (the autotuner's choice): per_cta
+ * ciphertexts per CTA, run in lockstep; ctas_per_sm > 0 makes the grid persistent with that
+ * many CTAs per SM, 0 launches one CTA per group of per_cta ciphertexts.  Default (1, 0). */
+int yg_ctx_set_launch(yg_ctx* ctx, int per_cta, int ctas_per_sm);
+
+/* Serving: a request loop over many tenants with continuous batching and an HBM key cache.
+ * Replaces the reference's CPU serving harness (ya_benchmark/blindrotate_serving.cpp:111-354,
+ * ya_benchmark/include/blindrotate_serving.h:25-350) for the GINX method: the keys of
+ * registered tenants are kept in pinned host memory in the device layout; at most
+ * floor(key_budget_bytes / per-tenant key bytes) of them are resident in HBM at a time (an
+ * LRU over tenants with no batch in flight), refilled on a miss by an asynchronous copy on
+ * a side stream.  One worker thread admits pending requests into batches of up to
+ * max_batch ciphertexts while up to max_inflight earlier batches run; a batch bootstraps
+ * every request's ciphertexts with its tenant's key and LUT.  Request buffers should be
+ * pinned host memory (pageable buffers serialise the copies). */
+typedef struct yg_server yg_server;
+typedef struct yg_server_config {
+    size_t key_budget_bytes;
+    int max_batch;
+    int max_inflight;
+    int max_tenants;
+} yg_server_config;
+typedef struct yg_server_counters {
+    uint64_t key_hits, key_misses, refill_bytes, batches, requests_done, ciphertexts_done;
+    int key_slots;
+} yg_server_counters;
+typedef struct yg_request_times {
+    double t_submit, t_start, t_done; /* seconds on a monotonic clock */
+} yg_request_times;
+int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out);
+/* Snapshots `key` (BSK + KSK, device layout) into pinned host memory; the key object may be
+ * destroyed afterwards.  h_lut: the tenant's test polynomial ([N] int64). */
+int yg_server_add_tenant(yg_server* s, int tenant, const yg_key* key, const int64_t* h_lut);
+int yg_server_start(yg_server* s);
+/* Returns a request id (> 0) or a negative status. */
+int64_t yg_server_submit(yg_server* s, int tenant, const int32_t* h_in, int32_t* h_out, int count);
+int yg_server_wait(yg_server* s, int64_t request, int timeout_ms, yg_request_times* times);
+int yg_server_stats(yg_server* s, yg_server_counters* out);
+void yg_server_destroy(yg_server* s);
+
+/* A whole serving trace, generated and timed inside the library: `requests` arrivals of a
+ * Poisson process at `rate` requests/s (exponential gaps from mt19937_64(seed ^
+ * 0x9e3779b97f4a7c15), as blindrotate_serving.cpp:184), tenants 0..tenants-1 drawn from
+ * Zipf(zipf_s) (ZipfDistribution, yatfhe/include/yautil/zipf.h:47-87, seeded zipf_seed),
+ * sizes floor(exp(U(0, ln(max_count + 1)))) clamped to [1, max_count].  Request r of tenant t
+ * bootstraps rows [0, size) of h_pool[t] ([tenants][max_count][n+1] pinned); when h_expect
+ * (same shape) is given every output is compared with it.  The first `warmup` requests are
+ * served but not measured.  Latencies (ms) are ceil-rank percentiles. */
+typedef struct yg_trace_config {
+    int requests, warmup;
+    double rate;
+    uint64_t seed;
+    double zipf_s;
+    uint64_t zipf_seed;
+    int tenants;
+    int max_count;
+    int queue_max; /* requests waiting beyond this are shed (0 = no bound) */
+    const int32_t* h_pool;
+    const int32_t* h_expect;
+} yg_trace_config;
+typedef struct yg_latency {
+    double mean_ms, p50_ms, p90_ms, p99_ms, p999_ms, max_ms;
+} yg_latency;
+typedef struct yg_trace_result {
+    int served, shed, mismatched_requests;
+    double seconds, requests_per_s, ciphertexts_per_s, offered_rate;
+    yg_latency sojourn, queue, service;
+    uint64_t key_hits, key_misses, refill_bytes, batches;
+    double hit_rate;
+} yg_trace_result;
+int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_trace_result* out);
+
 /* Calibration, no reference counterpart: measured 32-bit multiply-add throughput of
  * `device` (operations per second), the denominator of the bootstrap's roofline. */
 int yg_probe_int32_rate(int device, double* ops_per_second);

@@ -1,0 +1,70 @@
+"""GPU: the serving loop.  Requests from several tenants arrive while others run (continuous
+batching) through an HBM key cache too small for all tenants (LRU refills from pinned host
+memory); every output must equal the same computation done alone, which in turn equals
+the oracle."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Restatement
+from yatfhe_gb300 import lut as lutmod
+from yatfhe_gb300.params import T32_N1024, small
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def served(built_lib):
+    from yatfhe_gb300 import api, serving
+
+    p = small(T32_N1024, 24)
+    ctx = api.Context(p, 0)
+    tenants, max_count = 6, 16
+    oras, keys = [], []
+    for t in range(tenants):
+        o = Restatement(p)
+        o.keygen(1000 + t)
+        oras.append(o)
+        keys.append(api.BootstrapKey.from_ntt_words(ctx, o.bsk_ntt()).set_ksk(o.ksk()))
+    per_key = keys[0].device_bytes
+    srv = serving.Server(ctx, key_budget_bytes=2.5 * per_key, max_batch=64, max_inflight=2)
+    luts = [lutmod.sign_lut(p.N, 32), lutmod.box_lut(p.N, 32, np.arange(8) << 28)]
+    pool = torch.empty((tenants, max_count, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    rng = np.random.default_rng(3)
+    for t in range(tenants):
+        lut = luts[t % 2]
+        srv.add_tenant(t, keys[t], lut)
+        lwe = oras[t].encrypt(rng.integers(-(1 << 31), 1 << 31, max_count))
+        pool[t] = torch.from_numpy(lwe)
+        # the same computation alone: one call, this tenant's key and LUT only
+        alone = api.functional_bootstrapping_mp_ntt(ctx, keys[t], torch.from_numpy(lwe).cuda(),
+                                                    torch.from_numpy(lut).cuda()).cpu()
+        expect[t] = alone
+        if t < 2:
+            np.testing.assert_array_equal(alone.numpy()[:4], oras[t].pbs(lwe[:4], lut))
+    srv.start()
+    yield ctx, srv, pool, expect
+    srv.close()
+
+
+def test_requests_alone_and_in_the_mix(served):
+    ctx, srv, pool, expect = served
+    outs = [torch.zeros((16, ctx.params.n + 1), dtype=torch.int32).pin_memory() for _ in range(12)]
+    ids = [srv.submit(i % 6, pool[i % 6], outs[i], count=1 + (i * 5) % 16) for i in range(12)]
+    for i, rid in enumerate(ids):
+        t = srv.wait(rid)
+        assert t["t_submit"] <= t["t_start"] <= t["t_done"]
+        c = 1 + (i * 5) % 16
+        assert torch.equal(outs[i][:c], expect[i % 6][:c]), f"request {i}"
+
+
+def test_trace_with_evictions_is_bit_exact(served):
+    ctx, srv, pool, expect = served
+    res = srv.run_trace(pool, expect, requests=300, warmup=20, rate=2000.0, zipf_s=1.1, max_count=16, seed=7)
+    assert res["served"] == 300
+    assert res["mismatched_requests"] == 0
+    assert res["key_misses"] > 0 and 0 < res["hit_rate"] < 1  # 2 of 6 tenants fit: refills happened
+    assert res["sojourn"]["p50_ms"] > 0 and res["sojourn"]["p99_ms"] >= res["sojourn"]["p50_ms"]
+    c = srv.counters()
+    assert c["key_slots"] == 2

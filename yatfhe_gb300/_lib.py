@@ -27,6 +27,40 @@ class YgParams(ctypes.Structure):
         return cls(p.n, p.N, p.k, p.radix_bits, p.l_approx, p.ks_radix_bits, p.ks_level, p.torus_bits)
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("key_budget_bytes", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
+                ("max_tenants", ctypes.c_int)]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("key_hits", "key_misses", "refill_bytes", "batches", "requests_done",
+                                               "ciphertexts_done")] + [("key_slots", ctypes.c_int)]
+
+
+class RequestTimes(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_double) for f in ("t_submit", "t_start", "t_done")]
+
+
+class TraceConfig(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_int), ("warmup", ctypes.c_int), ("rate", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("zipf_s", ctypes.c_double), ("zipf_seed", ctypes.c_uint64),
+                ("tenants", ctypes.c_int), ("max_count", ctypes.c_int), ("queue_max", ctypes.c_int),
+                ("h_pool", ctypes.c_void_p), ("h_expect", ctypes.c_void_p)]
+
+
+class Latency(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_double) for f in ("mean_ms", "p50_ms", "p90_ms", "p99_ms", "p999_ms", "max_ms")]
+
+
+class TraceResult(ctypes.Structure):
+    _fields_ = [("served", ctypes.c_int), ("shed", ctypes.c_int), ("mismatched_requests", ctypes.c_int),
+                ("seconds", ctypes.c_double), ("requests_per_s", ctypes.c_double),
+                ("ciphertexts_per_s", ctypes.c_double), ("offered_rate", ctypes.c_double),
+                ("sojourn", Latency), ("queue", Latency), ("service", Latency),
+                ("key_hits", ctypes.c_uint64), ("key_misses", ctypes.c_uint64), ("refill_bytes", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("hit_rate", ctypes.c_double)]
+
+
 _vp = ctypes.c_void_p
 _SIGNATURES = {
     "yg_last_error": (ctypes.c_char_p, []),
@@ -46,6 +80,21 @@ _SIGNATURES = {
     "yg_key_create_ksk_only": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "yg_pbs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
     "yg_pbs_noalloc_max_count": (ctypes.c_size_t, [_vp]),
+    "yg_plan_create": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int,
+                                      ctypes.POINTER(_vp)]),
+    "yg_plan_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "yg_plan_run": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "yg_plan_destroy": (None, [_vp]),
+    "yg_ctas_per_sm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "yg_ctx_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "yg_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "yg_server_add_tenant": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
+    "yg_server_start": (ctypes.c_int, [_vp]),
+    "yg_server_submit": (ctypes.c_int64, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int]),
+    "yg_server_wait": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(RequestTimes)]),
+    "yg_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerCounters)]),
+    "yg_server_destroy": (None, [_vp]),
+    "yg_server_run_trace": (ctypes.c_int, [_vp, ctypes.POINTER(TraceConfig), ctypes.POINTER(TraceResult)]),
     "yg_probe_int32_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
 }
 

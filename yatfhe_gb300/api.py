@@ -117,6 +117,61 @@ class BootstrapKey:
             pass
 
 
+class BatchPlan:
+    """A batch of `count` ciphertexts under several keys / LUTs (yg_plan_*): key_ids[c] and
+    lut_ids[c] pick the key and LUT of ciphertext c.  run() only launches kernels, so it can be
+    captured in a CUDA graph."""
+
+    def __init__(self, ctx: Context, keys, luts, count: int, key_ids=None, lut_ids=None, grid: int = 0,
+                 per_cta: int = 0):
+        self.ctx, self.keys, self.luts, self.count = ctx, list(keys), list(luts), count
+        kt = (ctypes.c_void_p * len(self.keys))(*[k.handle.value for k in self.keys])
+        lt = (ctypes.c_void_p * len(self.luts))(*[ctypes.c_void_p(t.data_ptr()).value for t in self.luts])
+        kid = None if key_ids is None else np.ascontiguousarray(key_ids, np.int32)
+        lid = None if lut_ids is None else np.ascontiguousarray(lut_ids, np.int32)
+        for ids in (kid, lid):
+            if ids is not None and len(ids) != count:
+                raise ValueError("index arrays must have one entry per ciphertext")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_plan_create(
+            ctx.handle, ctypes.cast(kt, ctypes.c_void_p), len(self.keys),
+            None if kid is None else ctypes.c_void_p(kid.ctypes.data),
+            ctypes.cast(lt, ctypes.c_void_p), len(self.luts),
+            None if lid is None else ctypes.c_void_p(lid.ctypes.data), count, ctypes.byref(h)))
+        self._h = h
+        if grid or per_cta:
+            self.set_launch(per_cta or 1, grid)
+
+    def set_launch(self, per_cta: int, grid: int = 0):
+        _lib.check(_lib.lib().yg_plan_set_launch(self._h, int(per_cta), int(grid)))
+
+    def run(self, lwe_in, out, stream=None):
+        _lib.check(_lib.lib().yg_plan_run(self._h, _dptr(lwe_in, "int32", "lwe_in"), _dptr(out, "int32", "out"),
+                                          _stream_handle(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().yg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ctas_per_sm(ctx: Context, per_cta: int = 1) -> int:
+    v = ctypes.c_int()
+    _lib.check(_lib.lib().yg_ctas_per_sm(ctx.handle, int(per_cta), ctypes.byref(v)))
+    return v.value
+
+
+def set_launch(ctx: Context, per_cta: int, ctas_per_sm: int = 0) -> None:
+    _lib.check(_lib.lib().yg_ctx_set_launch(ctx.handle, int(per_cta), int(ctas_per_sm)))
+
+
 def functional_bootstrapping_mp_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, out=None, stream=None):
     """Bootstraps every row of ``lwe_in`` ([count, n+1] int32 CUDA tensor) through ``lut``."""
     torch = _torch()

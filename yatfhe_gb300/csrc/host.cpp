@@ -175,6 +175,11 @@ void ctx_init_tables(yg_ctx* c) {
     }
     ck(cudaMalloc(&c->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
     ck(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
+    std::vector<uint2> heads((size_t)yg::kChannels * 2 * 32);
+    for (int ci = 0; ci < yg::kChannels; ci++)
+        for (int dir = 0; dir < 2; dir++)
+            for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + dir) * 32 + k] = tw[((size_t)ci * 2 + dir) * N + k];
+    if (yg::set_twiddle_heads(c->logN, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimes[ci];
         uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
@@ -260,7 +265,7 @@ void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
             a.scale[ci] = c->conv_scale[ci];
             a.scale_s[ci] = c->conv_scale_s[ci];
         }
-        if (yg::launch_keyconv(c->logN, a, nullptr) != 0) ck(cudaGetLastError(), "keyconv launch");
+        yg::check_launch(yg::launch_keyconv(c->logN, a, nullptr), "keyconv launch");
         ck(cudaDeviceSynchronize(), "keyconv");
     } catch (...) {
         cudaFree(d_res);
@@ -342,13 +347,15 @@ std::vector<u64> read_bsk_file(const yg_params& p, const char* path) {
 
 yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     yg::BrArgs a{};
-    a.key = reinterpret_cast<const uint4*>(key->d_bsk);
+    a.key = key ? reinterpret_cast<const uint4*>(key->d_bsk) : nullptr;
     a.n = c->p.n;
     a.steps = c->p.n;
     a.L = c->p.l_approx;
     a.radix_bits = c->p.radix_bits;
     for (int ci = 0; ci < yg::kChannels; ci++) a.ch[ci] = c->ch[ci];
     a.crt = c->crt;
+    a.per_cta = c->per_cta;
+    a.grid = c->ctas_per_sm > 0 ? c->ctas_per_sm * c->sm_count : 0;
     return a;
 }
 
@@ -381,7 +388,7 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
         rc = yg::launch_keyswitch(k, s);
     }
     cudaError_t e = cudaFreeAsync(big, s);
-    if (rc != 0) ck(cudaGetLastError(), "bootstrap launch");
+    yg::check_launch(rc, "bootstrap launch");
     ck(e, "cudaFreeAsync");
     return YG_OK;
 }
@@ -404,6 +411,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
         c->logN = params->N == 1024 ? 10 : 11;
         c->q = params->torus_bits == 32 ? 562941363486721ULL : 1945555039024054273ULL;
         c->qinv = std::make_shared<QInverse>(params->N, c->q);
+        ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         ctx_init_tables(c.get());
         *out = c.release();
         return YG_OK;
@@ -523,8 +531,7 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
         a.acc_out = d_acc;
         a.count = count;
         a.steps = steps;
-        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
-            ck(cudaGetLastError(), "blind rotate launch");
+        yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
     });
 }
@@ -542,8 +549,7 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
         a.lut = d_lut;
         a.big_out = d_big;
         a.count = count;
-        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
-            ck(cudaGetLastError(), "blind rotate launch");
+        yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
     });
 }
@@ -561,8 +567,7 @@ int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled,
         a.acc_in = d_acc;
         a.acc_out = d_acc;
         a.count = count;
-        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
-            ck(cudaGetLastError(), "blind rotate launch");
+        yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
     });
 }
@@ -584,9 +589,179 @@ int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* 
         DeviceGuard g(ctx->device);
         const int kN = ctx->p.k * ctx->p.N;
         yg::KsArgs k{d_big, key->d_ksk, d_out, count, kN, ctx->p.n, ctx->p.ks_level, ctx->p.ks_radix_bits};
-        if (yg::launch_keyswitch(k, stream) != 0) ck(cudaGetLastError(), "keyswitch launch");
+        yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");
         return YG_OK;
     });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------- plans
+
+struct yg_plan {
+    yg_ctx* ctx = nullptr;
+    int count = 0;
+    int grid = 0;
+    int per_cta = 0;
+    const yg_key* key0 = nullptr;     // uniform batch: the one key
+    const int64_t* lut0 = nullptr;    // uniform LUT
+    const uint4** d_key_table = nullptr;
+    int32_t* d_key_of = nullptr;
+    const int64_t** d_lut_table = nullptr;
+    int32_t* d_lut_of = nullptr;
+    yg::KsTile* d_tiles = nullptr;
+    int num_tiles = 0;
+    int32_t* d_big = nullptr;
+};
+
+namespace {
+
+void plan_free(yg_plan* p) {
+    cudaFree(p->d_key_table);
+    cudaFree(p->d_key_of);
+    cudaFree(p->d_lut_table);
+    cudaFree(p->d_lut_of);
+    cudaFree(p->d_tiles);
+    cudaFree(p->d_big);
+}
+
+template <typename T>
+T* upload_vec(const std::vector<T>& v, const char* what) {
+    T* d = nullptr;
+    ck(cudaMalloc(&d, std::max<size_t>(1, v.size()) * sizeof(T)), what);
+    if (!v.empty()) ck(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), what);
+    return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const int32_t* h_key_ids,
+                   const int64_t* const* d_luts, int num_luts, const int32_t* h_lut_ids, int count, yg_plan** out) {
+    if (!ctx || !keys || num_keys < 1 || !d_luts || num_luts < 1 || count < 0 || !out)
+        return set_err(YG_ERR_INVALID, "yg_plan_create: bad arguments");
+    *out = nullptr;
+    for (int i = 0; i < num_keys; i++)
+        if (int rc = check_key(ctx, keys[i], true, true)) return rc;
+    for (int i = 0; i < num_luts; i++)
+        if (!d_luts[i]) return set_err(YG_ERR_INVALID, "yg_plan_create: null LUT");
+    for (int c = 0; c < count; c++) {
+        if (h_key_ids && (h_key_ids[c] < 0 || h_key_ids[c] >= num_keys))
+            return set_err(YG_ERR_INVALID, "yg_plan_create: key index out of range");
+        if (h_lut_ids && (h_lut_ids[c] < 0 || h_lut_ids[c] >= num_luts))
+            return set_err(YG_ERR_INVALID, "yg_plan_create: LUT index out of range");
+    }
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto p = std::make_unique<yg_plan>();
+        p->ctx = ctx;
+        p->count = count;
+        p->key0 = keys[0];
+        p->lut0 = d_luts[0];
+        try {
+            const bool multi_key = h_key_ids && num_keys > 1;
+            if (multi_key) {
+                std::vector<const uint4*> table(num_keys);
+                for (int i = 0; i < num_keys; i++) table[i] = reinterpret_cast<const uint4*>(keys[i]->d_bsk);
+                p->d_key_table = upload_vec(table, "plan key table");
+                p->d_key_of = upload_vec(std::vector<int32_t>(h_key_ids, h_key_ids + count), "plan key index");
+                std::vector<yg::KsTile> tiles;
+                for (int c = 0; c < count;) {
+                    int e = c + 1;
+                    while (e < count && e - c < yg::kKsTileCts && h_key_ids[e] == h_key_ids[c]) e++;
+                    tiles.push_back(yg::KsTile{c, e - c, keys[h_key_ids[c]]->d_ksk});
+                    c = e;
+                }
+                p->num_tiles = (int)tiles.size();
+                p->d_tiles = upload_vec(tiles, "plan key-switch tiles");
+            }
+            if (h_lut_ids && num_luts > 1) {
+                p->d_lut_table = upload_vec(std::vector<const int64_t*>(d_luts, d_luts + num_luts), "plan LUT table");
+                p->d_lut_of = upload_vec(std::vector<int32_t>(h_lut_ids, h_lut_ids + count), "plan LUT index");
+            }
+            const size_t big = (size_t)std::max(count, 1) * (ctx->p.k * ctx->p.N + 1) * sizeof(int32_t);
+            ck(cudaMalloc(&p->d_big, big), "plan extract buffer");
+        } catch (...) {
+            plan_free(p.get());
+            throw;
+        }
+        *out = p.release();
+        return YG_OK;
+    });
+}
+
+int yg_plan_set_launch(yg_plan* plan, int per_cta, int grid) {
+    if (!plan || per_cta < 0 || grid < 0) return set_err(YG_ERR_INVALID, "yg_plan_set_launch: bad arguments");
+    if (per_cta > 0) {
+        int fit = 0;
+        if (int rc = yg_ctas_per_sm(plan->ctx, per_cta, &fit)) return rc;
+        if (fit < 1) return set_err(YG_ERR_INVALID, "yg_plan_set_launch: a CTA of that size does not fit an SM");
+    }
+    plan->per_cta = per_cta;
+    plan->grid = grid;
+    return YG_OK;
+}
+
+int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream) {
+    if (!plan) return set_err(YG_ERR_INVALID, "null plan");
+    if (plan->count == 0) return YG_OK;
+    if (!d_in || !d_out) return set_err(YG_ERR_INVALID, "bad buffers");
+    yg_ctx* ctx = plan->ctx;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::BrArgs a = br_args(ctx, plan->key0);
+        a.lwe_in = d_in;
+        a.lut = plan->lut0;
+        a.key_table = plan->d_key_table;
+        a.key_of = plan->d_key_of;
+        a.lut_table = plan->d_lut_table;
+        a.lut_of = plan->d_lut_of;
+        a.big_out = plan->d_big;
+        a.count = plan->count;
+        if (plan->per_cta > 0) {
+            a.per_cta = plan->per_cta;
+            a.grid = plan->grid;
+        }
+        yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
+        const int kN = ctx->p.k * ctx->p.N;
+        yg::KsArgs k{plan->d_big, plan->key0->d_ksk, d_out, plan->count, kN, ctx->p.n, ctx->p.ks_level,
+                     ctx->p.ks_radix_bits, plan->d_tiles, plan->num_tiles};
+        yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");
+        return YG_OK;
+    });
+}
+
+void yg_plan_destroy(yg_plan* plan) {
+    if (!plan) return;
+    DeviceGuard g(plan->ctx->device);
+    plan_free(plan);
+    delete plan;
+}
+
+int yg_ctas_per_sm(yg_ctx* ctx, int per_cta, int* out) {
+    if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        const int b = yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, per_cta);
+        if (b == yg::kNoVariant) {
+            *out = 0;  // no kernel of that shape for these parameters: nothing fits
+            return YG_OK;
+        }
+        if (b < 0) ck(cudaGetLastError(), "occupancy query");
+        *out = b;
+        return YG_OK;
+    });
+}
+
+int yg_ctx_set_launch(yg_ctx* ctx, int per_cta, int ctas_per_sm) {
+    if (!ctx || per_cta < 1 || ctas_per_sm < 0) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: bad arguments");
+    int fit = 0;
+    if (int rc = yg_ctas_per_sm(ctx, per_cta, &fit)) return rc;
+    if (fit < 1) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: a CTA of that size does not fit an SM");
+    ctx->per_cta = per_cta;
+    ctx->ctas_per_sm = ctas_per_sm;
+    return YG_OK;
 }
 
 }  // extern "C"

@@ -47,6 +47,15 @@ int guarded(F&& f) {
     }
 }
 
+// A kernel launcher's status: a CUDA error if one was raised, else an unsupported launch
+// shape (e.g. more shared memory than an SM has); never silently nothing launched.
+inline void check_launch(int rc, const char* what) {
+    if (rc == 0) return;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+    throw std::invalid_argument(std::string(what) + ": launch shape not supported for these parameters");
+}
+
 struct DeviceGuard {
     int prev = -1;
     explicit DeviceGuard(int dev) {
@@ -72,6 +81,9 @@ struct yg_ctx {
     yg::Crt crt{};
     uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
     std::shared_ptr<yg::QInverse> qinv;
+    int sm_count = 0;
+    int per_cta = 1;       // ciphertexts per blind-rotation CTA (yg_ctx_set_launch)
+    int ctas_per_sm = 0;   // persistent CTAs per SM, 0 = one CTA per ciphertext group
 };
 
 struct yg_key {

@@ -75,10 +75,9 @@ extern "C" int yg_pbs_noalloc(yg_ctx* ctx, const yg_key* key, const int32_t* d_i
         a.lut = d_lut;
         a.big_out = big;
         a.count = count;
-        if (yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream) != 0)
-            yg::ck(cudaGetLastError(), "blind rotate launch");
+        yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         yg::KsArgs k{big, key->d_ksk, d_out, count, kN, ctx->p.n, ctx->p.ks_level, ctx->p.ks_radix_bits};
-        if (yg::launch_keyswitch(k, stream) != 0) yg::ck(cudaGetLastError(), "keyswitch launch");
+        yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");
         return YG_OK;
     });
 }

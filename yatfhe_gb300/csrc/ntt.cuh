@@ -21,6 +21,10 @@ namespace yg {
 
 __device__ __forceinline__ int tpad(int j) { return j + (j >> 5); }
 
+// The first 32 twiddles of each table: every thread of a team uses the same ones in the
+// natural-layout stages, so they come from the constant cache.  [logN-10][channel][fwd, inv][k]
+__constant__ uint2 c_tw_head[2][kChannels][2][32];
+
 template <int LOGN>
 struct TeamShape {
     static constexpr int N = 1 << LOGN;
@@ -30,13 +34,15 @@ struct TeamShape {
     static_assert(LOGN == 10 || LOGN == 11, "team NTT supports N = 1024 and 2048");
 };
 
-// Barrier over the warps of one channel team (ids 1..3 for teams 0..2; id 0 is __syncthreads).
+// Barrier over the warps of one channel team: a warp barrier at N = 1024, named barrier
+// 1 + bar (64 threads) at N = 2048; `bar` is unique per team in the CTA, and id 0 is left to
+// __syncthreads.
 template <int LOGN>
-__device__ __forceinline__ void team_sync(int team) {
+__device__ __forceinline__ void team_sync(int bar) {
     if constexpr (LOGN == 10) {
         __syncwarp();
     } else {
-        asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(64) : "memory");
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + bar), "r"(64) : "memory");
     }
 }
 
@@ -47,22 +53,26 @@ __device__ __forceinline__ int slot_pos(int tt, int r) {
 }
 
 template <int LOGN>
-__device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, const Chan& ch) {
+__device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
+    // Input residues < 2p.  Bounds after each stage (p < 2^29, so 8p < 2^32): natural-layout
+    // stages 4p, 6p, 8p, reduce -> 6p, 8p; slot-layout stages reduce -> 6p, 8p, reduce -> 6p,
+    // 8p, reduce -> 6p (then the N = 2048 shuffle stage, reduce -> 6p).  Output < 8p.
 #pragma unroll
     for (int sp = 4; sp >= 0; --sp) {
         const int h = 1 << sp;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], __ldg(&ch.twf[(1 << (4 - sp)) + (r >> (sp + 1))]), p, two_p);
+            ct_bfly(a[r], a[r + h], c_tw_head[LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p,
+                    sp == 1);
         }
     }
-    team_sync<LOGN>(team);
+    team_sync<LOGN>(bar);
 #pragma unroll
     for (int r = 0; r < 32; ++r) tb[tpad(r * S + tt)] = a[r];
-    team_sync<LOGN>(team);
+    team_sync<LOGN>(bar);
 #pragma unroll
     for (int r = 0; r < 32; ++r) a[r] = tb[tpad(slot_pos<LOGN>(tt, r))];
     const int gid = LOGN == 10 ? tt : (tt >> 1);
@@ -73,7 +83,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p);
+            ct_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p, (sp & 1) == 0);
         }
     }
     if constexpr (LOGN == 11) {
@@ -82,7 +92,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             const uint2 w = __ldg(&tw[r]);
-            const uint32_t xr = reduce_once(a[r], two_p);     // U, held by the even lane
+            const uint32_t xr = reduce_once(a[r], 2 * two_p);  // U (< 4p), held by the even lane
             const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
             const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
             a[r] = odd ? other - t + two_p : xr + other;
@@ -91,7 +101,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 }
 
 template <int LOGN>
-__device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int tt, int team, const Chan& ch) {
+__device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
     const int gid = LOGN == 10 ? tt : (tt >> 1);
@@ -118,10 +128,10 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
             gs_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p);
         }
     }
-    team_sync<LOGN>(team);
+    team_sync<LOGN>(bar);
 #pragma unroll
     for (int r = 0; r < 32; ++r) tb[tpad(slot_pos<LOGN>(tt, r))] = a[r];
-    team_sync<LOGN>(team);
+    team_sync<LOGN>(bar);
 #pragma unroll
     for (int r = 0; r < 32; ++r) a[r] = tb[tpad(r * S + tt)];
 #pragma unroll
@@ -130,7 +140,7 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            gs_bfly(a[r], a[r + h], __ldg(&ch.twi[(1 << (4 - sp)) + (r >> (sp + 1))]), p, two_p);
+            gs_bfly(a[r], a[r + h], c_tw_head[LOGN - 10][team][1][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p);
         }
     }
 }

@@ -10,6 +10,7 @@
 //                        ciphertexts x output columns, KSK rows streamed once per tile
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "ntt.cuh"
@@ -21,6 +22,22 @@ namespace {
 
 __device__ __forceinline__ Chan pick_chan(const Chan (&c)[kChannels], int team) {
     return team == 0 ? c[0] : (team == 1 ? c[1] : c[2]);
+}
+
+// L2 policy for bootstrapping-key reads: every ciphertext of a launch re-reads the whole
+// key, so its lines are kept in L2 ahead of the streamed inputs and outputs.
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ uint4 ldg_keep(const uint4* p, uint64_t pol) {
+    uint4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p), "l"(pol));
+    return v;
 }
 
 // zeroMeanDigits (yatfhe/include/yatfhe/gadget_decomposition.h:76-95): signed balanced
@@ -99,7 +116,7 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     uint32_t x[32];
 #pragma unroll
     for (int r = 0; r < 32; ++r) x[r] = src[r * S + tt];
-    ntt_forward<LOGN>(x, tb + team * Sh::TBUF, tt, team, ch);
+    ntt_forward<LOGN>(x, tb + team * Sh::TBUF, tt, team, team, ch);
     const int blk = poly >> 1, o = poly & 1;
     uint32_t* dst = a.key + ((size_t)blk * kChannels + team) * key_block_words(N);
 #pragma unroll
@@ -109,64 +126,99 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     }
 }
 
-template <int LOGN, int T>
-__global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) blind_rotate_kernel(const BrArgs a) {
+// Threads of one ciphertext slice: three channel teams.
+template <int LOGN>
+__host__ __device__ constexpr int slice_threads() { return 3 * TeamShape<LOGN>::S; }
+
+// Resident CTAs per SM the register budget is sized for (about 170 registers a thread).
+template <int LOGN, int G>
+__host__ __device__ constexpr int min_ctas() { return (LOGN == 10 ? 4 : 2) / G > 0 ? (LOGN == 10 ? 4 : 2) / G : 1; }
+
+// G ciphertexts per CTA run in lockstep: their warps execute the same phase at the same
+// time (one stretch of code in the instruction caches) and the G teams of a channel read
+// the same key lines, the first from L2 and the others from L1.
+template <int LOGN, int T, int G>
+__global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()) blind_rotate_kernel(const BrArgs a) {
     using Sh = TeamShape<LOGN>;
     using TorusT = typename TorusOf<T>::type;
     using U = typename TorusOf<T>::utype;
     constexpr int N = Sh::N, S = Sh::S;
+    constexpr int ST = slice_threads<LOGN>();
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* tb = reinterpret_cast<uint32_t*>(smem);               // [3][TBUF] transposes
-    uint32_t* xb = tb + kChannels * Sh::TBUF;                        // [3][2][N] INTT outputs
-    TorusT* acc = reinterpret_cast<TorusT*>(xb + kChannels * 2 * N); // [2][N] accumulator
-    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);          // [2][L][N] digits
-    int16_t* sa = dig + 2 * a.L * N;                                  // [n+1] mod-2N input
 
-    const int ct = blockIdx.x;
-    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int team = warp / Sh::WARPS;
-    const int tt = (warp % Sh::WARPS) * 32 + lane;
+    const int g = warp / (3 * Sh::WARPS);                   // ciphertext slice of this warp
+    const int wi = warp % (3 * Sh::WARPS);
+    const int team = wi / Sh::WARPS;                         // RNS channel
+    const int tt = (wi % Sh::WARPS) * 32 + lane;             // thread in the channel team
+    const int bar = g * kChannels + team;                    // named barrier of the team
+    const int ltid = tid - g * ST;                           // thread in the slice
     const Chan ch = pick_chan(a.ch, team);
     const int L = a.L, n = a.n;
+    const uint64_t keep = l2_evict_last_policy();
+
+    // the slice's shared memory: xb[team][o] padded regions (NTT transpose scratch, then
+    // inverse-NTT residues for the CRT), the accumulator, the digits, the mod-2N input
+    unsigned char* base = smem + (size_t)g * br_smem_bytes(LOGN, T, n, L);
+    uint32_t* xb = reinterpret_cast<uint32_t*>(base);                           // [3][2][TBUF]
+    TorusT* acc = reinterpret_cast<TorusT*>(xb + kChannels * 2 * Sh::TBUF);    // [2][N]
+    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [2][L][N]
+    int16_t* sa = dig + 2 * L * N;                                               // [n+1]
+    uint32_t* mine = xb + team * 2 * Sh::TBUF;
+
+    // G ciphertexts per iteration; a grid smaller than the batch makes the CTAs persistent
+    for (int first = blockIdx.x * G; first < a.count; first += gridDim.x * G) {
+    const int ct = first + g;
+    const bool valid = ct < a.count;
+    const uint4* key = !valid ? nullptr : (a.key_of ? a.key_table[a.key_of[ct]] : a.key);
+    const int64_t* lut = !valid ? nullptr : (a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut);
 
     // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81), unless given already scaled
-    if (a.scaled_in) {
-        const int32_t* in = a.scaled_in + (size_t)ct * n;
-        for (int i = tid; i < n; i += nth) sa[i] = (int16_t)in[i];
-    } else {
-        const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
-        for (int i = tid; i <= n; i += nth) sa[i] = (int16_t)modswitch_down(in[i], 31 - LOGN, LOGN + 1);
+    if (valid) {
+        if (a.scaled_in) {
+            const int32_t* in = a.scaled_in + (size_t)ct * n;
+            for (int i = ltid; i < n; i += ST) sa[i] = (int16_t)in[i];
+        } else {
+            const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+            for (int i = ltid; i <= n; i += ST) sa[i] = (int16_t)modswitch_down(in[i], 31 - LOGN, LOGN + 1);
+        }
     }
     __syncthreads();
 
-    if (a.acc_in) {
-        const int64_t* src = a.acc_in + (size_t)ct * 2 * N;
-        for (int idx = tid; idx < 2 * N; idx += nth) acc[idx] = (TorusT)src[idx];
-    } else {
-        // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
-        int t2 = -(int)sa[n];
-        t2 = ((t2 % (2 * N)) + 2 * N) % (2 * N);
-        const bool wrap = t2 >= N;
-        const int at = wrap ? t2 - N : t2;
-        for (int j = tid; j < N; j += nth) {
-            acc[j] = 0;
-            TorusT v = j < at ? tneg<T>((TorusT)a.lut[j - at + N]) : (TorusT)a.lut[j - at];
-            acc[N + j] = wrap ? tneg<T>(v) : v;
+    if (valid) {
+        if (a.acc_in) {
+            const int64_t* src = a.acc_in + (size_t)ct * 2 * N;
+            for (int idx = ltid; idx < 2 * N; idx += ST) acc[idx] = (TorusT)src[idx];
+        } else {
+            // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
+            int t2 = -(int)sa[n];
+            t2 = ((t2 % (2 * N)) + 2 * N) % (2 * N);
+            const bool wrap = t2 >= N;
+            const int at = wrap ? t2 - N : t2;
+            for (int j = ltid; j < N; j += ST) {
+                acc[j] = 0;
+                TorusT v = j < at ? tneg<T>((TorusT)lut[j - at + N]) : (TorusT)lut[j - at];
+                acc[N + j] = wrap ? tneg<T>(v) : v;
+            }
         }
     }
     __syncthreads();
 
     for (int i = 0; i < a.steps; ++i) {
-        const int ai = sa[i];
-        if (ai == 0) continue;  // result-neutral skip of blind_rotate.cpp:1557
+        const int ai = valid ? (int)sa[i] : 0;
+        // a_i == 0 leaves the accumulator unchanged (the skip of blind_rotate.cpp:1557); with
+        // one ciphertext per CTA the whole step is skipped, otherwise only its work
+        if (G == 1 && ai == 0) continue;
+        const bool active = ai != 0;
         // tmp = X^{a_i} acc - acc (rotateTrlweMinusOne, yatfhe/src/trlwe.cpp:284-289), then
         // gadgetDecomposeTrlwe (yatfhe/src/trlwe.cpp:185-198) into int16 digits
-        {
+        if (active) {
             const int t2 = ai < 0 ? ai + 2 * N : ai;
             const bool wrap = t2 >= N;
             const int at = wrap ? t2 - N : t2;
-            for (int idx = tid; idx < 2 * N; idx += nth) {
+#pragma unroll 2
+            for (int idx = ltid; idx < 2 * N; idx += ST) {
                 const int o = idx >= N;
                 const int j = idx - o * N;
                 const TorusT* A = acc + o * N;
@@ -180,70 +232,85 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) blind_rotate_kernel(co
         }
         __syncthreads();
 
-        // externalProductTrgswMPNttImpl (yatfhe/src/trgsw.cpp:712-767) in channel `team`:
-        // forward NTT of every digit poly, Montgomery MAC against the key, inverse NTT.
-        uint32_t oa[32], ob[32];
+        if (active) {
+            // externalProductTrgswMPNttImpl (yatfhe/src/trgsw.cpp:712-767) in channel `team`:
+            // forward NTT of every digit poly, Montgomery MAC against the key, inverse NTT.
+            uint32_t oa[32], ob[32];
 #pragma unroll
-        for (int r = 0; r < 32; ++r) oa[r] = ob[r] = 0;
-        for (int row = 0; row < 2; ++row) {
-            for (int lvl = 0; lvl < L; ++lvl) {
-                uint32_t x[32];
-                const int16_t* d = dig + ((size_t)row * L + lvl) * N;
+            for (int r = 0; r < 32; ++r) oa[r] = ob[r] = 0;
+            for (int row = 0; row < 2; ++row) {
+                for (int lvl = 0; lvl < L; ++lvl) {
+                    uint32_t x[32];
+                    const int16_t* d = dig + ((size_t)row * L + lvl) * N;
 #pragma unroll
-                for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                ntt_forward<LOGN>(x, tb + team * Sh::TBUF, tt, team, ch);
-                const uint4* kp = a.key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
+                    for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
+                    ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
+                    const uint4* kp =
+                        key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
 #pragma unroll
-                for (int rr = 0; rr < 8; ++rr) {
-                    const uint4 ka = __ldg(kp + rr * S + tt);
-                    const uint4 kb = __ldg(kp + (8 + rr) * S + tt);
-                    const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
-                    const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+                    for (int rr = 0; rr < 8; ++rr) {
+                        const uint4 ka = ldg_keep(kp + rr * S + tt, keep);
+                        const uint4 kb = ldg_keep(kp + (8 + rr) * S + tt, keep);
+                        const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+                        const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int r = rr * 4 + e;
-                        oa[r] = reduce_once(oa[r] + montmul(x[r], kav[e], ch.p, ch.pinv_neg), ch.two_p);
-                        ob[r] = reduce_once(ob[r] + montmul(x[r], kbv[e], ch.p, ch.pinv_neg), ch.two_p);
+                        for (int e = 0; e < 4; ++e) {
+                            const int r = rr * 4 + e;
+                            oa[r] = reduce_once(oa[r] + montmul(x[r], kav[e], ch.p, ch.pinv_neg), ch.two_p);
+                            ob[r] = reduce_once(ob[r] + montmul(x[r], kbv[e], ch.p, ch.pinv_neg), ch.two_p);
+                        }
                     }
                 }
             }
+            // one copy of the inverse transform, applied to the a then the b output poly
+#pragma unroll 1
+            for (int o = 0; o < 2; ++o) {
+                if (o == 1) {
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) oa[r] = ob[r];
+                }
+                uint32_t* region = mine + o * Sh::TBUF;
+                ntt_inverse<LOGN>(oa, region, tt, team, bar, ch);
+                team_sync<LOGN>(bar);
+#pragma unroll
+                for (int r = 0; r < 32; ++r) region[r * S + tt] = reduce_once(oa[r], ch.p);
+            }
         }
-        ntt_inverse<LOGN>(oa, tb + team * Sh::TBUF, tt, team, ch);
-#pragma unroll
-        for (int r = 0; r < 32; ++r) xb[(team * 2 + 0) * N + r * S + tt] = reduce_once(oa[r], ch.p);
-        ntt_inverse<LOGN>(ob, tb + team * Sh::TBUF, tt, team, ch);
-#pragma unroll
-        for (int r = 0; r < 32; ++r) xb[(team * 2 + 1) * N + r * S + tt] = reduce_once(ob[r], ch.p);
         __syncthreads();
 
         // CRT -> applyIntt's centred mod-q value mod 2^T, then accumulateTrlwe (trlwe.h:268-274)
-        for (int idx = tid; idx < 2 * N; idx += nth) {
-            const int o = idx >= N;
-            const int j = idx - o * N;
-            const int64_t v = crt_to_torus<T>(xb[(0 * 2 + o) * N + j], xb[(1 * 2 + o) * N + j],
-                                              xb[(2 * 2 + o) * N + j], a.crt);
-            if constexpr (T == 32) acc[idx] = (int32_t)((uint32_t)acc[idx] + (uint32_t)v);
-            else acc[idx] = sext<56>((int64_t)((uint64_t)acc[idx] + (uint64_t)v));
+        if (active) {
+#pragma unroll 2
+            for (int idx = ltid; idx < 2 * N; idx += ST) {
+                const int o = idx >= N;
+                const int j = idx - o * N;
+                const int64_t v = crt_to_torus<T>(xb[(0 * 2 + o) * Sh::TBUF + j], xb[(1 * 2 + o) * Sh::TBUF + j],
+                                                  xb[(2 * 2 + o) * Sh::TBUF + j], a.crt);
+                if constexpr (T == 32) acc[idx] = (int32_t)((uint32_t)acc[idx] + (uint32_t)v);
+                else acc[idx] = sext<56>((int64_t)((uint64_t)acc[idx] + (uint64_t)v));
+            }
         }
         __syncthreads();
     }
 
-    if (a.acc_out) {
+    if (valid && a.acc_out) {
         int64_t* dst = a.acc_out + (size_t)ct * 2 * N;
-        for (int idx = tid; idx < 2 * N; idx += nth) dst[idx] = (int64_t)acc[idx];
+        for (int idx = ltid; idx < 2 * N; idx += ST) dst[idx] = (int64_t)acc[idx];
     }
-    if (a.big_out) {
+    if (valid && a.big_out) {
         // extractTlweFromTrlwe(out, acc, 0): a'[j] = j ? -a[N-j] : a[0], b' = b[0], rescaled 2^T -> 2^32
         int32_t* dst = a.big_out + (size_t)ct * (N + 1);
-        for (int j = tid; j <= N; j += nth) {
+        for (int j = ltid; j <= N; j += ST) {
             TorusT x = j == N ? acc[N] : (j == 0 ? acc[0] : tneg<T>(acc[N - j]));
             if constexpr (T == 32) dst[j] = (int32_t)x;
             else dst[j] = (int32_t)modswitch_down((int64_t)x, T - 32, 32);
         }
     }
+    __syncthreads();  // the next ciphertexts reuse the shared-memory state
+    }
 }
 
-constexpr int kKsTile = 8;      // ciphertexts per block
+constexpr int kKsTile = kKsTileCts;  // ciphertexts per block
 constexpr int kKsCols = 128;    // output columns per block (= threads)
 constexpr int kKsChunk = 32;    // input coefficients per digit refresh
 constexpr int kKsMaxT = 16;
@@ -252,21 +319,32 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
     __shared__ int8_t sdig[kKsTile][kKsChunk][kKsMaxT];
     __shared__ int32_t sb[kKsTile];
     const int x = blockIdx.y * kKsCols + threadIdx.x;
-    const int c0 = blockIdx.x * kKsTile;
+    int c0, cnt;
+    const int32_t* ksk;
+    if (a.tiles) {
+        const KsTile tl = a.tiles[blockIdx.x];
+        c0 = tl.ct_begin;
+        cnt = tl.count;
+        ksk = tl.ksk;
+    } else {
+        c0 = blockIdx.x * kKsTile;
+        cnt = min(kKsTile, a.count - c0);
+        ksk = a.ksk;
+    }
     const int nb = a.n + 1;
     uint32_t acc[kKsTile];
 #pragma unroll
     for (int c = 0; c < kKsTile; ++c) acc[c] = 0;
     if (threadIdx.x < kKsTile) {
         const int ct = c0 + threadIdx.x;
-        sb[threadIdx.x] = ct < a.count ? a.big_in[(size_t)ct * (a.kN + 1) + a.kN] : 0;
+        sb[threadIdx.x] = (int)threadIdx.x < cnt ? a.big_in[(size_t)ct * (a.kN + 1) + a.kN] : 0;
     }
     for (int i0 = 0; i0 < a.kN; i0 += kKsChunk) {
         __syncthreads();
         for (int e = threadIdx.x; e < kKsTile * kKsChunk; e += kKsCols) {
             const int c = e / kKsChunk, ii = e % kKsChunk;
             const int ct = c0 + c, i = i0 + ii;
-            const int32_t v = (ct < a.count && i < a.kN) ? a.big_in[(size_t)ct * (a.kN + 1) + i] : 0;
+            const int32_t v = (c < cnt && i < a.kN) ? a.big_in[(size_t)ct * (a.kN + 1) + i] : 0;
             zero_mean_digits<uint32_t, 32>((uint32_t)v, a.t, a.ks_radix_bits,
                                            [&](int level, int d) { sdig[c][ii][level] = (int8_t)d; });
         }
@@ -274,7 +352,7 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
         if (x < nb) {
             const int iend = min(kKsChunk, a.kN - i0);
             for (int ii = 0; ii < iend; ++ii) {
-                const int32_t* row = a.ksk + ((size_t)(i0 + ii) * a.t) * nb + x;
+                const int32_t* row = ksk + ((size_t)(i0 + ii) * a.t) * nb + x;
                 for (int j = 0; j < a.t; ++j) {
                     const uint32_t w = (uint32_t)__ldg(row + (size_t)j * nb);
 #pragma unroll
@@ -287,35 +365,84 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
 #pragma unroll
         for (int c = 0; c < kKsTile; ++c) {
             const int ct = c0 + c;
-            if (ct < a.count) a.out[(size_t)ct * nb + x] = (int32_t)((x == a.n ? (uint32_t)sb[c] : 0u) - acc[c]);
+            if (c < cnt) a.out[(size_t)ct * nb + x] = (int32_t)((x == a.n ? (uint32_t)sb[c] : 0u) - acc[c]);
         }
     }
 }
 
-template <int LOGN, int T>
-int launch_br_t(const BrArgs& a, void* stream) {
-    const size_t smem = br_smem_bytes(LOGN, T, a.n, a.L);
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(blind_rotate_kernel<LOGN, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
-            cudaSuccess)
+template <int LOGN, int T, int G>
+int prepare_br_t() {
+    // the dynamic shared-memory opt-in is per device: done once on each
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    if (!done[dev].load()) {
+        if (cudaFuncSetAttribute(blind_rotate_kernel<LOGN, T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 227 * 1024) != cudaSuccess)
             return -1;
-        attr_set = true;
+        done[dev].store(true);
     }
-    blind_rotate_kernel<LOGN, T><<<a.count, 3 * TeamShape<LOGN>::S, smem, (cudaStream_t)stream>>>(a);
+    return 0;
+}
+
+template <int LOGN, int T, int G>
+int launch_br_t(const BrArgs& a, void* stream) {
+    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, a.n, a.L);
+    if (smem > 227 * 1024) return -1;
+    if (prepare_br_t<LOGN, T, G>() != 0) return -1;
+    const int need = (a.count + G - 1) / G;
+    const int grid = a.grid > 0 && a.grid < need ? a.grid : need;
+    blind_rotate_kernel<LOGN, T, G><<<grid, G * slice_threads<LOGN>(), smem, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int LOGN, int T, int G>
+int ctas_per_sm_t(int n, int L) {
+    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, n, L);
+    if (smem > 227 * 1024) return 0;
+    if (prepare_br_t<LOGN, T, G>() != 0) return -1;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_kernel<LOGN, T, G>,
+                                                      G * slice_threads<LOGN>(), smem) != cudaSuccess)
+        return -1;
+    return blocks;
+}
+
+struct LaunchBr {
+    const BrArgs& a;
+    void* stream;
+    template <int LN, int TB, int GG>
+    int operator()() const { return launch_br_t<LN, TB, GG>(a, stream); }
+};
+
+struct OccupancyBr {
+    int n, L;
+    template <int LN, int TB, int GG>
+    int operator()() const { return ctas_per_sm_t<LN, TB, GG>(n, L); }
+};
+
+// Dispatch on (N, torus width, ciphertexts per CTA); F(tag) gets the template arguments.
+// kNoVariant when that combination is not compiled.
+template <typename F>
+int dispatch_br(int logN, int torus_bits, int g, F&& f) {
+    if (g <= 0) g = 1;
+#define YG_BR_CASE(LN, TB, GG) \
+    if (logN == LN && torus_bits == TB && g == GG) return f.template operator()<LN, TB, GG>();
+    YG_BR_CASE(10, 32, 1) YG_BR_CASE(10, 32, 2) YG_BR_CASE(10, 32, 4)
+    YG_BR_CASE(10, 56, 1) YG_BR_CASE(10, 56, 2) YG_BR_CASE(10, 56, 4)
+    YG_BR_CASE(11, 32, 1) YG_BR_CASE(11, 32, 2)
+    YG_BR_CASE(11, 56, 1) YG_BR_CASE(11, 56, 2)
+#undef YG_BR_CASE
+    return kNoVariant;
 }
 
 }  // namespace
 
-size_t br_smem_bytes(int logN, int torus_bits, int n, int L) {
-    const size_t N = (size_t)1 << logN;
-    const size_t tbuf = N + N / 32;
-    size_t b = kChannels * tbuf * 4 + kChannels * 2 * N * 4;
-    b += 2 * N * (torus_bits == 32 ? 4 : 8);
-    b += 2 * (size_t)L * N * 2;
-    b += ((size_t)n + 1) * 2;
-    return (b + 15) & ~(size_t)15;
+
+int set_twiddle_heads(int logN, const uint2* heads) {
+    if (logN != 10 && logN != 11) return -1;
+    const size_t per = sizeof(uint2) * kChannels * 2 * 32;
+    return cudaMemcpyToSymbol(c_tw_head, heads, per, per * (logN - 10)) == cudaSuccess ? 0 : -1;
 }
 
 int launch_keyconv(int logN, const KeyConvArgs& a, void* stream) {
@@ -327,17 +454,19 @@ int launch_keyconv(int logN, const KeyConvArgs& a, void* stream) {
 
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream) {
     if (a.count <= 0) return 0;
-    if (logN == 10 && torus_bits == 32) return launch_br_t<10, 32>(a, stream);
-    if (logN == 10 && torus_bits == 56) return launch_br_t<10, 56>(a, stream);
-    if (logN == 11 && torus_bits == 32) return launch_br_t<11, 32>(a, stream);
-    if (logN == 11 && torus_bits == 56) return launch_br_t<11, 56>(a, stream);
-    return -1;
+    return dispatch_br(logN, torus_bits, a.per_cta, LaunchBr{a, stream});
+}
+
+int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta) {
+    return dispatch_br(logN, torus_bits, per_cta, OccupancyBr{n, L});
 }
 
 int launch_keyswitch(const KsArgs& a, void* stream) {
     if (a.count <= 0) return 0;
     if (a.t > kKsMaxT) return -1;
-    dim3 grid((a.count + kKsTile - 1) / kKsTile, (a.n + 1 + kKsCols - 1) / kKsCols);
+    const int blocks = a.tiles ? a.num_tiles : (a.count + kKsTile - 1) / kKsTile;
+    if (blocks <= 0) return 0;
+    dim3 grid(blocks, (a.n + 1 + kKsCols - 1) / kKsCols);
     keyswitch_kernel<<<grid, kKsCols, 0, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -13,10 +13,18 @@ struct BrArgs {
     const int32_t* scaled_in;// [count][n] mask already switched to mod 2N (ScaledTlwe::a), or null
     const int64_t* lut;      // [N] torus test polynomial, or null when acc_in is given
     const int64_t* acc_in;   // [count][(k+1) N] starting accumulator, or null
-    const uint4* key;        // device BSK, slot layout (see key_slot_words)
+    const uint4* key;        // device BSK, slot layout (see key_block_words)
+    // Multi-key batches: ciphertext c uses key_table[key_of[c]] and lut_table[lut_of[c]]
+    // when the index arrays are given (then `key` / `lut` are ignored).
+    const uint4* const* key_table;
+    const int32_t* key_of;
+    const int64_t* const* lut_table;
+    const int32_t* lut_of;
     int32_t* big_out;        // [count][k N + 1] extracted LWE, or null
     int64_t* acc_out;        // [count][(k+1) N] accumulator, or null
     int count;
+    int grid;                // CTAs to launch (0: enough for the batch; fewer: persistent CTAs)
+    int per_cta;             // ciphertexts per CTA, run in lockstep (1, 2 or 4; 0 means 1)
     int n;                   // LWE dimension
     int steps;               // CMux steps to run (n for a full blind rotation)
     int L;                   // gadget levels
@@ -24,6 +32,14 @@ struct BrArgs {
     Chan ch[kChannels];
     Crt crt;
 };
+
+// A run of at most kKsTileCts consecutive ciphertexts of a batch that share one KSK.
+struct KsTile {
+    int ct_begin;
+    int count;
+    const int32_t* ksk;
+};
+constexpr int kKsTileCts = 8;
 
 struct KsArgs {
     const int32_t* big_in;   // [count][kN + 1]
@@ -34,6 +50,8 @@ struct KsArgs {
     int n;
     int t;
     int ks_radix_bits;
+    const KsTile* tiles;     // multi-key batches: one tile per block (then `ksk` is ignored)
+    int num_tiles;
 };
 
 struct KeyConvArgs {
@@ -51,9 +69,27 @@ __host__ __device__ inline size_t key_words(int n, int L, int N) {
     return (size_t)n * L * 2 * kChannels * key_block_words(N);
 }
 
-size_t br_smem_bytes(int logN, int torus_bits, int n, int L);
+// Shared memory of one ciphertext slice of the blind-rotation kernel: per channel two
+// padded (N + N/32)-word regions, the accumulator, int16 digits, the mod-2N input.
+__host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L) {
+    const size_t N = (size_t)1 << logN;
+    const size_t tbuf = N + N / 32;
+    size_t b = kChannels * 2 * tbuf * 4;
+    b += 2 * N * (torus_bits == 32 ? 4 : 8);
+    b += 2 * (size_t)L * N * 2;
+    b += ((size_t)n + 1) * 2;
+    return (b + 15) & ~(size_t)15;
+}
+// Uploads the first 32 forward and inverse twiddles of each channel ([3][2][32] pairs) to
+// the constant bank of the current device.
+int set_twiddle_heads(int logN, const uint2* heads);
 int launch_keyconv(int logN, const KeyConvArgs& a, void* stream);
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream);
+// Resident blind-rotation CTAs per SM for these parameters and ciphertexts per CTA
+// (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,
+// -1 on a CUDA error.
+constexpr int kNoVariant = -2;
+int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta);
 int launch_keyswitch(const KsArgs& a, void* stream);
 
 }  // namespace yg

@@ -5,16 +5,18 @@
 // What reaches the accumulator is only centred(INTT(sum NTT(d) . K) mod q) mod 2^T
 // (yatfhe/src/ntt_hexl.cpp:153-175), i.e. the exact integer X = sum_j d_j * k_j
 // (negacyclic, k_j = INTT(K_j) centred) reduced mod q.  |X| < 2^83 for every supported
-// parameter set, so the GPU computes X exactly in an RNS of three primes p_c < 2^30
-// (product ~2^90) on the 32-bit integer pipes and reduces it mod q once per coefficient.
+// parameter set, so the GPU computes X exactly in an RNS of three primes p_c < 2^29
+// (product ~2^87) on the 32-bit integer pipes and reduces it mod q once per coefficient.
 #pragma once
 #include <cstdint>
 
 namespace yg {
 
 constexpr int kChannels = 3;
-// Largest primes below 2^30 with p == 1 mod 2^13 (negacyclic NTTs up to N = 4096).
-constexpr uint32_t kPrimes[kChannels] = {1073692673u, 1073668097u, 1073651713u};
+// Largest primes below 2^29 with p == 1 mod 2^13 (negacyclic NTTs up to N = 4096).  Below
+// 2^29 so that residues up to 8p fit 32 bits: the forward NTT reduces only every other
+// stage.  Product ~2^87: the 56-bit set's |X| < 2^82.8 keeps 3.2 bits of margin below M/2.
+constexpr uint32_t kPrimes[kChannels] = {536813569u, 536690689u, 536641537u};
 
 // Per-channel constants the kernels read.
 struct Chan {
@@ -46,7 +48,7 @@ __device__ __forceinline__ uint32_t mulshoup(uint32_t x, uint32_t w, uint32_t wp
     return x * w - qh * p;
 }
 
-// a b 2^-32 mod p in [0, 2p) for a < 4p, b < p, p < 2^30.
+// a b 2^-32 mod p in [0, 2p) for a < 8p, b < p, p < 2^29.
 __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv_neg) {
     const uint32_t lo = a * b;
     const uint32_t hi = __umulhi(a, b);
@@ -56,9 +58,12 @@ __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b, uint32_t p, 
 
 __device__ __forceinline__ uint32_t reduce_once(uint32_t x, uint32_t m) { return min(x, x - m); }
 
-// Forward Cooley-Tukey butterfly with lazy reduction: x, y in [0, 4p) -> [0, 4p).
-__device__ __forceinline__ void ct_bfly(uint32_t& x, uint32_t& y, uint2 w, uint32_t p, uint32_t two_p) {
-    const uint32_t xr = reduce_once(x, two_p);
+// Forward Cooley-Tukey butterfly, lazy: with x < B the outputs are < B + 2p (y may be any
+// 32-bit value).  RED first brings x < 8p down below 4p, so with p < 2^29 a stage may skip
+// the reduction whenever its x inputs are known to be below 6p.  (`red` is a constant at
+// every call site once the stage loops are unrolled.)
+__device__ __forceinline__ void ct_bfly(uint32_t& x, uint32_t& y, uint2 w, uint32_t p, uint32_t two_p, bool red) {
+    const uint32_t xr = red ? reduce_once(x, 2 * two_p) : x;
     const uint32_t t = mulshoup(y, w.x, w.y, p);
     x = xr + t;
     y = xr - t + two_p;
@@ -81,7 +86,7 @@ __device__ __forceinline__ int64_t sext(int64_t x) {
 // Residues x_c in [0, p_c) of the exact integer X with |X| < p0 p1 p2 / 2 -> the torus value
 // centred(X mod q) mod 2^T, i.e. what applyIntt (yatfhe/src/ntt_hexl.cpp:153-175) returns.
 // Garner's mixed radix gives X = v0 + v1 p0 + v2 p0 p1 exactly; the top digit is centred
-// (|X| << M/2 puts it within 2^24 of 0 or of p2); a single-precision estimate of X / q
+// (|X| << M/2 puts it within 2^25 of 0 or of p2); a single-precision estimate of X / q
 // picks the quotient to within +-2 and exact 64-bit arithmetic on X mod 2^64 settles it.
 template <int T>
 __device__ __forceinline__ int64_t crt_to_torus(uint32_t x0, uint32_t x1, uint32_t x2, const Crt& k) {

@@ -1,0 +1,693 @@
+// serve.cpp -- multi-tenant bootstrap serving with continuous batching and an HBM key cache.
+//
+// Semantics follow the reference's CPU serving harness (ya_benchmark/blindrotate_serving.cpp,
+// ya_benchmark/include/blindrotate_serving.h): requests (tenant, ciphertexts) arrive as a
+// Poisson process (ArrivalProcess, blindrotate_serving.h:309-350; generator mt19937_64 seeded
+// with seed ^ 0x9e3779b97f4a7c15, blindrotate_serving.cpp:184), tenants are Zipf-popular
+// (ZipfDistribution, yatfhe/include/yautil/zipf.h:47-87), keys live in an LRU cache
+// (ConcurrentKeyCache, blindrotate_serving.h:25-111) and latency is reported as ceil-rank
+// percentiles of sojourn / queue / service time (blindrotate_serving.cpp:60-82).
+//
+// GPU design.  One worker thread owns the device.  Tenant keys are kept, already in the
+// device layout, in pinned host memory; HBM holds `slots` of them (budget / key bytes),
+// refilled on a miss by cudaMemcpyAsync on a copy stream, with an event the compute stream
+// waits on.  The worker admits pending requests into a batch (up to max_batch ciphertexts)
+// as long as their keys are resident or can be brought in (an LRU slot whose tenant has no
+// batch in flight), groups the batch by tenant, and launches the multi-key blind rotation
+// and key switch.  Up to max_inflight batches are queued on the GPU at once, so requests
+// that arrive while one runs are admitted into the next (continuous batching).  Batch
+// completion is signalled by a host callback on the compute stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+using yg::ck;
+using yg::guarded;
+using yg::set_err;
+
+double now_s() { return std::chrono::duration<double>(Clock::now().time_since_epoch()).count(); }
+
+struct Request {
+    int64_t id = 0;
+    int tenant = 0;
+    int count = 0;
+    const int32_t* h_in = nullptr;
+    int32_t* h_out = nullptr;
+    double t_submit = 0, t_start = 0, t_done = 0;
+    std::atomic<bool> done{false};
+};
+
+struct Tenant {
+    int id = 0;
+    int index = 0;                 // dense index (LUT table)
+    uint32_t* h_bsk = nullptr;     // pinned, device layout
+    int32_t* h_ksk = nullptr;      // pinned
+    int64_t* d_lut = nullptr;
+    int slot = -1;
+    cudaEvent_t ready = nullptr;
+    int pins = 0;
+    uint64_t last_use = 0;
+};
+
+struct Batch {
+    int32_t* d_in = nullptr;
+    int32_t* d_out = nullptr;
+    int32_t* d_big = nullptr;
+    int32_t* d_key_of = nullptr;
+    int32_t* d_lut_of = nullptr;
+    yg::KsTile* d_tiles = nullptr;
+    int32_t* h_key_of = nullptr;   // pinned staging
+    int32_t* h_lut_of = nullptr;
+    yg::KsTile* h_tiles = nullptr;
+    std::vector<Request*> reqs;
+    std::vector<Tenant*> tenants;
+    std::atomic<bool> finished{false};
+    bool busy = false;
+    struct yg_server* server = nullptr;
+};
+
+}  // namespace
+
+struct yg_server {
+    yg_ctx* ctx = nullptr;
+    yg_server_config cfg{};
+    size_t bsk_bytes = 0, ksk_bytes = 0;
+    int nslots = 0;
+    std::vector<uint32_t*> slot_bsk;
+    std::vector<int32_t*> slot_ksk;
+    std::vector<int> slot_owner;
+    const uint4** d_slot_table = nullptr;
+    const int64_t** d_lut_table = nullptr;
+    std::map<int, std::unique_ptr<Tenant>> tenants;
+    std::vector<Tenant*> by_index;
+    cudaStream_t compute = nullptr, copy = nullptr;
+    std::vector<std::unique_ptr<Batch>> batches;
+
+    std::mutex mu;
+    std::condition_variable cv;        // worker wake-ups (arrivals, batch completion)
+    std::condition_variable cv_done;   // waiters in yg_server_wait
+    std::deque<Request*> incoming;
+    std::unordered_map<int64_t, std::unique_ptr<Request>> requests;
+    int64_t next_id = 1;
+    std::thread worker;
+    bool running = false, stopping = false;
+    uint64_t tick = 0;
+    std::string worker_error;
+
+    // statistics
+    uint64_t hits = 0, misses = 0, refill_bytes = 0, batches_run = 0, ciphertexts_done = 0, requests_done = 0;
+    double busy_since = 0;
+};
+
+namespace {
+
+// Host callback at the end of a batch.  It runs on a CUDA thread and must not take the
+// server lock (the worker holds it across CUDA calls), so it only stamps and flags; the
+// worker's timed wait picks the flag up.
+void CUDART_CB batch_done_cb(void* p) {
+    Batch* b = static_cast<Batch*>(p);
+    const double t = now_s();
+    for (Request* r : b->reqs) r->t_done = t;
+    b->finished.store(true);
+    b->server->cv.notify_all();
+}
+
+void free_batch(Batch* b) {
+    cudaFree(b->d_in);
+    cudaFree(b->d_out);
+    cudaFree(b->d_big);
+    cudaFree(b->d_key_of);
+    cudaFree(b->d_lut_of);
+    cudaFree(b->d_tiles);
+    cudaFreeHost(b->h_key_of);
+    cudaFreeHost(b->h_lut_of);
+    cudaFreeHost(b->h_tiles);
+}
+
+// Retires finished batches (caller holds the lock).
+void retire(yg_server* s) {
+    for (auto& bp : s->batches) {
+        Batch* b = bp.get();
+        if (!b->busy || !b->finished.load()) continue;
+        for (Request* r : b->reqs) {
+            r->done.store(true);
+            s->requests_done++;
+            s->ciphertexts_done += r->count;
+        }
+        for (Tenant* t : b->tenants) t->pins--;
+        b->reqs.clear();
+        b->tenants.clear();
+        b->busy = false;
+        b->finished.store(false);
+    }
+    s->cv_done.notify_all();
+}
+
+// A slot for tenant t: free, or the least recently used whose tenant has nothing in
+// flight and is not in the batch being formed (pins == 0).  -1 if none.
+int find_slot(yg_server* s) {
+    int best = -1;
+    uint64_t best_use = UINT64_MAX;
+    for (int i = 0; i < s->nslots; i++) {
+        const int owner = s->slot_owner[i];
+        if (owner < 0) return i;
+        Tenant* o = s->tenants[owner].get();
+        if (o->pins == 0 && o->last_use < best_use) {
+            best = i;
+            best_use = o->last_use;
+        }
+    }
+    return best;
+}
+
+// Builds and launches one batch from the pending queue (caller holds the lock).
+bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
+    const yg_params& p = s->ctx->p;
+    const int n1 = p.n + 1, kN = p.k * p.N;
+    int total = 0;
+    std::vector<Request*> take;
+    std::vector<Tenant*> used;
+    while (!pending.empty()) {
+        Request* r = pending.front();
+        if (total + r->count > s->cfg.max_batch && total > 0) break;
+        Tenant* t = s->tenants[r->tenant].get();
+        const bool in_batch = std::find(used.begin(), used.end(), t) != used.end();
+        if (t->slot < 0) {
+            const int slot = find_slot(s);
+            if (slot < 0) break;  // every slot is held by work in flight: admit later
+            const int prev = s->slot_owner[slot];
+            if (prev >= 0) s->tenants[prev]->slot = -1;
+            s->slot_owner[slot] = t->id;
+            t->slot = slot;
+            ck(cudaMemcpyAsync(s->slot_bsk[slot], t->h_bsk, s->bsk_bytes, cudaMemcpyHostToDevice, s->copy), "refill");
+            ck(cudaMemcpyAsync(s->slot_ksk[slot], t->h_ksk, s->ksk_bytes, cudaMemcpyHostToDevice, s->copy), "refill");
+            ck(cudaEventRecord(t->ready, s->copy), "refill event");
+            s->misses++;
+            s->refill_bytes += s->bsk_bytes + s->ksk_bytes;
+        } else if (!in_batch) {
+            s->hits++;
+        }
+        if (!in_batch) {
+            used.push_back(t);
+            t->pins++;  // from here on the slot cannot be taken by another tenant
+        }
+        t->last_use = ++s->tick;
+        take.push_back(r);
+        total += r->count;
+        pending.pop_front();
+    }
+    if (take.empty()) return false;
+    // group by tenant so the key switch streams one KSK per run of ciphertexts
+    std::stable_sort(take.begin(), take.end(), [](const Request* a, const Request* b) { return a->tenant < b->tenant; });
+    const double t0 = now_s();
+    int off = 0, ntiles = 0;
+    for (Request* r : take) {
+        Tenant* t = s->tenants[r->tenant].get();
+        r->t_start = t0;
+        ck(cudaMemcpyAsync(b->d_in + (size_t)off * n1, r->h_in, (size_t)r->count * n1 * 4, cudaMemcpyHostToDevice,
+                           s->compute),
+           "copy in");
+        for (int c = 0; c < r->count; c++) {
+            b->h_key_of[off + c] = t->slot;
+            b->h_lut_of[off + c] = t->index;
+        }
+        off += r->count;
+    }
+    for (int c = 0; c < total;) {
+        int e = c + 1;
+        while (e < total && e - c < yg::kKsTileCts && b->h_key_of[e] == b->h_key_of[c]) e++;
+        b->h_tiles[ntiles++] = yg::KsTile{c, e - c, s->slot_ksk[b->h_key_of[c]]};
+        c = e;
+    }
+    ck(cudaMemcpyAsync(b->d_key_of, b->h_key_of, (size_t)total * 4, cudaMemcpyHostToDevice, s->compute), "tables");
+    ck(cudaMemcpyAsync(b->d_lut_of, b->h_lut_of, (size_t)total * 4, cudaMemcpyHostToDevice, s->compute), "tables");
+    ck(cudaMemcpyAsync(b->d_tiles, b->h_tiles, (size_t)ntiles * sizeof(yg::KsTile), cudaMemcpyHostToDevice, s->compute),
+       "tables");
+    for (Tenant* t : used) ck(cudaStreamWaitEvent(s->compute, t->ready, 0), "wait refill");
+    yg::BrArgs a = yg::br_args(s->ctx, nullptr);
+    a.key = nullptr;
+    a.key_table = s->d_slot_table;
+    a.key_of = b->d_key_of;
+    a.lut_table = s->d_lut_table;
+    a.lut_of = b->d_lut_of;
+    a.lwe_in = b->d_in;
+    a.big_out = b->d_big;
+    a.count = total;
+    yg::check_launch(yg::launch_blind_rotate(s->ctx->logN, p.torus_bits, a, s->compute), "blind rotate launch");
+    yg::KsArgs k{b->d_big, nullptr, b->d_out, total, kN, p.n, p.ks_level, p.ks_radix_bits, b->d_tiles, ntiles};
+    yg::check_launch(yg::launch_keyswitch(k, s->compute), "keyswitch launch");
+    off = 0;
+    for (Request* r : take) {
+        ck(cudaMemcpyAsync(r->h_out, b->d_out + (size_t)off * n1, (size_t)r->count * n1 * 4, cudaMemcpyDeviceToHost,
+                           s->compute),
+           "copy out");
+        off += r->count;
+    }
+    b->reqs = std::move(take);
+    b->tenants = std::move(used);
+    b->busy = true;
+    b->finished.store(false);
+    ck(cudaLaunchHostFunc(s->compute, batch_done_cb, b), "completion callback");
+    s->batches_run++;
+    return true;
+}
+
+void worker_loop(yg_server* s) {
+    if (cudaSetDevice(s->ctx->device) != cudaSuccess) return;
+    std::deque<Request*> pending;
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        while (!s->incoming.empty()) {
+            pending.push_back(s->incoming.front());
+            s->incoming.pop_front();
+        }
+        retire(s);
+        if (s->stopping && pending.empty() && std::none_of(s->batches.begin(), s->batches.end(),
+                                                           [](const auto& b) { return b->busy; }))
+            break;
+        Batch* free_b = nullptr;
+        for (auto& b : s->batches)
+            if (!b->busy) {
+                free_b = b.get();
+                break;
+            }
+        bool launched = false;
+        if (free_b && !pending.empty()) {
+            try {
+                launched = launch_batch(s, pending, free_b);
+            } catch (const std::exception& e) {
+                s->worker_error = e.what();
+                s->stopping = true;
+                for (Request* r : pending) r->done.store(true);
+                pending.clear();
+                s->cv_done.notify_all();
+                break;
+            }
+        }
+        if (!launched) s->cv.wait_for(lk, std::chrono::microseconds(500));
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) {
+    if (!ctx || !cfg || !out || cfg->max_batch < 1 || cfg->max_inflight < 1 || cfg->max_inflight > 8)
+        return set_err(YG_ERR_INVALID, "yg_server_create: bad arguments");
+    *out = nullptr;
+    return guarded([&] {
+        yg::DeviceGuard g(ctx->device);
+        auto s = std::make_unique<yg_server>();
+        s->ctx = ctx;
+        s->cfg = *cfg;
+        const yg_params& p = ctx->p;
+        s->bsk_bytes = yg::key_words(p.n, p.l_approx, p.N) * 4;
+        s->ksk_bytes = (size_t)p.k * p.N * p.ks_level * (p.n + 1) * 4;
+        s->nslots = (int)(cfg->key_budget_bytes / (s->bsk_bytes + s->ksk_bytes));
+        if (s->nslots < 1) throw std::invalid_argument("key budget smaller than one tenant's keys");
+        if (cfg->max_tenants < 1) throw std::invalid_argument("max_tenants must be positive");
+        auto fail_clean = [&]() {
+            for (auto* b : s->slot_bsk) cudaFree(b);
+            for (auto* k : s->slot_ksk) cudaFree(k);
+            cudaFree(s->d_slot_table);
+            cudaFree(s->d_lut_table);
+            for (auto& b : s->batches) free_batch(b.get());
+            if (s->compute) cudaStreamDestroy(s->compute);
+            if (s->copy) cudaStreamDestroy(s->copy);
+        };
+        try {
+            for (int i = 0; i < s->nslots; i++) {
+                uint32_t* b = nullptr;
+                int32_t* k = nullptr;
+                ck(cudaMalloc(&b, s->bsk_bytes), "key slot");
+                s->slot_bsk.push_back(b);
+                ck(cudaMalloc(&k, s->ksk_bytes), "key slot");
+                s->slot_ksk.push_back(k);
+                s->slot_owner.push_back(-1);
+            }
+            std::vector<const uint4*> table;
+            for (uint32_t* b : s->slot_bsk) table.push_back(reinterpret_cast<const uint4*>(b));
+            ck(cudaMalloc(&s->d_slot_table, table.size() * sizeof(void*)), "slot table");
+            ck(cudaMemcpy(s->d_slot_table, table.data(), table.size() * sizeof(void*), cudaMemcpyHostToDevice),
+               "slot table");
+            ck(cudaMalloc(&s->d_lut_table, (size_t)cfg->max_tenants * sizeof(void*)), "LUT table");
+            ck(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "stream");
+            ck(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "stream");
+            const int n1 = p.n + 1, big = p.k * p.N + 1, mb = cfg->max_batch;
+            for (int i = 0; i < cfg->max_inflight; i++) {
+                auto b = std::make_unique<Batch>();
+                b->server = s.get();
+                ck(cudaMalloc(&b->d_in, (size_t)mb * n1 * 4), "batch buffer");
+                ck(cudaMalloc(&b->d_out, (size_t)mb * n1 * 4), "batch buffer");
+                ck(cudaMalloc(&b->d_big, (size_t)mb * big * 4), "batch buffer");
+                ck(cudaMalloc(&b->d_key_of, (size_t)mb * 4), "batch buffer");
+                ck(cudaMalloc(&b->d_lut_of, (size_t)mb * 4), "batch buffer");
+                ck(cudaMalloc(&b->d_tiles, (size_t)mb * sizeof(yg::KsTile)), "batch buffer");
+                ck(cudaMallocHost(&b->h_key_of, (size_t)mb * 4), "batch staging");
+                ck(cudaMallocHost(&b->h_lut_of, (size_t)mb * 4), "batch staging");
+                ck(cudaMallocHost(&b->h_tiles, (size_t)mb * sizeof(yg::KsTile)), "batch staging");
+                s->batches.push_back(std::move(b));
+            }
+        } catch (...) {
+            fail_clean();
+            throw;
+        }
+        *out = s.release();
+        return YG_OK;
+    });
+}
+
+int yg_server_add_tenant(yg_server* s, int tenant, const yg_key* key, const int64_t* h_lut) {
+    if (!s || !key || !h_lut || tenant < 0) return set_err(YG_ERR_INVALID, "yg_server_add_tenant: bad arguments");
+    if (int rc = yg::check_key(s->ctx, key, true, true)) return rc;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return set_err(YG_ERR_STATE, "tenants must be added before yg_server_start");
+    if (s->tenants.count(tenant)) return set_err(YG_ERR_INVALID, "tenant already registered");
+    if ((int)s->by_index.size() >= s->cfg.max_tenants) return set_err(YG_ERR_INVALID, "too many tenants");
+    return guarded([&] {
+        yg::DeviceGuard g(s->ctx->device);
+        auto t = std::make_unique<Tenant>();
+        t->id = tenant;
+        t->index = (int)s->by_index.size();
+        try {
+            ck(cudaMallocHost(&t->h_bsk, s->bsk_bytes), "pinned key image");
+            ck(cudaMallocHost(&t->h_ksk, s->ksk_bytes), "pinned key image");
+            ck(cudaMemcpy(t->h_bsk, key->d_bsk, s->bsk_bytes, cudaMemcpyDeviceToHost), "key image");
+            ck(cudaMemcpy(t->h_ksk, key->d_ksk, s->ksk_bytes, cudaMemcpyDeviceToHost), "key image");
+            ck(cudaMalloc(&t->d_lut, (size_t)s->ctx->p.N * 8), "LUT");
+            ck(cudaMemcpy(t->d_lut, h_lut, (size_t)s->ctx->p.N * 8, cudaMemcpyHostToDevice), "LUT");
+            ck(cudaMemcpy(s->d_lut_table + t->index, &t->d_lut, sizeof(void*), cudaMemcpyHostToDevice), "LUT table");
+            ck(cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming), "event");
+        } catch (...) {
+            cudaFreeHost(t->h_bsk);
+            cudaFreeHost(t->h_ksk);
+            cudaFree(t->d_lut);
+            throw;
+        }
+        s->by_index.push_back(t.get());
+        s->tenants[tenant] = std::move(t);
+        return YG_OK;
+    });
+}
+
+int yg_server_start(yg_server* s) {
+    if (!s) return set_err(YG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return YG_OK;
+    s->running = true;
+    s->stopping = false;
+    s->busy_since = now_s();
+    s->worker = std::thread(worker_loop, s);
+    return YG_OK;
+}
+
+int64_t yg_server_submit(yg_server* s, int tenant, const int32_t* h_in, int32_t* h_out, int count) {
+    if (!s || !h_in || !h_out || count < 1) return set_err(YG_ERR_INVALID, "yg_server_submit: bad arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->running || s->stopping) return set_err(YG_ERR_STATE, "server not running");
+    if (count > s->cfg.max_batch) return set_err(YG_ERR_INVALID, "request larger than max_batch");
+    if (!s->tenants.count(tenant)) return set_err(YG_ERR_INVALID, "unknown tenant");
+    auto r = std::make_unique<Request>();
+    r->id = s->next_id++;
+    r->tenant = tenant;
+    r->count = count;
+    r->h_in = h_in;
+    r->h_out = h_out;
+    r->t_submit = now_s();
+    Request* raw = r.get();
+    s->requests[raw->id] = std::move(r);
+    s->incoming.push_back(raw);
+    s->cv.notify_all();
+    return raw->id;
+}
+
+int yg_server_wait(yg_server* s, int64_t request, int timeout_ms, yg_request_times* times) {
+    if (!s) return set_err(YG_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(request);
+    if (it == s->requests.end()) return set_err(YG_ERR_INVALID, "unknown request");
+    Request* r = it->second.get();
+    const bool ok = s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms < 0 ? 1 << 30 : timeout_ms),
+                                        [&] { return r->done.load(); });
+    if (!s->worker_error.empty()) return set_err(YG_ERR_CUDA, "server worker failed: " + s->worker_error);
+    if (!ok) return set_err(YG_ERR_STATE, "timeout");
+    if (times) {
+        times->t_submit = r->t_submit;
+        times->t_start = r->t_start;
+        times->t_done = r->t_done;
+    }
+    s->requests.erase(it);
+    return YG_OK;
+}
+
+int yg_server_stats(yg_server* s, yg_server_counters* out) {
+    if (!s || !out) return set_err(YG_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    out->key_hits = s->hits;
+    out->key_misses = s->misses;
+    out->refill_bytes = s->refill_bytes;
+    out->batches = s->batches_run;
+    out->requests_done = s->requests_done;
+    out->ciphertexts_done = s->ciphertexts_done;
+    out->key_slots = s->nslots;
+    return YG_OK;
+}
+
+void yg_server_destroy(yg_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+        s->cv.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    yg::DeviceGuard g(s->ctx->device);
+    cudaStreamSynchronize(s->compute);
+    cudaStreamSynchronize(s->copy);
+    for (auto& b : s->batches) free_batch(b.get());
+    for (auto& kv : s->tenants) {
+        Tenant* t = kv.second.get();
+        cudaFreeHost(t->h_bsk);
+        cudaFreeHost(t->h_ksk);
+        cudaFree(t->d_lut);
+        cudaEventDestroy(t->ready);
+    }
+    for (auto* b : s->slot_bsk) cudaFree(b);
+    for (auto* k : s->slot_ksk) cudaFree(k);
+    cudaFree(s->d_slot_table);
+    cudaFree(s->d_lut_table);
+    cudaStreamDestroy(s->compute);
+    cudaStreamDestroy(s->copy);
+    delete s;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------- trace driver
+
+namespace {
+
+// Zipf(s) over ranks 0..n-1 by inverse CDF (ZipfDistribution, yatfhe/include/yautil/zipf.h:47-87):
+// harmonic normalisation, cumulative table with the last entry set to 1, lower_bound of a
+// uniform draw, ranks clamped to n-1.
+struct Zipf {
+    std::vector<double> cdf;
+    std::mt19937_64 gen;
+    std::uniform_real_distribution<double> uni{0.0, 1.0};
+    Zipf(double s, int n, uint64_t seed) : cdf(n), gen(seed) {
+        double h = 0;
+        for (int k = 1; k <= n; k++) h += 1.0 / std::pow(k, s);
+        double c = 0;
+        for (int r = 1; r <= n; r++) {
+            c += 1.0 / (std::pow(r, s) * h);
+            cdf[r - 1] = c;
+        }
+        cdf[n - 1] = 1.0;
+    }
+    int next() {
+        const double u = uni(gen);
+        int r = (int)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+        return std::min(r, (int)cdf.size() - 1);
+    }
+};
+
+yg_latency summarize(std::vector<double> v) {
+    yg_latency o{};
+    if (v.empty()) return o;
+    std::sort(v.begin(), v.end());
+    double sum = 0;
+    for (double x : v) sum += x;
+    auto pct = [&](double p) {
+        long i = (long)std::ceil(p / 100.0 * v.size()) - 1;
+        return v[std::min<long>(std::max<long>(i, 0), (long)v.size() - 1)];
+    };
+    o.mean_ms = sum / v.size();
+    o.p50_ms = pct(50);
+    o.p90_ms = pct(90);
+    o.p99_ms = pct(99);
+    o.p999_ms = pct(99.9);
+    o.max_ms = v.back();
+    return o;
+}
+
+}  // namespace
+
+extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_trace_result* out) {
+    if (!s || !cfg || !out || cfg->requests < 1 || cfg->warmup < 0 || cfg->rate <= 0 || cfg->tenants < 1 ||
+        cfg->max_count < 1 || cfg->max_count > s->cfg.max_batch || !cfg->h_pool)
+        return set_err(YG_ERR_INVALID, "yg_server_run_trace: bad arguments");
+    for (int t = 0; t < cfg->tenants; t++)
+        if (!s->tenants.count(t)) return set_err(YG_ERR_INVALID, "trace tenant not registered");
+    return guarded([&] {
+        yg::DeviceGuard g(s->ctx->device);
+        const int n1 = s->ctx->p.n + 1;
+        const size_t req_words = (size_t)cfg->max_count * n1;
+        const int total = cfg->warmup + cfg->requests;
+        // pinned output ring, one slot per request in flight
+        const int ring = 512;
+        int32_t* h_out = nullptr;
+        ck(cudaMallocHost(&h_out, (size_t)ring * req_words * 4), "output ring");
+        std::unique_ptr<int32_t, decltype(&cudaFreeHost)> ring_guard(h_out, &cudaFreeHost);
+        std::mutex fm;
+        std::condition_variable fcv;
+        std::deque<int> free_slots;
+        for (int i = 0; i < ring; i++) free_slots.push_back(i);
+
+        struct Issued {
+            int64_t id;
+            int slot, tenant, count;
+            bool measured;
+        };
+        std::mutex qm;
+        std::condition_variable qcv;
+        std::deque<Issued> issued;
+        bool producer_done = false;
+        std::atomic<int> shed{0};
+
+        if (int rc = yg_server_start(s)) return rc;
+        yg_server_counters before{};
+        yg_server_counters after{};
+        std::vector<double> soj, que, svc;
+        int mismatched = 0, served = 0;
+        double t_first = 0, t_last = 0;
+        int64_t measured_cts = 0;
+
+        std::thread producer([&] {
+            std::mt19937_64 arrivals(cfg->seed ^ 0x9e3779b97f4a7c15ULL);
+            std::exponential_distribution<double> gap(1.0);
+            std::mt19937_64 sizes(cfg->seed + 1);
+            std::uniform_real_distribution<double> lsz(0.0, std::log((double)cfg->max_count + 1.0));
+            Zipf zipf(cfg->zipf_s, cfg->tenants, cfg->zipf_seed);
+            const auto t0 = Clock::now();
+            double offset = 0;
+            for (int i = 0; i < total; i++) {
+                offset += gap(arrivals) / cfg->rate;
+                std::this_thread::sleep_until(t0 + std::chrono::duration_cast<Clock::duration>(
+                                                       std::chrono::duration<double>(offset)));
+                const int tenant = zipf.next();
+                const int count = std::min(cfg->max_count, std::max(1, (int)std::floor(std::exp(lsz(sizes)))));
+                if (cfg->queue_max > 0) {
+                    std::lock_guard<std::mutex> lk(qm);
+                    if ((int)issued.size() > cfg->queue_max) {
+                        shed++;
+                        continue;
+                    }
+                }
+                int slot;
+                {
+                    std::unique_lock<std::mutex> lk(fm);
+                    fcv.wait(lk, [&] { return !free_slots.empty(); });
+                    slot = free_slots.front();
+                    free_slots.pop_front();
+                }
+                const int32_t* in = cfg->h_pool + (size_t)tenant * req_words;
+                const int64_t id = yg_server_submit(s, tenant, in, h_out + (size_t)slot * req_words, count);
+                if (id <= 0) break;
+                std::lock_guard<std::mutex> lk(qm);
+                issued.push_back(Issued{id, slot, tenant, count, i >= cfg->warmup});
+                qcv.notify_all();
+            }
+            std::lock_guard<std::mutex> lk(qm);
+            producer_done = true;
+            qcv.notify_all();
+        });
+
+        int err = YG_OK;
+        for (;;) {
+            Issued it{};
+            {
+                std::unique_lock<std::mutex> lk(qm);
+                qcv.wait(lk, [&] { return !issued.empty() || producer_done; });
+                if (issued.empty()) break;
+                it = issued.front();
+                issued.pop_front();
+            }
+            yg_request_times tm{};
+            const int rc = yg_server_wait(s, it.id, 600000, &tm);
+            if (rc != YG_OK) {
+                err = rc;
+                break;
+            }
+            const int32_t* o = h_out + (size_t)it.slot * req_words;
+            if (cfg->h_expect &&
+                std::memcmp(o, cfg->h_expect + (size_t)it.tenant * req_words, (size_t)it.count * n1 * 4) != 0)
+                mismatched++;
+            if (it.measured) {
+                if (served == 0) {
+                    t_first = tm.t_submit;
+                    yg_server_stats(s, &before);
+                }
+                served++;
+                measured_cts += it.count;
+                t_last = std::max(t_last, tm.t_done);
+                soj.push_back(1e3 * (tm.t_done - tm.t_submit));
+                que.push_back(1e3 * (tm.t_start - tm.t_submit));
+                svc.push_back(1e3 * (tm.t_done - tm.t_start));
+            }
+            std::lock_guard<std::mutex> lk(fm);
+            free_slots.push_back(it.slot);
+            fcv.notify_all();
+        }
+        producer.join();
+        if (err != YG_OK) return err;
+        yg_server_stats(s, &after);
+        std::memset(out, 0, sizeof(*out));
+        out->served = served;
+        out->shed = shed.load();
+        out->mismatched_requests = mismatched;
+        out->seconds = t_last - t_first;
+        out->requests_per_s = out->seconds > 0 ? served / out->seconds : 0;
+        out->ciphertexts_per_s = out->seconds > 0 ? measured_cts / out->seconds : 0;
+        out->offered_rate = cfg->rate;
+        out->sojourn = summarize(soj);
+        out->queue = summarize(que);
+        out->service = summarize(svc);
+        out->key_hits = after.key_hits - before.key_hits;
+        out->key_misses = after.key_misses - before.key_misses;
+        out->refill_bytes = after.refill_bytes - before.refill_bytes;
+        out->batches = after.batches - before.batches;
+        const double lookups = (double)(out->key_hits + out->key_misses);
+        out->hit_rate = lookups > 0 ? out->key_hits / lookups : 0;
+        return YG_OK;
+    });
+}
