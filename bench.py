@@ -10,10 +10,13 @@ Printed JSON line (rank 0): value = whole-job bootstraps/s with inputs resident 
 host-buffer entry point (yg_pbs_host: pinned host -> device copy, bootstrap, copy back);
 roofline of the dominant kernel (blind rotation) against the measured 32-bit
 multiply-add rate; cpu_baseline = the CPU oracle on the host cores on a bounded sample,
-which also checks the sampled GPU outputs bit for bit.
+which also checks the sampled GPU outputs bit for bit.  Unless --no-extras, the line also
+carries the plain per-call form, a batch-size sweep and the other workloads under
+"workloads": the TORUS=56 set at 16,384 ciphertexts, the 32-tenant mixed-parameter batch
+in one CUDA graph, and the 128-tenant serving trace (p50/p99 at 50-100 % of peak).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--params t32_n1024|t56_n2048]
-                  [--count C] [--impl ours|reference]
+                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving]
 Multi-GPU: one process per GPU (torchrun); every rank bootstraps its own batch (weak
 scaling, no data-path collective).
 """
@@ -29,6 +32,7 @@ import subprocess
 import sys
 import threading
 import time
+import traceback
 from pathlib import Path
 
 import numpy as np
@@ -38,6 +42,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "bootstraps/s"
 L2_BYTES = 129 * 2**20
+FALLBACK_HBM_GBS = 6800.0
 
 
 def parse_args():
@@ -48,11 +53,14 @@ def parse_args():
     ap.add_argument("--params", default="t32_n1024")
     ap.add_argument("--count", type=int, default=0, help="ciphertexts per step (default 65536 / 16384)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip the per-call / batch-size sweep legs")
+    ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the per-call / sweep legs and other workloads")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="with --per-cta: persistent CTAs per SM (0 = off)")
     ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
+    ap.add_argument("--serving-requests", type=int, default=800, help="measured requests per offered rate")
+    ap.add_argument("--serving-fractions", default="0.5,0.6,0.7,0.8,0.9,1.0", help="offered rates / peak")
     return ap.parse_args()
 
 
@@ -60,18 +68,31 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def synthetic(p, count, seed):
-    """Seeded synthetic inputs with the shapes of a real key set: NTT-domain BSK words are
+def synthetic_keys(p, seed):
+    """Seeded synthetic keys with the shapes of a real key set: NTT-domain BSK words are
     uniform mod q (as a real key's are: its masks are sampled uniformly in that domain), KSK
-    and ciphertext words uniform mod 2^32 (as real masks are)."""
+    words uniform mod 2^32 (as real masks are)."""
     rng = np.random.default_rng(seed)
     bsk = rng.integers(0, p.q_ntt, size=p.bsk_ntt_words, dtype=np.uint64)
     ksk = rng.integers(-(1 << 31), 1 << 31, size=p.ksk_words, dtype=np.int64).astype(np.int32)
-    lwe = rng.integers(-(1 << 31), 1 << 31, size=(count, p.n + 1), dtype=np.int64).astype(np.int32)
+    return bsk, ksk
+
+
+def synthetic_lwe(p, count, seed):
+    """count LWE ciphertexts with uniform 32-bit words (what encryptions look like)."""
+    rng = np.random.default_rng(seed)
+    return rng.integers(-(1 << 31), 1 << 31, size=(count, p.n + 1), dtype=np.int64).astype(np.int32)
+
+
+def workload_lut(p, seed=5):
+    """TORUS=32: the sign bootstrap's constant test polynomial; TORUS=56: a random 4-bit
+    lookup table in the padded box layout (messages m in 0..15 -> LUT[m])."""
     from yatfhe_gb300 import lut as lutmod
 
-    lut = lutmod.sign_lut(p.N, p.torus_bits)
-    return bsk, ksk, lwe, lut
+    if p.torus_bits == 32:
+        return lutmod.sign_lut(p.N, p.torus_bits)
+    table = np.random.default_rng(seed).integers(0, 16, 16)
+    return lutmod.padded_message_lut(p.N, p.torus_bits, table)
 
 
 def ops_per_bootstrap(p):
@@ -83,6 +104,27 @@ def ops_per_bootstrap(p):
     M = p.n * (2 * L * (p.N // 2) * logN + 4 * L * p.N + 2 * (p.N // 2) * logN)
     ks = p.k * p.N * p.ks_level * (p.n + 1)
     return 9 * M, ks
+
+
+def zipf_counts(s: float, n: int, draws: int, seed: int) -> np.ndarray:
+    """Per-rank counts of `draws` Zipf(s) samples over n ranks, drawn by inverse CDF as the
+    reference's ZipfDistribution does (yatfhe/include/yautil/zipf.h:47-87: harmonic
+    normalisation, lower_bound of a uniform draw, rank clamped to n-1); numpy's generator
+    supplies the uniforms."""
+    k = np.arange(1, n + 1, dtype=np.float64)
+    w = k ** -s
+    cdf = np.cumsum(w / w.sum())
+    cdf[-1] = 1.0
+    u = np.random.default_rng(seed).random(draws)
+    r = np.minimum(np.searchsorted(cdf, u, side="left"), n - 1)
+    return np.bincount(r, minlength=n)
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        return json.loads(f.read_text())
+    return {}
 
 
 class ClockSampler:
@@ -170,6 +212,310 @@ def run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads):
     return out, sample / dt, dt
 
 
+def params_config(p) -> dict:
+    return {"n": p.n, "N": p.N, "k": p.k, "B": 1 << p.radix_bits, "l": p.l_approx, "ks_base": 1 << p.ks_radix_bits,
+            "ks_t": p.ks_level, "torus_bits": p.torus_bits}
+
+
+# ------------------------------------------------------------------------------ one key, one batch
+
+class BatchRun:
+    """One parameter set, one synthetic key, `count` resident ciphertexts; times the
+    blind-rotation(+extract) and key-switch launches of each step with CUDA events."""
+
+    def __init__(self, p, count, dev, seed, per_cta=0, ctas_per_sm=0, retune=False):
+        import torch
+
+        from yatfhe_gb300 import _lib, api
+
+        self.p, self.count, self.dev = p, count, dev
+        self.L = _lib.lib()
+        self.bsk, self.ksk = synthetic_keys(p, seed)
+        self.lwe = synthetic_lwe(p, count, seed + 1)
+        self.lut = workload_lut(p)
+        self.ctx = api.Context(p, dev)
+        t0 = time.perf_counter()
+        self.key = api.BootstrapKey.from_ntt_words(self.ctx, self.bsk).set_ksk(self.ksk)
+        self.key_upload_s = time.perf_counter() - t0
+        self.stream = torch.cuda.Stream(device=dev)
+        self.sh = ctypes.c_void_p(self.stream.cuda_stream)
+        self.d_in = torch.from_numpy(self.lwe).to(f"cuda:{dev}")
+        self.d_lut = torch.from_numpy(self.lut).to(f"cuda:{dev}")
+        if per_cta:
+            api.set_launch(self.ctx, per_cta, ctas_per_sm)
+            self.tuning = {"choice": {"per_cta": per_cta, "ctas_per_sm": ctas_per_sm}, "fixed": True}
+        else:
+            from yatfhe_gb300 import autotune
+
+            self.tuning = autotune.tune(self.ctx, self.key, self.d_lut, use_cache=not retune)
+        self.d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
+        self.d_out = torch.empty_like(self.d_in)
+        torch.cuda.synchronize(dev)
+
+    def step(self, ev=None):
+        from yatfhe_gb300 import _lib
+
+        if ev:
+            ev[0].record(self.stream)
+        _lib.check(self.L.yg_blind_rotate_extract(self.ctx.handle, self.key.handle, ctypes.c_void_p(self.d_in.data_ptr()),
+                                                  ctypes.c_void_p(self.d_lut.data_ptr()),
+                                                  ctypes.c_void_p(self.d_big.data_ptr()), self.count, self.sh))
+        if ev:
+            ev[1].record(self.stream)
+        _lib.check(self.L.yg_keyswitch(self.ctx.handle, self.key.handle, ctypes.c_void_p(self.d_big.data_ptr()),
+                                       ctypes.c_void_p(self.d_out.data_ptr()), self.count, self.sh))
+        if ev:
+            ev[2].record(self.stream)
+
+    def timed(self, steps, warmup, barrier=None, clocks=None):
+        import torch
+
+        for _ in range(warmup):
+            self.step()
+        self.stream.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if barrier:
+            barrier()
+        if clocks:
+            clocks.start()
+        start.record(self.stream)
+        for k in range(steps):
+            self.step(evs[k])
+        end.record(self.stream)
+        self.stream.synchronize()
+        if barrier:
+            barrier()
+        clock_info = clocks.stop() if clocks else None
+        return {"total_ms": start.elapsed_time(end), "br_ms": [e[0].elapsed_time(e[1]) for e in evs],
+                "ks_ms": [e[1].elapsed_time(e[2]) for e in evs], "clocks": clock_info}
+
+    def roofline(self, br_ms, int32_peak_tops, workload):
+        p = self.p
+        br_ops, _ = ops_per_bootstrap(p)
+        br_avg_s = statistics.mean(br_ms) / 1e3
+        achieved = br_ops * self.count / br_avg_s / 1e12
+        bsk_alg = p.n * p.l_approx * (p.k + 1) ** 2 * p.N * 8
+        io_alg = self.count * ((p.n + 1) + (p.k * p.N + 1)) * 4
+        hbm = measured_peaks().get("hbm_gbs", FALLBACK_HBM_GBS)
+        hbm_achieved = (bsk_alg + io_alg) / br_avg_s / 1e9
+        return {
+            "bound": "int32", "kernel": "blind_rotate_kernel", "achieved": achieved, "peak": int32_peak_tops,
+            "unit": "TOP/s", "frac": achieved / int32_peak_tops,
+            "peak_source": "measured: yg_probe_int32_rate (32-bit IMAD chains, all SMs)",
+            "ops_per_bootstrap": br_ops, "launch_ms": statistics.mean(br_ms),
+            "traffic": traffic_from_profiles("blind_rotate_kernel", workload),
+            "hbm_view": {"algorithmic_bytes_per_launch": bsk_alg + io_alg, "achieved_gbs": hbm_achieved,
+                         "peak_gbs": hbm, "frac": hbm_achieved / hbm,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if measured_peaks() else "fallback 6.8 TB/s"},
+        }
+
+
+def int32_peak(dev) -> float:
+    from yatfhe_gb300 import _lib
+
+    rate = ctypes.c_double()
+    _lib.check(_lib.lib().yg_probe_int32_rate(dev, ctypes.byref(rate)))
+    return rate.value / 1e12
+
+
+# ------------------------------------------------------------------------------ other workloads
+
+def leg_t56(dev, steps=2, warmup=1, count=16384):
+    """TORUS=56 set (n=750, N=2048, B=2^10, l=4, KS 2^3 x 10), 16,384 ciphertexts, random
+    4-bit LUT."""
+    from yatfhe_gb300.params import T56_N2048
+
+    run = BatchRun(T56_N2048, count, dev, seed=0x5EED0003)
+    t = run.timed(steps, warmup)
+    workload = f"t56_n2048_batch{count}"
+    return {"workload": workload, "params": params_config(T56_N2048), "ciphertexts_per_step": count,
+            "value": count * steps / (t["total_ms"] / 1e3), "unit": "bootstraps/s", "steps": steps,
+            "ms_per_step": t["total_ms"] / steps, "keyswitch_ms": statistics.mean(t["ks_ms"]),
+            "roofline": run.roofline(t["br_ms"], int32_peak(dev), workload), "launch_shape": run.tuning}
+
+
+def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
+    """32 tenants with their own keys: 24 on the TORUS=32 set, 8 on the TORUS=56 set;
+    per-tenant ciphertext counts from Zipf(1.1) over the 32 tenants (32,768 draws).  Each
+    parameter set is one multi-key plan (one blind-rotation + one key-switch launch over all
+    its tenants, launch shape from the autotuner); both plans run concurrently on two
+    streams inside ONE captured CUDA graph, and a step is one replay."""
+    import torch
+
+    from yatfhe_gb300 import api, autotune
+    from yatfhe_gb300.params import T32_N1024, T56_N2048
+
+    counts = zipf_counts(1.1, 32, total, 20260816)
+    groups = []
+    for p, tenants in ((T32_N1024, range(0, 24)), (T56_N2048, range(24, 32))):
+        ctx = api.Context(p, dev)
+        keys = []
+        for t in tenants:
+            bsk, ksk = synthetic_keys(p, 0x5EED1000 + t)
+            keys.append(api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk))
+        lut = torch.from_numpy(workload_lut(p)).to(f"cuda:{dev}")
+        tuning = autotune.tune(ctx, keys[0], lut)
+        key_ids = np.concatenate([np.full(counts[t], i, np.int32) for i, t in enumerate(tenants)])
+        n_ct = len(key_ids)
+        d_in = torch.from_numpy(synthetic_lwe(p, n_ct, 0x5EED1100 + p.torus_bits)).to(f"cuda:{dev}")
+        d_out = torch.empty_like(d_in)
+        plan = api.BatchPlan(ctx, keys, [lut], n_ct, key_ids=key_ids)
+        groups.append({"ctx": ctx, "keys": keys, "lut": lut, "plan": plan, "d_in": d_in, "d_out": d_out,
+                       "count": n_ct, "tenants": len(tenants), "tuning": tuning["choice"], "p": p})
+    s_main, s_side = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+
+    def launch_all():
+        cur = torch.cuda.current_stream(dev)
+        s_side.wait_stream(cur)
+        with torch.cuda.stream(s_side):
+            g = groups[1]
+            g["plan"].run(g["d_in"], g["d_out"], stream=s_side)
+        g = groups[0]
+        g["plan"].run(g["d_in"], g["d_out"], stream=cur)
+        cur.wait_stream(s_side)
+
+    with torch.cuda.stream(s_main):
+        launch_all()  # per-device kernel set-up happens outside the capture
+    torch.cuda.synchronize(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s_main):
+        launch_all()
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s_main):
+        a.record(s_main)
+        for _ in range(steps):
+            graph.replay()
+        b.record(s_main)
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / steps
+    # each parameter set alone (same plans, eager), to show what running them together buys
+    alone = {}
+    for g in groups:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s_main):
+            e0.record(s_main)
+            g["plan"].run(g["d_in"], g["d_out"], stream=s_main)
+            e1.record(s_main)
+        torch.cuda.synchronize(dev)
+        alone[f"t{g['p'].torus_bits}_ms"] = e0.elapsed_time(e1)
+    out = {"workload": "mixed_t32x24_t56x8_zipf32768", "value": total / (ms / 1e3), "unit": "bootstraps/s",
+           "steps": steps, "ms_per_step": ms, "graph": "one CUDA graph, 2 streams, 4 kernel launches per replay",
+           "alone_ms": alone,
+           "sets": [{"torus_bits": g["p"].torus_bits, "tenants": g["tenants"], "ciphertexts": g["count"],
+                     "launch_shape": g["tuning"]} for g in groups],
+           "tenant_counts": counts.tolist()}
+    for g in groups:
+        g["plan"].close()
+        for k in g["keys"]:
+            k.close()
+    return out
+
+
+def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), tenants=128, budget=4e9,
+                max_count=256, max_batch=2048, max_inflight=3):
+    """128 tenants on the TORUS=32 set, requests of 1..256 ciphertexts (log-uniform) arriving
+    as a Poisson process, tenants Zipf(1.1)-popular, BSK/KSK in an HBM LRU cache capped at
+    4 GB with refills from pinned host memory.  First the peak rate is measured with the
+    offered load far above capacity, then each fraction of it is offered; every output is
+    compared with the same tenant's ciphertexts bootstrapped alone."""
+    import torch
+
+    from yatfhe_gb300 import api, autotune, serving
+    from yatfhe_gb300.params import T32_N1024
+
+    p = T32_N1024
+    ctx = api.Context(p, dev)
+    lut_np = workload_lut(p)
+    d_lut = torch.from_numpy(lut_np).to(f"cuda:{dev}")
+    pool = torch.empty((tenants, max_count, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    srv = None
+    t_setup = time.perf_counter()
+    for t in range(tenants):
+        bsk, ksk = synthetic_keys(p, 0x5EED2000 + t)
+        key = api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk)
+        if srv is None:
+            autotune.tune(ctx, key, d_lut)
+            srv = serving.Server(ctx, key_budget_bytes=budget, max_batch=max_batch, max_inflight=max_inflight,
+                                 max_tenants=tenants)
+        lwe = synthetic_lwe(p, max_count, 0x5EED3000 + t)
+        pool[t] = torch.from_numpy(lwe)
+        d_in = pool[t].to(f"cuda:{dev}")
+        expect[t] = api.functional_bootstrapping_mp_ntt(ctx, key, d_in, d_lut).cpu()
+        srv.add_tenant(t, key, lut_np)
+        key.close()  # the server keeps its own pinned-host image; HBM holds only the cache
+    setup_s = time.perf_counter() - t_setup
+    srv.start()
+    slots = srv.counters()["key_slots"]
+    peak = srv.run_trace(pool, expect, requests=max(requests, 1000), warmup=100, rate=1e6, seed=11,
+                         max_count=max_count)
+    peak_rps = peak["requests_per_s"]
+    points = []
+    mismatches = peak["mismatched_requests"]
+    for i, f in enumerate(fractions):
+        r = srv.run_trace(pool, expect, requests=requests, warmup=100, rate=f * peak_rps, seed=100 + i,
+                          max_count=max_count)
+        mismatches += r["mismatched_requests"]
+        points.append({"fraction_of_peak": f, "offered_rps": r["offered_rate"], "served": r["served"],
+                       "requests_per_s": r["requests_per_s"], "bootstraps_per_s": r["ciphertexts_per_s"],
+                       "p50_ms": r["sojourn"]["p50_ms"], "p99_ms": r["sojourn"]["p99_ms"],
+                       "queue_p99_ms": r["queue"]["p99_ms"], "service_p50_ms": r["service"]["p50_ms"],
+                       "hit_rate": r["hit_rate"], "key_misses": r["key_misses"], "batches": r["batches"]})
+    srv.close()
+    at80 = min(points, key=lambda q: abs(q["fraction_of_peak"] - 0.8)) if points else None
+    return {"workload": "serving_t32_128tenants_4GB", "tenants": tenants, "key_budget_bytes": int(budget),
+            "key_slots": slots, "resident_fraction": slots / tenants, "max_batch": max_batch,
+            "max_inflight": max_inflight, "request_sizes": f"floor(exp(U(0, ln {max_count + 1}))), 1..{max_count}",
+            "peak": {"requests_per_s": peak_rps, "bootstraps_per_s": peak["ciphertexts_per_s"],
+                     "p50_ms": peak["sojourn"]["p50_ms"], "p99_ms": peak["sojourn"]["p99_ms"],
+                     "hit_rate": peak["hit_rate"]},
+            "points": points, "at_80pct": at80, "mismatched_requests": mismatches,
+            "bit_exact_vs_alone": mismatches == 0, "setup_s": setup_s}
+
+
+# ------------------------------------------------------------------------------ reference arm
+
+def reference_arm(args, p, config, threads):
+    """The reference's CPU path (the oracle's plain-C restatement of
+    functionalBootstrappingMPNtt, pinned bit-exact against the reference's own sources) on
+    all host threads, a bounded sample of the workload per step."""
+    bsk, ksk = synthetic_keys(p, 1234)
+    lwe = synthetic_lwe(p, max(64, threads * 32), 1235)
+    lut = workload_lut(p)
+    sample = args.cpu_sample or max(16, threads * 32)  # a few seconds of CPU work per step
+    for _ in range(args.warmup):
+        run_cpu_baseline(p, bsk, ksk, lwe, lut, min(sample, threads), threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads)
+    wall = time.perf_counter() - t0
+    v = args.steps * sample / wall
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "bootstraps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64 torus",
+        "data": "synthetic", "config": dict(config, cpu_sample_per_step=sample),
+        "cpu_baseline": {"value": v, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} ciphertexts per step of the same workload, plain-C restatement "
+                                   f"of functionalBootstrappingMPNtt, {threads} threads"},
+        "e2e": {"value": v, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def _safe(fn, *a, **kw):
+    t0 = time.perf_counter()
+    try:
+        r = fn(*a, **kw)
+    except Exception as e:  # a failing extra leg is reported, the headline line still prints
+        r = {"error": f"{type(e).__name__}: {e}", "trace": traceback.format_exc(limit=3)}
+    r["leg_seconds"] = time.perf_counter() - t0
+    return r
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -178,87 +524,22 @@ def main():
     p = PARAM_SETS[args.params]
     count = args.count or (65536 if p.torus_bits == 32 else 16384)
     workload = f"{args.params}_batch{count}"
-    config = {"workload": workload, "params": {"n": p.n, "N": p.N, "k": p.k, "B": 1 << p.radix_bits,
-                                                 "l": p.l_approx, "ks_base": 1 << p.ks_radix_bits,
-                                                 "ks_t": p.ks_level, "torus_bits": p.torus_bits},
-              "ciphertexts_per_step": count, "per_rank": True}
+    config = {"workload": workload, "params": params_config(p), "ciphertexts_per_step": count, "per_rank": True}
     threads = cpu_threads()
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        bsk, ksk, lwe, lut = synthetic(p, max(64, threads * 4), 1234)
-        sample = args.cpu_sample or max(16, threads * 2)
-        for _ in range(args.warmup):
-            run_cpu_baseline(p, bsk, ksk, lwe, lut, min(sample, threads), threads)
-        rates = []
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            _, r, _ = run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads)
-            rates.append(r)
-        wall = time.perf_counter() - t0
-        v = args.steps * sample / wall
-        print(json.dumps({
-            "impl": "reference", "metric": METRIC, "value": v, "unit": "bootstraps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64 torus",
-            "data": "synthetic", "config": dict(config, cpu_sample_per_step=sample),
-            "cpu_baseline": {"value": v, "unit": "bootstraps/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} ciphertexts per step of the same workload, plain-C restatement "
-                                       f"of functionalBootstrappingMPNtt, {threads} threads"},
-            "e2e": {"value": v, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }))
+        if rank == 0:
+            reference_arm(args, p, config, threads)
         return
 
     import torch
-
-    from yatfhe_gb300 import _lib, api
 
     dev = local
     torch.cuda.set_device(dev)
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    L = _lib.lib()
-
-    bsk, ksk, lwe, lut = synthetic(p, count, 1234 + rank)
-    ctx = api.Context(p, dev)
-    t_key = time.perf_counter()
-    key = api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk)
-    key_upload_s = time.perf_counter() - t_key
-
-    stream = torch.cuda.Stream()
-    sh = ctypes.c_void_p(stream.cuda_stream)
-    d_in = torch.from_numpy(lwe).to(f"cuda:{dev}")
-    d_lut = torch.from_numpy(lut).to(f"cuda:{dev}")
-    if args.per_cta:
-        api.set_launch(ctx, args.per_cta, args.ctas_per_sm)
-        tuning = {"choice": {"per_cta": args.per_cta, "ctas_per_sm": args.ctas_per_sm}, "fixed": True}
-    else:
-        from yatfhe_gb300 import autotune
-
-        tuning = autotune.tune(ctx, key, d_lut, use_cache=not args.retune)
-    d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
-    d_out = torch.empty_like(d_in)
-    torch.cuda.synchronize()
-
-    def step(ev=None):
-        if ev:
-            ev[0].record(stream)
-        _lib.check(L.yg_blind_rotate_extract(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
-                                             ctypes.c_void_p(d_lut.data_ptr()), ctypes.c_void_p(d_big.data_ptr()),
-                                             count, sh))
-        if ev:
-            ev[1].record(stream)
-        _lib.check(L.yg_keyswitch(ctx.handle, key.handle, ctypes.c_void_p(d_big.data_ptr()),
-                                  ctypes.c_void_p(d_out.data_ptr()), count, sh))
-        if ev:
-            ev[2].record(stream)
-
-    for _ in range(args.warmup):
-        step()
-    stream.synchronize()
+        dist.init_process_group("nccl")
 
     def barrier():
         if world > 1:
@@ -267,37 +548,50 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    clocks = ClockSampler(dev)
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    clocks.start()
-    start.record(stream)
-    for k in range(args.steps):
-        step(evs[k])
-    end.record(stream)
-    stream.synchronize()
-    barrier()
-    clock_info = clocks.stop()
-    total_ms = start.elapsed_time(end)
-    br_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    ks_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if args.workload != "batch":
+        if rank != 0:
+            return
+        if args.workload == "multi_tenant":
+            r = leg_multi_tenant(dev, steps=args.steps, warmup=args.warmup)
+            line = {"metric": METRIC, "value": r["value"], "unit": "bootstraps/s", "n_gpus": 1,
+                    "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "int32 torus / u32 RNS", "data": "synthetic",
+                    "config": {"workload": r["workload"]}, "result": r}
+        else:
+            fr = tuple(float(x) for x in args.serving_fractions.split(","))
+            r = leg_serving(dev, requests=args.serving_requests, fractions=fr)
+            a80 = r["at_80pct"] or {}
+            line = {"metric": "serving p99 sojourn at 80% of peak", "value": a80.get("p99_ms"), "unit": "ms",
+                    "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "int32 torus / u32 RNS", "data": "synthetic",
+                    "config": {"workload": r["workload"]}, "result": r}
+        print(json.dumps(line))
+        return
+
+    run = BatchRun(p, count, dev, seed=1234 + rank, per_cta=args.per_cta, ctas_per_sm=args.ctas_per_sm,
+                   retune=args.retune)
+    t = run.timed(args.steps, args.warmup, barrier=barrier, clocks=ClockSampler(dev))
+    total_ms = t["total_ms"]
     if world > 1:
         import torch.distributed as dist
 
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        tt = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
     value = world * count * args.steps / (total_ms / 1e3)
 
     # end to end through the host-buffer entry point, pinned buffers
-    h_in = torch.from_numpy(lwe).pin_memory()
+    L = run.L
+    from yatfhe_gb300 import _lib
+
+    h_in = torch.from_numpy(run.lwe).pin_memory()
     h_out = torch.empty_like(h_in).pin_memory()
-    h_lut = torch.from_numpy(lut).pin_memory()
+    h_lut = torch.from_numpy(run.lut).pin_memory()
 
     def e2e_step():
-        _lib.check(L.yg_pbs_host(ctx.handle, key.handle, ctypes.c_void_p(h_in.data_ptr()),
-                                 ctypes.c_void_p(h_out.data_ptr()), count, ctypes.c_void_p(h_lut.data_ptr()), sh))
+        _lib.check(L.yg_pbs_host(run.ctx.handle, run.key.handle, ctypes.c_void_p(h_in.data_ptr()),
+                                 ctypes.c_void_p(h_out.data_ptr()), count, ctypes.c_void_p(h_lut.data_ptr()), run.sh))
 
     e2e_step()
     barrier()
@@ -307,71 +601,67 @@ def main():
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * count * args.steps / e2e_s
-    if not torch.equal(h_out, d_out.cpu()):
+    if not torch.equal(h_out, run.d_out.cpu()):
         raise SystemExit("host-buffer and device-buffer entry points disagree")
 
     if rank != 0:
         return
 
-    # roofline of the dominant kernel (blind rotation + extract), against the measured
-    # 32-bit multiply-add rate of this GPU
-    rate = ctypes.c_double()
-    _lib.check(L.yg_probe_int32_rate(dev, ctypes.byref(rate)))
-    br_ops, ks_ops = ops_per_bootstrap(p)
-    br_avg_s = statistics.mean(br_ms) / 1e3
-    achieved = br_ops * count / br_avg_s / 1e12
-    peak = rate.value / 1e12
-    bsk_alg = p.n * p.l_approx * (p.k + 1) ** 2 * p.N * 8
-    io_alg = count * ((p.n + 1) + (p.k * p.N + 1)) * 4
-    hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"] if (
-        ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
-    hbm_achieved = (bsk_alg + io_alg) / br_avg_s / 1e9
-    roofline = {
-        "bound": "int32", "kernel": "blind_rotate_kernel", "achieved": achieved, "peak": peak, "unit": "TOP/s",
-        "frac": achieved / peak, "peak_source": "measured: yg_probe_int32_rate (32-bit IMAD chains, all SMs)",
-        "ops_per_bootstrap": br_ops, "launch_ms": statistics.mean(br_ms),
-        "traffic": traffic_from_profiles("blind_rotate_kernel", workload),
-        "hbm_view": {"algorithmic_bytes_per_launch": bsk_alg + io_alg, "achieved_gbs": hbm_achieved,
-                     "peak_gbs": hbm, "frac": hbm_achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-        "keyswitch_ms": statistics.mean(ks_ms),
-    }
+    roofline = run.roofline(t["br_ms"], int32_peak(dev), workload)
+    roofline["keyswitch_ms"] = statistics.mean(t["ks_ms"])
 
     extras = {}
     if not args.no_extras:
+        d_in, d_out, d_lut, sh = run.d_in, run.d_out, run.d_lut, run.sh
         # plain per-call form: one ciphertext per launch
         one_in, one_out = d_in[:1], d_out[:1]
+
+        def pbs(src, dst, n):
+            _lib.check(L.yg_pbs(run.ctx.handle, run.key.handle, ctypes.c_void_p(src.data_ptr()),
+                                ctypes.c_void_p(dst.data_ptr()), n, ctypes.c_void_p(d_lut.data_ptr()), sh))
+
         for _ in range(3):
-            _lib.check(L.yg_pbs(ctx.handle, key.handle, ctypes.c_void_p(one_in.data_ptr()),
-                                ctypes.c_void_p(one_out.data_ptr()), 1, ctypes.c_void_p(d_lut.data_ptr()), sh))
-        stream.synchronize()
+            pbs(one_in, one_out, 1)
+        run.stream.synchronize()
         reps = 20
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
+        a.record(run.stream)
         for _ in range(reps):
-            _lib.check(L.yg_pbs(ctx.handle, key.handle, ctypes.c_void_p(one_in.data_ptr()),
-                                ctypes.c_void_p(one_out.data_ptr()), 1, ctypes.c_void_p(d_lut.data_ptr()), sh))
-        b.record(stream)
-        stream.synchronize()
+            pbs(one_in, one_out, 1)
+        b.record(run.stream)
+        run.stream.synchronize()
         extras["plain_per_call_bps"] = reps / (a.elapsed_time(b) / 1e3)
+        extras["plain_per_call_latency_ms"] = a.elapsed_time(b) / reps
         sweep = {}
         for bs in (1, 64, 1024):
             if bs > count:
                 continue
-            a.record(stream)
+            a.record(run.stream)
             for _ in range(2):
-                _lib.check(L.yg_pbs(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
-                                    ctypes.c_void_p(d_out.data_ptr()), bs, ctypes.c_void_p(d_lut.data_ptr()), sh))
-            b.record(stream)
-            stream.synchronize()
+                pbs(d_in, d_out, bs)
+            b.record(run.stream)
+            run.stream.synchronize()
             sweep[str(bs)] = 2 * bs / (a.elapsed_time(b) / 1e3)
         sweep[str(count)] = value / world
         extras["batch_sweep_bps"] = sweep
         extras["batched_over_plain"] = value / world / extras["plain_per_call_bps"]
 
-    # CPU baseline on a bounded sample (oracle on the host cores), also the bit-exact check
-    sample = args.cpu_sample or max(16, threads * 4)
-    cpu_out, cpu_bps, cpu_s = run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads)
-    bit_exact = bool(np.array_equal(cpu_out, d_out[:sample].cpu().numpy()))
+    # CPU baseline on a bounded sample (oracle on the host cores), also the bit-exact check;
+    # the step's outputs are recomputed first (the sweep above overwrote part of them)
+    run.step()
+    run.stream.synchronize()
+    sample = args.cpu_sample or max(16, threads * 48)  # about 10 s of CPU work
+    cpu_out, cpu_bps, cpu_s = run_cpu_baseline(p, run.bsk, run.ksk, run.lwe, run.lut, sample, threads)
+    bit_exact = bool(np.array_equal(cpu_out, run.d_out[:sample].cpu().numpy()))
+
+    if not args.no_extras:
+        extras["workloads"] = {
+            "t56_n2048_batch16384": _safe(leg_t56, dev),
+            "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
+            "serving_t32_128tenants_4GB": _safe(
+                leg_serving, dev, requests=args.serving_requests,
+                fractions=tuple(float(x) for x in args.serving_fractions.split(","))),
+        }
 
     line = {
         "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": world, "steps": args.steps,
@@ -380,7 +670,7 @@ def main():
         "config": dict(config, l2="inputs larger than L2 (%.0f MB in + %.0f MB extract per step > %d MB)"
                        % (count * (p.n + 1) * 4 / 1e6, count * (p.N + 1) * 4 / 1e6, L2_BYTES // 2**20),
                        parallelism=f"replicas x{world}"),
-        "clocks": clock_info,
+        "clocks": t["clocks"],
         "e2e": {"value": e2e_value, "unit": "bootstraps/s", "h2d_bytes_per_step": count * (p.n + 1) * 4 + p.N * 8,
                 "d2h_bytes_per_step": count * (p.n + 1) * 4, "entry_point": "yg_pbs_host"},
         "gpu_launches": 2 * args.steps,
@@ -389,9 +679,9 @@ def main():
                          "sample": f"{sample} of the step's ciphertexts, plain-C restatement of "
                                    f"functionalBootstrappingMPNtt on {threads} threads ({cpu_s:.1f} s)"},
         "bit_exact_vs_oracle_sample": bit_exact,
-        "key_upload_s": key_upload_s,
-        "launch_shape": tuning,
-        "key_device_bytes": key.device_bytes,
+        "key_upload_s": run.key_upload_s,
+        "launch_shape": run.tuning,
+        "key_device_bytes": run.key.device_bytes,
     }
     line.update(extras)
     print(json.dumps(line))

@@ -10,13 +10,14 @@
 //
 // GPU design.  One worker thread owns the device.  Tenant keys are kept, already in the
 // device layout, in pinned host memory; HBM holds `slots` of them (budget / key bytes),
-// refilled on a miss by cudaMemcpyAsync on a copy stream, with an event the compute stream
+// refilled on a miss by cudaMemcpyAsync on a copy stream, with an event the batch's stream
 // waits on.  The worker admits pending requests into a batch (up to max_batch ciphertexts)
 // as long as their keys are resident or can be brought in (an LRU slot whose tenant has no
 // batch in flight), groups the batch by tenant, and launches the multi-key blind rotation
-// and key switch.  Up to max_inflight batches are queued on the GPU at once, so requests
-// that arrive while one runs are admitted into the next (continuous batching).  Batch
-// completion is signalled by a host callback on the compute stream.
+// and key switch.  Up to max_inflight batches are on the GPU at once, each on its own
+// stream, so requests that arrive while one runs are admitted into the next (continuous
+// batching) and the next batch fills the SMs the previous one's last wave leaves idle.
+// Batch completion is signalled by a host callback on the batch's stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -69,6 +70,7 @@ struct Tenant {
 };
 
 struct Batch {
+    cudaStream_t stream = nullptr;  // batches in flight run on their own streams and overlap
     int32_t* d_in = nullptr;
     int32_t* d_out = nullptr;
     int32_t* d_big = nullptr;
@@ -99,7 +101,7 @@ struct yg_server {
     const int64_t** d_lut_table = nullptr;
     std::map<int, std::unique_ptr<Tenant>> tenants;
     std::vector<Tenant*> by_index;
-    cudaStream_t compute = nullptr, copy = nullptr;
+    cudaStream_t copy = nullptr;
     std::vector<std::unique_ptr<Batch>> batches;
 
     std::mutex mu;
@@ -132,6 +134,8 @@ void CUDART_CB batch_done_cb(void* p) {
 }
 
 void free_batch(Batch* b) {
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->stream) cudaStreamDestroy(b->stream);
     cudaFree(b->d_in);
     cudaFree(b->d_out);
     cudaFree(b->d_big);
@@ -224,7 +228,7 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
         Tenant* t = s->tenants[r->tenant].get();
         r->t_start = t0;
         ck(cudaMemcpyAsync(b->d_in + (size_t)off * n1, r->h_in, (size_t)r->count * n1 * 4, cudaMemcpyHostToDevice,
-                           s->compute),
+                           b->stream),
            "copy in");
         for (int c = 0; c < r->count; c++) {
             b->h_key_of[off + c] = t->slot;
@@ -238,11 +242,11 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
         b->h_tiles[ntiles++] = yg::KsTile{c, e - c, s->slot_ksk[b->h_key_of[c]]};
         c = e;
     }
-    ck(cudaMemcpyAsync(b->d_key_of, b->h_key_of, (size_t)total * 4, cudaMemcpyHostToDevice, s->compute), "tables");
-    ck(cudaMemcpyAsync(b->d_lut_of, b->h_lut_of, (size_t)total * 4, cudaMemcpyHostToDevice, s->compute), "tables");
-    ck(cudaMemcpyAsync(b->d_tiles, b->h_tiles, (size_t)ntiles * sizeof(yg::KsTile), cudaMemcpyHostToDevice, s->compute),
+    ck(cudaMemcpyAsync(b->d_key_of, b->h_key_of, (size_t)total * 4, cudaMemcpyHostToDevice, b->stream), "tables");
+    ck(cudaMemcpyAsync(b->d_lut_of, b->h_lut_of, (size_t)total * 4, cudaMemcpyHostToDevice, b->stream), "tables");
+    ck(cudaMemcpyAsync(b->d_tiles, b->h_tiles, (size_t)ntiles * sizeof(yg::KsTile), cudaMemcpyHostToDevice, b->stream),
        "tables");
-    for (Tenant* t : used) ck(cudaStreamWaitEvent(s->compute, t->ready, 0), "wait refill");
+    for (Tenant* t : used) ck(cudaStreamWaitEvent(b->stream, t->ready, 0), "wait refill");
     yg::BrArgs a = yg::br_args(s->ctx, nullptr);
     a.key = nullptr;
     a.key_table = s->d_slot_table;
@@ -252,13 +256,13 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     a.lwe_in = b->d_in;
     a.big_out = b->d_big;
     a.count = total;
-    yg::check_launch(yg::launch_blind_rotate(s->ctx->logN, p.torus_bits, a, s->compute), "blind rotate launch");
+    yg::check_launch(yg::launch_blind_rotate(s->ctx->logN, p.torus_bits, a, b->stream), "blind rotate launch");
     yg::KsArgs k{b->d_big, nullptr, b->d_out, total, kN, p.n, p.ks_level, p.ks_radix_bits, b->d_tiles, ntiles};
-    yg::check_launch(yg::launch_keyswitch(k, s->compute), "keyswitch launch");
+    yg::check_launch(yg::launch_keyswitch(k, b->stream), "keyswitch launch");
     off = 0;
     for (Request* r : take) {
         ck(cudaMemcpyAsync(r->h_out, b->d_out + (size_t)off * n1, (size_t)r->count * n1 * 4, cudaMemcpyDeviceToHost,
-                           s->compute),
+                           b->stream),
            "copy out");
         off += r->count;
     }
@@ -266,7 +270,7 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     b->tenants = std::move(used);
     b->busy = true;
     b->finished.store(false);
-    ck(cudaLaunchHostFunc(s->compute, batch_done_cb, b), "completion callback");
+    ck(cudaLaunchHostFunc(b->stream, batch_done_cb, b), "completion callback");
     s->batches_run++;
     return true;
 }
@@ -332,7 +336,6 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
             cudaFree(s->d_slot_table);
             cudaFree(s->d_lut_table);
             for (auto& b : s->batches) free_batch(b.get());
-            if (s->compute) cudaStreamDestroy(s->compute);
             if (s->copy) cudaStreamDestroy(s->copy);
         };
         try {
@@ -351,12 +354,12 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
             ck(cudaMemcpy(s->d_slot_table, table.data(), table.size() * sizeof(void*), cudaMemcpyHostToDevice),
                "slot table");
             ck(cudaMalloc(&s->d_lut_table, (size_t)cfg->max_tenants * sizeof(void*)), "LUT table");
-            ck(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "stream");
             ck(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "stream");
             const int n1 = p.n + 1, big = p.k * p.N + 1, mb = cfg->max_batch;
             for (int i = 0; i < cfg->max_inflight; i++) {
                 auto b = std::make_unique<Batch>();
                 b->server = s.get();
+                ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
                 ck(cudaMalloc(&b->d_in, (size_t)mb * n1 * 4), "batch buffer");
                 ck(cudaMalloc(&b->d_out, (size_t)mb * n1 * 4), "batch buffer");
                 ck(cudaMalloc(&b->d_big, (size_t)mb * big * 4), "batch buffer");
@@ -482,7 +485,6 @@ void yg_server_destroy(yg_server* s) {
     }
     if (s->worker.joinable()) s->worker.join();
     yg::DeviceGuard g(s->ctx->device);
-    cudaStreamSynchronize(s->compute);
     cudaStreamSynchronize(s->copy);
     for (auto& b : s->batches) free_batch(b.get());
     for (auto& kv : s->tenants) {
@@ -496,7 +498,6 @@ void yg_server_destroy(yg_server* s) {
     for (auto* k : s->slot_ksk) cudaFree(k);
     cudaFree(s->d_slot_table);
     cudaFree(s->d_lut_table);
-    cudaStreamDestroy(s->compute);
     cudaStreamDestroy(s->copy);
     delete s;
 }
