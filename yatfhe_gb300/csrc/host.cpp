@@ -80,6 +80,20 @@ u64 minimal_root(u64 N, u64 m) {
 
 uint32_t shoup32(uint32_t w, uint32_t p) { return (uint32_t)(((u64)w << 32) / p); }
 
+// Reorders one twiddle table (N entries, index order psi^brv(k)) into the layout the team
+// NTT reads (ntt.cuh): the per-thread entries of each slot-layout stage, 2^(9-sp) + gid K + k
+// with K = 2^(4-sp), move to 2^(9-sp) + k 32 + gid; at N = 2048 the index-bit-0 stage's
+// 1024 + gid 32 + r moves to 1024 + r 32 + gid.  Entries 0..31 stay.
+void thread_minor_layout(uint2* t, int N) {
+    std::vector<uint2> src(t, t + N);
+    auto region = [&](int base, int K) {
+        for (int gid = 0; gid < 32; gid++)
+            for (int k = 0; k < K; k++) t[base + k * 32 + gid] = src[base + gid * K + k];
+    };
+    for (int sp = 0; sp <= 4; sp++) region(1 << (9 - sp), 1 << (4 - sp));
+    if (N == 2048) region(1024, 32);
+}
+
 }  // namespace
 
 namespace yg {
@@ -168,6 +182,8 @@ void ctx_init_tables(yg_ctx* c) {
             tw[((size_t)ci * 2 + 0) * N + k] = make_uint2(wf, shoup32(wf, p));
             tw[((size_t)ci * 2 + 1) * N + k] = make_uint2(wi, shoup32(wi, p));
         }
+        thread_minor_layout(&tw[((size_t)ci * 2 + 0) * N], N);
+        thread_minor_layout(&tw[((size_t)ci * 2 + 1) * N], N);
         // Montgomery form with N^-1 folded in: N^-1 2^32 mod p
         const uint32_t sc = (uint32_t)mulmod(invmod(N, p), ((u64)1 << 32) % p, p);
         c->conv_scale[ci] = sc;

@@ -4,7 +4,13 @@
 // Forward transform = Cooley-Tukey with psi^brv(k) twiddles (output in bit-reversed
 // slots), inverse = Gentleman-Sande with psi^-brv(k) (bit-reversed in, natural out,
 // NOT scaled by N^-1: that factor is folded into the stored key).  For a stage on index
-// bit s the twiddle is tw[2^(logN-1-s) + (j >> (s+1))].
+// bit s the twiddle is psi^brv(2^(logN-1-s) + (j >> (s+1))).  The tables keep that index
+// for the stages on the top five bits (the first 32 entries, also in __constant__), but
+// store the per-thread twiddles of the other stages stage by stage with the thread's
+// group index fastest: entry (gid, k) of the stage whose natural entries are
+// 2^(9-sp) + gid K + k (K = 2^(4-sp) per thread) sits at 2^(9-sp) + k 32 + gid, and at
+// N = 2048 the index-bit-0 stage's entry 1024 + gid 32 + r sits at 1024 + r 32 + gid.  A
+// warp's twiddle load then reads one contiguous run of 256 bytes instead of 32 lines.
 //
 // Layouts (tt = thread index in the team, S = N/32 threads):
 //   natural : register r holds coefficient j = r*S + tt           (the 5 top index bits)
@@ -79,19 +85,19 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
     for (int sp = 4; sp >= 0; --sp) {
         const int h = 1 << sp;
-        const uint2* tw = ch.twf + (1 << (9 - sp)) + gid * (1 << (4 - sp));
+        const uint2* tw = ch.twf + (1 << (9 - sp)) + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p, (sp & 1) == 0);
+            ct_bfly(a[r], a[r + h], __ldg(&tw[(r >> (sp + 1)) * 32]), p, two_p, (sp & 1) == 0);
         }
     }
     if constexpr (LOGN == 11) {
         const bool odd = tt & 1;
-        const uint2* tw = ch.twf + 1024 + gid * 32;
+        const uint2* tw = ch.twf + 1024 + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
-            const uint2 w = __ldg(&tw[r]);
+            const uint2 w = __ldg(&tw[r * 32]);
             const uint32_t xr = reduce_once(a[r], 2 * two_p);  // U (< 4p), held by the even lane
             const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
             const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
@@ -107,10 +113,10 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
     const int gid = LOGN == 10 ? tt : (tt >> 1);
     if constexpr (LOGN == 11) {
         const bool odd = tt & 1;
-        const uint2* tw = ch.twi + 1024 + gid * 32;
+        const uint2* tw = ch.twi + 1024 + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
-            const uint2 w = __ldg(&tw[r]);
+            const uint2 w = __ldg(&tw[r * 32]);
             const uint32_t mine = a[r];
             const uint32_t other = __shfl_xor_sync(0xffffffffu, mine, 1);
             const uint32_t s = mine + other;
@@ -121,11 +127,11 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
     for (int sp = 0; sp <= 4; ++sp) {
         const int h = 1 << sp;
-        const uint2* tw = ch.twi + (1 << (9 - sp)) + gid * (1 << (4 - sp));
+        const uint2* tw = ch.twi + (1 << (9 - sp)) + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            gs_bfly(a[r], a[r + h], __ldg(&tw[r >> (sp + 1)]), p, two_p);
+            gs_bfly(a[r], a[r + h], __ldg(&tw[(r >> (sp + 1)) * 32]), p, two_p);
         }
     }
     team_sync<LOGN>(bar);

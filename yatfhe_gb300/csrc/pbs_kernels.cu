@@ -163,8 +163,11 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
     unsigned char* base = smem + (size_t)g * br_smem_bytes(LOGN, T, n, L);
     uint32_t* xb = reinterpret_cast<uint32_t*>(base);                           // [3][2][TBUF]
     TorusT* acc = reinterpret_cast<TorusT*>(xb + kChannels * 2 * Sh::TBUF);    // [2][N]
-    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [2][L][N]
-    int16_t* sa = dig + 2 * L * N;                                               // [n+1]
+    // digit rows decomposed per phase: both at T = 32; one at a time at T = 56, where the
+    // halved digit buffer lets two ciphertext slices share an SM
+    constexpr int DROWS = digit_rows(T);
+    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [DROWS][L][N]
+    int16_t* sa = dig + DROWS * L * N;                                           // [n+1]
     uint32_t* mine = xb + team * 2 * Sh::TBUF;
 
     // G ciphertexts per iteration; a grid smaller than the batch makes the CTAs persistent
@@ -211,57 +214,75 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
         // one ciphertext per CTA the whole step is skipped, otherwise only its work
         if (G == 1 && ai == 0) continue;
         const bool active = ai != 0;
-        // tmp = X^{a_i} acc - acc (rotateTrlweMinusOne, yatfhe/src/trlwe.cpp:284-289), then
-        // gadgetDecomposeTrlwe (yatfhe/src/trlwe.cpp:185-198) into int16 digits
-        if (active) {
-            const int t2 = ai < 0 ? ai + 2 * N : ai;
-            const bool wrap = t2 >= N;
-            const int at = wrap ? t2 - N : t2;
+        const int t2 = ai < 0 ? ai + 2 * N : ai;
+        const bool wrap = t2 >= N;
+        const int at = wrap ? t2 - N : t2;
+        // externalProductTrgswMPNttImpl (yatfhe/src/trgsw.cpp:712-767) in channel `team`:
+        // forward NTT of every digit poly, Montgomery MAC against the key, inverse NTT.
+        uint32_t oa[32], ob[32];
+        const uint32_t pinv = 0u - ch.pinv_neg;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) oa[r] = ob[r] = 0;
+#pragma unroll 1
+        for (int row0 = 0; row0 < 2; row0 += DROWS) {
+            // tmp = X^{a_i} acc - acc (rotateTrlweMinusOne, yatfhe/src/trlwe.cpp:284-289) for
+            // DROWS rows, then gadgetDecomposeTrlwe (yatfhe/src/trlwe.cpp:185-198) into int16 digits
+            if (active) {
 #pragma unroll 2
-            for (int idx = ltid; idx < 2 * N; idx += ST) {
-                const int o = idx >= N;
-                const int j = idx - o * N;
-                const TorusT* A = acc + o * N;
-                TorusT rot = j < at ? tneg<T>(A[j - at + N]) : A[j - at];
-                if (wrap) rot = tneg<T>(rot);
-                const TorusT tmp = tsub<T>(rot, A[j]);
-                int16_t* d = dig + (size_t)o * L * N + j;
-                zero_mean_digits<U, T>((U)tmp, L, a.radix_bits,
-                                       [&](int level, int v) { d[(size_t)level * N] = (int16_t)v; });
+                for (int idx = ltid; idx < DROWS * N; idx += ST) {
+                    const int dr = idx >= N;
+                    const int j = idx - dr * N;
+                    const TorusT* A = acc + (row0 + dr) * N;
+                    TorusT rot = j < at ? tneg<T>(A[j - at + N]) : A[j - at];
+                    if (wrap) rot = tneg<T>(rot);
+                    const TorusT tmp = tsub<T>(rot, A[j]);
+                    int16_t* d = dig + (size_t)dr * L * N + j;
+                    zero_mean_digits<U, T>((U)tmp, L, a.radix_bits,
+                                           [&](int level, int v) { d[(size_t)level * N] = (int16_t)v; });
+                }
             }
-        }
-        __syncthreads();
+            __syncthreads();
 
-        if (active) {
-            // externalProductTrgswMPNttImpl (yatfhe/src/trgsw.cpp:712-767) in channel `team`:
-            // forward NTT of every digit poly, Montgomery MAC against the key, inverse NTT.
-            uint32_t oa[32], ob[32];
+            if (active) {
+                for (int dr = 0; dr < DROWS; ++dr) {
+                    const int row = row0 + dr;
+                    for (int lvl = 0; lvl < L; ++lvl) {
+                        uint32_t x[32];
+                        const int16_t* d = dig + ((size_t)dr * L + lvl) * N;
 #pragma unroll
-            for (int r = 0; r < 32; ++r) oa[r] = ob[r] = 0;
-            for (int row = 0; row < 2; ++row) {
-                for (int lvl = 0; lvl < L; ++lvl) {
-                    uint32_t x[32];
-                    const int16_t* d = dig + ((size_t)row * L + lvl) * N;
+                        for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
+                        ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
+                        const uint4* kp =
+                            key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
 #pragma unroll
-                    for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                    ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
-                    const uint4* kp =
-                        key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
+                        for (int rr = 0; rr < 8; ++rr) {
+                            const uint4 ka = ldg_keep(kp + rr * S + tt, keep);
+                            const uint4 kb = ldg_keep(kp + (8 + rr) * S + tt, keep);
+                            const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+                            const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
-                    for (int rr = 0; rr < 8; ++rr) {
-                        const uint4 ka = ldg_keep(kp + rr * S + tt, keep);
-                        const uint4 kb = ldg_keep(kp + (8 + rr) * S + tt, keep);
-                        const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
-                        const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+                            for (int e = 0; e < 4; ++e) {
+                                const int r = rr * 4 + e;
+                                oa[r] += montdiff(x[r], kav[e], ch.p, pinv);
+                                ob[r] += montdiff(x[r], kbv[e], ch.p, pinv);
+                            }
+                        }
+                        // lazy accumulation: each montdiff term lies in (-p, p), so after a
+                        // reduction oa, ob in [0, 4p) take two terms ((-2p, 6p)) before the next
+                        // one brings (oa + 2p) in (0, 8p) back to [0, 4p); 2 l terms in all (even)
+                        if ((row * L + lvl) & 1) {
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int r = rr * 4 + e;
-                            oa[r] = reduce_once(oa[r] + montmul(x[r], kav[e], ch.p, ch.pinv_neg), ch.two_p);
-                            ob[r] = reduce_once(ob[r] + montmul(x[r], kbv[e], ch.p, ch.pinv_neg), ch.two_p);
+                            for (int r = 0; r < 32; ++r) {
+                                oa[r] = reduce_once(oa[r] + ch.two_p, 2 * ch.two_p);
+                                ob[r] = reduce_once(ob[r] + ch.two_p, 2 * ch.two_p);
+                            }
                         }
                     }
                 }
             }
+            if (DROWS == 1 && row0 == 0) __syncthreads();  // the next row's digits overwrite these
+        }
+        if (active) {
             // one copy of the inverse transform, applied to the a then the b output poly
 #pragma unroll 1
             for (int o = 0; o < 2; ++o) {
@@ -270,6 +291,8 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
                     for (int r = 0; r < 32; ++r) oa[r] = ob[r];
                 }
                 uint32_t* region = mine + o * Sh::TBUF;
+#pragma unroll
+                for (int r = 0; r < 32; ++r) oa[r] = reduce_once(oa[r], ch.two_p);  // [0, 2p) in
                 ntt_inverse<LOGN>(oa, region, tt, team, bar, ch);
                 team_sync<LOGN>(bar);
 #pragma unroll

@@ -71,12 +71,16 @@ __host__ __device__ inline size_t key_words(int n, int L, int N) {
 
 // Shared memory of one ciphertext slice of the blind-rotation kernel: per channel two
 // padded (N + N/32)-word regions, the accumulator, int16 digits, the mod-2N input.
+// Rows of the accumulator whose digits are held at once (the digit buffer is
+// digit_rows x l x N int16).
+__host__ __device__ constexpr int digit_rows(int torus_bits) { return torus_bits == 32 ? 2 : 1; }
+
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
     size_t b = kChannels * 2 * tbuf * 4;
     b += 2 * N * (torus_bits == 32 ? 4 : 8);
-    b += 2 * (size_t)L * N * 2;
+    b += (size_t)digit_rows(torus_bits) * L * N * 2;
     b += ((size_t)n + 1) * 2;
     return (b + 15) & ~(size_t)15;
 }

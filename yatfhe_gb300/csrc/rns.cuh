@@ -48,12 +48,12 @@ __device__ __forceinline__ uint32_t mulshoup(uint32_t x, uint32_t w, uint32_t wp
     return x * w - qh * p;
 }
 
-// a b 2^-32 mod p in [0, 2p) for a < 8p, b < p, p < 2^29.
-__device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv_neg) {
+// hi(a b) - hi(m p) with m = (a b mod 2^32) p^-1 mod 2^32: the low words of a b and m p are
+// equal, so this is exactly (a b - m p) / 2^32 = a b 2^-32 mod p, as a signed value in (-p, p)
+// for a < 8p, b < p (p < 2^29): a Montgomery product without the carry fix-up.
+__device__ __forceinline__ uint32_t montdiff(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
     const uint32_t lo = a * b;
-    const uint32_t hi = __umulhi(a, b);
-    const uint32_t m = lo * pinv_neg;
-    return hi + __umulhi(m, p) + (lo != 0u);
+    return __umulhi(a, b) - __umulhi(lo * pinv, p);
 }
 
 __device__ __forceinline__ uint32_t reduce_once(uint32_t x, uint32_t m) { return min(x, x - m); }
@@ -87,7 +87,7 @@ __device__ __forceinline__ int64_t sext(int64_t x) {
 // centred(X mod q) mod 2^T, i.e. what applyIntt (yatfhe/src/ntt_hexl.cpp:153-175) returns.
 // Garner's mixed radix gives X = v0 + v1 p0 + v2 p0 p1 exactly; the top digit is centred
 // (|X| << M/2 puts it within 2^25 of 0 or of p2); a single-precision estimate of X / q
-// picks the quotient to within +-2 and exact 64-bit arithmetic on X mod 2^64 settles it.
+// picks the quotient to within +-1 and exact 64-bit arithmetic on X mod 2^64 settles it.
 template <int T>
 __device__ __forceinline__ int64_t crt_to_torus(uint32_t x0, uint32_t x1, uint32_t x2, const Crt& k) {
     const uint32_t x0m1 = reduce_once(x0, k.p1);
@@ -102,8 +102,11 @@ __device__ __forceinline__ int64_t crt_to_torus(uint32_t x0, uint32_t x1, uint32
     const uint64_t xlo = (uint64_t)x0 + (uint64_t)v1 * k.p0 + (uint64_t)(int64_t)v2s * k.p01;
     int64_t y = (int64_t)(xlo - (uint64_t)test * k.q);
     const int64_t hq = (int64_t)k.half_q, q = (int64_t)k.q;
+    // |X / q - test| < 1.5 (T = 32: the estimate is within 2^-5 of X / q; T = 56: within
+    // about 0.7), so y is within q of the centred range: one fix-up pass suffices; the 56-bit
+    // set takes a second one as margin.
 #pragma unroll
-    for (int it = 0; it < 3; ++it) {
+    for (int it = 0; it < (T == 32 ? 1 : 2); ++it) {
         y = y > hq ? y - q : y;
         y = y < -hq ? y + q : y;
     }
