@@ -220,7 +220,6 @@ void ctx_init_tables(yg_ctx* c) {
     k.half_q = (c->q - 1) / 2;
     k.a2 = (float)((double)k.p01 / (double)c->q);
     k.a1 = (float)((double)p0 / (double)c->q);
-    k.a0 = (float)(1.0 / (double)c->q);
 }
 
 // NTT-domain key words -> device key.  Layout in: [n][L][k+1][k+1][N] u64.

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
             // tmp = X^{a_i} acc - acc (rotateTrlweMinusOne, yatfhe/src/trlwe.cpp:284-289) for
             // DROWS rows, then gadgetDecomposeTrlwe (yatfhe/src/trlwe.cpp:185-198) into int16 digits
             if (active) {
-#pragma unroll 2
+#pragma unroll 1
                 for (int idx = ltid; idx < DROWS * N; idx += ST) {
                     const int dr = idx >= N;
                     const int j = idx - dr * N;
@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
                                 const int r = rr * 4 + e;
-                                oa[r] += montdiff(x[r], kav[e], ch.p, pinv);
-                                ob[r] += montdiff(x[r], kbv[e], ch.p, pinv);
+                                oa[r] += montdiff<T == 32>(x[r], kav[e], ch.p, pinv);
+                                ob[r] += montdiff<T == 32>(x[r], kbv[e], ch.p, pinv);
                             }
                         }
                         // lazy accumulation: each montdiff term lies in (-p, p), so after a
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
 
         // CRT -> applyIntt's centred mod-q value mod 2^T, then accumulateTrlwe (trlwe.h:268-274)
         if (active) {
-#pragma unroll 2
+#pragma unroll 1
             for (int idx = ltid; idx < 2 * N; idx += ST) {
                 const int o = idx >= N;
                 const int j = idx - o * N;

@@ -38,7 +38,7 @@ struct Crt {
     uint64_t p01;                        // p0 p1
     uint64_t q;                          // qNtt of the reference
     uint64_t half_q;                     // (q - 1) / 2
-    float a2, a1, a0;                    // p0 p1 / q, p0 / q, 1 / q
+    float a2, a1;                        // p0 p1 / q, p0 / q
 };
 
 #ifdef __CUDACC__
@@ -51,9 +51,18 @@ __device__ __forceinline__ uint32_t mulshoup(uint32_t x, uint32_t w, uint32_t wp
 // hi(a b) - hi(m p) with m = (a b mod 2^32) p^-1 mod 2^32: the low words of a b and m p are
 // equal, so this is exactly (a b - m p) / 2^32 = a b 2^-32 mod p, as a signed value in (-p, p)
 // for a < 8p, b < p (p < 2^29): a Montgomery product without the carry fix-up.
+// WIDE selects how a b is formed: one 32 x 32 -> 64 multiply, or separate low and high
+// halves; the results are identical, the instruction schedules differ (the wide form
+// measured faster in the 32-bit-torus kernels, the split form in the 56-bit ones).
+template <bool WIDE>
 __device__ __forceinline__ uint32_t montdiff(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
-    const uint32_t lo = a * b;
-    return __umulhi(a, b) - __umulhi(lo * pinv, p);
+    if constexpr (WIDE) {
+        const uint64_t ab = (uint64_t)a * b;
+        return (uint32_t)(ab >> 32) - __umulhi((uint32_t)ab * pinv, p);
+    } else {
+        const uint32_t lo = a * b;
+        return __umulhi(a, b) - __umulhi(lo * pinv, p);
+    }
 }
 
 __device__ __forceinline__ uint32_t reduce_once(uint32_t x, uint32_t m) { return min(x, x - m); }
@@ -90,14 +99,14 @@ __device__ __forceinline__ int64_t sext(int64_t x) {
 // picks the quotient to within +-1 and exact 64-bit arithmetic on X mod 2^64 settles it.
 template <int T>
 __device__ __forceinline__ int64_t crt_to_torus(uint32_t x0, uint32_t x1, uint32_t x2, const Crt& k) {
-    const uint32_t x0m1 = reduce_once(x0, k.p1);
-    uint32_t v1 = reduce_once(mulshoup(x1 + k.p1 - x0m1, k.inv_p0_m1, k.inv_p0_m1_s, k.p1), k.p1);
-    const uint32_t v0m2 = reduce_once(x0, k.p2);
-    uint32_t t = reduce_once(mulshoup(v1, k.p0_m2, k.p0_m2_s, k.p2), k.p2) + v0m2;
-    t = reduce_once(t, k.p2);
-    const uint32_t v2 = reduce_once(mulshoup(x2 + k.p2 - t, k.inv_p01_m2, k.inv_p01_m2_s, k.p2), k.p2);
+    // p2 < p1 < p0 < 2 p2 < 2^29: x0 < 2 p1 and x0 < 2 p2 need no reduction before the
+    // subtractions, and every intermediate stays below 5 p2 < 2^32
+    const uint32_t v1 = reduce_once(mulshoup(x1 + 2 * k.p1 - x0, k.inv_p0_m1, k.inv_p0_m1_s, k.p1), k.p1);
+    const uint32_t ms = mulshoup(v1, k.p0_m2, k.p0_m2_s, k.p2);  // v1 p0 mod p2, in [0, 2 p2)
+    const uint32_t v2 = reduce_once(mulshoup(x2 + 4 * k.p2 - x0 - ms, k.inv_p01_m2, k.inv_p01_m2_s, k.p2), k.p2);
     const int32_t v2s = v2 > k.half_p2 ? (int32_t)(v2 - k.p2) : (int32_t)v2;
-    const float tf = __fmaf_rn((float)v2s, k.a2, __fmaf_rn((float)v1, k.a1, (float)x0 * k.a0));
+    // x0 / q < 2^-20 is below the estimate's resolution and is left out
+    const float tf = __fmaf_rn((float)v2s, k.a2, (float)v1 * k.a1);
     const int64_t test = (int64_t)__float2ll_rn(tf);
     const uint64_t xlo = (uint64_t)x0 + (uint64_t)v1 * k.p0 + (uint64_t)(int64_t)v2s * k.p01;
     int64_t y = (int64_t)(xlo - (uint64_t)test * k.q);
