@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
     ap.add_argument("--serving-requests", type=int, default=800, help="measured requests per offered rate")
     ap.add_argument("--serving-fractions", default="0.5,0.6,0.7,0.8,0.9,1.0", help="offered rates / peak")
+    ap.add_argument("--serving-max-batch", type=int, default=608, help="ciphertexts per serving batch")
+    ap.add_argument("--serving-inflight", type=int, default=2, help="serving batches on the GPU at once")
     return ap.parse_args()
 
 
@@ -416,7 +418,7 @@ def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
 
 
 def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), tenants=128, budget=4e9,
-                max_count=256, max_batch=2048, max_inflight=3):
+                max_count=256, max_batch=608, max_inflight=2):
     """128 tenants on the TORUS=32 set, requests of 1..256 ciphertexts (log-uniform) arriving
     as a Poisson process, tenants Zipf(1.1)-popular, BSK/KSK in an HBM LRU cache capped at
     4 GB with refills from pinned host memory.  First the peak rate is measured with the
@@ -560,7 +562,8 @@ def main():
                     "config": {"workload": r["workload"]}, "result": r}
         else:
             fr = tuple(float(x) for x in args.serving_fractions.split(","))
-            r = leg_serving(dev, requests=args.serving_requests, fractions=fr)
+            r = leg_serving(dev, requests=args.serving_requests, fractions=fr, max_batch=args.serving_max_batch,
+                            max_inflight=args.serving_inflight)
             a80 = r["at_80pct"] or {}
             line = {"metric": "serving p99 sojourn at 80% of peak", "value": a80.get("p99_ms"), "unit": "ms",
                     "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -660,7 +663,8 @@ def main():
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
             "serving_t32_128tenants_4GB": _safe(
                 leg_serving, dev, requests=args.serving_requests,
-                fractions=tuple(float(x) for x in args.serving_fractions.split(","))),
+                fractions=tuple(float(x) for x in args.serving_fractions.split(",")),
+                max_batch=args.serving_max_batch, max_inflight=args.serving_inflight),
         }
 
     line = {
