@@ -58,6 +58,7 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="with --per-cta: persistent CTAs per SM (0 = off)")
+    ap.add_argument("--layout", type=int, default=0, help="with --per-cta: 0 = team per channel, 1 = per channel and row")
     ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
     ap.add_argument("--serving-requests", type=int, default=800, help="measured requests per offered rate")
     ap.add_argument("--serving-fractions", default="0.5,0.6,0.7,0.8,0.9,1.0", help="offered rates / peak")
@@ -225,7 +226,7 @@ class BatchRun:
     """One parameter set, one synthetic key, `count` resident ciphertexts; times the
     blind-rotation(+extract) and key-switch launches of each step with CUDA events."""
 
-    def __init__(self, p, count, dev, seed, per_cta=0, ctas_per_sm=0, retune=False):
+    def __init__(self, p, count, dev, seed, per_cta=0, ctas_per_sm=0, retune=False, layout=0):
         import torch
 
         from yatfhe_gb300 import _lib, api
@@ -244,8 +245,9 @@ class BatchRun:
         self.d_in = torch.from_numpy(self.lwe).to(f"cuda:{dev}")
         self.d_lut = torch.from_numpy(self.lut).to(f"cuda:{dev}")
         if per_cta:
-            api.set_launch(self.ctx, per_cta, ctas_per_sm)
-            self.tuning = {"choice": {"per_cta": per_cta, "ctas_per_sm": ctas_per_sm}, "fixed": True}
+            api.set_launch(self.ctx, per_cta, ctas_per_sm, layout)
+            self.tuning = {"choice": {"layout": layout, "per_cta": per_cta, "ctas_per_sm": ctas_per_sm},
+                           "fixed": True}
         else:
             from yatfhe_gb300 import autotune
 
@@ -441,7 +443,7 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
         bsk, ksk = synthetic_keys(p, 0x5EED2000 + t)
         key = api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk)
         if srv is None:
-            autotune.tune(ctx, key, d_lut)
+            tuning = autotune.tune(ctx, key, d_lut, objective="latency")
             srv = serving.Server(ctx, key_budget_bytes=budget, max_batch=max_batch, max_inflight=max_inflight,
                                  max_tenants=tenants)
         lwe = synthetic_lwe(p, max_count, 0x5EED3000 + t)
@@ -472,6 +474,7 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
     return {"workload": "serving_t32_128tenants_4GB", "tenants": tenants, "key_budget_bytes": int(budget),
             "key_slots": slots, "resident_fraction": slots / tenants, "max_batch": max_batch,
             "max_inflight": max_inflight, "request_sizes": f"floor(exp(U(0, ln {max_count + 1}))), 1..{max_count}",
+            "launch_shape": tuning["choice"],
             "peak": {"requests_per_s": peak_rps, "bootstraps_per_s": peak["ciphertexts_per_s"],
                      "p50_ms": peak["sojourn"]["p50_ms"], "p99_ms": peak["sojourn"]["p99_ms"],
                      "hit_rate": peak["hit_rate"]},
@@ -573,7 +576,7 @@ def main():
         return
 
     run = BatchRun(p, count, dev, seed=1234 + rank, per_cta=args.per_cta, ctas_per_sm=args.ctas_per_sm,
-                   retune=args.retune)
+                   retune=args.retune, layout=args.layout)
     t = run.timed(args.steps, args.warmup, barrier=barrier, clocks=ClockSampler(dev))
     total_ms = t["total_ms"]
     if world > 1:

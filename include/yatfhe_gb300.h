@@ -136,18 +136,26 @@ int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* 
 typedef struct yg_plan yg_plan;
 int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const int32_t* h_key_ids,
                    const int64_t* const* d_luts, int num_luts, const int32_t* h_lut_ids, int count, yg_plan** out);
-/* Launch shape for this plan: per_cta ciphertexts per blind-rotation CTA (1, 2 or 4;
- * 0 = the context's setting) and grid CTAs (0 = enough for the batch; fewer = persistent
- * CTAs that loop over it). */
-int yg_plan_set_launch(yg_plan* plan, int per_cta, int grid);
+/* Work split of one ciphertext in the blind rotation.  YG_LAYOUT_CHANNEL: one team of
+ * N/32 threads per RNS channel runs every NTT of a CMux step.  YG_LAYOUT_CHANNEL_ROW: two
+ * teams per channel, one per accumulator row, each running half the forward transforms and
+ * one inverse transform: twice the threads per ciphertext, about half the latency. */
+#define YG_LAYOUT_CHANNEL 0
+#define YG_LAYOUT_CHANNEL_ROW 1
+/* Launch shape for this plan: layout, per_cta ciphertexts per blind-rotation CTA (1, 2 or
+ * 4; 0 = the context's setting, layout included) and grid CTAs (0 = enough for the batch;
+ * fewer = persistent CTAs that loop over it). */
+int yg_plan_set_launch(yg_plan* plan, int layout, int per_cta, int grid);
 int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream);
 void yg_plan_destroy(yg_plan* plan);
-/* Blind-rotation CTAs of per_cta ciphertexts each that fit on one SM (0: none fits). */
-int yg_ctas_per_sm(yg_ctx* ctx, int per_cta, int* out);
-/* Launch shape of every bootstrap on this context (the autotuner's choice): per_cta
- * ciphertexts per CTA, run in lockstep; ctas_per_sm > 0 makes the grid persistent with that
- * many CTAs per SM, 0 launches one CTA per group of per_cta ciphertexts.  Default (1, 0). */
-int yg_ctx_set_launch(yg_ctx* ctx, int per_cta, int ctas_per_sm);
+/* Blind-rotation CTAs of per_cta ciphertexts each, in `layout`, that fit on one SM
+ * (0: none fits, or no such kernel). */
+int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out);
+/* Launch shape of every bootstrap on this context (the autotuner's choice): layout,
+ * per_cta ciphertexts per CTA, run in lockstep; ctas_per_sm > 0 makes the grid persistent
+ * with that many CTAs per SM, 0 launches one CTA per group of per_cta ciphertexts.
+ * Default (YG_LAYOUT_CHANNEL, 1, 0). */
+int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm);
 
 /* Serving: a request loop over many tenants with continuous batching and an HBM key cache.
  * Replaces the reference's CPU serving harness (ya_benchmark/blindrotate_serving.cpp:111-354,

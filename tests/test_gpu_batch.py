@@ -40,19 +40,21 @@ def test_multi_key_batch_matches_per_tenant_oracle(base, built_lib):
     lwe = np.concatenate([oras[t].encrypt(rng.integers(-(1 << 31), 1 << 31, c)) for t, c in enumerate(counts)])
     luts = [torch.from_numpy(v).cuda() for v in luts_np]
     d_in = torch.from_numpy(lwe).cuda()
-    shapes = [(g, grid) for g in (1, 2, 4) if api.ctas_per_sm(ctx, g) > 0 for grid in (0, 3)]
-    assert (1, 0) in shapes and (2, 0) in shapes or p.N == 2048
-    if api.ctas_per_sm(ctx, 2) == 0:  # too large for one SM: rejected, never silently skipped
-        with pytest.raises(ValueError):
-            api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids, per_cta=2)
-    for per_cta, grid in shapes:
-        plan = api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids, grid=grid, per_cta=per_cta)
+    shapes = [(lay, g, grid) for lay in (0, 1) for g in (1, 2, 4) if api.ctas_per_sm(ctx, g, lay) > 0
+              for grid in (0, 3)]
+    assert (0, 1, 0) in shapes and (1, 1, 0) in shapes
+    assert (0, 2, 0) in shapes or p.N == 2048
+    for lay, g in ((0, 4), (1, 4)):
+        if api.ctas_per_sm(ctx, g, lay) == 0:  # no such kernel or too large: rejected, never skipped
+            with pytest.raises(ValueError):
+                api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids, per_cta=g, layout=lay)
+    want = np.concatenate([oras[key_ids[c]].pbs(lwe[c:c + 1], luts_np[lut_ids[c]]) for c in range(len(lwe))])
+    for layout, per_cta, grid in shapes:
+        plan = api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids, grid=grid, per_cta=per_cta,
+                             layout=layout)
         out = plan.run(d_in, torch.empty_like(d_in))
         torch.cuda.synchronize()
-        got = out.cpu().numpy()
-        for c in range(len(lwe)):
-            want = oras[key_ids[c]].pbs(lwe[c:c + 1], luts_np[lut_ids[c]])
-            np.testing.assert_array_equal(got[c:c + 1], want, err_msg=f"ciphertext {c}, {per_cta}/CTA, grid {grid}")
+        np.testing.assert_array_equal(out.cpu().numpy(), want, err_msg=f"layout {layout}, {per_cta}/CTA, grid {grid}")
 
 
 def test_plan_replays_in_a_cuda_graph(built_lib):

@@ -15,6 +15,8 @@ from .params import PbsParams
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libyatfhe_gb300.so"
 
 YG_OK = 0
+LAYOUT_CHANNEL = 0      # YG_LAYOUT_CHANNEL
+LAYOUT_CHANNEL_ROW = 1  # YG_LAYOUT_CHANNEL_ROW
 _ERRORS = {-1: ValueError, -2: RuntimeError, -3: OSError, -4: MemoryError, -5: RuntimeError}
 
 
@@ -82,11 +84,11 @@ _SIGNATURES = {
     "yg_pbs_noalloc_max_count": (ctypes.c_size_t, [_vp]),
     "yg_plan_create": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int,
                                       ctypes.POINTER(_vp)]),
-    "yg_plan_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "yg_plan_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "yg_plan_run": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "yg_plan_destroy": (None, [_vp]),
-    "yg_ctas_per_sm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
-    "yg_ctx_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "yg_ctas_per_sm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "yg_ctx_set_launch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "yg_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "yg_server_add_tenant": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "yg_server_start": (ctypes.c_int, [_vp]),

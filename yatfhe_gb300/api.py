@@ -123,7 +123,7 @@ class BatchPlan:
     captured in a CUDA graph."""
 
     def __init__(self, ctx: Context, keys, luts, count: int, key_ids=None, lut_ids=None, grid: int = 0,
-                 per_cta: int = 0):
+                 per_cta: int = 0, layout: int = 0):
         self.ctx, self.keys, self.luts, self.count = ctx, list(keys), list(luts), count
         kt = (ctypes.c_void_p * len(self.keys))(*[k.handle.value for k in self.keys])
         lt = (ctypes.c_void_p * len(self.luts))(*[ctypes.c_void_p(t.data_ptr()).value for t in self.luts])
@@ -139,11 +139,11 @@ class BatchPlan:
             ctypes.cast(lt, ctypes.c_void_p), len(self.luts),
             None if lid is None else ctypes.c_void_p(lid.ctypes.data), count, ctypes.byref(h)))
         self._h = h
-        if grid or per_cta:
-            self.set_launch(per_cta or 1, grid)
+        if grid or per_cta or layout:
+            self.set_launch(per_cta or 1, grid, layout)
 
-    def set_launch(self, per_cta: int, grid: int = 0):
-        _lib.check(_lib.lib().yg_plan_set_launch(self._h, int(per_cta), int(grid)))
+    def set_launch(self, per_cta: int, grid: int = 0, layout: int = 0):
+        _lib.check(_lib.lib().yg_plan_set_launch(self._h, int(layout), int(per_cta), int(grid)))
 
     def run(self, lwe_in, out, stream=None):
         _lib.check(_lib.lib().yg_plan_run(self._h, _dptr(lwe_in, "int32", "lwe_in"), _dptr(out, "int32", "out"),
@@ -162,14 +162,15 @@ class BatchPlan:
             pass
 
 
-def ctas_per_sm(ctx: Context, per_cta: int = 1) -> int:
+def ctas_per_sm(ctx: Context, per_cta: int = 1, layout: int = 0) -> int:
+    """CTAs of `per_cta` ciphertexts in `layout` (_lib.LAYOUT_*) that fit one SM (0: none)."""
     v = ctypes.c_int()
-    _lib.check(_lib.lib().yg_ctas_per_sm(ctx.handle, int(per_cta), ctypes.byref(v)))
+    _lib.check(_lib.lib().yg_ctas_per_sm(ctx.handle, int(layout), int(per_cta), ctypes.byref(v)))
     return v.value
 
 
-def set_launch(ctx: Context, per_cta: int, ctas_per_sm: int = 0) -> None:
-    _lib.check(_lib.lib().yg_ctx_set_launch(ctx.handle, int(per_cta), int(ctas_per_sm)))
+def set_launch(ctx: Context, per_cta: int, ctas_per_sm: int = 0, layout: int = 0) -> None:
+    _lib.check(_lib.lib().yg_ctx_set_launch(ctx.handle, int(layout), int(per_cta), int(ctas_per_sm)))
 
 
 def functional_bootstrapping_mp_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, out=None, stream=None):

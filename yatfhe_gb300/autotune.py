@@ -1,14 +1,19 @@
 """Launch-shape autotuner for the blind-rotation kernel.
 
 The knobs (yg_ctx_set_launch / yg_plan_set_launch):
+  layout       work split of one ciphertext: a thread team per RNS channel (LAYOUT_CHANNEL)
+               or per channel and accumulator row (LAYOUT_CHANNEL_ROW: twice the threads,
+               about half the latency per ciphertext);
   per_cta      ciphertexts per CTA run in lockstep (1, 2, 4 at N = 1024; 1, 2 at N = 2048):
                more share instruction-cache lines and key lines in L1, fewer keep more
                independent CTAs per SM;
   ctas_per_sm  0 = one CTA per group of per_cta ciphertexts (the hardware scheduler fills
                the SMs), c > 0 = a persistent grid of c CTAs per SM looping over the batch.
-Each candidate that fits an SM is timed with CUDA events on a sample batch; the fastest is
+Each candidate that fits an SM is timed with CUDA events on a sample batch (throughput)
+and on one ciphertext alone (latency); the best for the objective -- the most bootstraps
+per second, or for serving the lowest lone-ciphertext latency within 5 % of that -- is
 applied to the context and cached in yatfhe_gb300/_build/autotune.json per (GPU,
-parameter set), so later processes reuse it without measuring.
+parameter set, objective), so later processes reuse it without measuring.
 """
 from __future__ import annotations
 
@@ -19,7 +24,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import api
+from . import _lib, api
 
 CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 
@@ -45,22 +50,26 @@ def _store(table: dict) -> None:
     os.replace(tmp, CACHE)
 
 
-def candidates(ctx) -> list[tuple[int, int]]:
+def candidates(ctx) -> list[tuple[int, int, int]]:
+    """(layout, per_cta, ctas_per_sm) shapes that fit an SM."""
     out = []
-    for per_cta in (1, 2, 4):
-        try:
-            fit = api.ctas_per_sm(ctx, per_cta)
-        except ValueError:
-            continue
-        if fit < 1:
-            continue
-        out.append((per_cta, 0))
-        out.append((per_cta, fit))
+    for layout in (_lib.LAYOUT_CHANNEL, _lib.LAYOUT_CHANNEL_ROW):
+        for per_cta in (1, 2, 4):
+            try:
+                fit = api.ctas_per_sm(ctx, per_cta, layout)
+            except ValueError:
+                continue
+            if fit < 1:
+                continue
+            out.append((layout, per_cta, 0))
+            out.append((layout, per_cta, fit))
     return out
 
 
-def measure(ctx, key, lut, count: int, per_cta: int, ctas_per_sm: int, reps: int = 2, seed: int = 0) -> float:
-    """Bootstraps per second of one launch shape on `count` random ciphertexts."""
+def measure(ctx, key, lut, count: int, per_cta: int, ctas_per_sm: int, reps: int = 2, seed: int = 0,
+            layout: int = 0) -> tuple[float, float]:
+    """(bootstraps per second on `count` random ciphertexts, milliseconds for one ciphertext
+    alone) of one launch shape."""
     import torch
 
     sms = torch.cuda.get_device_properties(ctx.device).multi_processor_count
@@ -68,42 +77,69 @@ def measure(ctx, key, lut, count: int, per_cta: int, ctas_per_sm: int, reps: int
     lwe = rng.integers(-(1 << 31), 1 << 31, size=(count, ctx.params.n + 1), dtype=np.int64).astype(np.int32)
     d_in = torch.from_numpy(lwe).to(f"cuda:{ctx.device}")
     d_out = torch.empty_like(d_in)
-    plan = api.BatchPlan(ctx, [key], [lut], count, per_cta=per_cta, grid=ctas_per_sm * sms)
+    plan = api.BatchPlan(ctx, [key], [lut], count, per_cta=per_cta, grid=ctas_per_sm * sms, layout=layout)
+    one = api.BatchPlan(ctx, [key], [lut], 1, per_cta=per_cta, layout=layout)
     s = torch.cuda.Stream(device=ctx.device)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     with torch.cuda.stream(s):
         plan.run(d_in, d_out, stream=s)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s)
+        ev[0].record(s)
         for _ in range(reps):
             plan.run(d_in, d_out, stream=s)
-        b.record(s)
+        ev[1].record(s)
+        one.run(d_in[:1], d_out[:1], stream=s)
+        ev[2].record(s)
+        for _ in range(reps):
+            one.run(d_in[:1], d_out[:1], stream=s)
+        ev[3].record(s)
     s.synchronize()
     plan.close()
-    return reps * count / (a.elapsed_time(b) / 1e3)
+    one.close()
+    return reps * count / (ev[0].elapsed_time(ev[1]) / 1e3), ev[2].elapsed_time(ev[3]) / reps
 
 
-def tune(ctx, key, lut, count: int | None = None, use_cache: bool = True, verbose: bool = False) -> dict:
-    """Picks, applies and caches the fastest launch shape; returns {choice, results, cached}."""
+OBJECTIVES = ("throughput", "latency")
+
+
+def pick(results: list[dict], objective: str) -> dict:
+    """throughput: the most bootstraps per second; latency: of the shapes within 5 % of that,
+    the one that finishes a lone ciphertext soonest (what a serving loop under partial load
+    sees)."""
+    best = max(results, key=lambda r: r["bootstraps_per_s"])
+    if objective == "throughput":
+        return best
+    near = [r for r in results if r["bootstraps_per_s"] >= 0.95 * best["bootstraps_per_s"]]
+    return min(near, key=lambda r: r["single_ms"])
+
+
+def tune(ctx, key, lut, count: int | None = None, use_cache: bool = True, verbose: bool = False,
+         objective: str = "throughput") -> dict:
+    """Picks, applies and caches the best launch shape for `objective`; returns
+    {choice, results, cached}."""
     import torch
 
-    k = _key(ctx)
+    if objective not in OBJECTIVES:
+        raise ValueError(f"objective must be one of {OBJECTIVES}")
+    k = _key(ctx) + f"|{objective}"
     table = _load() if use_cache else {}
     if k in table:
         c = table[k]
-        api.set_launch(ctx, c["per_cta"], c["ctas_per_sm"])
+        api.set_launch(ctx, c["per_cta"], c["ctas_per_sm"], c.get("layout", 0))
         return {"choice": c, "cached": True}
     sms = torch.cuda.get_device_properties(ctx.device).multi_processor_count
     if count is None:
         count = sms * 16  # several waves for every candidate
     results = []
-    for per_cta, cps in candidates(ctx):
-        bps = measure(ctx, key, lut, count, per_cta, cps)
-        results.append({"per_cta": per_cta, "ctas_per_sm": cps, "bootstraps_per_s": bps})
+    for layout, per_cta, cps in candidates(ctx):
+        bps, single = measure(ctx, key, lut, count, per_cta, cps, layout=layout)
+        results.append({"layout": layout, "per_cta": per_cta, "ctas_per_sm": cps, "bootstraps_per_s": bps,
+                        "single_ms": single})
         if verbose:
-            print(f"autotune {per_cta}/CTA, {cps or 'all'} CTAs/SM: {bps:.0f} bootstraps/s")
-    best = max(results, key=lambda r: r["bootstraps_per_s"])
+            print(f"autotune layout {layout}, {per_cta}/CTA, {cps or 'all'} CTAs/SM: {bps:.0f} bootstraps/s, "
+                  f"{single:.2f} ms alone")
+    best = pick(results, objective)
     table = _load()
-    table[k] = {**best, "sample": count}
+    table[k] = {**best, "sample": count, "objective": objective}
     _store(table)
-    api.set_launch(ctx, best["per_cta"], best["ctas_per_sm"])
+    api.set_launch(ctx, best["per_cta"], best["ctas_per_sm"], best["layout"])
     return {"choice": table[k], "results": results, "cached": False}

@@ -370,6 +370,7 @@ yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     for (int ci = 0; ci < yg::kChannels; ci++) a.ch[ci] = c->ch[ci];
     a.crt = c->crt;
     a.per_cta = c->per_cta;
+    a.layout = c->layout;
     a.grid = c->ctas_per_sm > 0 ? c->ctas_per_sm * c->sm_count : 0;
     return a;
 }
@@ -618,6 +619,7 @@ struct yg_plan {
     int count = 0;
     int grid = 0;
     int per_cta = 0;
+    int layout = 0;
     const yg_key* key0 = nullptr;     // uniform batch: the one key
     const int64_t* lut0 = nullptr;    // uniform LUT
     const uint4** d_key_table = nullptr;
@@ -706,13 +708,15 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
     });
 }
 
-int yg_plan_set_launch(yg_plan* plan, int per_cta, int grid) {
-    if (!plan || per_cta < 0 || grid < 0) return set_err(YG_ERR_INVALID, "yg_plan_set_launch: bad arguments");
+int yg_plan_set_launch(yg_plan* plan, int layout, int per_cta, int grid) {
+    if (!plan || per_cta < 0 || grid < 0 || (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW))
+        return set_err(YG_ERR_INVALID, "yg_plan_set_launch: bad arguments");
     if (per_cta > 0) {
         int fit = 0;
-        if (int rc = yg_ctas_per_sm(plan->ctx, per_cta, &fit)) return rc;
-        if (fit < 1) return set_err(YG_ERR_INVALID, "yg_plan_set_launch: a CTA of that size does not fit an SM");
+        if (int rc = yg_ctas_per_sm(plan->ctx, layout, per_cta, &fit)) return rc;
+        if (fit < 1) return set_err(YG_ERR_INVALID, "yg_plan_set_launch: a CTA of that shape does not fit an SM");
     }
+    plan->layout = layout;
     plan->per_cta = per_cta;
     plan->grid = grid;
     return YG_OK;
@@ -736,6 +740,7 @@ int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream
         a.count = plan->count;
         if (plan->per_cta > 0) {
             a.per_cta = plan->per_cta;
+            a.layout = plan->layout;
             a.grid = plan->grid;
         }
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
@@ -754,11 +759,13 @@ void yg_plan_destroy(yg_plan* plan) {
     delete plan;
 }
 
-int yg_ctas_per_sm(yg_ctx* ctx, int per_cta, int* out) {
+int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out) {
     if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
+    if (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW)
+        return set_err(YG_ERR_INVALID, "yg_ctas_per_sm: unknown layout");
     return guarded([&] {
         DeviceGuard g(ctx->device);
-        const int b = yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, per_cta);
+        const int b = yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, per_cta, layout);
         if (b == yg::kNoVariant) {
             *out = 0;  // no kernel of that shape for these parameters: nothing fits
             return YG_OK;
@@ -769,11 +776,12 @@ int yg_ctas_per_sm(yg_ctx* ctx, int per_cta, int* out) {
     });
 }
 
-int yg_ctx_set_launch(yg_ctx* ctx, int per_cta, int ctas_per_sm) {
+int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm) {
     if (!ctx || per_cta < 1 || ctas_per_sm < 0) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: bad arguments");
     int fit = 0;
-    if (int rc = yg_ctas_per_sm(ctx, per_cta, &fit)) return rc;
-    if (fit < 1) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: a CTA of that size does not fit an SM");
+    if (int rc = yg_ctas_per_sm(ctx, layout, per_cta, &fit)) return rc;
+    if (fit < 1) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: a CTA of that shape does not fit an SM");
+    ctx->layout = layout;
     ctx->per_cta = per_cta;
     ctx->ctas_per_sm = ctas_per_sm;
     return YG_OK;

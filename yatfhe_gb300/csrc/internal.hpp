@@ -82,6 +82,7 @@ struct yg_ctx {
     uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
     std::shared_ptr<yg::QInverse> qinv;
     int sm_count = 0;
+    int layout = 0;        // YG_LAYOUT_* of the blind rotation (yg_ctx_set_launch)
     int per_cta = 1;       // ciphertexts per blind-rotation CTA (yg_ctx_set_launch)
     int ctas_per_sm = 0;   // persistent CTAs per SM, 0 = one CTA per ciphertext group
 };

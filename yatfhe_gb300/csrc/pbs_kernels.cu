@@ -126,33 +126,61 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     }
 }
 
-// Threads of one ciphertext slice: three channel teams.
-template <int LOGN>
-__host__ __device__ constexpr int slice_threads() { return 3 * TeamShape<LOGN>::S; }
+// Teams of one ciphertext slice: one per RNS channel (kLayoutChannel), or one per channel
+// and accumulator row (kLayoutChannelRow).
+template <int SPLIT>
+__host__ __device__ constexpr int slice_teams() { return SPLIT ? 2 * kChannels : kChannels; }
+template <int LOGN, int SPLIT>
+__host__ __device__ constexpr int slice_threads() { return slice_teams<SPLIT>() * TeamShape<LOGN>::S; }
 
 // Resident CTAs per SM the register budget is sized for (about 170 registers a thread).
-template <int LOGN, int G>
-__host__ __device__ constexpr int min_ctas() { return (LOGN == 10 ? 4 : 2) / G > 0 ? (LOGN == 10 ? 4 : 2) / G : 1; }
+template <int LOGN, int G, int SPLIT>
+__host__ __device__ constexpr int min_ctas() {
+    return 65536 / (170 * G * slice_threads<LOGN, SPLIT>()) > 0 ? 65536 / (170 * G * slice_threads<LOGN, SPLIT>())
+                                                               : 1;
+}
+
+// Barrier over the two teams of one channel in the channel-row layout: named barrier
+// `id` (1..15; 0 is __syncthreads) over their 2 S threads.
+template <int LOGN>
+__device__ __forceinline__ void pair_sync(int id) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(2 * TeamShape<LOGN>::S) : "memory");
+}
 
 // G ciphertexts per CTA run in lockstep: their warps execute the same phase at the same
 // time (one stretch of code in the instruction caches) and the G teams of a channel read
 // the same key lines, the first from L2 and the others from L1.
-template <int LOGN, int T, int G>
-__global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()) blind_rotate_kernel(const BrArgs a) {
+//
+// Layouts (SPLIT):
+//   kLayoutChannel     one team per RNS channel runs all 2 l forward NTTs of a CMux step,
+//                      the MAC into both output polys and both inverse NTTs;
+//   kLayoutChannelRow  two teams per channel, one per accumulator row: each runs the l
+//                      forward NTTs of its row's digits and accumulates partial products
+//                      for both outputs, the teams swap the partial sum the other one
+//                      finishes through shared memory, and each runs one inverse NTT.
+//                      Twice the threads per ciphertext, about half the time per step.
+template <int LOGN, int T, int G, int SPLIT>
+__global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOGN, G, SPLIT>())
+    blind_rotate_kernel(const BrArgs a) {
     using Sh = TeamShape<LOGN>;
     using TorusT = typename TorusOf<T>::type;
     using U = typename TorusOf<T>::utype;
     constexpr int N = Sh::N, S = Sh::S;
-    constexpr int ST = slice_threads<LOGN>();
+    constexpr int TEAMS = slice_teams<SPLIT>();
+    constexpr int ST = slice_threads<LOGN, SPLIT>();
     extern __shared__ __align__(16) unsigned char smem[];
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int g = warp / (3 * Sh::WARPS);                   // ciphertext slice of this warp
-    const int wi = warp % (3 * Sh::WARPS);
-    const int team = wi / Sh::WARPS;                         // RNS channel
-    const int tt = (wi % Sh::WARPS) * 32 + lane;             // thread in the channel team
-    const int bar = g * kChannels + team;                    // named barrier of the team
+    const int g = warp / (TEAMS * Sh::WARPS);               // ciphertext slice of this warp
+    const int wi = warp % (TEAMS * Sh::WARPS);
+    const int tm = wi / Sh::WARPS;                           // team in the slice
+    const int team = SPLIT ? tm >> 1 : tm;                   // RNS channel
+    const int hrow = SPLIT ? tm & 1 : 0;                     // accumulator row (channel-row layout)
+    const int tt = (wi % Sh::WARPS) * 32 + lane;             // thread in the team
+    const int bar = g * TEAMS + tm;                          // named barrier of the team (N = 2048)
+    // named barrier of the channel's team pair, after the team barriers
+    const int pair_bar = 1 + (LOGN == 10 ? 0 : G * TEAMS) + g * kChannels + team;
     const int ltid = tid - g * ST;                           // thread in the slice
     const Chan ch = pick_chan(a.ch, team);
     const int L = a.L, n = a.n;
@@ -160,15 +188,17 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
 
     // the slice's shared memory: xb[team][o] padded regions (NTT transpose scratch, then
     // inverse-NTT residues for the CRT), the accumulator, the digits, the mod-2N input
-    unsigned char* base = smem + (size_t)g * br_smem_bytes(LOGN, T, n, L);
+    unsigned char* base = smem + (size_t)g * br_smem_bytes(LOGN, T, n, L, SPLIT);
     uint32_t* xb = reinterpret_cast<uint32_t*>(base);                           // [3][2][TBUF]
     TorusT* acc = reinterpret_cast<TorusT*>(xb + kChannels * 2 * Sh::TBUF);    // [2][N]
-    // digit rows decomposed per phase: both at T = 32; one at a time at T = 56, where the
-    // halved digit buffer lets two ciphertext slices share an SM
-    constexpr int DROWS = digit_rows(T);
+    // digit rows decomposed per phase: both at T = 32 and in the channel-row layout; one at
+    // a time at T = 56, where the halved digit buffer lets two ciphertext slices share an SM
+    constexpr int DROWS = SPLIT ? 2 : digit_rows(T);
     int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [DROWS][L][N]
     int16_t* sa = dig + DROWS * L * N;                                           // [n+1]
-    uint32_t* mine = xb + team * 2 * Sh::TBUF;
+    // the team's transpose region: region 0 of its channel (channel layout, the inverse
+    // uses both), or region `hrow` (channel-row layout, each team owns one)
+    uint32_t* mine = xb + (team * 2 + hrow) * Sh::TBUF;
 
     // G ciphertexts per iteration; a grid smaller than the batch makes the CTAs persistent
     for (int first = blockIdx.x * G; first < a.count; first += gridDim.x * G) {
@@ -243,6 +273,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
             }
             __syncthreads();
 
+            if (SPLIT) break;  // the channel-row layout continues below
             if (active) {
                 for (int dr = 0; dr < DROWS; ++dr) {
                     const int row = row0 + dr;
@@ -282,7 +313,60 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN>(), min_ctas<LOGN, G>()
             }
             if (DROWS == 1 && row0 == 0) __syncthreads();  // the next row's digits overwrite these
         }
-        if (active) {
+        if constexpr (SPLIT) {
+            if (active) {
+                // this team's row: l forward NTTs; oa gathers the output this team finishes
+                // (row 0 -> a, row 1 -> b), ob the other output's partial sum
+                const int row = hrow;
+                for (int lvl = 0; lvl < L; ++lvl) {
+                    uint32_t x[32];
+                    const int16_t* d = dig + ((size_t)row * L + lvl) * N;
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
+                    ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
+                    const uint4* kp =
+                        key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
+                    const uint4* kown = kp + (row ? 8 : 0) * S;
+                    const uint4* kother = kp + (row ? 0 : 8) * S;
+#pragma unroll
+                    for (int rr = 0; rr < 8; ++rr) {
+                        const uint4 ka = ldg_keep(kown + rr * S + tt, keep);
+                        const uint4 kb = ldg_keep(kother + rr * S + tt, keep);
+                        const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+                        const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int r = rr * 4 + e;
+                            oa[r] += montdiff<T == 32>(x[r], kav[e], ch.p, pinv);
+                            ob[r] += montdiff<T == 32>(x[r], kbv[e], ch.p, pinv);
+                        }
+                    }
+                    // lazy accumulation as in the channel layout, reduced after odd levels
+                    // and once more at the end when l is odd: [0, 4p) on exit
+                    if ((lvl & 1) || lvl == L - 1) {
+#pragma unroll
+                        for (int r = 0; r < 32; ++r) {
+                            oa[r] = reduce_once(oa[r] + ch.two_p, 2 * ch.two_p);
+                            ob[r] = reduce_once(ob[r] + ch.two_p, 2 * ch.two_p);
+                        }
+                    }
+                }
+                // swap partial sums with the channel's other team: write the one it
+                // finishes into this team's region (its own transposes are done), wait,
+                // add the partner's, wait until the partner has read this region
+#pragma unroll
+                for (int r = 0; r < 32; ++r) mine[r * S + tt] = ob[r];
+                pair_sync<LOGN>(pair_bar);
+                const uint32_t* other = xb + (team * 2 + (1 - hrow)) * Sh::TBUF;
+#pragma unroll
+                for (int r = 0; r < 32; ++r) oa[r] = reduce_once(reduce_once(oa[r] + other[r * S + tt], 2 * ch.two_p), ch.two_p);
+                pair_sync<LOGN>(pair_bar);
+                ntt_inverse<LOGN>(oa, mine, tt, team, bar, ch);
+                team_sync<LOGN>(bar);
+#pragma unroll
+                for (int r = 0; r < 32; ++r) mine[r * S + tt] = reduce_once(oa[r], ch.p);
+            }
+        } else if (active) {
             // one copy of the inverse transform, applied to the a then the b output poly
 #pragma unroll 1
             for (int o = 0; o < 2; ++o) {
@@ -393,14 +477,14 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
     }
 }
 
-template <int LOGN, int T, int G>
+template <int LOGN, int T, int G, int SPLIT>
 int prepare_br_t() {
     // the dynamic shared-memory opt-in is per device: done once on each
     static std::atomic<bool> done[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
     if (!done[dev].load()) {
-        if (cudaFuncSetAttribute(blind_rotate_kernel<LOGN, T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(blind_rotate_kernel<LOGN, T, G, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  227 * 1024) != cudaSuccess)
             return -1;
         done[dev].store(true);
@@ -408,25 +492,26 @@ int prepare_br_t() {
     return 0;
 }
 
-template <int LOGN, int T, int G>
+template <int LOGN, int T, int G, int SPLIT>
 int launch_br_t(const BrArgs& a, void* stream) {
-    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, a.n, a.L);
+    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, a.n, a.L, SPLIT);
     if (smem > 227 * 1024) return -1;
-    if (prepare_br_t<LOGN, T, G>() != 0) return -1;
+    if (prepare_br_t<LOGN, T, G, SPLIT>() != 0) return -1;
     const int need = (a.count + G - 1) / G;
     const int grid = a.grid > 0 && a.grid < need ? a.grid : need;
-    blind_rotate_kernel<LOGN, T, G><<<grid, G * slice_threads<LOGN>(), smem, (cudaStream_t)stream>>>(a);
+    blind_rotate_kernel<LOGN, T, G, SPLIT>
+        <<<grid, G * slice_threads<LOGN, SPLIT>(), smem, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int LOGN, int T, int G>
+template <int LOGN, int T, int G, int SPLIT>
 int ctas_per_sm_t(int n, int L) {
-    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, n, L);
+    const size_t smem = (size_t)G * br_smem_bytes(LOGN, T, n, L, SPLIT);
     if (smem > 227 * 1024) return 0;
-    if (prepare_br_t<LOGN, T, G>() != 0) return -1;
+    if (prepare_br_t<LOGN, T, G, SPLIT>() != 0) return -1;
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_kernel<LOGN, T, G>,
-                                                      G * slice_threads<LOGN>(), smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_kernel<LOGN, T, G, SPLIT>,
+                                                      G * slice_threads<LOGN, SPLIT>(), smem) != cudaSuccess)
         return -1;
     return blocks;
 }
@@ -434,27 +519,31 @@ int ctas_per_sm_t(int n, int L) {
 struct LaunchBr {
     const BrArgs& a;
     void* stream;
-    template <int LN, int TB, int GG>
-    int operator()() const { return launch_br_t<LN, TB, GG>(a, stream); }
+    template <int LN, int TB, int GG, int SP>
+    int operator()() const { return launch_br_t<LN, TB, GG, SP>(a, stream); }
 };
 
 struct OccupancyBr {
     int n, L;
-    template <int LN, int TB, int GG>
-    int operator()() const { return ctas_per_sm_t<LN, TB, GG>(n, L); }
+    template <int LN, int TB, int GG, int SP>
+    int operator()() const { return ctas_per_sm_t<LN, TB, GG, SP>(n, L); }
 };
 
-// Dispatch on (N, torus width, ciphertexts per CTA); F(tag) gets the template arguments.
-// kNoVariant when that combination is not compiled.
+// Dispatch on (N, torus width, ciphertexts per CTA, layout); F(tag) gets the template
+// arguments.  kNoVariant when that combination is not compiled.
 template <typename F>
-int dispatch_br(int logN, int torus_bits, int g, F&& f) {
+int dispatch_br(int logN, int torus_bits, int g, int layout, F&& f) {
     if (g <= 0) g = 1;
-#define YG_BR_CASE(LN, TB, GG) \
-    if (logN == LN && torus_bits == TB && g == GG) return f.template operator()<LN, TB, GG>();
-    YG_BR_CASE(10, 32, 1) YG_BR_CASE(10, 32, 2) YG_BR_CASE(10, 32, 4)
-    YG_BR_CASE(10, 56, 1) YG_BR_CASE(10, 56, 2) YG_BR_CASE(10, 56, 4)
-    YG_BR_CASE(11, 32, 1) YG_BR_CASE(11, 32, 2)
-    YG_BR_CASE(11, 56, 1) YG_BR_CASE(11, 56, 2)
+#define YG_BR_CASE(LN, TB, GG, SP)                                                          \
+    if (logN == LN && torus_bits == TB && g == GG && layout == SP)                          \
+        return f.template operator()<LN, TB, GG, SP>();
+    YG_BR_CASE(10, 32, 1, 0) YG_BR_CASE(10, 32, 2, 0) YG_BR_CASE(10, 32, 4, 0)
+    YG_BR_CASE(10, 56, 1, 0) YG_BR_CASE(10, 56, 2, 0) YG_BR_CASE(10, 56, 4, 0)
+    YG_BR_CASE(11, 32, 1, 0) YG_BR_CASE(11, 32, 2, 0)
+    YG_BR_CASE(11, 56, 1, 0) YG_BR_CASE(11, 56, 2, 0)
+    YG_BR_CASE(10, 32, 1, 1) YG_BR_CASE(10, 32, 2, 1)
+    YG_BR_CASE(10, 56, 1, 1) YG_BR_CASE(10, 56, 2, 1)
+    YG_BR_CASE(11, 32, 1, 1) YG_BR_CASE(11, 56, 1, 1)
 #undef YG_BR_CASE
     return kNoVariant;
 }
@@ -477,11 +566,11 @@ int launch_keyconv(int logN, const KeyConvArgs& a, void* stream) {
 
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream) {
     if (a.count <= 0) return 0;
-    return dispatch_br(logN, torus_bits, a.per_cta, LaunchBr{a, stream});
+    return dispatch_br(logN, torus_bits, a.per_cta, a.layout, LaunchBr{a, stream});
 }
 
-int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta) {
-    return dispatch_br(logN, torus_bits, per_cta, OccupancyBr{n, L});
+int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout) {
+    return dispatch_br(logN, torus_bits, per_cta, layout, OccupancyBr{n, L});
 }
 
 int launch_keyswitch(const KsArgs& a, void* stream) {

@@ -25,6 +25,7 @@ struct BrArgs {
     int count;
     int grid;                // CTAs to launch (0: enough for the batch; fewer: persistent CTAs)
     int per_cta;             // ciphertexts per CTA, run in lockstep (1, 2 or 4; 0 means 1)
+    int layout;              // kLayoutChannel or kLayoutChannelRow
     int n;                   // LWE dimension
     int steps;               // CMux steps to run (n for a full blind rotation)
     int L;                   // gadget levels
@@ -75,12 +76,17 @@ __host__ __device__ inline size_t key_words(int n, int L, int N) {
 // digit_rows x l x N int16).
 __host__ __device__ constexpr int digit_rows(int torus_bits) { return torus_bits == 32 ? 2 : 1; }
 
-__host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L) {
+// Work split of one ciphertext (blind_rotate_kernel): a team of threads per RNS channel,
+// or per channel and accumulator row.
+constexpr int kLayoutChannel = 0;
+constexpr int kLayoutChannelRow = 1;
+
+__host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
     size_t b = kChannels * 2 * tbuf * 4;
     b += 2 * N * (torus_bits == 32 ? 4 : 8);
-    b += (size_t)digit_rows(torus_bits) * L * N * 2;
+    b += (size_t)(layout == kLayoutChannelRow ? 2 : digit_rows(torus_bits)) * L * N * 2;
     b += ((size_t)n + 1) * 2;
     return (b + 15) & ~(size_t)15;
 }
@@ -93,7 +99,7 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 // (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,
 // -1 on a CUDA error.
 constexpr int kNoVariant = -2;
-int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta);
+int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
 int launch_keyswitch(const KsArgs& a, void* stream);
 
 }  // namespace yg
