@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
     ap.add_argument("--serving-requests", type=int, default=800, help="measured requests per offered rate")
     ap.add_argument("--serving-fractions", default="0.5,0.6,0.7,0.8,0.9,1.0", help="offered rates / peak")
-    ap.add_argument("--serving-max-batch", type=int, default=608, help="ciphertexts per serving batch")
+    ap.add_argument("--serving-max-batch", type=int, default=304, help="ciphertexts per serving batch")
     ap.add_argument("--serving-inflight", type=int, default=2, help="serving batches on the GPU at once")
     return ap.parse_args()
 
@@ -420,7 +420,7 @@ def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
 
 
 def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), tenants=128, budget=4e9,
-                max_count=256, max_batch=608, max_inflight=2):
+                max_count=256, max_batch=304, max_inflight=2):
     """128 tenants on the TORUS=32 set, requests of 1..256 ciphertexts (log-uniform) arriving
     as a Poisson process, tenants Zipf(1.1)-popular, BSK/KSK in an HBM LRU cache capped at
     4 GB with refills from pinned host memory.  First the peak rate is measured with the

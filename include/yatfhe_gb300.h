@@ -208,7 +208,7 @@ typedef struct yg_trace_config {
     uint64_t zipf_seed;
     int tenants;
     int max_count;
-    int queue_max; /* requests waiting beyond this are shed (0 = no bound) */
+    int queue_max; /* arrivals that find more requests than this unfinished are shed (0 = no bound) */
     const int32_t* h_pool;
     const int32_t* h_expect;
 } yg_trace_config;

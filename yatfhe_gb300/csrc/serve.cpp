@@ -576,6 +576,7 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
 
         struct Issued {
             int64_t id;
+            Request* req;
             int slot, tenant, count;
             bool measured;
         };
@@ -584,6 +585,8 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
         std::deque<Issued> issued;
         bool producer_done = false;
         std::atomic<int> shed{0};
+        std::atomic<bool> aborted{false};  // the consumer hit an error: the producer stops
+        std::atomic<int> in_system{0};     // submitted and not yet reaped
 
         if (int rc = yg_server_start(s)) return rc;
         yg_server_counters before{};
@@ -607,25 +610,30 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
                                                        std::chrono::duration<double>(offset)));
                 const int tenant = zipf.next();
                 const int count = std::min(cfg->max_count, std::max(1, (int)std::floor(std::exp(lsz(sizes)))));
-                if (cfg->queue_max > 0) {
-                    std::lock_guard<std::mutex> lk(qm);
-                    if ((int)issued.size() > cfg->queue_max) {
-                        shed++;
-                        continue;
-                    }
+                if (cfg->queue_max > 0 && in_system.load() > cfg->queue_max) {
+                    shed++;
+                    continue;
                 }
                 int slot;
                 {
                     std::unique_lock<std::mutex> lk(fm);
-                    fcv.wait(lk, [&] { return !free_slots.empty(); });
+                    fcv.wait(lk, [&] { return !free_slots.empty() || aborted.load(); });
+                    if (aborted.load()) break;
                     slot = free_slots.front();
                     free_slots.pop_front();
                 }
                 const int32_t* in = cfg->h_pool + (size_t)tenant * req_words;
+                if (i == cfg->warmup) yg_server_stats(s, &before);  // counters of the measured window
                 const int64_t id = yg_server_submit(s, tenant, in, h_out + (size_t)slot * req_words, count);
                 if (id <= 0) break;
+                in_system++;
+                Request* req;
+                {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    req = s->requests[id].get();
+                }
                 std::lock_guard<std::mutex> lk(qm);
-                issued.push_back(Issued{id, slot, tenant, count, i >= cfg->warmup});
+                issued.push_back(Issued{id, req, slot, tenant, count, i >= cfg->warmup});
                 qcv.notify_all();
             }
             std::lock_guard<std::mutex> lk(qm);
@@ -633,41 +641,75 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
             qcv.notify_all();
         });
 
+        // Completions are reaped in whatever order they happen, and each frees its output
+        // slot at once: a request that waits long (a cold tenant) must not hold back the
+        // slots of the requests behind it, or the driver would stop offering load.
         int err = YG_OK;
+        std::vector<Issued> outstanding;
         for (;;) {
-            Issued it{};
             {
                 std::unique_lock<std::mutex> lk(qm);
-                qcv.wait(lk, [&] { return !issued.empty() || producer_done; });
-                if (issued.empty()) break;
-                it = issued.front();
-                issued.pop_front();
+                qcv.wait_for(lk, std::chrono::milliseconds(1), [&] { return !issued.empty() || producer_done; });
+                while (!issued.empty()) {
+                    outstanding.push_back(issued.front());
+                    issued.pop_front();
+                }
+                if (outstanding.empty()) {
+                    if (producer_done) break;
+                    continue;
+                }
             }
-            yg_request_times tm{};
-            const int rc = yg_server_wait(s, it.id, 600000, &tm);
-            if (rc != YG_OK) {
-                err = rc;
+            bool failed = false;
+            {
+                std::unique_lock<std::mutex> lk(s->mu);
+                s->cv_done.wait_for(lk, std::chrono::milliseconds(1), [&] {
+                    failed = !s->worker_error.empty();
+                    if (failed) return true;
+                    for (const Issued& it : outstanding)
+                        if (it.req->done.load()) return true;
+                    return false;
+                });
+            }
+            for (size_t k = 0; k < outstanding.size();) {
+                const Issued it = outstanding[k];
+                if (!failed && !it.req->done.load()) {
+                    k++;
+                    continue;
+                }
+                outstanding[k] = outstanding.back();
+                outstanding.pop_back();
+                in_system--;
+                yg_request_times tm{};
+                const int rc = yg_server_wait(s, it.id, 600000, &tm);
+                if (rc != YG_OK) {
+                    err = rc;
+                    break;
+                }
+                const int32_t* o = h_out + (size_t)it.slot * req_words;
+                if (cfg->h_expect &&
+                    std::memcmp(o, cfg->h_expect + (size_t)it.tenant * req_words, (size_t)it.count * n1 * 4) != 0)
+                    mismatched++;
+                if (it.measured) {
+                    t_first = served == 0 ? tm.t_submit : std::min(t_first, tm.t_submit);
+                    served++;
+                    measured_cts += it.count;
+                    t_last = std::max(t_last, tm.t_done);
+                    soj.push_back(1e3 * (tm.t_done - tm.t_submit));
+                    que.push_back(1e3 * (tm.t_start - tm.t_submit));
+                    svc.push_back(1e3 * (tm.t_done - tm.t_start));
+                }
+                std::lock_guard<std::mutex> lk(fm);
+                free_slots.push_back(it.slot);
+                fcv.notify_all();
+            }
+            if (err != YG_OK) {
+                {
+                    std::lock_guard<std::mutex> lk(fm);
+                    aborted.store(true);
+                }
+                fcv.notify_all();
                 break;
             }
-            const int32_t* o = h_out + (size_t)it.slot * req_words;
-            if (cfg->h_expect &&
-                std::memcmp(o, cfg->h_expect + (size_t)it.tenant * req_words, (size_t)it.count * n1 * 4) != 0)
-                mismatched++;
-            if (it.measured) {
-                if (served == 0) {
-                    t_first = tm.t_submit;
-                    yg_server_stats(s, &before);
-                }
-                served++;
-                measured_cts += it.count;
-                t_last = std::max(t_last, tm.t_done);
-                soj.push_back(1e3 * (tm.t_done - tm.t_submit));
-                que.push_back(1e3 * (tm.t_start - tm.t_submit));
-                svc.push_back(1e3 * (tm.t_done - tm.t_start));
-            }
-            std::lock_guard<std::mutex> lk(fm);
-            free_slots.push_back(it.slot);
-            fcv.notify_all();
         }
         producer.join();
         if (err != YG_OK) return err;
