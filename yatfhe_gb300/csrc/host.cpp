@@ -165,7 +165,8 @@ void validate(const yg_params& p) {
     // exactness of the three-prime RNS: |X| <= (B/2)(q/2)(k+1) l N must stay below M/2
     const double q = p.torus_bits == 32 ? 562941363486721.0 : 1945555039024054273.0;
     const double bound = std::ldexp(1.0, p.radix_bits - 1) * (q / 2) * (p.k + 1) * p.l_approx * p.N;
-    const double M = (double)yg::kPrimes[0] * yg::kPrimes[1] * yg::kPrimes[2];
+    const uint32_t* P = yg::kPrimeSet[yg::prime_set_for(p.torus_bits)];
+    const double M = (double)P[0] * P[1] * P[2];
     if (bound >= M / 4) throw std::invalid_argument("parameters exceed the exact range of the RNS");
 }
 
@@ -173,7 +174,7 @@ void ctx_init_tables(yg_ctx* c) {
     const int N = c->p.N;
     std::vector<uint2> tw((size_t)yg::kChannels * 2 * N);
     for (int ci = 0; ci < yg::kChannels; ci++) {
-        const uint32_t p = yg::kPrimes[ci];
+        const uint32_t p = yg::kPrimeSet[c->ps][ci];
         const u64 psi = minimal_root(N, p);
         const u64 psi_inv = invmod(psi, p);
         for (int k = 0; k < N; k++) {
@@ -195,15 +196,15 @@ void ctx_init_tables(yg_ctx* c) {
     for (int ci = 0; ci < yg::kChannels; ci++)
         for (int dir = 0; dir < 2; dir++)
             for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + dir) * 32 + k] = tw[((size_t)ci * 2 + dir) * N + k];
-    if (yg::set_twiddle_heads(c->logN, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
+    if (yg::set_twiddle_heads(c->logN, c->ps, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
     for (int ci = 0; ci < yg::kChannels; ci++) {
-        const uint32_t p = yg::kPrimes[ci];
+        const uint32_t p = yg::kPrimeSet[c->ps][ci];
         uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
         for (int it = 0; it < 5; it++) pinv *= 2 - p * pinv;
         c->ch[ci] = yg::Chan{p, 2 * p, (uint32_t)(0u - pinv), 0, c->d_tw + (size_t)ci * 2 * N,
                              c->d_tw + ((size_t)ci * 2 + 1) * N};
     }
-    const u64 p0 = yg::kPrimes[0], p1 = yg::kPrimes[1], p2 = yg::kPrimes[2];
+    const u64 p0 = yg::kPrimeSet[c->ps][0], p1 = yg::kPrimeSet[c->ps][1], p2 = yg::kPrimeSet[c->ps][2];
     yg::Crt& k = c->crt;
     k.p0 = (uint32_t)p0;
     k.p1 = (uint32_t)p1;
@@ -237,7 +238,7 @@ void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
                 if (buf[j] >= q) throw std::invalid_argument("key word not reduced mod q");
             qi.run(buf.data());
             for (int ci = 0; ci < yg::kChannels; ci++) {
-                const u64 p = yg::kPrimes[ci];
+                const u64 p = yg::kPrimeSet[c->ps][ci];
                 uint32_t* dst = res.data() + (poly * yg::kChannels + ci) * N;
                 for (int j = 0; j < N; j++) {
                     const u64 v = buf[j];
@@ -280,7 +281,7 @@ void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
             a.scale[ci] = c->conv_scale[ci];
             a.scale_s[ci] = c->conv_scale_s[ci];
         }
-        yg::check_launch(yg::launch_keyconv(c->logN, a, nullptr), "keyconv launch");
+        yg::check_launch(yg::launch_keyconv(c->logN, c->ps, a, nullptr), "keyconv launch");
         ck(cudaDeviceSynchronize(), "keyconv");
     } catch (...) {
         cudaFree(d_res);
@@ -425,6 +426,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
         c->p = *params;
         c->device = device;
         c->logN = params->N == 1024 ? 10 : 11;
+        c->ps = yg::prime_set_for(params->torus_bits);
         c->q = params->torus_bits == 32 ? 562941363486721ULL : 1945555039024054273ULL;
         c->qinv = std::make_shared<QInverse>(params->N, c->q);
         ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");

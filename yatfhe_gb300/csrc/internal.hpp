@@ -74,6 +74,7 @@ struct DeviceGuard {
 struct yg_ctx {
     yg_params p{};
     int logN = 0;
+    int ps = 0;             // RNS prime set (rns.cuh), fixed by the torus width
     int device = 0;
     uint64_t q = 0;
     uint2* d_tw = nullptr;  // [3][2][N]: forward then inverse twiddles per channel

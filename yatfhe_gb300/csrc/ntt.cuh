@@ -28,8 +28,9 @@ namespace yg {
 __device__ __forceinline__ int tpad(int j) { return j + (j >> 5); }
 
 // The first 32 twiddles of each table: every thread of a team uses the same ones in the
-// natural-layout stages, so they come from the constant cache.  [logN-10][channel][fwd, inv][k]
-__constant__ uint2 c_tw_head[2][kChannels][2][32];
+// natural-layout stages, so they come from the constant cache.
+// [prime set][logN-10][channel][fwd, inv][k]
+__constant__ uint2 c_tw_head[kPrimeSets][2][kChannels][2][32];
 
 template <int LOGN>
 struct TeamShape {
@@ -58,21 +59,25 @@ __device__ __forceinline__ int slot_pos(int tt, int r) {
     else return (tt >> 1) * 64 + 2 * r + (tt & 1);
 }
 
-template <int LOGN>
+// PS is the prime set (rns.cuh) of `ch`: it picks the constant-bank twiddles and the
+// reduction schedule of the forward transform.
+template <int LOGN, int PS>
 __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
-    // Input residues < 2p.  Bounds after each stage (p < 2^29, so 8p < 2^32): natural-layout
-    // stages 4p, 6p, 8p, reduce -> 6p, 8p; slot-layout stages reduce -> 6p, 8p, reduce -> 6p,
-    // 8p, reduce -> 6p (then the N = 2048 shuffle stage, reduce -> 6p).  Output < 8p.
+    // Input residues < 2p; every butterfly adds at most 2p to the bound of its x input.
+    // Prime set 0 (p < 2^29, 8p < 2^32): natural-layout stages 4p, 6p, 8p, reduce -> 6p, 8p;
+    // slot-layout stages reduce -> 6p, 8p, reduce -> 6p, 8p, reduce -> 6p (then the N = 2048
+    // shuffle stage, reduce -> 6p).  Output < 8p.  Prime set 1 (p < 2^27, 32p < 2^32): no
+    // reduction; output < 22p (N = 1024) or 24p (N = 2048).
 #pragma unroll
     for (int sp = 4; sp >= 0; --sp) {
         const int h = 1 << sp;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], c_tw_head[LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p,
-                    sp == 1);
+            ct_bfly(a[r], a[r + h], c_tw_head[PS][LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p,
+                    PS == 0 && sp == 1);
         }
     }
     team_sync<LOGN>(bar);
@@ -89,7 +94,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], __ldg(&tw[(r >> (sp + 1)) * 32]), p, two_p, (sp & 1) == 0);
+            ct_bfly(a[r], a[r + h], __ldg(&tw[(r >> (sp + 1)) * 32]), p, two_p, PS == 0 && (sp & 1) == 0);
         }
     }
     if constexpr (LOGN == 11) {
@@ -98,7 +103,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             const uint2 w = __ldg(&tw[r * 32]);
-            const uint32_t xr = reduce_once(a[r], 2 * two_p);  // U (< 4p), held by the even lane
+            const uint32_t xr = PS == 0 ? reduce_once(a[r], 2 * two_p) : a[r];  // U, held by the even lane
             const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
             const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
             a[r] = odd ? other - t + two_p : xr + other;
@@ -106,7 +111,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
     }
 }
 
-template <int LOGN>
+template <int LOGN, int PS>
 __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
@@ -146,7 +151,7 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            gs_bfly(a[r], a[r + h], c_tw_head[LOGN - 10][team][1][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p);
+            gs_bfly(a[r], a[r + h], c_tw_head[PS][LOGN - 10][team][1][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p);
         }
     }
 }

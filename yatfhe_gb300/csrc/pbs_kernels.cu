@@ -100,7 +100,7 @@ __device__ __forceinline__ typename TorusOf<T>::type tneg(typename TorusOf<T>::t
     else return sext<56>((int64_t)(U(0) - (U)a));
 }
 
-template <int LOGN>
+template <int LOGN, int PS>
 __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const KeyConvArgs a) {
     using Sh = TeamShape<LOGN>;
     constexpr int N = Sh::N, S = Sh::S;
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     uint32_t x[32];
 #pragma unroll
     for (int r = 0; r < 32; ++r) x[r] = src[r * S + tt];
-    ntt_forward<LOGN>(x, tb + team * Sh::TBUF, tt, team, team, ch);
+    ntt_forward<LOGN, PS>(x, tb + team * Sh::TBUF, tt, team, team, ch);
     const int blk = poly >> 1, o = poly & 1;
     uint32_t* dst = a.key + ((size_t)blk * kChannels + team) * key_block_words(N);
 #pragma unroll
@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOG
     using U = typename TorusOf<T>::utype;
     constexpr int N = Sh::N, S = Sh::S;
     constexpr int TEAMS = slice_teams<SPLIT>();
+    constexpr int PS = prime_set_for(T);  // the context's RNS primes (rns.cuh)
     constexpr int ST = slice_threads<LOGN, SPLIT>();
     extern __shared__ __align__(16) unsigned char smem[];
 
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOG
                         const int16_t* d = dig + ((size_t)dr * L + lvl) * N;
 #pragma unroll
                         for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                        ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
+                        ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
                         const uint4* kp =
                             key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
 #pragma unroll
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOG
                     const int16_t* d = dig + ((size_t)row * L + lvl) * N;
 #pragma unroll
                     for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                    ntt_forward<LOGN>(x, mine, tt, team, bar, ch);
+                    ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
                     const uint4* kp =
                         key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
                     const uint4* kown = kp + (row ? 8 : 0) * S;
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOG
 #pragma unroll
                 for (int r = 0; r < 32; ++r) oa[r] = reduce_once(reduce_once(oa[r] + other[r * S + tt], 2 * ch.two_p), ch.two_p);
                 pair_sync<LOGN>(pair_bar);
-                ntt_inverse<LOGN>(oa, mine, tt, team, bar, ch);
+                ntt_inverse<LOGN, PS>(oa, mine, tt, team, bar, ch);
                 team_sync<LOGN>(bar);
 #pragma unroll
                 for (int r = 0; r < 32; ++r) mine[r * S + tt] = reduce_once(oa[r], ch.p);
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOG
                 uint32_t* region = mine + o * Sh::TBUF;
 #pragma unroll
                 for (int r = 0; r < 32; ++r) oa[r] = reduce_once(oa[r], ch.two_p);  // [0, 2p) in
-                ntt_inverse<LOGN>(oa, region, tt, team, bar, ch);
+                ntt_inverse<LOGN, PS>(oa, region, tt, team, bar, ch);
                 team_sync<LOGN>(bar);
 #pragma unroll
                 for (int r = 0; r < 32; ++r) region[r * S + tt] = reduce_once(oa[r], ch.p);
@@ -551,15 +552,18 @@ int dispatch_br(int logN, int torus_bits, int g, int layout, F&& f) {
 }  // namespace
 
 
-int set_twiddle_heads(int logN, const uint2* heads) {
-    if (logN != 10 && logN != 11) return -1;
+int set_twiddle_heads(int logN, int ps, const uint2* heads) {
+    if ((logN != 10 && logN != 11) || ps < 0 || ps >= kPrimeSets) return -1;
     const size_t per = sizeof(uint2) * kChannels * 2 * 32;
-    return cudaMemcpyToSymbol(c_tw_head, heads, per, per * (logN - 10)) == cudaSuccess ? 0 : -1;
+    return cudaMemcpyToSymbol(c_tw_head, heads, per, per * (ps * 2 + logN - 10)) == cudaSuccess ? 0 : -1;
 }
 
-int launch_keyconv(int logN, const KeyConvArgs& a, void* stream) {
-    if (logN == 10) keyconv_kernel<10><<<a.polys, 3 * TeamShape<10>::S, 0, (cudaStream_t)stream>>>(a);
-    else if (logN == 11) keyconv_kernel<11><<<a.polys, 3 * TeamShape<11>::S, 0, (cudaStream_t)stream>>>(a);
+int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream) {
+    const dim3 grid(a.polys);
+    if (logN == 10 && ps == 0) keyconv_kernel<10, 0><<<grid, 3 * TeamShape<10>::S, 0, (cudaStream_t)stream>>>(a);
+    else if (logN == 10 && ps == 1) keyconv_kernel<10, 1><<<grid, 3 * TeamShape<10>::S, 0, (cudaStream_t)stream>>>(a);
+    else if (logN == 11 && ps == 0) keyconv_kernel<11, 0><<<grid, 3 * TeamShape<11>::S, 0, (cudaStream_t)stream>>>(a);
+    else if (logN == 11 && ps == 1) keyconv_kernel<11, 1><<<grid, 3 * TeamShape<11>::S, 0, (cudaStream_t)stream>>>(a);
     else return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -90,10 +90,10 @@ __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n,
     b += ((size_t)n + 1) * 2;
     return (b + 15) & ~(size_t)15;
 }
-// Uploads the first 32 forward and inverse twiddles of each channel ([3][2][32] pairs) to
-// the constant bank of the current device.
-int set_twiddle_heads(int logN, const uint2* heads);
-int launch_keyconv(int logN, const KeyConvArgs& a, void* stream);
+// Uploads the first 32 forward and inverse twiddles of each channel of prime set ps
+// ([3][2][32] pairs) to the constant bank of the current device.
+int set_twiddle_heads(int logN, int ps, const uint2* heads);
+int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream);
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream);
 // Resident blind-rotation CTAs per SM for these parameters and ciphertexts per CTA
 // (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,

@@ -13,10 +13,18 @@
 namespace yg {
 
 constexpr int kChannels = 3;
-// Largest primes below 2^29 with p == 1 mod 2^13 (negacyclic NTTs up to N = 4096).  Below
-// 2^29 so that residues up to 8p fit 32 bits: the forward NTT reduces only every other
-// stage.  Product ~2^87: the 56-bit set's |X| < 2^82.8 keeps 3.2 bits of margin below M/2.
-constexpr uint32_t kPrimes[kChannels] = {536813569u, 536690689u, 536641537u};
+// Two sets of three primes p == 1 mod 2^13 (negacyclic NTTs up to N = 4096), each the
+// largest below its bound, so p2 < p1 < p0 < 2 p2 in both.
+//   set 0: below 2^29, product ~2^87, for the 56-bit torus (|X| < 2^82.8 keeps 3.2 bits of
+//          margin below M/2); residues up to 8p fit 32 bits, so the forward NTT reduces
+//          every other stage;
+//   set 1: below 2^27, product ~2^81, for the 32-bit torus (|X| < 2^75 for every accepted
+//          parameter set, 2^66.6 at n=630/N=1024); residues up to 32p fit 32 bits, so the
+//          forward NTT (at most 11 stages adding 2p each to a < 2p input) never reduces.
+constexpr int kPrimeSets = 2;
+constexpr uint32_t kPrimeSet[kPrimeSets][kChannels] = {{536813569u, 536690689u, 536641537u},
+                                                       {134176769u, 134111233u, 134012929u}};
+__host__ __device__ constexpr int prime_set_for(int torus_bits) { return torus_bits == 32 ? 1 : 0; }
 
 // Per-channel constants the kernels read.
 struct Chan {
@@ -50,7 +58,8 @@ __device__ __forceinline__ uint32_t mulshoup(uint32_t x, uint32_t w, uint32_t wp
 
 // hi(a b) - hi(m p) with m = (a b mod 2^32) p^-1 mod 2^32: the low words of a b and m p are
 // equal, so this is exactly (a b - m p) / 2^32 = a b 2^-32 mod p, as a signed value in (-p, p)
-// for a < 8p, b < p (p < 2^29): a Montgomery product without the carry fix-up.
+// whenever a b < 2^32 p (b < p and a < 8p with p < 2^29, or a < 32p with p < 2^27): a
+// Montgomery product without the carry fix-up.
 // WIDE selects how a b is formed: one 32 x 32 -> 64 multiply, or separate low and high
 // halves; the results are identical, the instruction schedules differ (the wide form
 // measured faster in the 32-bit-torus kernels, the split form in the 56-bit ones).
