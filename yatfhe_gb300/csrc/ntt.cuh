@@ -27,6 +27,16 @@ namespace yg {
 
 __device__ __forceinline__ int tpad(int j) { return j + (j >> 5); }
 
+// The per-thread twiddle addresses depend only on the thread, so the compiler would hoist
+// those loads out of the CMux loop and keep them live in registers across the whole step;
+// reading the table pointer through a volatile move inside each transform keeps the loads
+// next to their use (measured faster, and it frees registers for the butterflies).
+__device__ __forceinline__ const uint2* pinned(const uint2* t) {
+    const uint2* r;
+    asm volatile("mov.b64 %0, %1;" : "=l"(r) : "l"(t));
+    return r;
+}
+
 // The first 32 twiddles of each table: every thread of a team uses the same ones in the
 // natural-layout stages, so they come from the constant cache.
 // [prime set][logN-10][channel][fwd, inv][k]
@@ -90,7 +100,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
     for (int sp = 4; sp >= 0; --sp) {
         const int h = 1 << sp;
-        const uint2* tw = ch.twf + (1 << (9 - sp)) + gid;
+        const uint2* tw = pinned(ch.twf) + (1 << (9 - sp)) + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
@@ -99,7 +109,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
     }
     if constexpr (LOGN == 11) {
         const bool odd = tt & 1;
-        const uint2* tw = ch.twf + 1024 + gid;
+        const uint2* tw = pinned(ch.twf) + 1024 + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             const uint2 w = __ldg(&tw[r * 32]);
@@ -118,7 +128,7 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
     const int gid = LOGN == 10 ? tt : (tt >> 1);
     if constexpr (LOGN == 11) {
         const bool odd = tt & 1;
-        const uint2* tw = ch.twi + 1024 + gid;
+        const uint2* tw = pinned(ch.twi) + 1024 + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             const uint2 w = __ldg(&tw[r * 32]);
@@ -132,7 +142,7 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
     for (int sp = 0; sp <= 4; ++sp) {
         const int h = 1 << sp;
-        const uint2* tw = ch.twi + (1 << (9 - sp)) + gid;
+        const uint2* tw = pinned(ch.twi) + (1 << (9 - sp)) + gid;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;

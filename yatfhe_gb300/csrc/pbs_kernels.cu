@@ -133,12 +133,10 @@ __host__ __device__ constexpr int slice_teams() { return SPLIT ? 2 * kChannels :
 template <int LOGN, int SPLIT>
 __host__ __device__ constexpr int slice_threads() { return slice_teams<SPLIT>() * TeamShape<LOGN>::S; }
 
-// Resident CTAs per SM the register budget is sized for (about 170 registers a thread).
-template <int LOGN, int G, int SPLIT>
-__host__ __device__ constexpr int min_ctas() {
-    return 65536 / (170 * G * slice_threads<LOGN, SPLIT>()) > 0 ? 65536 / (170 * G * slice_threads<LOGN, SPLIT>())
-                                                               : 1;
-}
+// Register cap of the blind-rotation kernels: 168 lets four 3-warp slices (or two 6-warp
+// ones) share an SM.  (A lower cap for more resident warps measured slower: the kernel
+// spills or loses more to its smaller instruction window than the extra warps hide.)
+constexpr int kBrMaxRegs = 168;
 
 // Barrier over the two teams of one channel in the channel-row layout: named barrier
 // `id` (1..15; 0 is __syncthreads) over their 2 S threads.
@@ -160,8 +158,7 @@ __device__ __forceinline__ void pair_sync(int id) {
 //                      finishes through shared memory, and each runs one inverse NTT.
 //                      Twice the threads per ciphertext, about half the time per step.
 template <int LOGN, int T, int G, int SPLIT>
-__global__ void __launch_bounds__(G * slice_threads<LOGN, SPLIT>(), min_ctas<LOGN, G, SPLIT>())
-    blind_rotate_kernel(const BrArgs a) {
+__global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
     using Sh = TeamShape<LOGN>;
     using TorusT = typename TorusOf<T>::type;
     using U = typename TorusOf<T>::utype;
