@@ -483,23 +483,6 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
             "bit_exact_vs_alone": mismatches == 0, "setup_s": setup_s}
 
 
-def leg_serving_process(dev, args):
-    """The serving leg in a process of its own, as a serving deployment runs: measured in the
-    same process after the other legs, its peak came out about 30 % lower (clocks unchanged,
-    cause not found)."""
-    cmd = [sys.executable, str(ROOT / "bench.py"), "--workload", "serving", "--serving-requests",
-           str(args.serving_requests), "--serving-fractions", args.serving_fractions, "--serving-max-batch",
-           str(args.serving_max_batch), "--serving-inflight", str(args.serving_inflight)]
-    env = {k: v for k, v in os.environ.items()
-           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT")}
-    visible = os.environ.get("CUDA_VISIBLE_DEVICES")
-    env["CUDA_VISIBLE_DEVICES"] = visible.split(",")[dev] if visible else str(dev)  # this process's GPU
-    out = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=900)
-    if out.returncode != 0:
-        raise RuntimeError(f"serving process exited {out.returncode}: {out.stderr[-400:]}")
-    return json.loads(out.stdout.strip().splitlines()[-1])["result"]
-
-
 # ------------------------------------------------------------------------------ reference arm
 
 def reference_arm(args, p, config, threads):
@@ -686,7 +669,10 @@ def main():
         extras["workloads"] = {
             "t56_n2048_batch16384": _safe(leg_t56, dev),
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
-            "serving_t32_128tenants_4GB": _safe(leg_serving_process, dev, args),
+            "serving_t32_128tenants_4GB": _safe(
+                leg_serving, dev, requests=args.serving_requests,
+                fractions=tuple(float(x) for x in args.serving_fractions.split(",")),
+                max_batch=args.serving_max_batch, max_inflight=args.serving_inflight),
         }
 
     line = {
