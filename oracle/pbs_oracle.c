@@ -2,8 +2,8 @@
  * pbs_oracle.c -- plain-C restatement of the reference's GINX/MP21 programmable
  * bootstrap and of the seeded key generation that feeds it.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker: tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py may call it; the shipped library (yatfhe_gb300/) never
+ * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the cpu_baseline and
+ * reference legs of bench.py may call it, to check or time against; the shipped library (yatfhe_gb300/) never
  * links, loads or runs it.  Every function cites the reference source it restates
  * (paths relative to the reference project).  Torus values are carried in int64 and
  * brought back to the torus width T with sext(), which reproduces both the reference's

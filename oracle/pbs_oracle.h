@@ -3,7 +3,7 @@
  * path (GINX / MP21), used as the correctness oracle.
  *
  * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the CPU-baseline leg
- * of bench.py call it as the checker; the shipped library never links it.
+ * of bench.py call it to check or time against; the shipped library never links it.
  *
  * Conventions: torus values are int64 sign-extended from the torus width T (32 or 56);
  * LWE ciphertexts are int32 words [a_0 .. a_{n-1}, b] (mod 2^32);

@@ -504,7 +504,7 @@ void yg_server_destroy(yg_server* s) {
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------- trace driver
+// ---------------------------------------------------------------------------- trace replay
 
 namespace {
 
@@ -643,7 +643,7 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
 
         // Completions are reaped in whatever order they happen, and each frees its output
         // slot at once: a request that waits long (a cold tenant) must not hold back the
-        // slots of the requests behind it, or the driver would stop offering load.
+        // slots of the requests behind it, or the producer would stop offering load.
         int err = YG_OK;
         std::vector<Issued> outstanding;
         for (;;) {
