@@ -3,8 +3,8 @@
  * bootstrap and of the seeded key generation that feeds it.
  *
  * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the cpu_baseline and
- * reference legs of bench.py may call it, to check or time against; the shipped library (yatfhe_gb300/) never
- * links, loads or runs it.  Every function cites the reference source it restates
+ * reference legs of bench.py may call it, to check or time against; the shipped library
+ * (yatfhe_gb300/) never links, loads or runs it.  Every function cites the reference source it restates
  * (paths relative to the reference project).  Torus values are carried in int64 and
  * brought back to the torus width T with sext(), which reproduces both the reference's
  * int32 wrap arithmetic (TORUS32) and its longModPow2 reductions (TORUS56).
