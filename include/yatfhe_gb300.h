@@ -152,7 +152,7 @@ void yg_plan_destroy(yg_plan* plan);
  * (0: none fits, or no such kernel). */
 int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out);
 /* Launch shape of every bootstrap on this context (the autotuner's choice): layout,
- * per_cta ciphertexts per CTA, run in lockstep; ctas_per_sm > 0 makes the grid persistent
+ * per_cta ciphertexts per CTA (sharing its L1); ctas_per_sm > 0 makes the grid persistent
  * with that many CTAs per SM, 0 launches one CTA per group of per_cta ciphertexts.
  * Default (YG_LAYOUT_CHANNEL, 1, 0). */
 int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm);

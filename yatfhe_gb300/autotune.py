@@ -4,7 +4,7 @@ The knobs (yg_ctx_set_launch / yg_plan_set_launch):
   layout       work split of one ciphertext: a thread team per RNS channel (LAYOUT_CHANNEL)
                or per channel and accumulator row (LAYOUT_CHANNEL_ROW: twice the threads,
                about half the latency per ciphertext);
-  per_cta      ciphertexts per CTA run in lockstep (1, 2, 4 at N = 1024; 1, 2 at N = 2048):
+  per_cta      ciphertexts per CTA, sharing its L1 (1, 2, 4 at N = 1024; 1, 2 at N = 2048):
                more share instruction-cache lines and key lines in L1, fewer keep more
                independent CTAs per SM;
   ctas_per_sm  0 = one CTA per group of per_cta ciphertexts (the hardware scheduler fills

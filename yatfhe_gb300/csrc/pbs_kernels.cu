@@ -145,9 +145,10 @@ __device__ __forceinline__ void pair_sync(int id) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(2 * TeamShape<LOGN>::S) : "memory");
 }
 
-// G ciphertexts per CTA run in lockstep: their warps execute the same phase at the same
-// time (one stretch of code in the instruction caches) and the G teams of a channel read
-// the same key lines, the first from L2 and the others from L1.
+// G ciphertexts (slices) per CTA share its L1: slices under one key read the same key lines
+// at about the same time, the first from L2 and the others from L1.  Each slice
+// synchronises only its own threads, so the slices drift apart freely (measured faster than
+// running them in lockstep under CTA-wide barriers).
 //
 // Layouts (SPLIT):
 //   kLayoutChannel     one team per RNS channel runs all 2 l forward NTTs of a CMux step,
@@ -180,6 +181,13 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
     // named barrier of the channel's team pair, after the team barriers
     const int pair_bar = 1 + (LOGN == 10 ? 0 : G * TEAMS) + g * kChannels + team;
     const int ltid = tid - g * ST;                           // thread in the slice
+    // barrier over this slice's threads (the CTA's when it holds one slice): slices of a CTA
+    // run independently and only share the L1
+    const int slice_bar = 1 + (LOGN == 10 ? 0 : G * TEAMS) + (SPLIT ? G * kChannels : 0) + g;
+    auto slice_sync = [&]() {
+        if constexpr (G == 1) __syncthreads();
+        else asm volatile("bar.sync %0, %1;" ::"r"(slice_bar), "r"(ST) : "memory");
+    };
     const Chan ch = pick_chan(a.ch, team);
     const int L = a.L, n = a.n;
     const uint64_t keep = l2_evict_last_policy();
@@ -215,7 +223,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             for (int i = ltid; i <= n; i += ST) sa[i] = (int16_t)modswitch_down(in[i], 31 - LOGN, LOGN + 1);
         }
     }
-    __syncthreads();
+    slice_sync();
 
     if (valid) {
         if (a.acc_in) {
@@ -234,7 +242,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             }
         }
     }
-    __syncthreads();
+    slice_sync();
 
     for (int i = 0; i < a.steps; ++i) {
         const int ai = valid ? (int)sa[i] : 0;
@@ -269,7 +277,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                                            [&](int level, int v) { d[(size_t)level * N] = (int16_t)v; });
                 }
             }
-            __syncthreads();
+            slice_sync();
 
             if (SPLIT) break;  // the channel-row layout continues below
             if (active) {
@@ -309,7 +317,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                     }
                 }
             }
-            if (DROWS == 1 && row0 == 0) __syncthreads();  // the next row's digits overwrite these
+            if (DROWS == 1 && row0 == 0) slice_sync();  // the next row's digits overwrite these
         }
         if constexpr (SPLIT) {
             if (active) {
@@ -381,7 +389,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 for (int r = 0; r < 32; ++r) region[r * S + tt] = reduce_once(oa[r], ch.p);
             }
         }
-        __syncthreads();
+        slice_sync();
 
         // CRT -> applyIntt's centred mod-q value mod 2^T, then accumulateTrlwe (trlwe.h:268-274)
         if (active) {
@@ -395,7 +403,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 else acc[idx] = sext<56>((int64_t)((uint64_t)acc[idx] + (uint64_t)v));
             }
         }
-        __syncthreads();
+        slice_sync();
     }
 
     if (valid && a.acc_out) {
@@ -411,7 +419,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             else dst[j] = (int32_t)modswitch_down((int64_t)x, T - 32, 32);
         }
     }
-    __syncthreads();  // the next ciphertexts reuse the shared-memory state
+    slice_sync();  // the next ciphertexts reuse the shared-memory state
     }
 }
 

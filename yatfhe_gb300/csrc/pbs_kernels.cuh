@@ -24,7 +24,7 @@ struct BrArgs {
     int64_t* acc_out;        // [count][(k+1) N] accumulator, or null
     int count;
     int grid;                // CTAs to launch (0: enough for the batch; fewer: persistent CTAs)
-    int per_cta;             // ciphertexts per CTA, run in lockstep (1, 2 or 4; 0 means 1)
+    int per_cta;             // ciphertexts per CTA, sharing its L1 (1, 2 or 4; 0 means 1)
     int layout;              // kLayoutChannel or kLayoutChannelRow
     int n;                   // LWE dimension
     int steps;               // CMux steps to run (n for a full blind rotation)
