@@ -68,3 +68,14 @@ def test_trace_with_evictions_is_bit_exact(served):
     assert res["sojourn"]["p50_ms"] > 0 and res["sojourn"]["p99_ms"] >= res["sojourn"]["p50_ms"]
     c = srv.counters()
     assert c["key_slots"] == 2
+
+
+def test_trace_sheds_beyond_queue_bound(served):
+    """queue_max: arrivals that find more unfinished requests than the bound are shed (the
+    reference's shed at queueMax); what is served stays bit-exact."""
+    ctx, srv, pool, expect = served
+    res = srv.run_trace(pool, expect, requests=200, warmup=0, rate=1e6, zipf_s=1.1, max_count=16, seed=9,
+                        queue_max=4)
+    assert res["shed"] > 0
+    assert res["served"] + res["shed"] == 200
+    assert res["mismatched_requests"] == 0
