@@ -141,7 +141,9 @@ def test_pbs_empty_and_single(t32_small):
 
 @pytest.mark.parametrize("which", ["t32", "t56"])
 def test_pbs_full_size_bit_exact(which, built_lib):
-    """Full parameter sets (n = 630 / N = 1024 and n = 750 / N = 2048)."""
+    """Full parameter sets: n = 630 / N = 1024 with 256 sign-bootstrapped ciphertexts of
+    random bits (the CPU-runnable sign bootstrap workload, keyset seed 0x5EED0001), and
+    n = 750 / N = 2048 with 4-bit messages through a random lookup table."""
     if which == "t32":
         p, seed = T32_N1024, 0x5EED0001
     else:
@@ -149,12 +151,12 @@ def test_pbs_full_size_bit_exact(which, built_lib):
     ora, ctx, key = _setup(p, seed, built_lib)
     rng = np.random.default_rng(6)
     if which == "t32":
-        mu, lwe = _sign_inputs(ora, 24, 7)
+        mu, lwe = _sign_inputs(ora, 256, 7)
         lut = lutmod.sign_lut(p.N, 32)
         expect = np.where(mu > 0, 1, -1)
         base = 8
     else:
-        m = rng.integers(0, 16, 16)
+        m = rng.integers(0, 16, 48)
         table = rng.integers(0, 16, 16)
         lwe = ora.encrypt((m * (1 << 27)).astype(np.int64))
         lut = lutmod.padded_message_lut(p.N, 56, table)
