@@ -166,3 +166,17 @@ def test_pbs_full_size_bit_exact(which, built_lib):
     want = ora.pbs(lwe, lut, threads=16)
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(ora.decrypt(got, base), expect)
+
+
+def test_key_words_must_be_reduced(built_lib):
+    """A key word >= q is rejected (std::invalid_argument in the reference's NTT loader)."""
+    from yatfhe_gb300 import api
+
+    p = small(T32_N1024, 4)
+    ctx = api.Context(p, 0)
+    words = np.zeros(p.bsk_ntt_words, np.uint64)
+    words[123] = p.q_ntt
+    with pytest.raises(ValueError):
+        api.BootstrapKey.from_ntt_words(ctx, words)
+    words[123] = p.q_ntt - 1
+    api.BootstrapKey.from_ntt_words(ctx, words).close()

@@ -7,8 +7,9 @@
 // only ever uses them through centred(INTT(sum NTT(d) . K) mod q) (ntt_hexl.cpp:153-175),
 // so the loader takes each key polynomial back to coefficients once (inverse negacyclic
 // transform mod q with the minimal primitive 2N-th root, bit-reversed slot order: the
-// convention HEXL documents), centres them, reduces them into the three RNS channels
-// and hands them to keyconv_kernel, which applies the GPU's own per-channel NTT.
+// convention HEXL documents), centres them and reduces them into the three RNS channels
+// (key_intt_kernel, on the GPU, with the tables QInverse builds here), and keyconv_kernel
+// applies the GPU's own per-channel NTT.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,7 +21,6 @@
 #include <new>
 #include <stdexcept>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "../../include/yatfhe_gb300.h"
@@ -224,70 +224,68 @@ void ctx_init_tables(yg_ctx* c) {
 }
 
 // NTT-domain key words -> device key.  Layout in: [n][L][k+1][k+1][N] u64.
+// Device scratch freed on every exit path.
+struct DeviceScratch {
+    std::vector<void*> ptrs;
+    template <typename T>
+    T* alloc(size_t count, const char* what) {
+        void* p = nullptr;
+        ck(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)), what);
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~DeviceScratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+// NTT-domain key words mod q -> the device key: the words go to the GPU as they are, the
+// inverse transform mod q and the split into channel residues run there (key_intt_kernel),
+// then keyconv_kernel applies each channel's forward NTT into the slot layout.
 void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
     const int n = c->p.n, N = c->p.N, L = c->p.l_approx;
     const size_t polys = (size_t)n * L * 2 * 2;
-    std::vector<uint32_t> res(polys * yg::kChannels * N);
     const QInverse& qi = *c->qinv;
-    const u64 q = c->q, half = (q + 1) / 2;
-    auto work = [&](size_t begin, size_t end) {
-        std::vector<u64> buf(N);
-        for (size_t poly = begin; poly < end; poly++) {
-            std::memcpy(buf.data(), words + poly * N, sizeof(u64) * N);
-            for (int j = 0; j < N; j++)
-                if (buf[j] >= q) throw std::invalid_argument("key word not reduced mod q");
-            qi.run(buf.data());
-            for (int ci = 0; ci < yg::kChannels; ci++) {
-                const u64 p = yg::kPrimeSet[c->ps][ci];
-                uint32_t* dst = res.data() + (poly * yg::kChannels + ci) * N;
-                for (int j = 0; j < N; j++) {
-                    const u64 v = buf[j];
-                    // centred representative: v >= (q+1)/2 stands for v - q
-                    dst[j] = v >= half ? (uint32_t)((p - (q - v) % p) % p) : (uint32_t)(v % p);
-                }
-            }
-        }
-    };
-    const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> th;
-    std::vector<std::exception_ptr> errs(hw);
-    for (unsigned t = 0; t < hw; t++) {
-        const size_t b = polys * t / hw, e = polys * (t + 1) / hw;
-        th.emplace_back([&, t, b, e] {
-            try {
-                work(b, e);
-            } catch (...) {
-                errs[t] = std::current_exception();
-            }
-        });
-    }
-    for (auto& x : th) x.join();
-    for (auto& e : errs)
-        if (e) std::rethrow_exception(e);
-
     const size_t key_words = yg::key_words(n, L, N);
     key->bsk_bytes = key_words * sizeof(uint32_t);
     ck(cudaMalloc(&key->d_bsk, key->bsk_bytes), "cudaMalloc bsk");
-    uint32_t* d_res = nullptr;
-    ck(cudaMalloc(&d_res, res.size() * sizeof(uint32_t)), "cudaMalloc key residues");
-    try {
-        ck(cudaMemcpy(d_res, res.data(), res.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload residues");
-        yg::KeyConvArgs a{};
-        a.residues = d_res;
-        a.key = key->d_bsk;
-        a.polys = (int)polys;
-        for (int ci = 0; ci < yg::kChannels; ci++) {
-            a.ch[ci] = c->ch[ci];
-            a.scale[ci] = c->conv_scale[ci];
-            a.scale_s[ci] = c->conv_scale_s[ci];
-        }
-        yg::check_launch(yg::launch_keyconv(c->logN, c->ps, a, nullptr), "keyconv launch");
-        ck(cudaDeviceSynchronize(), "keyconv");
-    } catch (...) {
-        cudaFree(d_res);
-        throw;
+    DeviceScratch scratch;
+    u64* d_words = scratch.alloc<u64>(polys * N, "cudaMalloc key words");
+    u64* d_w = scratch.alloc<u64>(N, "cudaMalloc inverse twiddles");
+    u64* d_wp = scratch.alloc<u64>(N, "cudaMalloc inverse twiddles");
+    uint32_t* d_res = scratch.alloc<uint32_t>(polys * yg::kChannels * N, "cudaMalloc key residues");
+    int* d_bad = scratch.alloc<int>(1, "cudaMalloc flag");
+    ck(cudaMemcpy(d_words, words, polys * N * sizeof(u64), cudaMemcpyHostToDevice), "upload key words");
+    ck(cudaMemcpy(d_w, qi.w.data(), N * sizeof(u64), cudaMemcpyHostToDevice), "upload inverse twiddles");
+    ck(cudaMemcpy(d_wp, qi.wp.data(), N * sizeof(u64), cudaMemcpyHostToDevice), "upload inverse twiddles");
+    ck(cudaMemset(d_bad, 0, sizeof(int)), "clear flag");
+    yg::KeyInttArgs ia{};
+    ia.words = d_words;
+    ia.residues = d_res;
+    ia.w = d_w;
+    ia.wp = d_wp;
+    ia.q = c->q;
+    ia.ninv = qi.ninv;
+    ia.ninvp = qi.ninvp;
+    for (int ci = 0; ci < yg::kChannels; ci++) ia.p[ci] = yg::kPrimeSet[c->ps][ci];
+    ia.N = N;
+    ia.polys = (int)polys;
+    ia.bad = d_bad;
+    yg::check_launch(yg::launch_key_intt(ia, nullptr), "key inverse-transform launch");
+    int bad = 0;
+    ck(cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost), "key inverse transform");
+    if (bad) throw std::invalid_argument("key word not reduced mod q");
+    yg::KeyConvArgs a{};
+    a.residues = d_res;
+    a.key = key->d_bsk;
+    a.polys = (int)polys;
+    for (int ci = 0; ci < yg::kChannels; ci++) {
+        a.ch[ci] = c->ch[ci];
+        a.scale[ci] = c->conv_scale[ci];
+        a.scale_s[ci] = c->conv_scale_s[ci];
     }
-    cudaFree(d_res);
+    yg::check_launch(yg::launch_keyconv(c->logN, c->ps, a, nullptr), "keyconv launch");
+    ck(cudaDeviceSynchronize(), "keyconv");
 }
 
 // deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)

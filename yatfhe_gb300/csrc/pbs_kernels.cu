@@ -126,6 +126,49 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     }
 }
 
+// x w mod q for x < q < 2^63, w < q, wp = floor(w 2^64 / q) (Shoup).
+__device__ __forceinline__ uint64_t mulshoup64(uint64_t x, uint64_t w, uint64_t wp, uint64_t q) {
+    const uint64_t qh = __umul64hi(x, wp);
+    const uint64_t r = x * w - qh * q;
+    return r >= q ? r - q : r;
+}
+
+__global__ void __launch_bounds__(1024) key_intt_kernel(const KeyInttArgs a) {
+    extern __shared__ uint64_t sw[];  // [N]
+    const int N = a.N, poly = blockIdx.x;
+    const uint64_t q = a.q;
+    const uint64_t* src = a.words + (size_t)poly * N;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const uint64_t v = src[j];
+        if (v >= q) atomicExch(a.bad, 1);
+        sw[j] = v < q ? v : 0;
+    }
+    __syncthreads();
+    // stage with butterfly span t: pairs (2 i t + j, 2 i t + j + t), twiddle w[N / (2t) + i]
+    for (int t = 1; t < N; t <<= 1) {
+        const int h = N / (2 * t);
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int i = b / t, j = b - i * t;
+            const int xi = 2 * i * t + j, yi = xi + t;
+            const uint64_t u = sw[xi], v = sw[yi];
+            const uint64_t s = u + v;
+            sw[xi] = s >= q ? s - q : s;
+            sw[yi] = mulshoup64(u >= v ? u - v : u + q - v, a.w[h + i], a.wp[h + i], q);
+        }
+        __syncthreads();
+    }
+    const uint64_t half = (q + 1) / 2;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const uint64_t v = mulshoup64(sw[j], a.ninv, a.ninvp, q);
+        for (int c = 0; c < kChannels; ++c) {
+            const uint64_t p = a.p[c];
+            // centred representative: v >= (q+1)/2 stands for v - q
+            a.residues[((size_t)poly * kChannels + c) * N + j] =
+                v >= half ? (uint32_t)((p - (q - v) % p) % p) : (uint32_t)(v % p);
+        }
+    }
+}
+
 // Teams of one ciphertext slice: one per RNS channel (kLayoutChannel), or one per channel
 // and accumulator row (kLayoutChannelRow).
 template <int SPLIT>
@@ -580,6 +623,13 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout) {
     return dispatch_br(logN, torus_bits, per_cta, layout, OccupancyBr{n, L});
+}
+
+int launch_key_intt(const KeyInttArgs& a, void* stream) {
+    if (a.polys <= 0) return 0;
+    if (a.N != 1024 && a.N != 2048) return -1;
+    key_intt_kernel<<<a.polys, a.N / 2, (size_t)a.N * sizeof(uint64_t), (cudaStream_t)stream>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_keyswitch(const KsArgs& a, void* stream) {

@@ -64,6 +64,22 @@ struct KeyConvArgs {
     uint32_t scale_s[kChannels];  // Shoup companions
 };
 
+// The key loader's first step, on the GPU: the inverse negacyclic transform mod q of each
+// NTT-domain key polynomial (the convention of the host's QInverse: Gentleman-Sande with
+// psi^-brv(k) twiddles and Shoup companions, bit-reversed slots in, natural coefficients
+// out, times N^-1), then each coefficient's centred representative reduced mod the three
+// RNS primes.  One CTA per polynomial.
+struct KeyInttArgs {
+    const uint64_t* words;  // [polys][N] NTT-domain words mod q
+    uint32_t* residues;     // [polys][3][N] centred coefficient residues mod p_c
+    const uint64_t* w;      // [N] psi^-brv(k) mod q
+    const uint64_t* wp;     // [N] floor(w 2^64 / q)
+    uint64_t q, ninv, ninvp;
+    uint32_t p[kChannels];
+    int N, polys;
+    int* bad;               // set to 1 when a word is not reduced mod q
+};
+
 // u32 words of one (step, level, row, channel) block of the device key: 2 output polys.
 __host__ __device__ inline size_t key_block_words(int N) { return 2 * (size_t)N; }
 __host__ __device__ inline size_t key_words(int n, int L, int N) {
@@ -94,6 +110,7 @@ __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n,
 // ([3][2][32] pairs) to the constant bank of the current device.
 int set_twiddle_heads(int logN, int ps, const uint2* heads);
 int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream);
+int launch_key_intt(const KeyInttArgs& a, void* stream);
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream);
 // Resident blind-rotation CTAs per SM for these parameters and ciphertexts per CTA
 // (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,
