@@ -98,8 +98,9 @@ void thread_minor_layout(uint2* t, int N) {
 
 namespace yg {
 
-// Inverse negacyclic transform mod q (Gentleman-Sande, psi^-brv(k) twiddles with Shoup
-// companions): bit-reversed NTT slots in, natural-order coefficients in [0, q) out.
+// Tables of the inverse negacyclic transform mod q that key_intt_kernel runs
+// (Gentleman-Sande, psi^-brv(k) twiddles with Shoup companions, bit-reversed NTT slots in,
+// natural-order coefficients out, times N^-1).
 struct QInverse {
     int N = 0, logN = 0;
     u64 q = 0;
@@ -117,31 +118,6 @@ struct QInverse {
         }
         ninv = invmod(N, q);
         ninvp = (u64)(((u128)ninv << 64) / q);
-    }
-
-    u64 mulshoup(u64 x, u64 ww, u64 wwp) const {
-        const u64 qh = (u64)(((u128)x * wwp) >> 64);
-        const u64 r = x * ww - qh * q;
-        return r >= q ? r - q : r;
-    }
-
-    void run(u64* a) const {
-        int t = 1;
-        for (int m = N; m > 1; m >>= 1) {
-            const int h = m >> 1;
-            for (int i = 0; i < h; i++) {
-                u64* x = a + 2 * i * t;
-                u64* y = x + t;
-                for (int j = 0; j < t; j++) {
-                    const u64 u = x[j], v = y[j];
-                    const u64 s = u + v;
-                    x[j] = s >= q ? s - q : s;
-                    y[j] = mulshoup(u >= v ? u - v : u + q - v, w[h + i], wp[h + i]);
-                }
-            }
-            t <<= 1;
-        }
-        for (int j = 0; j < N; j++) a[j] = mulshoup(a[j], ninv, ninvp);
     }
 };
 
