@@ -1,11 +1,14 @@
 // pbs_kernels.cu -- GB300 kernels of the GINX/MP21 programmable bootstrap.
 //
+//   key_intt_kernel      NTT-domain key words mod q -> centred coefficient residues in the
+//                        three RNS channels (done once per key upload)
 //   keyconv_kernel       BSK coefficient residues -> per-channel NTT, slot layout, Montgomery
 //                        form with N^-1 folded in (done once per key upload)
 //   blind_rotate_kernel  rescaleTlweToNewMod + genNoiselessTrlweSample + the MP21 CMux loop
 //                        (yatfhe/src/blind_rotate.cpp:1538-1565) + extractTlweFromTrlwe
-//                        (yatfhe/src/trlwe.cpp:240-250); one CTA per ciphertext, its
-//                        accumulator resident in shared memory for all n steps
+//                        (yatfhe/src/trlwe.cpp:240-250); one slice of threads per
+//                        ciphertext, its accumulator resident in shared memory for all n
+//                        steps
 //   keyswitch_kernel     switchKeyForTlwe (yatfhe/src/keyswitching.cpp:48-72) for a tile of
 //                        ciphertexts x output columns, KSK rows streamed once per tile
 #include <cuda_runtime.h>
