@@ -11,7 +11,7 @@ The knobs (yg_ctx_set_launch / yg_plan_set_launch):
                the SMs), c > 0 = a persistent grid of c CTAs per SM looping over the batch.
 Each candidate that fits an SM is timed with CUDA events on a sample batch (throughput)
 and on one ciphertext alone (latency); the best for the objective -- the most bootstraps
-per second, or for serving the lowest lone-ciphertext latency within 5 % of that -- is
+per second, or for serving the lowest lone-ciphertext latency within 15 % of that -- is
 applied to the context and cached in yatfhe_gb300/_build/autotune.json per (GPU,
 parameter set, objective), so later processes reuse it without measuring.
 """
@@ -101,14 +101,17 @@ def measure(ctx, key, lut, count: int, per_cta: int, ctas_per_sm: int, reps: int
 OBJECTIVES = ("throughput", "latency")
 
 
+LATENCY_WINDOW = 0.85  # the latency objective considers shapes with this share of peak throughput
+
+
 def pick(results: list[dict], objective: str) -> dict:
-    """throughput: the most bootstraps per second; latency: of the shapes within 5 % of that,
+    """throughput: the most bootstraps per second; latency: of the shapes within 15 % of that,
     the one that finishes a lone ciphertext soonest (what a serving loop under partial load
     sees)."""
     best = max(results, key=lambda r: r["bootstraps_per_s"])
     if objective == "throughput":
         return best
-    near = [r for r in results if r["bootstraps_per_s"] >= 0.95 * best["bootstraps_per_s"]]
+    near = [r for r in results if r["bootstraps_per_s"] >= LATENCY_WINDOW * best["bootstraps_per_s"]]
     return min(near, key=lambda r: r["single_ms"])
 
 
