@@ -67,7 +67,10 @@ int yg_key_load_bsk_file(yg_ctx* ctx, const char* path, yg_key** out);
 
 /* Same, from the NTT-domain words of BootstrappingKeyMP::bskDft
  * (yatfhe/include/yatfhe/bootstrapping.h:47-114) laid out [n][l][k+1][k+1][N]:
- * row r < k is c[lvl][r], row k is cPrime[lvl]; poly p < k is a[p], poly k is b. */
+ * row r < k is c[lvl][r], row k is cPrime[lvl]; poly p < k is a[p], poly k is b.  The
+ * conversion to the device form (inverse transform mod q, split into the RNS channels,
+ * each channel's forward transform) runs on the GPU; a word not reduced mod q is rejected
+ * with YG_ERR_INVALID.  Synchronizes the device. */
 int yg_key_upload_bsk_ntt(yg_ctx* ctx, const uint64_t* h_bsk_ntt, yg_key** out);
 
 /* Attaches the key-switching key (TlweKeySwitchingKey::decomposedKsk,
