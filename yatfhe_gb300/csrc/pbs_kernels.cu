@@ -310,18 +310,30 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             // tmp = X^{a_i} acc - acc (rotateTrlweMinusOne, yatfhe/src/trlwe.cpp:284-289) for
             // DROWS rows, then gadgetDecomposeTrlwe (yatfhe/src/trlwe.cpp:185-198) into int16 digits
             if (active) {
+                // LC, RC > 0 fix the level count and radix at compile time (the digit loop
+                // unrolls with constant shifts); 0 reads them from the arguments
+                auto decompose = [&](auto lc, auto rc) {
+                    constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
+                    const int levels = LC ? LC : L, radix = RC ? RC : a.radix_bits;
 #pragma unroll 1
-                for (int idx = ltid; idx < DROWS * N; idx += ST) {
-                    const int dr = idx >= N;
-                    const int j = idx - dr * N;
-                    const TorusT* A = acc + (row0 + dr) * N;
-                    TorusT rot = j < at ? tneg<T>(A[j - at + N]) : A[j - at];
-                    if (wrap) rot = tneg<T>(rot);
-                    const TorusT tmp = tsub<T>(rot, A[j]);
-                    int16_t* d = dig + (size_t)dr * L * N + j;
-                    zero_mean_digits<U, T>((U)tmp, L, a.radix_bits,
-                                           [&](int level, int v) { d[(size_t)level * N] = (int16_t)v; });
-                }
+                    for (int idx = ltid; idx < DROWS * N; idx += ST) {
+                        const int dr = idx >= N;
+                        const int j = idx - dr * N;
+                        const TorusT* A = acc + (row0 + dr) * N;
+                        TorusT rot = j < at ? tneg<T>(A[j - at + N]) : A[j - at];
+                        if (wrap) rot = tneg<T>(rot);
+                        const TorusT tmp = tsub<T>(rot, A[j]);
+                        int16_t* d = dig + dr * levels * N + j;
+                        zero_mean_digits<U, T>((U)tmp, levels, radix, [&](int level, int v) { d[level * N] = (int16_t)v; });
+                    }
+                };
+                using std::integral_constant;
+                if (T == 32 && L == 3 && a.radix_bits == 7)
+                    decompose(integral_constant<int, 3>{}, integral_constant<int, 7>{});
+                else if (T == 56 && L == 4 && a.radix_bits == 10)
+                    decompose(integral_constant<int, 4>{}, integral_constant<int, 10>{});
+                else
+                    decompose(integral_constant<int, 0>{}, integral_constant<int, 0>{});
             }
             slice_sync();
 
