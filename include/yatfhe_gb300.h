@@ -73,6 +73,22 @@ int yg_key_load_bsk_file(yg_ctx* ctx, const char* path, yg_key** out);
  * with YG_ERR_INVALID.  Synchronizes the device. */
 int yg_key_upload_bsk_ntt(yg_ctx* ctx, const uint64_t* h_bsk_ntt, yg_key** out);
 
+/* WWL+24 keys (BootstrappingKeyWWL24, yatfhe/include/yatfhe/bootstrapping.h:116-135): the
+ * half TRGSW rows cPrime of every key index, [n][l_approx][k+1][N], and the s2 key s2Dft
+ * with s2_levels (the reference's param.l) levels, [s2_levels][k+1][N], NTT-domain words
+ * mod q (poly p < k is a[p], poly k is b).  The GPU derives,
+ * once per key, the GINX rows blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412)
+ * rebuilds before every external product (switchTrlweToSecretEmbeddingNtt,
+ * yatfhe/src/trgsw.cpp:861-905), so the key handle then runs every bootstrap and
+ * blind-rotation entry point below with the WWL+24 results.  Requires s2_levels <= 8 and
+ * s2_levels * radix_bits <= torus_bits; a word not reduced mod q is rejected with YG_ERR_INVALID.  Synchronizes the device. */
+int yg_key_upload_wwl24_ntt(yg_ctx* ctx, const uint64_t* h_cprime, const uint64_t* h_s2, int s2_levels,
+                            yg_key** out);
+
+/* Replaces deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): reads a file written
+ * by serializeBskWWL24 (:220-229) and uploads it as above. */
+int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);
+
 /* Attaches the key-switching key (TlweKeySwitchingKey::decomposedKsk,
  * yatfhe/include/yatfhe/keyswitching.h:14-31) as int32 words [k N][t][n + 1]. */
 int yg_key_set_ksk(yg_key* key, const int32_t* h_ksk);

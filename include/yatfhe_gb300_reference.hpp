@@ -14,6 +14,7 @@
 //   functionalBootstrappingMPNtt   yatfhe/include/yatfhe/bootstrapping.h:369-370
 //   blindRotateMP21Ntt             yatfhe/include/yatfhe/blind_rotate.h:69
 //   blindRotateJP22Ntt             yatfhe/include/yatfhe/blind_rotate.h:65 (binary keys)
+//   blindRotateWWL24Ntt            yatfhe/include/yatfhe/blind_rotate.h:61
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
 // plus a batched form of the first, which the reference does not have.
 #ifndef YATFHE_GB300_REFERENCE_HPP
@@ -121,6 +122,28 @@ inline yg_key* device_key(yg_ctx* c, const std::vector<std::vector<TrgswMPDft>>&
     return key;
 }
 
+// BootstrappingKeyWWL24 (yatfhe/include/yatfhe/bootstrapping.h:116-135) -> device key: the
+// cPrime rows [n][l][k+1][N] and the s2 key [levels][k+1][N]; the GPU derives the GINX rows.
+inline yg_key* device_key_wwl24(yg_ctx* c, const BootstrappingKeyWWL24& bsk, int k, int N) {
+    auto& r = reg();
+    auto it = r.keys.find(&bsk);
+    if (it != r.keys.end()) return it->second;
+    std::vector<uint64_t> cprime, s2;
+    auto put = [&](std::vector<uint64_t>& w, const TrlweDft& t) {
+        for (int poly = 0; poly <= k; poly++) {
+            const auto& P = poly < k ? t.a[poly] : t.b;
+            w.insert(w.end(), P.coeffs.begin(), P.coeffs.begin() + N);
+        }
+    };
+    for (const auto& g : bsk.bskDft)
+        for (const auto& t : g.cPrime) put(cprime, t);
+    for (const auto& t : bsk.s2Dft.trlweDfts) put(s2, t);
+    yg_key* key = nullptr;
+    check(yg_key_upload_wwl24_ntt(c, cprime.data(), s2.data(), static_cast<int>(bsk.s2Dft.trlweDfts.size()), &key));
+    r.keys[&bsk] = key;
+    return key;
+}
+
 template <typename T>
 struct DeviceBuf {
     T* p = nullptr;
@@ -170,6 +193,30 @@ inline void functionalBootstrappingMPNtt(Tlwe& out, const Tlwe& input, const Boo
     out = o[0];
 }
 
+namespace detail {
+
+// accum (already genNoiselessTrlweSample'd) rotated in place under `key`.
+inline void rotate_accumulator(yg_ctx* c, yg_key* key, Trlwe& accum, const ScaledTlwe& input,
+                               const YatfheParameters& param) {
+    const int n = param.n, N = param.N, k = param.k;
+    std::vector<int32_t> a(input.a.begin(), input.a.end());
+    std::vector<int64_t> acc(static_cast<size_t>(k + 1) * N);
+    for (int p = 0; p < k; p++)
+        for (int j = 0; j < N; j++) acc[static_cast<size_t>(p) * N + j] = accum.a[p].coeffs[j];
+    for (int j = 0; j < N; j++) acc[static_cast<size_t>(k) * N + j] = accum.b.coeffs[j];
+    DeviceBuf<int32_t> d_a(n);
+    DeviceBuf<int64_t> d_acc(acc.size());
+    cuda(cudaMemcpy(d_a.p, a.data(), a.size() * 4, cudaMemcpyHostToDevice));
+    cuda(cudaMemcpy(d_acc.p, acc.data(), acc.size() * 8, cudaMemcpyHostToDevice));
+    check(yg_blind_rotate_acc(c, key, d_a.p, d_acc.p, 1, nullptr));
+    cuda(cudaMemcpy(acc.data(), d_acc.p, acc.size() * 8, cudaMemcpyDeviceToHost));
+    for (int p = 0; p < k; p++)
+        for (int j = 0; j < N; j++) accum.a[p].coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(p) * N + j]);
+    for (int j = 0; j < N; j++) accum.b.coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(k) * N + j]);
+}
+
+}  // namespace detail
+
 // blindRotateMP21Ntt: accum (already genNoiselessTrlweSample'd) is rotated in place.
 inline void blindRotateMP21Ntt(Trlwe& accum, const std::vector<std::vector<TrgswMPDft>>& bskDft,
                                const ScaledTlwe& input, const YatfheParameters& param) {
@@ -177,21 +224,18 @@ inline void blindRotateMP21Ntt(Trlwe& accum, const std::vector<std::vector<Trgsw
     std::lock_guard<std::mutex> g(r.mu);
     yg_ctx* c = detail::context(detail::params_of(param, bskDft[0][0].l));
     yg_key* key = detail::device_key(c, bskDft, nullptr, param.k, param.N);
-    const int n = param.n, N = param.N, k = param.k;
-    std::vector<int32_t> a(input.a.begin(), input.a.end());
-    std::vector<int64_t> acc(static_cast<size_t>(k + 1) * N);
-    for (int p = 0; p < k; p++)
-        for (int j = 0; j < N; j++) acc[static_cast<size_t>(p) * N + j] = accum.a[p].coeffs[j];
-    for (int j = 0; j < N; j++) acc[static_cast<size_t>(k) * N + j] = accum.b.coeffs[j];
-    detail::DeviceBuf<int32_t> d_a(n);
-    detail::DeviceBuf<int64_t> d_acc(acc.size());
-    detail::cuda(cudaMemcpy(d_a.p, a.data(), a.size() * 4, cudaMemcpyHostToDevice));
-    detail::cuda(cudaMemcpy(d_acc.p, acc.data(), acc.size() * 8, cudaMemcpyHostToDevice));
-    detail::check(yg_blind_rotate_acc(c, key, d_a.p, d_acc.p, 1, nullptr));
-    detail::cuda(cudaMemcpy(acc.data(), d_acc.p, acc.size() * 8, cudaMemcpyDeviceToHost));
-    for (int p = 0; p < k; p++)
-        for (int j = 0; j < N; j++) accum.a[p].coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(p) * N + j]);
-    for (int j = 0; j < N; j++) accum.b.coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(k) * N + j]);
+    detail::rotate_accumulator(c, key, accum, input, param);
+}
+
+// blindRotateWWL24Ntt: the same rotation on a WWL+24 key (its GINX rows derived once, on the GPU).
+inline void blindRotateWWL24Ntt(Trlwe& accum, const BootstrappingKeyWWL24& bsk, const ScaledTlwe& input,
+                                const YatfheParameters& param) {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    const int levels = bsk.bskDft.empty() ? param.lApprox : bsk.bskDft[0].l;
+    yg_ctx* c = detail::context(detail::params_of(param, levels));
+    yg_key* key = detail::device_key_wwl24(c, bsk, param.k, param.N);
+    detail::rotate_accumulator(c, key, accum, input, param);
 }
 
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,

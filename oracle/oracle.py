@@ -165,6 +165,28 @@ class _Common:
         self._call("pbs", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), threads)
         return out
 
+    # WWL+24 keys: cprime [n][l_approx][k+1][N] and s2 [l][k+1][N] NTT-domain words.
+    def keygen_wwl24(self, seed: int) -> None:
+        self._call("keygen_wwl24", ctypes.c_uint64(seed))
+
+    def wwl24_words(self):
+        p = self.p
+        cprime = np.zeros((p.n, p.l_approx, p.k + 1, p.N), np.uint64)
+        s2 = np.zeros((p.l, p.k + 1, p.N), np.uint64)
+        self._call("get_wwl24" if self.prefix == "po_" else "export_wwl24", _ptr(cprime, _u64p), _ptr(s2, _u64p))
+        return cprime, s2
+
+    def wwl24_expanded(self) -> np.ndarray:
+        """The GINX rows blindRotateWWL24Ntt derives from the WWL+24 key, [n][l_approx][k+1][k+1][N]
+        (the layout of bsk_ntt())."""
+        p = self.p
+        if self.prefix == "po_":
+            self._call("wwl24_expand")
+            return self.bsk_ntt()
+        out = np.zeros(p.n * p.l_approx * (p.k + 1) ** 2 * p.N, np.uint64)
+        self._call("wwl24_expand", _ptr(out, _u64p))
+        return out
+
 
 class Restatement(_Common):
     """The plain-C oracle for one parameter set."""
@@ -224,6 +246,22 @@ class Restatement(_Common):
     def load_bsk_file(self, path) -> None:
         self._call("load_bsk_file", str(path).encode())
 
+    def set_wwl24(self, cprime, s2) -> None:
+        a = np.ascontiguousarray(cprime, np.uint64)
+        b = np.ascontiguousarray(s2, np.uint64)
+        self._call("set_wwl24", _ptr(a, _u64p), _ptr(b, _u64p))
+
+    def save_wwl24_file(self, path) -> None:
+        self._call("save_wwl24_file", str(path).encode())
+
+    def load_wwl24_file(self, path) -> None:
+        self._call("load_wwl24_file", str(path).encode())
+
+    def pbs_wwl24(self, lwe, v, threads: int = 1) -> np.ndarray:
+        """The WWL+24 bootstrap: the GINX bootstrap on the expanded key."""
+        self._call("wwl24_expand")
+        return self.pbs(lwe, v, threads)
+
     @property
     def q(self) -> int:
         return int(Restatement._lib.po_qntt(self._h))
@@ -264,6 +302,22 @@ class Reference(_Common):
 
     def load_bsk_file(self, path) -> None:
         self._call("load_bsk", str(path).encode())
+
+    def save_wwl24_file(self, path) -> None:
+        self._call("save_wwl24", str(path).encode())
+
+    def load_wwl24_file(self, path) -> None:
+        self._call("load_wwl24", str(path).encode())
+
+    def pbs_wwl24(self, lwe, v, with_acc: bool = False):
+        """functionalBootstrappingMPNtt's composition around blindRotateWWL24Ntt; with_acc also
+        returns ciphertext 0's accumulator after the blind rotation."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
+        self._call("pbs_wwl24", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
+        return (out, acc) if with_acc else out
 
     def set_keys(self, lwe_s, rlwe_s) -> None:
         a = np.ascontiguousarray(lwe_s, np.int32)

@@ -149,6 +149,8 @@ struct po_ctx {
     uint64_t* rlwe_s_ntt;/* k*N */
     uint64_t* bsk;       /* [n][L][k+1][k+1][N] */
     int32_t* ksk;        /* [k*N][t][n+1] */
+    uint64_t* wwl_cprime;/* WWL+24 key: [n][L][k+1][N] (allocated on first use) */
+    uint64_t* wwl_s2;    /* [l][k+1][N] */
     char err[256];
 };
 
@@ -203,6 +205,8 @@ void po_destroy(po_ctx* c) {
     free(c->rlwe_s_ntt);
     free(c->bsk);
     free(c->ksk);
+    free(c->wwl_cprime);
+    free(c->wwl_s2);
     free(c);
 }
 
@@ -330,12 +334,36 @@ static void enc_tlwe(po_ctx* c, int32_t* out, int64_t message, const int32_t* s,
  * per-i body of genBootstrappingKeyMP, bootstrapping.cpp:150-174), genTlweKeySwitchingKey
  * (yatfhe/src/keyswitching.cpp:19-29).
  */
-int po_keygen(po_ctx* c, uint64_t seed) {
-    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, T = c->T;
-    const int k1 = k + 1;
+/* genTlweKey (yatfhe/src/tlwe.cpp:10-18) and genTrlweKey (yatfhe/src/trlwe.cpp:70-81) on a
+ * fresh stream 0 of `seed`; tmpT is N words of scratch. */
+static void keygen_secrets(po_ctx* c, uint64_t seed, int64_t* tmpT) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k;
     rng_seed(&c->rng, seed, 0);
     c->have_rng = 1;
     for (int i = 0; i < n; i++) c->lwe_s[i] = rng_binary(&c->rng);
+    for (int r = 0; r < k; r++) {
+        for (int j = 0; j < N; j++) c->rlwe_s[(size_t)r * N + j] = rng_binary(&c->rng);
+        for (int j = 0; j < N; j++) tmpT[j] = c->rlwe_s[(size_t)r * N + j];
+        ntt_from_torus(c, c->rlwe_s_ntt + (size_t)r * N, tmpT);
+    }
+}
+
+/* genTlweKeySwitchingKey (yatfhe/src/keyswitching.cpp:19-29):
+ * ksk[i][j] = LWE_s(s'_i * 2^(32 - (j+1) ksRadix)). */
+static void keygen_ksk(po_ctx* c) {
+    const int kN = c->p.k * c->p.N, t = c->p.ks_level, n = c->p.n, nb = n + 1;
+    for (int i = 0; i < kN; i++) {
+        for (int j = 0; j < t; j++) {
+            const int sh = 32 - (j + 1) * c->p.ks_radix_bits;
+            const int64_t m = sext((int64_t)c->rlwe_s[i] << sh, c->T);
+            enc_tlwe(c, c->ksk + ((size_t)i * t + j) * nb, m, c->lwe_s, n);
+        }
+    }
+}
+
+int po_keygen(po_ctx* c, uint64_t seed) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, T = c->T;
+    const int k1 = k + 1;
     int64_t* tmpT = (int64_t*)calloc((size_t)N, sizeof(int64_t));
     int64_t* muPoly = (int64_t*)calloc((size_t)N, sizeof(int64_t));
     uint64_t* muNtt = (uint64_t*)calloc((size_t)N, sizeof(uint64_t));
@@ -344,11 +372,7 @@ int po_keygen(po_ctx* c, uint64_t seed) {
         free(tmpT); free(muPoly); free(muNtt); free(zeroPoly);
         return fail(c, "po_keygen: out of memory");
     }
-    for (int r = 0; r < k; r++) {
-        for (int j = 0; j < N; j++) c->rlwe_s[(size_t)r * N + j] = rng_binary(&c->rng);
-        for (int j = 0; j < N; j++) tmpT[j] = c->rlwe_s[(size_t)r * N + j];
-        ntt_from_torus(c, c->rlwe_s_ntt + (size_t)r * N, tmpT);
-    }
+    keygen_secrets(c, seed, tmpT);
     const size_t rowWords = (size_t)k1 * N;           /* one RLWE sample */
     const size_t lvlWords = (size_t)k1 * rowWords;    /* c[lvl][0..k-1] + cPrime[lvl] */
     for (int i = 0; i < n; i++) {
@@ -368,15 +392,7 @@ int po_keygen(po_ctx* c, uint64_t seed) {
             }
         }
     }
-    /* key switching key: ksk[i][j] = LWE_s(s'_i * 2^(32 - (j+1) ksRadix)) */
-    const int kN = k * N, t = c->p.ks_level, nb = n + 1;
-    for (int i = 0; i < kN; i++) {
-        for (int j = 0; j < t; j++) {
-            const int sh = 32 - (j + 1) * c->p.ks_radix_bits;
-            const int64_t m = sext((int64_t)c->rlwe_s[i] << sh, T);
-            enc_tlwe(c, c->ksk + ((size_t)i * t + j) * nb, m, c->lwe_s, n);
-        }
-    }
+    keygen_ksk(c);
     free(tmpT);
     free(muPoly);
     free(muNtt);
@@ -821,4 +837,250 @@ int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* o
     free(jobs);
     free(tids);
     return rc ? fail(c, "po_pbs: worker failed") : 0;
+}
+
+/* ------------------------------------------------------------------ WWL+24 keys */
+
+static size_t wwl_cprime_words(const po_ctx* c) {
+    return (size_t)c->p.n * c->L * (c->p.k + 1) * c->p.N;
+}
+static size_t wwl_s2_words(const po_ctx* c) { return (size_t)c->p.l * (c->p.k + 1) * c->p.N; }
+
+static int wwl_alloc(po_ctx* c) {
+    if (!c->wwl_cprime) c->wwl_cprime = (uint64_t*)calloc(wwl_cprime_words(c), sizeof(uint64_t));
+    if (!c->wwl_s2) c->wwl_s2 = (uint64_t*)calloc(wwl_s2_words(c), sizeof(uint64_t));
+    return c->wwl_cprime && c->wwl_s2 ? 0 : -1;
+}
+
+/* uniformTorusDistrib(TORUS_MIN, TORUS_MAX) (yatfhe/src/numeric.cpp:223-227), TORUS_MIN/MAX =
+ * -2^(T-1) and 2^(T-1)-1 (yatfhe/src/initializer.cpp:56-57). */
+static inline int64_t rng_torus(po_ctx* c) {
+    return rng_uniform_i64(&c->rng, -((int64_t)1 << (c->T - 1)), ((int64_t)1 << (c->T - 1)) - 1);
+}
+
+/* multTorusPolynomialAcc (yatfhe/src/polynomial.cpp:355-368): res += a * s, negacyclic, mod 2^T
+ * (the int64 accumulator only ever matters mod 2^T, so it is kept as a wrapping uint64). */
+static void mult_torus_acc(const po_ctx* c, int64_t* res, const int64_t* a, const int32_t* s) {
+    const int N = c->p.N;
+    for (int i = 0; i < N; i++) {
+        uint64_t t = 0;
+        for (int j = 0; j < N; j++) {
+            const uint64_t prod = (uint64_t)a[j] * (uint64_t)(int64_t)(j <= i ? s[i - j] : s[N + i - j]);
+            t = j <= i ? t + prod : t - prod;
+        }
+        res[i] = sext((int64_t)((uint64_t)res[i] + t), c->T);
+    }
+}
+
+/*
+ * symEncTrlweMultiSampleNtt (yatfhe/src/trlwe.cpp:103-106): initTrlweMultiSample (:32-38) draws
+ * b = mu + TUniform noise, then the masks a[r] uniformly on the torus; symEncTrlweNtt (:53-57)
+ * keeps the NTT-domain sample (NTT(a), NTT(b) + NTT(a) . NTT(s)) mod q.  out = [a_0..a_{k-1}, b].
+ */
+static void enc_trlwe_coef_ntt(po_ctx* c, uint64_t* out, const int64_t* mu, int64_t* tmpT) {
+    const int N = c->p.N, k = c->p.k;
+    uint64_t* b = out + (size_t)k * N;
+    for (int j = 0; j < N; j++) tmpT[j] = sext(mu[j] + rng_tuniform(&c->rng, c->p.rlwe_noise_b), c->T);
+    ntt_from_torus(c, b, tmpT);
+    for (int r = 0; r < k; r++) {
+        for (int j = 0; j < N; j++) tmpT[j] = rng_torus(c);
+        ntt_from_torus(c, out + (size_t)r * N, tmpT);
+    }
+    for (int r = 0; r < k; r++)
+        for (int j = 0; j < N; j++)
+            b[j] = addmod(b[j], nq_mulmod(&c->plan.br, out[(size_t)r * N + j], c->rlwe_s_ntt[(size_t)r * N + j]), c->q);
+}
+
+/*
+ * symEncTrlevWithKeyNtt(out, key, key.s, isPos = true) (yatfhe/src/trlev.cpp:75-96): l RLWE
+ * encryptions of 0 in the coefficient domain (encTrlevSingleSample, :10-16, each one
+ * symEncTrlweSingleSample = noise b, uniform masks, b += a s, trlwe.cpp:18-23,48-52,81-84),
+ * then per level a[r] -= s_r 2^(T - (i+1) radix) and both polynomials to the NTT domain.
+ * out = [l][a_0..a_{k-1}, b][N].
+ */
+static int enc_trlev_s(po_ctx* c, uint64_t* out) {
+    const int N = c->p.N, k = c->p.k, l = c->p.l, T = c->T;
+    const size_t row = (size_t)(k + 1) * N;
+    int64_t* smp = (int64_t*)malloc(sizeof(int64_t) * row * l);
+    if (!smp) return -1;
+    for (int i = 0; i < l; i++) {
+        int64_t* a = smp + (size_t)i * row;
+        int64_t* b = a + (size_t)k * N;
+        for (int j = 0; j < N; j++) b[j] = sext(rng_tuniform(&c->rng, c->p.rlwe_noise_b), T);
+        for (int r = 0; r < k; r++)
+            for (int j = 0; j < N; j++) a[(size_t)r * N + j] = rng_torus(c);
+        for (int r = 0; r < k; r++) mult_torus_acc(c, b, a + (size_t)r * N, c->rlwe_s + (size_t)r * N);
+    }
+    for (int i = 0; i < l; i++) {
+        int64_t* a = smp + (size_t)i * row;
+        uint64_t* o = out + (size_t)i * row;
+        ntt_from_torus(c, o + (size_t)k * N, a + (size_t)k * N);
+        const int sh = T - (i + 1) * c->p.radix_bits;
+        for (int r = 0; r < k; r++) {
+            for (int j = 0; j < N; j++)
+                a[(size_t)r * N + j] = sext(a[(size_t)r * N + j] - ((int64_t)c->rlwe_s[(size_t)r * N + j] << sh), T);
+            ntt_from_torus(c, o + (size_t)r * N, a + (size_t)r * N);
+        }
+    }
+    free(smp);
+    return 0;
+}
+
+/*
+ * WWL+24 keys from a seed, in the order oracle/ref_capi.cpp:ref_keygen_wwl24 draws them on one
+ * stream: the LWE and RLWE secrets, then per i and level the half-TRGSW row
+ * cPrime[i][lvl] = RLWE(s_i g_lvl) (the per-i body of genBootstrappingKeyWWL24,
+ * yatfhe/src/bootstrapping.cpp:106-126), then the key s2 = RLev(-s . s) (enc_trlev_s), then
+ * the key-switching key.
+ */
+int po_keygen_wwl24(po_ctx* c, uint64_t seed) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, T = c->T;
+    if (wwl_alloc(c)) return fail(c, "po_keygen_wwl24: out of memory");
+    int64_t* tmpT = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    int64_t* muPoly = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    if (!tmpT || !muPoly) {
+        free(tmpT); free(muPoly);
+        return fail(c, "po_keygen_wwl24: out of memory");
+    }
+    keygen_secrets(c, seed, tmpT);
+    const size_t row = (size_t)(k + 1) * N;
+    for (int i = 0; i < n; i++) {
+        memset(muPoly, 0, sizeof(int64_t) * N);
+        for (int lvl = 0; lvl < L; lvl++) {
+            muPoly[0] = sext((int64_t)c->lwe_s[i] << (T - (lvl + 1) * c->p.radix_bits), T);
+            enc_trlwe_coef_ntt(c, c->wwl_cprime + ((size_t)i * L + lvl) * row, muPoly, tmpT);
+        }
+    }
+    int rc = enc_trlev_s(c, c->wwl_s2);
+    free(tmpT);
+    free(muPoly);
+    if (rc) return fail(c, "po_keygen_wwl24: out of memory");
+    keygen_ksk(c);
+    return 0;
+}
+
+int po_get_wwl24(po_ctx* c, uint64_t* cprime, uint64_t* s2) {
+    if (!c->wwl_cprime || !c->wwl_s2) return fail(c, "po_get_wwl24: no WWL+24 key");
+    memcpy(cprime, c->wwl_cprime, sizeof(uint64_t) * wwl_cprime_words(c));
+    memcpy(s2, c->wwl_s2, sizeof(uint64_t) * wwl_s2_words(c));
+    return 0;
+}
+
+int po_set_wwl24(po_ctx* c, const uint64_t* cprime, const uint64_t* s2) {
+    if (wwl_alloc(c)) return fail(c, "po_set_wwl24: out of memory");
+    memcpy(c->wwl_cprime, cprime, sizeof(uint64_t) * wwl_cprime_words(c));
+    memcpy(c->wwl_s2, s2, sizeof(uint64_t) * wwl_s2_words(c));
+    return 0;
+}
+
+/*
+ * switchTrlweToSecretEmbeddingNtt (yatfhe/src/trgsw.cpp:861-905) for every key index and
+ * level, written into the GINX key (c->bsk, [i][lvl][row][poly][N]): the mask polynomials of
+ * cPrime[lvl] go back to the torus (applyIntt), decomposeRow splits them into l digit
+ * polynomials, and
+ *   c[lvl][k1].a[k2] = sum_l' NTT(d_l'(a_k1)) . s2[l'].a[k2] + cPrime[lvl].b,
+ *   c[lvl][k1].b     = sum_l' NTT(d_l'(a_k1)) . s2[l'].b            (mod q);
+ * row k is cPrime[lvl] itself.  These are the rows blindRotateWWL24Ntt hands to its external
+ * product (yatfhe/src/blind_rotate.cpp:1394-1408), so the GINX bootstrap on this key is the
+ * WWL+24 bootstrap.
+ */
+int po_wwl24_expand(po_ctx* c) {
+    if (!c->wwl_cprime || !c->wwl_s2) return fail(c, "po_wwl24_expand: no WWL+24 key");
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, Ls = c->p.l, T = c->T;
+    const uint64_t q = c->q;
+    const size_t row = (size_t)(k + 1) * N, lvlWords = (size_t)(k + 1) * row;
+    uint64_t* scratch = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    int64_t* torus = (int64_t*)malloc(sizeof(int64_t) * N);
+    int64_t* digits = (int64_t*)malloc(sizeof(int64_t) * (size_t)Ls * N);
+    int64_t* dpoly = (int64_t*)malloc(sizeof(int64_t) * N);
+    uint64_t* dntt = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    int64_t dg[64];
+    if (!scratch || !torus || !digits || !dpoly || !dntt || Ls > 64) {
+        free(scratch); free(torus); free(digits); free(dpoly); free(dntt);
+        return fail(c, "po_wwl24_expand: out of memory");
+    }
+    for (int i = 0; i < n; i++) {
+        for (int lvl = 0; lvl < L; lvl++) {
+            const uint64_t* cp = c->wwl_cprime + ((size_t)i * L + lvl) * row;
+            uint64_t* g = c->bsk + ((size_t)i * L + lvl) * lvlWords;
+            memcpy(g + (size_t)k * row, cp, sizeof(uint64_t) * row);
+            for (int k1 = 0; k1 < k; k1++) {
+                uint64_t* out = g + (size_t)k1 * row;
+                memset(out, 0, sizeof(uint64_t) * row);
+                memcpy(scratch, cp + (size_t)k1 * N, sizeof(uint64_t) * N);
+                intt_to_torus(c, torus, scratch);
+                for (int j = 0; j < N; j++) {
+                    zero_mean_digits((uint64_t)torus[j], Ls, c->p.radix_bits, T, dg);
+                    for (int lv = 0; lv < Ls; lv++) digits[(size_t)lv * N + j] = dg[lv];
+                }
+                for (int lv = 0; lv < Ls; lv++) {
+                    memcpy(dpoly, digits + (size_t)lv * N, sizeof(int64_t) * N);
+                    ntt_from_torus(c, dntt, dpoly);
+                    const uint64_t* s2 = c->wwl_s2 + (size_t)lv * row;
+                    for (int poly = 0; poly <= k; poly++)
+                        for (int j = 0; j < N; j++)
+                            out[(size_t)poly * N + j] = addmod(out[(size_t)poly * N + j],
+                                nq_mulmod(&c->plan.br, dntt[j], s2[(size_t)poly * N + j]), q);
+                }
+                for (int k2 = 0; k2 < k; k2++)
+                    for (int j = 0; j < N; j++)
+                        out[(size_t)k2 * N + j] = addmod(out[(size_t)k2 * N + j], cp[(size_t)k * N + j], q);
+            }
+        }
+    }
+    free(scratch); free(torus); free(digits); free(dpoly); free(dntt);
+    return 0;
+}
+
+/*
+ * serializeBskWWL24 / deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:220-246): n half
+ * TrgswMPDft (`[int l][int k][bool isHalf = 1][int l]` + l TrlweDft, :176-218), the TrlevDft
+ * s2 (`[int l][int l]` + l TrlweDft, :101-115), then `[int n][int group]`.
+ */
+int po_save_wwl24_file(po_ctx* c, const char* path) {
+    if (!c->wwl_cprime || !c->wwl_s2) return fail(c, "po_save_wwl24_file: no WWL+24 key");
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, "po_save_wwl24_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, Ls = c->p.l;
+    const size_t row = (size_t)(k + 1) * N;
+    int e = 0;
+    for (int i = 0; i < n; i++) {
+        int32_t l = L, kk = k;
+        uint8_t half = 1;
+        e |= wr(f, &l, 4);
+        e |= wr(f, &kk, 4);
+        e |= wr(f, &half, 1);
+        e |= wr(f, &l, 4);
+        for (int lvl = 0; lvl < L; lvl++) e |= wr_trlwe_dft(f, c->wwl_cprime + ((size_t)i * L + lvl) * row, k, N);
+    }
+    int32_t ls = Ls;
+    e |= wr(f, &ls, 4);
+    e |= wr(f, &ls, 4);
+    for (int lv = 0; lv < Ls; lv++) e |= wr_trlwe_dft(f, c->wwl_s2 + (size_t)lv * row, k, N);
+    int32_t nn = n, group = 1;
+    e |= wr(f, &nn, 4);
+    e |= wr(f, &group, 4);
+    if (fclose(f) != 0) e = -1;
+    return e ? fail(c, "po_save_wwl24_file: write failed") : 0;
+}
+
+int po_load_wwl24_file(po_ctx* c, const char* path) {
+    if (wwl_alloc(c)) return fail(c, "po_load_wwl24_file: out of memory");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(c, "po_load_wwl24_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, Ls = c->p.l;
+    const size_t row = (size_t)(k + 1) * N;
+    int e = 0;
+    for (int i = 0; i < n && !e; i++) {
+        uint8_t half = 0;
+        e |= rd_expect_i32(f, L) | rd_expect_i32(f, k) | rd(f, &half, 1);
+        if (e || half != 1) { e = -1; break; }
+        e |= rd_expect_i32(f, L);
+        for (int lvl = 0; lvl < L && !e; lvl++) e |= rd_trlwe_dft(f, c->wwl_cprime + ((size_t)i * L + lvl) * row, k, N);
+    }
+    if (!e) e |= rd_expect_i32(f, Ls) | rd_expect_i32(f, Ls);
+    for (int lv = 0; lv < Ls && !e; lv++) e |= rd_trlwe_dft(f, c->wwl_s2 + (size_t)lv * row, k, N);
+    if (!e) e |= rd_expect_i32(f, n);
+    fclose(f);
+    return e ? fail(c, "po_load_wwl24_file: %s is not a WWL+24 key for these parameters", path) : 0;
 }

@@ -57,6 +57,16 @@ int po_blind_rotate_trace(po_ctx* c, const int32_t* in, const int64_t* v, const 
                           int64_t* acc_out, int64_t* acc_final);
 int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
 
+/* WWL+24 keys (half TRGSW rows cPrime [n][l_approx][k+1][N] + s2 [l][k+1][N], NTT domain):
+ * po_wwl24_expand writes the GINX rows the WWL+24 blind rotation derives from them into the
+ * context's BSK, after which po_pbs / po_blind_rotate_trace run the WWL+24 bootstrap. */
+int po_keygen_wwl24(po_ctx* c, uint64_t seed);
+int po_get_wwl24(po_ctx* c, uint64_t* cprime, uint64_t* s2);
+int po_set_wwl24(po_ctx* c, const uint64_t* cprime, const uint64_t* s2);
+int po_wwl24_expand(po_ctx* c);
+int po_save_wwl24_file(po_ctx* c, const char* path);
+int po_load_wwl24_file(po_ctx* c, const char* path);
+
 #ifdef __cplusplus
 }
 #endif

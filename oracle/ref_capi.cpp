@@ -25,6 +25,7 @@
 #include "yatfhe/polynomial.h"
 #include "yatfhe/tlwe.h"
 #include "yatfhe/trgsw.h"
+#include "yatfhe/trlev.h"
 #include "yatfhe/trlwe.h"
 #include "yautil/initializer.h"
 #include "yautil/multi_threading.h"
@@ -40,6 +41,7 @@ struct RefState {
     std::unique_ptr<TlweKey> lweKey;
     std::unique_ptr<TrgswKey> trgswKey;
     std::unique_ptr<BootstrappingKeyMP> bsk;
+    std::unique_ptr<BootstrappingKeyWWL24> wwl;
     std::unique_ptr<TlweKeySwitchingKey> ksk;
     std::string lastError;
 };
@@ -117,6 +119,7 @@ int ref_setup(const ref_params* p) {
         s.lweKey.reset();
         s.trgswKey.reset();
         s.bsk.reset();
+        s.wwl.reset();
         s.ksk.reset();
         s.ready = true;
     });
@@ -464,6 +467,140 @@ int ref_pbs(const int32_t* in, int count, const int64_t* v, int32_t* out, int wo
         fs.reserve(count);
         for (int c = 0; c < count; c++) fs.emplace_back(ThreadPool::instance().enqueue(one, c));
         for (auto& f : fs) f.get();
+    });
+}
+
+// ---------------------------------------------------------------- WWL+24 keys
+// Key generation for the WWL+24 family on the calling thread's RNG stream 0: genTlweKey,
+// genTrlweKey, then the per-i body of genBootstrappingKeyWWL24
+// (yatfhe/src/bootstrapping.cpp:106-126) for i = 0..n-1 in order -- one
+// symEncTrlweMultiSampleNtt of s_i g_lvl per level (yatfhe/src/trlwe.cpp:103-106) --,
+// then its symEncTrlevWithKeyNtt of the RLWE secret (yatfhe/src/trlev.cpp:75-96) and
+// genTlweKeySwitchingKey.  As for ref_keygen, the per-i calls run in order on one thread
+// so that a seed gives one key.
+int ref_keygen_wwl24(uint64_t seed) {
+    if (!st().ready) return fail("ref_keygen_wwl24: ref_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        auto& p = s.param;
+        (void)rng();
+        yatfhe_oracle_set_seed(seed);
+        rng = ChaCha20Rng();
+        s.lweKey = std::make_unique<TlweKey>(p);
+        s.trgswKey = std::make_unique<TrgswKey>(p);
+        s.wwl = std::make_unique<BootstrappingKeyWWL24>(p, p.lApprox);
+        s.ksk = std::make_unique<TlweKeySwitchingKey>(p);
+        genTlweKey(*s.lweKey);
+        genTrlweKey(s.trgswKey->trlweKey);
+        for (int i = 0; i < s.wwl->n; i++) {
+            TorusPolynomial muPoly{p.N};
+            Trlwe tmp{p.k, p.N};
+            for (int lvl = 0; lvl < s.wwl->bskDft[i].l; lvl++) {
+                muPoly.coeffs[0] = s.lweKey->s[i] << (p.torusBits - (lvl + 1) * p.radixBits);
+                symEncTrlweMultiSampleNtt(tmp, s.wwl->bskDft[i].cPrime[lvl], s.trgswKey->trlweKey, muPoly.coeffs);
+            }
+        }
+        symEncTrlevWithKeyNtt(s.wwl->s2Dft, s.trgswKey->trlweKey, s.trgswKey->trlweKey.s, true, p);
+        TlweKey ksTarget = *s.lweKey;
+        genTlweKeySwitchingKey(*s.ksk, s.trgswKey->trlweKey, ksTarget, p);
+    });
+}
+
+// The WWL+24 key's NTT-domain words: cprime = [i][lvl][poly][N] (poly = a[0..k-1] then b of
+// bskDft[i].cPrime[lvl]), s2 = [lvl][poly][N] of s2Dft (yatfhe/include/yatfhe/bootstrapping.h:116-135).
+int ref_export_wwl24(uint64_t* cprime, uint64_t* s2) {
+    auto& s = st();
+    if (!s.wwl) return fail("ref_export_wwl24: no WWL+24 key");
+    const int k = s.param.k, N = s.param.N;
+    auto put = [&](uint64_t*& o, const TrlweDft& t) {
+        for (int poly = 0; poly <= k; poly++) {
+            const NttPolynomial& P = poly < k ? t.a[poly] : t.b;
+            std::memcpy(o, P.coeffs.data(), sizeof(uint64_t) * N);
+            o += N;
+        }
+    };
+    uint64_t* o = cprime;
+    for (int i = 0; i < s.wwl->n; i++)
+        for (const auto& t : s.wwl->bskDft[i].cPrime) put(o, t);
+    o = s2;
+    for (const auto& t : s.wwl->s2Dft.trlweDfts) put(o, t);
+    return 0;
+}
+
+// The GINX rows the WWL+24 blind rotation builds for every key index before its external
+// product: cRows[lvl] = switchTrlweToSecretEmbeddingNtt(cPrime[lvl], s2Dft)
+// (yatfhe/src/trgsw.cpp:861-905, called from blindRotateWWL24Ntt, blind_rotate.cpp:1394-1397),
+// written with cPrime[lvl] as [i][lvl][row][poly][N] -- the layout of ref_export_bsk_ntt.
+int ref_wwl24_expand(uint64_t* out) {
+    auto& s = st();
+    if (!s.wwl) return fail("ref_wwl24_expand: no WWL+24 key");
+    return guarded([&] {
+        const auto& p = s.param;
+        const int k = p.k, N = p.N;
+        uint64_t* o = out;
+        auto put = [&](const TrlweDft& t) {
+            for (int poly = 0; poly <= k; poly++) {
+                const NttPolynomial& P = poly < k ? t.a[poly] : t.b;
+                std::memcpy(o, P.coeffs.data(), sizeof(uint64_t) * N);
+                o += N;
+            }
+        };
+        for (int i = 0; i < s.wwl->n; i++) {
+            const auto& g = s.wwl->bskDft[i];
+            for (int lvl = 0; lvl < g.l; lvl++) {
+                std::vector<TrlweDft> rows(k, TrlweDft(k, N));
+                switchTrlweToSecretEmbeddingNtt(rows, g.cPrime[lvl], s.wwl->s2Dft, p);
+                for (int r = 0; r < k; r++) put(rows[r]);
+                put(g.cPrime[lvl]);
+            }
+        }
+    });
+}
+
+// serializeBskWWL24 / deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:220-246).
+int ref_save_wwl24(const char* path) {
+    if (!st().wwl) return fail("ref_save_wwl24: no WWL+24 key");
+    return guarded([&] { serializeBskWWL24(*st().wwl, path); });
+}
+
+int ref_load_wwl24(const char* path) {
+    if (!st().ready) return fail("ref_load_wwl24: ref_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        s.wwl = std::make_unique<BootstrappingKeyWWL24>();
+        deserializeBskWWL24(*s.wwl, path, s.param.n);
+    });
+}
+
+// functionalBootstrappingMPNtt's composition (yatfhe/src/bootstrapping.cpp:71-80) with the
+// WWL+24 blind rotation blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412) in
+// place of blindRotateMP21Ntt, one ciphertext after the other.  acc0 (may be null) receives
+// the accumulator of ciphertext 0 after the blind rotation, [a..., b].
+int ref_pbs_wwl24(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
+    auto& s = st();
+    if (!s.wwl || !s.ksk) return fail("ref_pbs_wwl24: keys not loaded");
+    return guarded([&] {
+        const auto& p = s.param;
+        const int n = p.n, N = p.N, k = p.k;
+        TorusPolynomial vp{N};
+        toPoly(vp, v, N);
+        for (int c = 0; c < count; c++) {
+            Tlwe x{n}, y{n};
+            toTlwe(x, in + static_cast<size_t>(c) * (n + 1), n);
+            ScaledTlwe sc{2 * N, n};
+            Trlwe acc{k, N};
+            Tlwe big{s.ksk->nCurrKey};
+            rescaleTlweToNewMod(sc, x);
+            genNoiselessTrlweSample(acc, vp, sc);
+            blindRotateWWL24Ntt(acc, *s.wwl, sc, p);
+            if (c == 0 && acc0) {
+                for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
+                fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);
+            }
+            extractTlweFromTrlwe(big, acc, p.driftPhase);
+            switchKeyForTlwe(y, *s.ksk, big, p);
+            fromTlwe(out + static_cast<size_t>(c) * (n + 1), y, n);
+        }
     });
 }
 

@@ -25,13 +25,19 @@ sys.path.insert(0, str(HERE.parents[1]))
 
 from oracle.oracle import Reference  # noqa: E402
 from yatfhe_gb300 import lut as lutmod  # noqa: E402
-from yatfhe_gb300.params import T32_N1024, T56_N2048, small  # noqa: E402
+from yatfhe_gb300.params import T32_N1024, T56_N2048, WWL24_T32_N2048, WWL24_T56_N2048, small  # noqa: E402
 
 CASES = {
     # name: (params, key seed, number of ciphertexts, message seed)
     "t32_n1024_seed5eed0001": (T32_N1024, 0x5EED0001, 8, 11),
     "t56_n2048_seed5eed0003": (T56_N2048, 0x5EED0003, 6, 12),
     "t32_n1024_small40_seed7": (small(T32_N1024, 40), 7, 16, 13),
+}
+
+WWL24_CASES = {
+    # name: (params, key seed, number of ciphertexts, message seed); sign bootstrap
+    "wwl24_t32_n2048_seed5eed0005": (WWL24_T32_N2048, 0x5EED0005, 8, 14),
+    "wwl24_t56_n2048_seed5eed0006": (WWL24_T56_N2048, 0x5EED0006, 8, 15),
 }
 
 
@@ -76,6 +82,36 @@ def make(name, p, seed, count, mseed):
     print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
 
 
+def make_wwl24(name, p, seed, count, mseed):
+    ref = Reference(p)
+    ref.keygen_wwl24(seed)
+    s, z = ref.keys()
+    cprime, s2 = ref.wwl24_words()
+    expanded = ref.wwl24_expanded()
+    ksk = ref.ksk()
+    rng = np.random.default_rng(mseed)
+    bits = rng.integers(0, 2, count)
+    mu = np.where(bits == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    lut = lutmod.sign_lut(p.N, p.torus_bits)
+    lwe = ref.encrypt(mu)
+    out, acc0 = ref.pbs_wwl24(lwe, lut, with_acc=True)
+    dec = ref.decrypt(out, 8)
+    expect = np.where(bits == 1, 1, -1)
+    if not np.array_equal(dec, expect):
+        raise SystemExit(f"{name}: the reference's own decryptions {dec} differ from the messages {expect}")
+    np.savez_compressed(
+        HERE / f"{name}.npz",
+        params=np.array([p.n, p.N, p.k, p.radix_bits, p.l, p.l_approx, p.ks_radix_bits, p.ks_level, p.lwe_noise_b,
+                         p.rlwe_noise_b, p.torus_base, p.torus_bits], np.int64),
+        seed=np.array([seed], np.uint64),
+        sha_lwe_s=digest(s), sha_rlwe_s=digest(z), sha_cprime=digest(cprime), sha_s2=digest(s2),
+        sha_expanded=digest(expanded), sha_ksk=digest(ksk),
+        mu=mu, lwe_in=lwe, lut=lut, lwe_out=out, decrypted=dec, base=np.array([8]), acc0=acc0)
+    print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
+
+
 if __name__ == "__main__":
     for name, (p, seed, count, mseed) in CASES.items():
         make(name, p, seed, count, mseed)
+    for name, (p, seed, count, mseed) in WWL24_CASES.items():
+        make_wwl24(name, p, seed, count, mseed)

@@ -74,6 +74,7 @@ class BootstrapKey:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self._h = handle
+        self.family = "ginx"  # key format it was made from: "ginx" (BootstrappingKeyMP) or "wwl24"
 
     @classmethod
     def from_file(cls, ctx: Context, path) -> "BootstrapKey":
@@ -89,6 +90,35 @@ class BootstrapKey:
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().yg_key_upload_bsk_ntt(ctx.handle, ctypes.c_void_p(w.ctypes.data), ctypes.byref(h)))
         return cls(ctx, h)
+
+    @classmethod
+    def from_wwl24_words(cls, ctx: Context, cprime: np.ndarray, s2: np.ndarray) -> "BootstrapKey":
+        """A WWL+24 key (BootstrappingKeyWWL24: cPrime rows [n][l_approx][k+1][N] and the s2 key
+        [levels][k+1][N], NTT-domain words mod q).  The GPU derives the GINX rows the WWL+24 blind
+        rotation uses once, at upload; every entry point then gives the WWL+24 results."""
+        p = ctx.params
+        c = np.ascontiguousarray(cprime, np.uint64)
+        s = np.ascontiguousarray(s2, np.uint64)
+        row = (p.k + 1) * p.N
+        if c.size != p.n * p.l_approx * row:
+            raise ValueError(f"expected {p.n * p.l_approx * row} cPrime words, got {c.size}")
+        if s.size == 0 or s.size % row:
+            raise ValueError(f"the s2 key must be a whole number of [{p.k + 1}][{p.N}] levels")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_upload_wwl24_ntt(ctx.handle, ctypes.c_void_p(c.ctypes.data),
+                                                       ctypes.c_void_p(s.ctypes.data), s.size // row, ctypes.byref(h)))
+        key = cls(ctx, h)
+        key.family = "wwl24"
+        return key
+
+    @classmethod
+    def from_wwl24_file(cls, ctx: Context, path) -> "BootstrapKey":
+        """A WWL+24 key file written by serializeBskWWL24."""
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_load_wwl24_file(ctx.handle, str(path).encode(), ctypes.byref(h)))
+        key = cls(ctx, h)
+        key.family = "wwl24"
+        return key
 
     def set_ksk(self, ksk: np.ndarray) -> "BootstrapKey":
         k = np.ascontiguousarray(ksk, np.int32)
@@ -210,6 +240,14 @@ def blind_rotate_mp21_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: i
                                           _dptr(lut, "int64", "lut"), _dptr(acc, "int64", "acc"),
                                           lwe_in.shape[0], steps, _stream_handle(stream)))
     return acc
+
+
+def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
+    """blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412): the blind rotation on a
+    WWL+24 key, whose GINX rows were derived on the GPU at upload."""
+    if key.family != "wwl24":
+        raise ValueError("blind_rotate_wwl24_ntt needs a key made by BootstrapKey.from_wwl24_words/_file")
+    return blind_rotate_mp21_ntt(ctx, key, lwe_in, lut, steps=steps, stream=stream)
 
 
 def switch_key_for_tlwe(ctx: Context, key: BootstrapKey, big, stream=None):

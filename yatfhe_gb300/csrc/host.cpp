@@ -8,7 +8,7 @@
 // so the loader takes each key polynomial back to coefficients once (inverse negacyclic
 // transform mod q with the minimal primitive 2N-th root, bit-reversed slot order: the
 // convention HEXL documents), centres them and reduces them into the three RNS channels
-// (key_intt_kernel, on the GPU, with the tables QInverse builds here), and keyconv_kernel
+// (key_intt_kernel, on the GPU, with the tables QTables builds here), and keyconv_kernel
 // applies the GPU's own per-channel NTT.
 #include <cuda_runtime.h>
 
@@ -98,23 +98,29 @@ void thread_minor_layout(uint2* t, int N) {
 
 namespace yg {
 
-// Tables of the inverse negacyclic transform mod q that key_intt_kernel runs
-// (Gentleman-Sande, psi^-brv(k) twiddles with Shoup companions, bit-reversed NTT slots in,
-// natural-order coefficients out, times N^-1).
-struct QInverse {
+// Tables of the negacyclic transforms mod q the key kernels run: the inverse
+// (Gentleman-Sande, psi^-brv(k) twiddles, bit-reversed NTT slots in, natural-order
+// coefficients out, times N^-1) and the forward one (Cooley-Tukey, psi^brv(k)), with Shoup
+// companions, psi the minimal primitive 2N-th root of unity mod q.
+struct QTables {
     int N = 0, logN = 0;
     u64 q = 0;
-    std::vector<u64> w, wp;
+    std::vector<u64> w, wp;    // inverse
+    std::vector<u64> wf, wfp;  // forward
     u64 ninv = 0, ninvp = 0;
 
-    QInverse(int N_, u64 q_) : N(N_), q(q_) {
+    QTables(int N_, u64 q_) : N(N_), q(q_) {
         while ((1 << logN) < N) logN++;
-        const u64 psi_inv = invmod(minimal_root(N, q), q);
+        const u64 psi = minimal_root(N, q), psi_inv = invmod(psi, q);
         w.resize(N);
         wp.resize(N);
+        wf.resize(N);
+        wfp.resize(N);
         for (int k = 0; k < N; k++) {
             w[k] = powmod(psi_inv, brv(k, logN), q);
             wp[k] = (u64)(((u128)w[k] << 64) / q);
+            wf[k] = powmod(psi, brv(k, logN), q);
+            wfp[k] = (u64)(((u128)wf[k] << 64) / q);
         }
         ninv = invmod(N, q);
         ninvp = (u64)(((u128)ninv << 64) / q);
@@ -125,7 +131,7 @@ struct QInverse {
 
 namespace {
 
-using yg::QInverse;
+using yg::QTables;
 
 void validate(const yg_params& p) {
     if (p.torus_bits != 32 && p.torus_bits != 56) throw std::invalid_argument("torus_bits must be 32 or 56");
@@ -215,25 +221,34 @@ struct DeviceScratch {
     }
 };
 
-// NTT-domain key words mod q -> the device key: the words go to the GPU as they are, the
-// inverse transform mod q and the split into channel residues run there (key_intt_kernel),
-// then keyconv_kernel applies each channel's forward NTT into the slot layout.
-void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
+// The mod-q transform tables on the device, for the key kernels.
+struct DeviceQTables {
+    u64 *w, *wp, *wf, *wfp;
+    DeviceQTables(DeviceScratch& scratch, const QTables& qt) {
+        const int N = qt.N;
+        w = scratch.alloc<u64>(4 * (size_t)N, "cudaMalloc mod-q twiddles");
+        wp = w + N;
+        wf = wp + N;
+        wfp = wf + N;
+        const std::vector<u64>* src[4] = {&qt.w, &qt.wp, &qt.wf, &qt.wfp};
+        for (int t = 0; t < 4; t++)
+            ck(cudaMemcpy(w + (size_t)t * N, src[t]->data(), N * sizeof(u64), cudaMemcpyHostToDevice),
+               "upload mod-q twiddles");
+    }
+};
+
+// NTT-domain key words already on the device ([n][L][k+1][k+1][N]) -> the device key.
+void convert_bsk_words(yg_ctx* c, yg_key* key, const u64* d_words, DeviceScratch& scratch, const DeviceQTables& tw) {
     const int n = c->p.n, N = c->p.N, L = c->p.l_approx;
     const size_t polys = (size_t)n * L * 2 * 2;
-    const QInverse& qi = *c->qinv;
+    const QTables& qi = *c->qtab;
     const size_t key_words = yg::key_words(n, L, N);
     key->bsk_bytes = key_words * sizeof(uint32_t);
     ck(cudaMalloc(&key->d_bsk, key->bsk_bytes), "cudaMalloc bsk");
-    DeviceScratch scratch;
-    u64* d_words = scratch.alloc<u64>(polys * N, "cudaMalloc key words");
-    u64* d_w = scratch.alloc<u64>(N, "cudaMalloc inverse twiddles");
-    u64* d_wp = scratch.alloc<u64>(N, "cudaMalloc inverse twiddles");
     uint32_t* d_res = scratch.alloc<uint32_t>(polys * yg::kChannels * N, "cudaMalloc key residues");
     int* d_bad = scratch.alloc<int>(1, "cudaMalloc flag");
-    ck(cudaMemcpy(d_words, words, polys * N * sizeof(u64), cudaMemcpyHostToDevice), "upload key words");
-    ck(cudaMemcpy(d_w, qi.w.data(), N * sizeof(u64), cudaMemcpyHostToDevice), "upload inverse twiddles");
-    ck(cudaMemcpy(d_wp, qi.wp.data(), N * sizeof(u64), cudaMemcpyHostToDevice), "upload inverse twiddles");
+    const u64* d_w = tw.w;
+    const u64* d_wp = tw.wp;
     ck(cudaMemset(d_bad, 0, sizeof(int)), "clear flag");
     yg::KeyInttArgs ia{};
     ia.words = d_words;
@@ -262,6 +277,69 @@ void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
     }
     yg::check_launch(yg::launch_keyconv(c->logN, c->ps, a, nullptr), "keyconv launch");
     ck(cudaDeviceSynchronize(), "keyconv");
+}
+
+// NTT-domain key words mod q -> the device key: the words go to the GPU as they are, the
+// inverse transform mod q and the split into channel residues run there (key_intt_kernel),
+// then keyconv_kernel applies each channel's forward NTT into the slot layout.
+void upload_bsk(yg_ctx* c, yg_key* key, const u64* words) {
+    const size_t polys = (size_t)c->p.n * c->p.l_approx * 2 * 2;
+    DeviceScratch scratch;
+    DeviceQTables tw(scratch, *c->qtab);
+    u64* d_words = scratch.alloc<u64>(polys * c->p.N, "cudaMalloc key words");
+    ck(cudaMemcpy(d_words, words, polys * c->p.N * sizeof(u64), cudaMemcpyHostToDevice), "upload key words");
+    convert_bsk_words(c, key, d_words, scratch, tw);
+}
+
+// WWL+24 half key -> the device key.  The key's cPrime rows ([n][L][2][N]) and s2 key
+// ([l][2][N]) go to the GPU, wwl24_expand_kernel derives the GINX rows blindRotateWWL24Ntt
+// would build at every step (switchTrlweToSecretEmbeddingNtt, yatfhe/src/trgsw.cpp:861-905)
+// once for the whole key, and the result is converted like any NTT-domain key.
+void upload_wwl24(yg_ctx* c, yg_key* key, const u64* cprime, const u64* s2, int Ls) {
+    const int n = c->p.n, N = c->p.N, L = c->p.l_approx;
+    if (Ls < 1 || Ls > yg::kWwlMaxLevels || Ls * c->p.radix_bits > c->p.torus_bits)
+        throw std::invalid_argument("WWL+24 s2 key: 1 <= levels <= 8 and levels * radix_bits <= torus_bits");
+    const u64 q = c->q;
+    const size_t s2_words = (size_t)Ls * 2 * N, cp_words = (size_t)n * L * 2 * N;
+    std::vector<u64> s2p(s2_words);
+    for (size_t j = 0; j < s2_words; j++) {
+        if (s2[j] >= q) throw std::invalid_argument("WWL+24 s2 key word not reduced mod q");
+        s2p[j] = (u64)(((u128)s2[j] << 64) / q);
+    }
+    DeviceScratch scratch;
+    DeviceQTables tw(scratch, *c->qtab);
+    u64* d_cp = scratch.alloc<u64>(cp_words, "cudaMalloc WWL+24 key");
+    u64* d_s2 = scratch.alloc<u64>(2 * s2_words, "cudaMalloc WWL+24 s2 key");
+    u64* d_out = scratch.alloc<u64>(2 * cp_words, "cudaMalloc expanded key");
+    int* d_bad = scratch.alloc<int>(1, "cudaMalloc flag");
+    ck(cudaMemcpy(d_cp, cprime, cp_words * sizeof(u64), cudaMemcpyHostToDevice), "upload WWL+24 key");
+    ck(cudaMemcpy(d_s2, s2, s2_words * sizeof(u64), cudaMemcpyHostToDevice), "upload WWL+24 s2 key");
+    ck(cudaMemcpy(d_s2 + s2_words, s2p.data(), s2_words * sizeof(u64), cudaMemcpyHostToDevice), "upload s2 key");
+    ck(cudaMemset(d_bad, 0, sizeof(int)), "clear flag");
+    yg::WwlExpandArgs a{};
+    a.cprime = d_cp;
+    a.s2 = d_s2;
+    a.s2p = d_s2 + s2_words;
+    a.out = d_out;
+    a.wi = tw.w;
+    a.wip = tw.wp;
+    a.wf = tw.wf;
+    a.wfp = tw.wfp;
+    a.q = q;
+    a.ninv = c->qtab->ninv;
+    a.ninvp = c->qtab->ninvp;
+    a.n = n;
+    a.N = N;
+    a.L = L;
+    a.Ls = Ls;
+    a.radix_bits = c->p.radix_bits;
+    a.torus_bits = c->p.torus_bits;
+    a.bad = d_bad;
+    yg::check_launch(yg::launch_wwl24_expand(a, nullptr), "WWL+24 key expansion launch");
+    int bad = 0;
+    ck(cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost), "WWL+24 key expansion");
+    if (bad) throw std::invalid_argument("WWL+24 key word not reduced mod q");
+    convert_bsk_words(c, key, d_out, scratch, tw);
 }
 
 // deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)
@@ -333,6 +411,40 @@ std::vector<u64> read_bsk_file(const yg_params& p, const char* path) {
     return words;
 }
 
+// deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): n half TrgswMPDft (cPrime rows
+// only, :193-218), the TrlevDft s2 (:107-115), then [int n][int group].  cprime out =
+// [n][L][k+1][N], s2 out = [l][k+1][N].
+int read_wwl24_file(const yg_params& p, const char* path, std::vector<u64>& cprime, std::vector<u64>& s2) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    Reader r{f, path};
+    const int n = p.n, N = p.N, k = p.k, L = p.l_approx;
+    const size_t row = (size_t)(k + 1) * N;
+    cprime.assign((size_t)n * L * row, 0);
+    int Ls = 0;
+    try {
+        for (int i = 0; i < n; i++) {
+            r.expect(L, "TrgswMPDft l");
+            r.expect(k, "TrgswMPDft k");
+            if (r.b8() != 1) throw std::runtime_error(std::string(path) + ": full TRGSW rows are not a WWL+24 key");
+            r.expect(L, "cPrime size");
+            for (int l = 0; l < L; l++) read_trlwe_dft(r, cprime.data() + ((size_t)i * L + l) * row, k, N);
+        }
+        Ls = r.i32();
+        if (Ls < 1 || Ls > yg::kWwlMaxLevels) throw std::runtime_error(std::string(path) + ": s2 key levels out of range");
+        r.expect(Ls, "TrlevDft size");
+        s2.assign((size_t)Ls * row, 0);
+        for (int l = 0; l < Ls; l++) read_trlwe_dft(r, s2.data() + (size_t)l * row, k, N);
+        r.expect(n, "key n");
+        r.expect(1, "key group");
+    } catch (...) {
+        std::fclose(f);
+        throw;
+    }
+    std::fclose(f);
+    return Ls;
+}
+
 }  // namespace
 
 yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
@@ -402,7 +514,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
         c->logN = params->N == 1024 ? 10 : 11;
         c->ps = yg::prime_set_for(params->torus_bits);
         c->q = params->torus_bits == 32 ? 562941363486721ULL : 1945555039024054273ULL;
-        c->qinv = std::make_shared<QInverse>(params->N, c->q);
+        c->qtab = std::make_shared<QTables>(params->N, c->q);
         ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         ctx_init_tables(c.get());
         *out = c.release();
@@ -441,6 +553,35 @@ int yg_key_load_bsk_file(yg_ctx* ctx, const char* path, yg_key** out) {
     return guarded([&] {
         std::vector<u64> words = read_bsk_file(ctx->p, path);
         return yg_key_upload_bsk_ntt(ctx, words.data(), out);
+    });
+}
+
+int yg_key_upload_wwl24_ntt(yg_ctx* ctx, const uint64_t* h_cprime, const uint64_t* h_s2, int s2_levels, yg_key** out) {
+    if (!ctx || !h_cprime || !h_s2 || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            upload_wwl24(ctx, k.get(), h_cprime, h_s2, s2_levels);
+        } catch (...) {
+            if (k->d_bsk) cudaFree(k->d_bsk);
+            k->d_bsk = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out) {
+    if (!ctx || !path || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<u64> cprime, s2;
+        const int levels = read_wwl24_file(ctx->p, path, cprime, s2);
+        return yg_key_upload_wwl24_ntt(ctx, cprime.data(), s2.data(), levels, out);
     });
 }
 

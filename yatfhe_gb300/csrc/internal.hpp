@@ -13,7 +13,7 @@
 
 namespace yg {
 
-struct QInverse;
+struct QTables;
 
 // Message of the last failure on this thread (yg_last_error).
 std::string& last_error_slot();
@@ -81,7 +81,7 @@ struct yg_ctx {
     yg::Chan ch[yg::kChannels]{};
     yg::Crt crt{};
     uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};
-    std::shared_ptr<yg::QInverse> qinv;
+    std::shared_ptr<yg::QTables> qtab;
     int sm_count = 0;
     int layout = 0;        // YG_LAYOUT_* of the blind rotation (yg_ctx_set_launch)
     int per_cta = 1;       // ciphertexts per blind-rotation CTA (yg_ctx_set_launch)

@@ -136,6 +136,43 @@ __device__ __forceinline__ uint64_t mulshoup64(uint64_t x, uint64_t w, uint64_t 
     return r >= q ? r - q : r;
 }
 
+// Inverse negacyclic transform mod q of the N words in shared memory, without the N^-1
+// factor: Gentleman-Sande, stage with butterfly span t pairs (2 i t + j, 2 i t + j + t)
+// with twiddle w[N / (2t) + i] = psi^-brv(N / (2t) + i); bit-reversed slots in, natural
+// coefficients out.  All threads of the block take part; ends synchronised.
+__device__ void q_inverse_in_smem(uint64_t* sw, int N, const uint64_t* w, const uint64_t* wp, uint64_t q) {
+    for (int t = 1; t < N; t <<= 1) {
+        const int h = N / (2 * t);
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int i = b / t, j = b - i * t;
+            const int xi = 2 * i * t + j, yi = xi + t;
+            const uint64_t u = sw[xi], v = sw[yi];
+            const uint64_t s = u + v;
+            sw[xi] = s >= q ? s - q : s;
+            sw[yi] = mulshoup64(u >= v ? u - v : u + q - v, w[h + i], wp[h + i], q);
+        }
+        __syncthreads();
+    }
+}
+
+// Forward negacyclic transform mod q in shared memory, the exact inverse of the above:
+// Cooley-Tukey, stage m (= 1, 2, .., N/2) with span t = N / (2m) pairs (2 i t + j,
+// 2 i t + j + t) with twiddle w[m + i] = psi^brv(m + i); natural coefficients in,
+// bit-reversed slots out (the transform HEXL's ComputeForward documents).  Ends synchronised.
+__device__ void q_forward_in_smem(uint64_t* sw, int N, const uint64_t* w, const uint64_t* wp, uint64_t q) {
+    for (int m = 1, t = N / 2; m < N; m <<= 1, t >>= 1) {
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int i = b / t, j = b - i * t;
+            const int xi = 2 * i * t + j, yi = xi + t;
+            const uint64_t u = sw[xi], v = mulshoup64(sw[yi], w[m + i], wp[m + i], q);
+            const uint64_t s = u + v;
+            sw[xi] = s >= q ? s - q : s;
+            sw[yi] = u >= v ? u - v : u + q - v;
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(1024) key_intt_kernel(const KeyInttArgs a) {
     extern __shared__ uint64_t sw[];  // [N]
     const int N = a.N, poly = blockIdx.x;
@@ -147,19 +184,7 @@ __global__ void __launch_bounds__(1024) key_intt_kernel(const KeyInttArgs a) {
         sw[j] = v < q ? v : 0;
     }
     __syncthreads();
-    // stage with butterfly span t: pairs (2 i t + j, 2 i t + j + t), twiddle w[N / (2t) + i]
-    for (int t = 1; t < N; t <<= 1) {
-        const int h = N / (2 * t);
-        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-            const int i = b / t, j = b - i * t;
-            const int xi = 2 * i * t + j, yi = xi + t;
-            const uint64_t u = sw[xi], v = sw[yi];
-            const uint64_t s = u + v;
-            sw[xi] = s >= q ? s - q : s;
-            sw[yi] = mulshoup64(u >= v ? u - v : u + q - v, a.w[h + i], a.wp[h + i], q);
-        }
-        __syncthreads();
-    }
+    q_inverse_in_smem(sw, N, a.w, a.wp, q);
     const uint64_t half = (q + 1) / 2;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
         const uint64_t v = mulshoup64(sw[j], a.ninv, a.ninvp, q);
@@ -169,6 +194,81 @@ __global__ void __launch_bounds__(1024) key_intt_kernel(const KeyInttArgs a) {
             a.residues[((size_t)poly * kChannels + c) * N + j] =
                 v >= half ? (uint32_t)((p - (q - v) % p) % p) : (uint32_t)(v % p);
         }
+    }
+}
+
+// switchTrlweToSecretEmbeddingNtt (yatfhe/src/trgsw.cpp:861-905) for one (key index i,
+// level lvl) per block, k = 1: the mask of cPrime[lvl] back to the torus (applyIntt,
+// ntt_hexl.cpp:153-175: inverse transform, centred mod q, low T bits), its zero-mean digits
+// (decomposeRow), and per digit level l' one forward transform and the products with the s2
+// key: c.a = sum NTT(d_l') . s2[l'].a + cPrime.b, c.b = sum NTT(d_l') . s2[l'].b (mod q).
+// Writes the GINX level [c (a, b) | cPrime (a, b)] in the layout of the NTT-domain BSK.
+// N / 2 threads; thread t owns coefficients / slots t and t + N / 2 outside the transforms.
+template <int T>
+__global__ void __launch_bounds__(1024) wwl24_expand_kernel(const WwlExpandArgs a) {
+    using U = typename TorusOf<T>::utype;
+    extern __shared__ uint64_t sw[];  // [N]
+    const int N = a.N, H = N / 2, t = threadIdx.x;
+    const int i = blockIdx.x / a.L, lvl = blockIdx.x - i * a.L;
+    const uint64_t q = a.q;
+    const size_t row = 2 * (size_t)N;
+    const uint64_t* cp = a.cprime + ((size_t)i * a.L + lvl) * row;  // [a | b]
+    uint64_t* g = a.out + ((size_t)i * a.L + lvl) * 2 * row;         // [c: a | b][cPrime: a | b]
+    uint64_t own[2][2];  // this thread's cPrime words: [coefficient e][a, b]
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int j = t + e * H;
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly) {
+            const uint64_t v = cp[poly * N + j];
+            if (v >= q) atomicExch(a.bad, 1);
+            own[e][poly] = v < q ? v : 0;
+            g[row + poly * N + j] = own[e][poly];
+        }
+        sw[j] = own[e][0];
+    }
+    __syncthreads();
+    q_inverse_in_smem(sw, N, a.wi, a.wip, q);
+    int dg[2][kWwlMaxLevels];
+    const uint64_t half = (q + 1) / 2;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const uint64_t v = mulshoup64(sw[t + e * H], a.ninv, a.ninvp, q);
+        const int64_t centred = v >= half ? (int64_t)(v - q) : (int64_t)v;
+        zero_mean_digits<U, T>((U)sext<T>(centred), a.Ls, a.radix_bits, [&](int level, int d) {
+#pragma unroll
+            for (int x = 0; x < kWwlMaxLevels; ++x)
+                if (x == level) dg[e][x] = d;
+        });
+    }
+    uint64_t acc[2][2] = {{0, 0}, {0, 0}};  // [coefficient e][a, b]
+#pragma unroll
+    for (int lv = 0; lv < kWwlMaxLevels; ++lv) {
+        if (lv >= a.Ls) break;
+        __syncthreads();  // the previous transform's slots have been read
+#pragma unroll
+        for (int e = 0; e < 2; ++e) sw[t + e * H] = dg[e][lv] < 0 ? q - (uint64_t)(-dg[e][lv]) : (uint64_t)dg[e][lv];
+        __syncthreads();
+        q_forward_in_smem(sw, N, a.wf, a.wfp, q);
+        const size_t s2o = (size_t)lv * row;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = t + e * H;
+            const uint64_t D = sw[j];
+#pragma unroll
+            for (int poly = 0; poly < 2; ++poly) {
+                const uint64_t m = mulshoup64(D, a.s2[s2o + poly * N + j], a.s2p[s2o + poly * N + j], q);
+                const uint64_t s = acc[e][poly] + m;
+                acc[e][poly] = s >= q ? s - q : s;
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int j = t + e * H;
+        const uint64_t s = acc[e][0] + own[e][1];  // c.a += cPrime.b
+        g[j] = s >= q ? s - q : s;
+        g[N + j] = acc[e][1];
     }
 }
 
@@ -644,6 +744,19 @@ int launch_key_intt(const KeyInttArgs& a, void* stream) {
     if (a.polys <= 0) return 0;
     if (a.N != 1024 && a.N != 2048) return -1;
     key_intt_kernel<<<a.polys, a.N / 2, (size_t)a.N * sizeof(uint64_t), (cudaStream_t)stream>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_wwl24_expand(const WwlExpandArgs& a, void* stream) {
+    if (a.n <= 0) return 0;
+    if ((a.N != 1024 && a.N != 2048) || a.L < 1 || a.Ls < 1 || a.Ls > kWwlMaxLevels) return -1;
+    const size_t smem = (size_t)a.N * sizeof(uint64_t);
+    if (a.torus_bits == 32)
+        wwl24_expand_kernel<32><<<a.n * a.L, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else if (a.torus_bits == 56)
+        wwl24_expand_kernel<56><<<a.n * a.L, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else
+        return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

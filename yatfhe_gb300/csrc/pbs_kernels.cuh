@@ -80,6 +80,24 @@ struct KeyInttArgs {
     int* bad;               // set to 1 when a word is not reduced mod q
 };
 
+// The GINX rows the WWL+24 blind rotation derives from its half key (cPrime rows and the s2
+// key, both NTT-domain words mod q), written as NTT-domain BSK words [n][L][row][poly][N]
+// for the key conversion above.  One CTA per (key index, level); k = 1.
+constexpr int kWwlMaxLevels = 8;  // digit levels of the s2 key handled by the kernel
+struct WwlExpandArgs {
+    const uint64_t* cprime;  // [n][L][2][N]
+    const uint64_t* s2;      // [Ls][2][N]
+    const uint64_t* s2p;     // [Ls][2][N] floor(s2 2^64 / q)
+    uint64_t* out;           // [n][L][2][2][N]
+    const uint64_t* wi;      // [N] psi^-brv(k) mod q, and Shoup companions
+    const uint64_t* wip;
+    const uint64_t* wf;      // [N] psi^brv(k) mod q, and Shoup companions
+    const uint64_t* wfp;
+    uint64_t q, ninv, ninvp;
+    int n, N, L, Ls, radix_bits, torus_bits;
+    int* bad;                // set to 1 when a word is not reduced mod q
+};
+
 // u32 words of one (step, level, row, channel) block of the device key: 2 output polys.
 __host__ __device__ inline size_t key_block_words(int N) { return 2 * (size_t)N; }
 __host__ __device__ inline size_t key_words(int n, int L, int N) {
@@ -111,6 +129,7 @@ __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n,
 int set_twiddle_heads(int logN, int ps, const uint2* heads);
 int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream);
 int launch_key_intt(const KeyInttArgs& a, void* stream);
+int launch_wwl24_expand(const WwlExpandArgs& a, void* stream);
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream);
 // Resident blind-rotation CTAs per SM for these parameters and ciphertexts per CTA
 // (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,

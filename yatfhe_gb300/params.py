@@ -89,6 +89,14 @@ T32_N1024 = PbsParams(n=630, N=1024, k=1, radix_bits=7, l=3, l_approx=3, ks_radi
 T56_N2048 = PbsParams(n=750, N=2048, k=1, radix_bits=10, l=4, l_approx=4, ks_radix_bits=3, ks_level=10,
                       lwe_noise_b=14, rlwe_noise_b=17, torus_base=32, torus_bits=56)
 
+# The reference's default parameter sets (yatfhe/include/yatfhe/yatfhe_parameters.h:9-40,
+# setKsRadixBits(2) -> ksLevel 16), on which its WWL+24 test runs: blind rotation with
+# lApprox levels, the s2 key of the WWL+24 family with l levels.
+WWL24_T32_N2048 = PbsParams(n=680, N=2048, k=1, radix_bits=4, l=8, l_approx=4, ks_radix_bits=2, ks_level=16,
+                            lwe_noise_b=18, rlwe_noise_b=3, torus_base=4, torus_bits=32)
+WWL24_T56_N2048 = PbsParams(n=680, N=2048, k=1, radix_bits=14, l=4, l_approx=1, ks_radix_bits=2, ks_level=16,
+                            lwe_noise_b=18, rlwe_noise_b=8, torus_base=4, torus_bits=56)
+
 # Reduced-n variants of the two sets (same ring, gadget and key-switching parameters, fewer
 # CMux steps); used where the oracle must finish in seconds.
 def small(p: PbsParams, n: int) -> PbsParams:
