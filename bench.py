@@ -340,6 +340,70 @@ def leg_t56(dev, steps=2, warmup=1, count=16384):
             "roofline": run.roofline(t["br_ms"], int32_peak(dev), workload), "launch_shape": run.tuning}
 
 
+def leg_wwl24(dev, steps=2, warmup=1, count=16384):
+    """WWL+24 keys on the reference's default TORUS=32 set (n=680, N=2048, B=2^4, lApprox=4,
+    s2 key with l=8 levels, KS 2^2 x 16): seeded synthetic half key (cPrime rows and s2 key
+    uniform mod q, like a real key's NTT-domain words), uploaded through
+    yg_key_upload_wwl24_ntt (the GINX rows derived on the GPU, then the usual conversion),
+    then `count` bootstraps per step.  Reports the upload's wall time and host bytes beside
+    the GINX key's, and the throughput on the derived key."""
+    import torch
+
+    from yatfhe_gb300 import _lib, api
+    from yatfhe_gb300.params import WWL24_T32_N2048 as p
+
+    rng = np.random.default_rng(0x5EED0005)
+    row = (p.k + 1) * p.N
+    cprime = rng.integers(0, p.q_ntt, size=p.n * p.l_approx * row, dtype=np.uint64)
+    s2 = rng.integers(0, p.q_ntt, size=p.l * row, dtype=np.uint64)
+    ksk = rng.integers(-(1 << 31), 1 << 31, size=p.ksk_words, dtype=np.int64).astype(np.int32)
+    ctx = api.Context(p, dev)
+    uploads = []
+    for _ in range(3):  # the first call also pays one-time setup; the best of three is reported
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        key = api.BootstrapKey.from_wwl24_words(ctx, cprime, s2)
+        uploads.append(time.perf_counter() - t0)
+        key.close()
+    key = api.BootstrapKey.from_wwl24_words(ctx, cprime, s2).set_ksk(ksk)
+    lwe = synthetic_lwe(p, count, 0x5EED0006)
+    lut = workload_lut(p)
+    d_in = torch.from_numpy(lwe).to(f"cuda:{dev}")
+    d_lut = torch.from_numpy(lut).to(f"cuda:{dev}")
+    d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
+    d_out = torch.empty_like(d_in)
+    from yatfhe_gb300 import autotune
+
+    tuning = autotune.tune(ctx, key, d_lut)
+    L = _lib.lib()
+    stream = torch.cuda.Stream(device=dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        _lib.check(L.yg_blind_rotate_extract(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
+                                             ctypes.c_void_p(d_lut.data_ptr()), ctypes.c_void_p(d_big.data_ptr()),
+                                             count, sh))
+        _lib.check(L.yg_keyswitch(ctx.handle, key.handle, ctypes.c_void_p(d_big.data_ptr()),
+                                  ctypes.c_void_p(d_out.data_ptr()), count, sh))
+
+    for _ in range(warmup):
+        step()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        step()
+    b.record(stream)
+    stream.synchronize()
+    ms = a.elapsed_time(b)
+    return {"workload": f"wwl24_t32_n2048_batch{count}", "params": params_config(p),
+            "ciphertexts_per_step": count, "value": count * steps / (ms / 1e3), "unit": "bootstraps/s",
+            "steps": steps, "ms_per_step": ms / steps, "launch_shape": tuning,
+            "key_upload_s": min(uploads), "key_upload_s_all": uploads,
+            "key_host_bytes": int(cprime.nbytes + s2.nbytes), "ginx_key_host_bytes": p.bsk_ntt_words * 8,
+            "key_device_bytes": key.device_bytes}
+
+
 def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
     """32 tenants with their own keys: 24 on the TORUS=32 set, 8 on the TORUS=56 set;
     per-tenant ciphertext counts from Zipf(1.1) over the 32 tenants (32,768 draws).  Each
@@ -668,6 +732,7 @@ def main():
     if not args.no_extras:
         extras["workloads"] = {
             "t56_n2048_batch16384": _safe(leg_t56, dev),
+            "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
             "serving_t32_128tenants_4GB": _safe(
                 leg_serving, dev, requests=args.serving_requests,

@@ -71,17 +71,31 @@ __device__ __forceinline__ int slot_pos(int tt, int r) {
 
 // PS is the prime set (rns.cuh) of `ch`: it picks the constant-bank twiddles and the
 // reduction schedule of the forward transform.
-template <int LOGN, int PS>
-__device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
+// TAB: the input holds signed digits d (|d| <= 64, as int32) instead of residues, and the
+// first stage (pairs j, j + N/2, twiddle psi^(N/2)) reads psi^(N/2) d mod p from `tab`
+// (indexed by d) instead of multiplying: x' = d_x + p + t, y' = d_x + 3p - t, both < 4p as
+// in the residue path.
+template <int LOGN, int PS, bool TAB = false>
+__device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch,
+                                            const uint32_t* tab = nullptr) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
+    if constexpr (TAB) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int dx = (int)a[r], dy = (int)a[r + 16];
+            const uint32_t t = tab[dy];
+            a[r] = (uint32_t)(dx + (int)p) + t;
+            a[r + 16] = (uint32_t)(dx + 3 * (int)p) - t;
+        }
+    }
     // Input residues < 2p; every butterfly adds at most 2p to the bound of its x input.
     // Prime set 0 (p < 2^29, 8p < 2^32): natural-layout stages 4p, 6p, 8p, reduce -> 6p, 8p;
     // slot-layout stages reduce -> 6p, 8p, reduce -> 6p, 8p, reduce -> 6p (then the N = 2048
     // shuffle stage, reduce -> 6p).  Output < 8p.  Prime set 1 (p < 2^27, 32p < 2^32): no
     // reduction; output < 22p (N = 1024) or 24p (N = 2048).
 #pragma unroll
-    for (int sp = 4; sp >= 0; --sp) {
+    for (int sp = TAB ? 3 : 4; sp >= 0; --sp) {
         const int h = 1 << sp;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {

@@ -348,9 +348,35 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
     constexpr int DROWS = SPLIT ? 2 : digit_rows(T);
     int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [DROWS][L][N]
     int16_t* sa = dig + DROWS * L * N;                                           // [n+1]
+    // T = 32: first-stage product tables of the forward transforms, [3][kTab0Words]
+    uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
+    const bool use_tab0 = T == 32 && a.radix_bits <= 7;
+    if (use_tab0) {
+        for (int idx = ltid; idx < kChannels * (2 * kTab0Half + 1); idx += ST) {
+            const int c = idx / (2 * kTab0Half + 1), d = idx - c * (2 * kTab0Half + 1) - kTab0Half;
+            const uint32_t pc = pick_chan(a.ch, c).p;
+            const int64_t v = (int64_t)c_tw_head[PS][LOGN - 10][c][0][1].x * d % pc;
+            tab0[c * kTab0Words + kTab0Half + d] = (uint32_t)(v < 0 ? v + pc : v);
+        }
+    }
     // the team's transpose region: region 0 of its channel (channel layout, the inverse
     // uses both), or region `hrow` (channel-row layout, each team owns one)
     uint32_t* mine = xb + (team * 2 + hrow) * Sh::TBUF;
+
+    // one digit polynomial of this team's channel into x, forward transform
+    auto load_and_forward = [&](uint32_t (&x)[32], const int16_t* d) {
+        if constexpr (T == 32) {
+            if (use_tab0) {
+#pragma unroll
+                for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + tt];
+                ntt_forward<LOGN, PS, true>(x, mine, tt, team, bar, ch, tab0 + team * kTab0Words + kTab0Half);
+                return;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
+        ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
+    };
 
     // G ciphertexts per iteration; a grid smaller than the batch makes the CTAs persistent
     for (int first = blockIdx.x * G; first < a.count; first += gridDim.x * G) {
@@ -444,9 +470,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                     for (int lvl = 0; lvl < L; ++lvl) {
                         uint32_t x[32];
                         const int16_t* d = dig + ((size_t)dr * L + lvl) * N;
-#pragma unroll
-                        for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                        ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
+                        load_and_forward(x, d);
                         const uint4* kp =
                             key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
 #pragma unroll
@@ -485,9 +509,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 for (int lvl = 0; lvl < L; ++lvl) {
                     uint32_t x[32];
                     const int16_t* d = dig + ((size_t)row * L + lvl) * N;
-#pragma unroll
-                    for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
-                    ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
+                    load_and_forward(x, d);
                     const uint4* kp =
                         key + ((((size_t)i * L + lvl) * 2 + row) * kChannels + team) * (key_block_words(N) / 4);
                     const uint4* kown = kp + (row ? 8 : 0) * S;

@@ -115,6 +115,10 @@ __host__ __device__ constexpr int digit_rows(int torus_bits) { return torus_bits
 constexpr int kLayoutChannel = 0;
 constexpr int kLayoutChannelRow = 1;
 
+// At T = 32 each slice also keeps the first-stage product table of its forward transforms:
+// psi_c^(N/2) d mod p_c for the digits d in [-64, 64] (radices up to 7), per channel.
+constexpr int kTab0Half = 64;
+constexpr int kTab0Words = 2 * kTab0Half + 4;  // 129 used
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
@@ -122,6 +126,7 @@ __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n,
     b += 2 * N * (torus_bits == 32 ? 4 : 8);
     b += (size_t)(layout == kLayoutChannelRow ? 2 : digit_rows(torus_bits)) * L * N * 2;
     b += ((size_t)n + 1) * 2;
+    if (torus_bits == 32) b = ((b + 3) & ~(size_t)3) + (size_t)kChannels * kTab0Words * 4;
     return (b + 15) & ~(size_t)15;
 }
 // Uploads the first 32 forward and inverse twiddles of each channel of prime set ps
