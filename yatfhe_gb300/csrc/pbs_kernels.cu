@@ -501,7 +501,60 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             }
             if (DROWS == 1 && row0 == 0) slice_sync();  // the next row's digits overwrite these
         }
-        if constexpr (SPLIT) {
+        if constexpr (SPLIT && T == 32) {
+            if (active) {
+                // this team's row: l forward NTTs.  After each one the two teams of the
+                // channel swap their transforms through their own regions, and each
+                // accumulates only the output it finishes (row 0 -> a, row 1 -> b) from both
+                // rows' digits, as exact 64-bit sums: 2 l products below 22p * p each stay
+                // under 2^64 with the 27-bit primes; one Montgomery reduction at the end.
+                const int row = hrow;
+                const uint32_t* other = xb + (team * 2 + (1 - hrow)) * Sh::TBUF;
+                uint64_t acc64[32];
+#pragma unroll
+                for (int r = 0; r < 32; ++r) acc64[r] = 0;
+                for (int lvl = 0; lvl < L; ++lvl) {
+                    uint32_t x[32];
+                    load_and_forward(x, dig + ((size_t)row * L + lvl) * N);
+                    team_sync<LOGN>(bar);  // the team's transpose reads of its region are done
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) mine[r * S + tt] = x[r];
+                    pair_sync<LOGN>(pair_bar);  // the partner's transform is in its region
+                    const size_t blk = (size_t)i * L + lvl;
+                    const uint4* kown = key + ((blk * 2 + row) * kChannels + team) * (key_block_words(N) / 4) +
+                                        (row ? 8 : 0) * S;
+                    const uint4* kpar = key + ((blk * 2 + (1 - row)) * kChannels + team) * (key_block_words(N) / 4) +
+                                        (row ? 8 : 0) * S;
+#pragma unroll
+                    for (int rr = 0; rr < 8; ++rr) {
+                        const uint4 ka = ldg_keep(kown + rr * S + tt, keep);
+                        const uint4 kb = ldg_keep(kpar + rr * S + tt, keep);
+                        const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+                        const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int r = rr * 4 + e;
+                            acc64[r] += (uint64_t)x[r] * kav[e];
+                            acc64[r] += (uint64_t)other[r * S + tt] * kbv[e];
+                        }
+                    }
+                    pair_sync<LOGN>(pair_bar);  // the partner has read this region
+                }
+                // S 2^-32 mod p: m = lo(S) p^-1, (S - m p) / 2^32 = hi(S) - hi(m p) in (-p, 2^29.2),
+                // + p, then one Shoup reduction by 1 to [0, 2p) for the inverse transform
+                const uint32_t one_s = 0xFFFFFFFFu / ch.p;
+#pragma unroll
+                for (int r = 0; r < 32; ++r) {
+                    const uint32_t lo = (uint32_t)acc64[r], hi = (uint32_t)(acc64[r] >> 32);
+                    const uint32_t t = hi - __umulhi(lo * pinv, ch.p) + ch.p;
+                    oa[r] = t - __umulhi(t, one_s) * ch.p;
+                }
+                ntt_inverse<LOGN, PS>(oa, mine, tt, team, bar, ch);
+                team_sync<LOGN>(bar);
+#pragma unroll
+                for (int r = 0; r < 32; ++r) mine[r * S + tt] = reduce_once(oa[r], ch.p);
+            }
+        } else if constexpr (SPLIT) {
             if (active) {
                 // this team's row: l forward NTTs; oa gathers the output this team finishes
                 // (row 0 -> a, row 1 -> b), ob the other output's partial sum
@@ -538,8 +591,9 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                     }
                 }
                 // swap partial sums with the channel's other team: write the one it
-                // finishes into this team's region (its own transposes are done), wait,
+                // finishes into this team's region once its transposes are done, wait,
                 // add the partner's, wait until the partner has read this region
+                team_sync<LOGN>(bar);
 #pragma unroll
                 for (int r = 0; r < 32; ++r) mine[r * S + tt] = ob[r];
                 pair_sync<LOGN>(pair_bar);
