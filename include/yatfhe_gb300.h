@@ -38,7 +38,11 @@ extern "C" {
 
 /* The fields of YatfheParameters (yatfhe/include/yatfhe/yatfhe_parameters.h:9-110) that
  * the bootstrap reads: l_approx is the gadget level count of the key and of the
- * decomposition; ks_level / ks_radix_bits the key-switching decomposition. */
+ * decomposition; ks_level / ks_radix_bits the key-switching decomposition.  Supported:
+ * torus_bits 32 or 56, N 1024 or 2048, k = 1, n <= 4096, radix_bits <= 15, l_approx <= 15,
+ * l_approx * radix_bits <= torus_bits, ks_level <= 16, ks_radix_bits <= 7, and gadgets
+ * whose exact products stay inside the three-prime RNS; yg_ctx_create rejects the rest
+ * with YG_ERR_INVALID. */
 typedef struct yg_params {
     int n;
     int N;

@@ -141,6 +141,9 @@ void validate(const yg_params& p) {
     if (p.l_approx < 1 || p.radix_bits < 1 || p.l_approx * p.radix_bits > p.torus_bits)
         throw std::invalid_argument("decomposeRow: l * radixBits exceeds the torus width");
     if (p.radix_bits > 15) throw std::invalid_argument("radix_bits must be <= 15 (int16 digits)");
+    // the channel-row layout at T = 32 sums 2 l products of transform outputs (< 22p) and
+    // key words (< p) exactly in 64 bits: below 2^64 for l <= 15
+    if (p.l_approx > 15) throw std::invalid_argument("l must be <= 15");
     if (p.ks_level < 1 || p.ks_level > 16 || p.ks_radix_bits < 1 || p.ks_level * p.ks_radix_bits > 32 ||
         p.ks_radix_bits > 7)
         throw std::invalid_argument("key-switching decomposition must fit 32 bits, t <= 16, radix <= 7");
