@@ -52,6 +52,7 @@ def test_invalid_parameters_are_rejected_before_any_device_work(built_lib):
         dict(l_approx=5, radix_bits=7),   # 35 bits > T = 32
         dict(ks_level=17, ks_radix_bits=1),
         dict(radix_bits=16, l_approx=2),
+        dict(radix_bits=1, l_approx=16),  # 64-bit channel-row sums need l <= 15
     ]
     for change in bad:
         fields = {f: getattr(T32_N1024, f) for f in ("n", "N", "k", "radix_bits", "l_approx", "ks_radix_bits",
@@ -70,6 +71,8 @@ def test_null_arguments_are_rejected(built_lib):
     L = _lib.lib()
     assert L.yg_ctx_create(None, 0, None) == -1
     assert L.yg_pbs(None, None, None, None, 1, None, None) == -1
+    assert L.yg_key_upload_wwl24_ntt(None, None, None, 1, None) == -1
+    assert L.yg_key_load_wwl24_file(None, None, None) == -1
     assert L.yg_key_device_bytes(None) == 0
     L.yg_ctx_destroy(None)
     L.yg_key_destroy(None)
