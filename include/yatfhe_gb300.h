@@ -206,7 +206,9 @@ typedef struct yg_request_times {
 } yg_request_times;
 int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out);
 /* Snapshots `key` (BSK + KSK, device layout) into pinned host memory; the key object may be
- * destroyed afterwards.  h_lut: the tenant's test polynomial ([N] int64). */
+ * destroyed afterwards.  Any key handle works, whatever format it was made from (GINX or
+ * WWL+24), so tenants of both families share one cache.  h_lut: the tenant's test
+ * polynomial ([N] int64). */
 int yg_server_add_tenant(yg_server* s, int tenant, const yg_key* key, const int64_t* h_lut);
 int yg_server_start(yg_server* s);
 /* Returns a request id (> 0) or a negative status. */

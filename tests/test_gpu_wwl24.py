@@ -97,3 +97,40 @@ def test_gpu_wwl24_file_and_errors(tmp_path, built_lib):
     (tmp_path / "short.bin").write_bytes(raw[:-64])
     with pytest.raises(Exception):
         api.BootstrapKey.from_wwl24_file(ctx, tmp_path / "short.bin")
+
+
+def test_serving_mixes_wwl24_and_ginx_tenants(built_lib):
+    """yg_server_add_tenant snapshots any key handle: WWL+24 tenants (rows derived at upload)
+    and GINX tenants share the HBM key cache, evictions included, bit-exact."""
+    from yatfhe_gb300 import api, serving
+    from yatfhe_gb300 import lut as lutmod
+
+    p = small(WWL24_T32_N2048, 10)
+    ctx = api.Context(p, 0)
+    keys = []
+    for t in range(4):
+        o = Restatement(p)
+        if t % 2:
+            o.keygen_wwl24(500 + t)
+            keys.append(api.BootstrapKey.from_wwl24_words(ctx, *o.wwl24_words()).set_ksk(o.ksk()))
+        else:
+            o.keygen(500 + t)
+            keys.append(api.BootstrapKey.from_ntt_words(ctx, o.bsk_ntt()).set_ksk(o.ksk()))
+    srv = serving.Server(ctx, key_budget_bytes=1.5 * keys[0].device_bytes, max_batch=32, max_inflight=2)
+    lut = lutmod.sign_lut(p.N, 32)
+    rng = np.random.default_rng(12)
+    pool = torch.empty((4, 8, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    for t in range(4):
+        srv.add_tenant(t, keys[t], lut)
+        lwe = rng.integers(-(1 << 31), 1 << 31, size=(8, p.n + 1), dtype=np.int64).astype(np.int32)
+        pool[t] = torch.from_numpy(lwe)
+        expect[t] = api.functional_bootstrapping_mp_ntt(ctx, keys[t], torch.from_numpy(lwe).cuda(),
+                                                        torch.from_numpy(lut).cuda()).cpu()
+    srv.start()
+    try:
+        res = srv.run_trace(pool, expect, requests=60, warmup=0, rate=500.0, zipf_s=1.1, max_count=8, seed=3)
+        assert res["served"] == 60 and res["mismatched_requests"] == 0
+        assert res["key_misses"] > 0
+    finally:
+        srv.close()
