@@ -658,7 +658,7 @@ def main():
 
     # end to end through the host-buffer entry point, pinned buffers
     L = run.L
-    from yatfhe_gb300 import _lib
+    from yatfhe_gb300 import _lib, api
 
     h_in = torch.from_numpy(run.lwe).pin_memory()
     h_out = torch.empty_like(h_in).pin_memory()
@@ -720,6 +720,24 @@ def main():
         sweep[str(count)] = value / world
         extras["batch_sweep_bps"] = sweep
         extras["batched_over_plain"] = value / world / extras["plain_per_call_bps"]
+        # one ciphertext per call in each layout that exists for these parameters (one
+        # ciphertext per CTA), then the tuned shape back
+        lone = {}
+        for name, lay in (("channel", 0), ("channel_row", 1), ("row_cluster", 2)):
+            if api.ctas_per_sm(run.ctx, 1, lay) < 1:
+                continue
+            api.set_launch(run.ctx, 1, 0, lay)
+            for _ in range(3):
+                pbs(one_in, one_out, 1)
+            a.record(run.stream)
+            for _ in range(10):
+                pbs(one_in, one_out, 1)
+            b.record(run.stream)
+            run.stream.synchronize()
+            lone[name] = a.elapsed_time(b) / 10
+        c = run.tuning["choice"]
+        api.set_launch(run.ctx, c["per_cta"], c["ctas_per_sm"], c.get("layout", 0))
+        extras["lone_latency_ms_by_layout"] = lone
 
     # CPU baseline on a bounded sample (oracle on the host cores), also the bit-exact check;
     # the step's outputs are recomputed first (the sweep above overwrote part of them)

@@ -162,9 +162,14 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
 /* Work split of one ciphertext in the blind rotation.  YG_LAYOUT_CHANNEL: one team of
  * N/32 threads per RNS channel runs every NTT of a CMux step.  YG_LAYOUT_CHANNEL_ROW: two
  * teams per channel, one per accumulator row, each running half the forward transforms and
- * one inverse transform: twice the threads per ciphertext, about half the latency. */
+ * one inverse transform: twice the threads per ciphertext, about half the latency.
+ * YG_LAYOUT_ROW_CLUSTER (T = 32, N = 1024, l_approx <= 4, per_cta 1): a cluster of two CTAs
+ * per ciphertext, one per accumulator row, with one team per (channel, digit level), so the
+ * levels' transforms run side by side: the shortest latency for lone ciphertexts (the
+ * grid is always two CTAs per ciphertext; a persistent grid does not apply). */
 #define YG_LAYOUT_CHANNEL 0
 #define YG_LAYOUT_CHANNEL_ROW 1
+#define YG_LAYOUT_ROW_CLUSTER 2
 /* Launch shape for this plan: layout, per_cta ciphertexts per blind-rotation CTA (1, 2 or
  * 4; 0 = the context's setting, layout included) and grid CTAs (0 = enough for the batch;
  * fewer = persistent CTAs that loop over it). */

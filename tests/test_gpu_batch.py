@@ -40,11 +40,12 @@ def test_multi_key_batch_matches_per_tenant_oracle(base, built_lib):
     lwe = np.concatenate([oras[t].encrypt(rng.integers(-(1 << 31), 1 << 31, c)) for t, c in enumerate(counts)])
     luts = [torch.from_numpy(v).cuda() for v in luts_np]
     d_in = torch.from_numpy(lwe).cuda()
-    shapes = [(lay, g, grid) for lay in (0, 1) for g in (1, 2, 4) if api.ctas_per_sm(ctx, g, lay) > 0
+    shapes = [(lay, g, grid) for lay in (0, 1, 2) for g in (1, 2, 4) if api.ctas_per_sm(ctx, g, lay) > 0
               for grid in (0, 3)]
     assert (0, 1, 0) in shapes and (1, 1, 0) in shapes
     assert (0, 2, 0) in shapes or p.N == 2048
-    for lay, g in ((0, 4), (1, 4)):
+    assert ((2, 1, 0) in shapes) == (p.torus_bits == 32 and p.N == 1024)  # the row-cluster layout
+    for lay, g in ((0, 4), (1, 4), (2, 2)):
         if api.ctas_per_sm(ctx, g, lay) == 0:  # no such kernel or too large: rejected, never skipped
             with pytest.raises(ValueError):
                 api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids, per_cta=g, layout=lay)

@@ -58,11 +58,14 @@ def test_pbs_t32_small_bit_exact(t32_small):
     np.testing.assert_array_equal(ora.decrypt(got, 8), np.where(mu > 0, 1, -1))
 
 
-def test_blind_rotate_checkpoints_t32(t32_small):
-    """Accumulator after 1, 2, 7 and all CMux steps equals the oracle's trace."""
+@pytest.mark.parametrize("layout", [0, 2])
+def test_blind_rotate_checkpoints_t32(t32_small, layout):
+    """Accumulator after 1, 2, 7 and all CMux steps equals the oracle's trace (channel and
+    row-cluster layouts)."""
     from yatfhe_gb300 import api
 
     ora, ctx, key = t32_small
+    api.set_launch(ctx, 1, 0, layout)
     _, lwe = _sign_inputs(ora, 2, 2)
     lut = ora.test_polynomial(0, 8)
     cps = [0, 1, 6, ctx.params.n - 1]
@@ -74,16 +77,20 @@ def test_blind_rotate_checkpoints_t32(t32_small):
             acc = api.blind_rotate_mp21_ntt(ctx, key, d_in[c:c + 1], d_lut, steps=step + 1).cpu().numpy()[0]
             np.testing.assert_array_equal(acc, want[k], err_msg=f"ciphertext {c}, after step {step}")
         np.testing.assert_array_equal(want[-1], final)
+    api.set_launch(ctx, 1, 0, 0)
 
 
-def test_blind_rotate_acc_reference_semantics(t32_small):
+@pytest.mark.parametrize("layout", [0, 2])
+def test_blind_rotate_acc_reference_semantics(t32_small, layout):
     """yg_blind_rotate_acc = blindRotateMP21Ntt(accum, bsk, scaled, param): a caller-built
-    accumulator and already-switched mask, rotated in place."""
+    accumulator and already-switched mask, rotated in place (channel and row-cluster
+    layouts)."""
     import ctypes
 
-    from yatfhe_gb300 import _lib
+    from yatfhe_gb300 import _lib, api
 
     ora, ctx, key = t32_small
+    api.set_launch(ctx, 1, 0, layout)
     p = ctx.params
     _, lwe = _sign_inputs(ora, 3, 8)
     lut = ora.test_polynomial(1, 8)
@@ -99,6 +106,7 @@ def test_blind_rotate_acc_reference_semantics(t32_small):
     for c in range(3):
         _, final = ora.blind_rotate_trace(lwe[c], lut, [])
         np.testing.assert_array_equal(got[c], final)
+    api.set_launch(ctx, 1, 0, 0)
 
 
 def test_keyswitch_alone_t32(t32_small):

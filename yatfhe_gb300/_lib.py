@@ -17,6 +17,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_build" / "libyatfhe_gb300.so"
 YG_OK = 0
 LAYOUT_CHANNEL = 0      # YG_LAYOUT_CHANNEL
 LAYOUT_CHANNEL_ROW = 1  # YG_LAYOUT_CHANNEL_ROW
+LAYOUT_ROW_CLUSTER = 2  # YG_LAYOUT_ROW_CLUSTER
 _ERRORS = {-1: ValueError, -2: RuntimeError, -3: OSError, -4: MemoryError, -5: RuntimeError}
 
 

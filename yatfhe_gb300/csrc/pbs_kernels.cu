@@ -11,6 +11,7 @@
 //                        steps
 //   keyswitch_kernel     switchKeyForTlwe (yatfhe/src/keyswitching.cpp:48-72) for a tile of
 //                        ciphertexts x output columns, KSK rows streamed once per tile
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -657,6 +658,202 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
     }
 }
 
+// Row-cluster layout (kLayoutRowCluster), T = 32, N = 1024: one ciphertext per cluster of
+// two CTAs.  CTA h (its rank in the cluster) owns accumulator row h (0: a, 1: b) and computes
+// output h of every external product; warp w = c L + lvl is the team of RNS channel c and
+// digit level lvl.  Per CMux step: (1) all threads rotate and decompose row h into l digit
+// rows; (2) each team runs the forward transform of its level's digits and writes it into
+// the partner CTA's exchange region of the same team (distributed shared memory; two
+// regions used alternately by the active steps, so a region is rewritten only after the
+// partner has passed the next cluster barrier); after the cluster barrier (3) each team
+// multiplies its transform and the partner's with the key words for output h, an exact
+// 64-bit sum of two products reduced once, into its partial region; (4) the level-0 team of
+// each channel adds the l partials and runs the inverse transform; (5) all threads
+// recombine the channels (CRT) and add into row h.  The levels' transforms run side by
+// side, so a step takes about one forward and one inverse transform instead of l forward
+// ones: the latency shape for lone ciphertexts.
+template <int T>
+__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster_kernel(const BrArgs a) {
+    static_assert(T == 32, "the row-cluster layout is built for the 32-bit torus");
+    namespace cg = cooperative_groups;
+    using Sh = TeamShape<10>;
+    constexpr int N = Sh::N, S = Sh::S;
+    constexpr int PS = prime_set_for(T);
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int h = (int)cluster.block_rank();
+    const int L = a.L, n = a.n;
+    const int ct = (int)(blockIdx.x >> 1);
+    const bool valid = ct < a.count;  // the grid is two CTAs per ciphertext: uniform per cluster
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int c = warp / L, lvl = warp - c * L;
+    const Chan ch = pick_chan(a.ch, c);
+    const uint64_t keep = l2_evict_last_policy();
+    const uint32_t pinv = 0u - ch.pinv_neg;
+    const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
+
+    const size_t team_words = (size_t)kChannels * L * Sh::TBUF;
+    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);  // [3][L][TBUF] transposes, inverse outputs
+    uint32_t* partials = regions + team_words;              // [3][L][TBUF]
+    uint32_t* exch = partials + team_words;                 // [2][3][L][TBUF] written by the partner
+    int32_t* acc = reinterpret_cast<int32_t*>(exch + 2 * team_words);  // [N] row h
+    int16_t* dig = reinterpret_cast<int16_t*>(acc + N);               // [L][N]
+    int16_t* sa = dig + (size_t)L * N;                                // [n+1]
+    uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
+    uint32_t* mine = regions + (size_t)(c * L + lvl) * Sh::TBUF;
+    uint32_t* part = partials + (size_t)(c * L + lvl) * Sh::TBUF;
+    uint32_t* my_exch = exch + (size_t)(c * L + lvl) * Sh::TBUF;     // + ph * team_words
+    uint32_t* their_exch = cluster.map_shared_rank(my_exch, 1 - h);  // the partner CTA's same team
+    int ph = 0;                                                      // exchange region of this step
+
+    const uint4* key = !valid ? nullptr : (a.key_of ? a.key_table[a.key_of[ct]] : a.key);
+    const int64_t* lut = !valid ? nullptr : (a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut);
+    const bool use_tab0 = a.radix_bits <= 7;
+    if (use_tab0) {
+        for (int idx = tid; idx < kChannels * 129; idx += NT) {
+            const int cc = idx / 129, d = idx - cc * 129 - 64;
+            const uint32_t pc = pick_chan(a.ch, cc).p;
+            const int64_t v = (int64_t)c_tw_head[PS][0][cc][0][1].x * d % pc;
+            tab0[cc * 132 + 64 + d] = (uint32_t)(v < 0 ? v + pc : v);
+        }
+    }
+    if (valid) {
+        if (a.scaled_in) {
+            for (int i = tid; i < n; i += NT) sa[i] = (int16_t)a.scaled_in[(size_t)ct * n + i];
+        } else {
+            const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+            for (int i = tid; i <= n; i += NT) sa[i] = (int16_t)modswitch_down(in[i], 31 - 10, 11);
+        }
+    } else {
+        for (int i = tid; i <= n; i += NT) sa[i] = 0;
+    }
+    __syncthreads();
+    if (valid && a.acc_in) {
+        for (int j = tid; j < N; j += NT) acc[j] = (int32_t)a.acc_in[(size_t)ct * 2 * N + h * N + j];
+    } else if (valid) {
+        // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
+        int t2 = -(int)sa[n];
+        t2 = ((t2 % (2 * N)) + 2 * N) % (2 * N);
+        const bool wrap = t2 >= N;
+        const int at = wrap ? t2 - N : t2;
+        for (int j = tid; j < N; j += NT) {
+            int32_t v = j < at ? tneg<T>((int32_t)lut[j - at + N]) : (int32_t)lut[j - at];
+            acc[j] = h == 0 ? 0 : (wrap ? tneg<T>(v) : v);
+        }
+    } else {
+        for (int j = tid; j < N; j += NT) acc[j] = 0;
+    }
+    __syncthreads();
+
+    for (int i = 0; i < a.steps; ++i) {
+        const int ai = (int)sa[i];
+        if (ai == 0) continue;  // the a_i = 0 skip (blind_rotate.cpp:1557), the same in both CTAs
+        const int t2 = ai < 0 ? ai + 2 * N : ai;
+        const bool wrap = t2 >= N;
+        const int at = wrap ? t2 - N : t2;
+        // (1) X^{a_i} row - row, zero-mean digits (rotateTrlweMinusOne, gadgetDecomposeTrlwe)
+        auto decompose = [&](auto lc, auto rc) {
+            constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
+            const int levels = LC ? LC : L, radix = RC ? RC : a.radix_bits;
+#pragma unroll 1
+            for (int j = tid; j < N; j += NT) {
+                int32_t rot = j < at ? tneg<T>(acc[j - at + N]) : acc[j - at];
+                if (wrap) rot = tneg<T>(rot);
+                const int32_t tmp = tsub<T>(rot, acc[j]);
+                int16_t* d = dig + j;
+                zero_mean_digits<uint32_t, 32>((uint32_t)tmp, levels, radix, [&](int level, int v) { d[level * N] = (int16_t)v; });
+            }
+        };
+        if (L == 3 && a.radix_bits == 7)
+            decompose(std::integral_constant<int, 3>{}, std::integral_constant<int, 7>{});
+        else
+            decompose(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+        __syncthreads();
+        // (2) this team's forward transform, written into the partner's exchange region
+        uint32_t x[32];
+        const int16_t* d = dig + (size_t)lvl * N;
+        if (use_tab0) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane];
+            ntt_forward<10, PS, true>(x, mine, lane, c, 0, ch, tab0 + c * 132 + 64);
+        } else {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + lane] + (int32_t)ch.p);
+            ntt_forward<10, PS>(x, mine, lane, c, 0, ch);
+        }
+        {
+            uint32_t* dst = their_exch + (size_t)ph * team_words;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) dst[r * S + lane] = x[r];
+        }
+        cluster.sync();  // both CTAs' transforms are in the partner's exchange regions
+        const uint32_t* theirs = my_exch + (size_t)ph * team_words;
+        ph ^= 1;
+        // (3) output h: own row with K(lvl, h, h), the partner's row with K(lvl, 1-h, h);
+        // x < 22p and key words < p: the sum of two products fits 64 bits
+        {
+            const size_t blk = (size_t)i * L + lvl;
+            const uint4* kown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+            const uint4* kpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+#pragma unroll
+            for (int rr = 0; rr < 8; ++rr) {
+                const uint4 ka = ldg_keep(kown + rr * S + lane, keep);
+                const uint4 kb = ldg_keep(kpar + rr * S + lane, keep);
+                const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int r = rr * 4 + e;
+                    const uint64_t s = (uint64_t)x[r] * kav[e] + (uint64_t)theirs[r * S + lane] * kbv[e];
+                    // s 2^-32 mod p in [0, 2p): Montgomery, then a Shoup reduction by 1
+                    const uint32_t tt = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
+                    part[r * S + lane] = tt - __umulhi(tt, one_s) * ch.p;
+                }
+            }
+        }
+        __syncthreads();  // every partial is written
+        // (4) the level-0 team of each channel: sum of the l partials, inverse transform
+        if (lvl == 0) {
+            uint32_t oa[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                uint32_t v = 0;
+                for (int q = 0; q < L; ++q) v += partials[(size_t)(c * L + q) * Sh::TBUF + r * S + lane];
+                oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 2p each: < 8p; reduced to [0, 2p)
+            }
+            ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < 32; ++r) mine[r * S + lane] = reduce_once(oa[r], ch.p);
+        }
+        __syncthreads();
+        // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h
+#pragma unroll 1
+        for (int j = tid; j < N; j += NT) {
+            const int64_t v = crt_to_torus<T>(regions[(size_t)(0 * L) * Sh::TBUF + j], regions[(size_t)(1 * L) * Sh::TBUF + j],
+                                              regions[(size_t)(2 * L) * Sh::TBUF + j], a.crt);
+            acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
+        }
+        __syncthreads();
+    }
+
+    if (valid && a.acc_out) {
+        int64_t* dst = a.acc_out + (size_t)ct * 2 * N + h * N;
+        for (int j = tid; j < N; j += NT) dst[j] = (int64_t)acc[j];
+    }
+    if (valid && a.big_out) {
+        // extractTlweFromTrlwe(out, acc, 0): a'[j] = j ? -a[N-j] : a[0] from row 0, b' = b[0] from row 1
+        int32_t* dst = a.big_out + (size_t)ct * (N + 1);
+        if (h == 0) {
+            for (int j = tid; j < N; j += NT) dst[j] = j == 0 ? acc[0] : tneg<T>(acc[N - j]);
+        } else if (tid == 0) {
+            dst[N] = acc[0];
+        }
+    }
+    cluster.sync();  // neither CTA leaves while the other may still write into its regions
+}
+
 constexpr int kKsTile = kKsTileCts;  // ciphertexts per block
 constexpr int kKsCols = 128;    // output columns per block (= threads)
 constexpr int kKsChunk = 32;    // input coefficients per digit refresh
@@ -807,12 +1004,56 @@ int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+namespace {
+
+// The row-cluster kernel exists for T = 32, N = 1024, one ciphertext per cluster, l <= 4.
+bool cluster_variant(int logN, int torus_bits, int per_cta, int L) {
+    return logN == 10 && torus_bits == 32 && per_cta <= 1 && L >= 1 && L <= kClusterMaxLevels;
+}
+
+int prepare_brc() {
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    if (!done[dev].load()) {
+        if (cudaFuncSetAttribute(blind_rotate_cluster_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 227 * 1024) != cudaSuccess)
+            return -1;
+        done[dev].store(true);
+    }
+    return 0;
+}
+
+}  // namespace
+
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream) {
     if (a.count <= 0) return 0;
+    if (a.layout == kLayoutRowCluster) {
+        if (!cluster_variant(logN, torus_bits, a.per_cta, a.L)) return kNoVariant;
+        const size_t smem = brc_smem_bytes(a.n, a.L);
+        if (smem > 227 * 1024 || prepare_brc() != 0) return -1;
+        blind_rotate_cluster_kernel<32><<<2 * a.count, kChannels * a.L * 32, smem, (cudaStream_t)stream>>>(a);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
     return dispatch_br(logN, torus_bits, a.per_cta, a.layout, LaunchBr{a, stream});
 }
 
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout) {
+    if (layout == kLayoutRowCluster) {
+        if (!cluster_variant(logN, torus_bits, per_cta, L)) return 0;
+        const size_t smem = brc_smem_bytes(n, L);
+        if (smem > 227 * 1024) return 0;
+        if (prepare_brc() != 0) return -1;
+        int blocks = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_cluster_kernel<32>, kChannels * L * 32,
+                                                          smem) != cudaSuccess) {
+            // the calculator may decline cluster kernels: its shared memory fits and 168
+            // registers x 3 l warps (l <= 4) fit one SM's register file
+            (void)cudaGetLastError();
+            blocks = 1;
+        }
+        return blocks;
+    }
     return dispatch_br(logN, torus_bits, per_cta, layout, OccupancyBr{n, L});
 }
 

@@ -25,7 +25,7 @@ struct BrArgs {
     int count;
     int grid;                // CTAs to launch (0: enough for the batch; fewer: persistent CTAs)
     int per_cta;             // ciphertexts per CTA, sharing its L1 (1, 2 or 4; 0 means 1)
-    int layout;              // kLayoutChannel or kLayoutChannelRow
+    int layout;              // kLayoutChannel, kLayoutChannelRow or kLayoutRowCluster
     int n;                   // LWE dimension
     int steps;               // CMux steps to run (n for a full blind rotation)
     int L;                   // gadget levels
@@ -114,11 +114,26 @@ __host__ __device__ constexpr int digit_rows(int torus_bits) { return torus_bits
 // or per channel and accumulator row.
 constexpr int kLayoutChannel = 0;
 constexpr int kLayoutChannelRow = 1;
+// A cluster of two CTAs per ciphertext, CTA h owning accumulator row h, one warp per (RNS
+// channel, digit level): the levels' transforms run side by side (T = 32, N = 1024, l <= 4).
+constexpr int kLayoutRowCluster = 2;
+constexpr int kClusterMaxLevels = 4;
 
 // At T = 32 each slice also keeps the first-stage product table of its forward transforms:
 // psi_c^(N/2) d mod p_c for the digits d in [-64, 64] (radices up to 7), per channel.
 constexpr int kTab0Half = 64;
 constexpr int kTab0Words = 2 * kTab0Half + 4;  // 129 used
+// Shared memory of one CTA of the row-cluster layout (N = 1024, T = 32): per team (channel,
+// level) a padded transpose region, a partial-sum region and two exchange regions the
+// partner CTA writes into, the accumulator row, its digits, the mod-2N input and the
+// first-stage digit tables.
+__host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
+    const size_t N = 1024, tbuf = N + N / 32;
+    size_t b = (size_t)kChannels * L * 4 * tbuf * 4;  // transposes, partials, 2 exchange buffers
+    b += N * 4 + (size_t)L * N * 2 + ((size_t)n + 1) * 2;
+    b = ((b + 3) & ~(size_t)3) + (size_t)kChannels * 132 * 4;
+    return (b + 15) & ~(size_t)15;
+}
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
