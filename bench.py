@@ -58,7 +58,8 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="with --per-cta: persistent CTAs per SM (0 = off)")
-    ap.add_argument("--layout", type=int, default=0, help="with --per-cta: 0 = team per channel, 1 = per channel and row")
+    ap.add_argument("--layout", type=int, default=0,
+                    help="with --per-cta: 0 = team per channel, 1 = per channel and row, 2 = two-CTA row cluster")
     ap.add_argument("--retune", action="store_true", help="re-measure launch shapes instead of the cached choice")
     ap.add_argument("--serving-requests", type=int, default=800, help="measured requests per offered rate")
     ap.add_argument("--serving-fractions", default="0.5,0.6,0.7,0.8,0.9,1.0", help="offered rates / peak")
