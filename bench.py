@@ -405,6 +405,37 @@ def leg_wwl24(dev, steps=2, warmup=1, count=16384):
             "key_device_bytes": key.device_bytes}
 
 
+def leg_keygen(dev, reps=3):
+    """Key generation on the GPU for the TORUS=32 set (n=630, N=1024): seeded synthetic
+    samples with the distributions of real ones (binary secrets, TUniform(2^8) / (2^18)
+    noise, uniform masks), turned into a device key (BSK + KSK) by yg_keygen_from_samples;
+    the best of `reps` wall times, the samples' host bytes."""
+    import torch
+
+    from yatfhe_gb300 import api
+    from yatfhe_gb300.params import T32_N1024 as p
+
+    rng = np.random.default_rng(0x5EED0007)
+    k1, kN = p.k + 1, p.k * p.N
+    smp = {"lwe_s": rng.integers(0, 2, p.n).astype(np.int32), "rlwe_s": rng.integers(0, 2, kN).astype(np.int32),
+           "bsk_noise": rng.integers(-(1 << p.rlwe_noise_b), (1 << p.rlwe_noise_b) + 1,
+                                     size=(p.n, p.l_approx, k1, p.N)).astype(np.int32),
+           "bsk_mask": rng.integers(0, p.q_ntt, size=(p.n, p.l_approx, k1, p.k, p.N), dtype=np.uint64),
+           "ksk_mask": rng.integers(-(1 << 31), 1 << 31, size=(kN, p.ks_level, p.n), dtype=np.int64).astype(np.int32),
+           "ksk_noise": rng.integers(-(1 << p.lwe_noise_b), (1 << p.lwe_noise_b) + 1,
+                                     size=(kN, p.ks_level)).astype(np.int32)}
+    ctx = api.Context(p, dev)
+    times = []
+    for _ in range(reps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        key = api.keygen_from_samples(ctx, smp)
+        times.append(time.perf_counter() - t0)
+        key.close()
+    return {"params": params_config(p), "keygen_s": min(times), "keygen_s_all": times,
+            "sample_host_bytes": int(sum(v.nbytes for v in smp.values()))}
+
+
 def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
     """32 tenants with their own keys: 24 on the TORUS=32 set, 8 on the TORUS=56 set;
     per-tenant ciphertext counts from Zipf(1.1) over the 32 tenants (32,768 draws).  Each
@@ -752,6 +783,7 @@ def main():
         extras["workloads"] = {
             "t56_n2048_batch16384": _safe(leg_t56, dev),
             "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
+            "keygen_t32_n1024": _safe(leg_keygen, dev),
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
             "serving_t32_128tenants_4GB": _safe(
                 leg_serving, dev, requests=args.serving_requests,

@@ -89,6 +89,24 @@ int yg_key_upload_bsk_ntt(yg_ctx* ctx, const uint64_t* h_bsk_ntt, yg_key** out);
 int yg_key_upload_wwl24_ntt(yg_ctx* ctx, const uint64_t* h_cprime, const uint64_t* h_s2, int s2_levels,
                             yg_key** out);
 
+/* Key generation on the GPU from caller-drawn randomness: the arithmetic of
+ * genBootstrappingKeyMP's per-index encryptTrgswMPNtt (yatfhe/src/bootstrapping.cpp:150-174,
+ * yatfhe/src/trgsw.cpp:36-51) and of genTlweKeySwitchingKey (yatfhe/src/keyswitching.cpp:19-29),
+ * with the random samples supplied by the caller (the library draws none):
+ *   h_lwe_s [n], h_rlwe_s [k N]: the binary secrets;
+ *   h_bsk_noise [n][l_approx][k+1][N] int32: the TUniform noise of each RLWE sample's b
+ *       (row k of a level is cPrime, rows r < k are c[lvl][r]);
+ *   h_bsk_mask [n][l_approx][k+1][k][N]: each sample's uniform NTT-domain masks (< q);
+ *   h_ksk_mask [k N][ks_level][n] int32, h_ksk_noise [k N][ks_level] int32: the key-switching
+ *       samples' masks and noise.
+ * Drawn in the reference's order from its RNG these give the reference's keys bit for bit.
+ * Makes a device key with BSK and KSK; h_bsk_words ([n][l_approx][k+1][k+1][N], the layout of
+ * yg_key_upload_bsk_ntt) and h_ksk ([k N][ks_level][n+1]) receive the keys when not null.
+ * Non-binary secrets and unreduced masks are rejected with YG_ERR_INVALID.  Synchronizes. */
+int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h_rlwe_s, const int32_t* h_bsk_noise,
+                           const uint64_t* h_bsk_mask, const int32_t* h_ksk_mask, const int32_t* h_ksk_noise,
+                           uint64_t* h_bsk_words, int32_t* h_ksk, yg_key** out);
+
 /* Replaces deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): reads a file written
  * by serializeBskWWL24 (:220-229) and uploads it as above. */
 int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);

@@ -246,6 +246,22 @@ class Restatement(_Common):
     def load_bsk_file(self, path) -> None:
         self._call("load_bsk_file", str(path).encode())
 
+    def keygen_samples(self, seed: int) -> dict:
+        """keygen(seed) that also returns its random samples: the secrets, the BSK samples'
+        noise [n][l][k+1][N] and masks [n][l][k+1][k][N], the KSK samples' masks [kN][t][n]
+        and noise [kN][t]."""
+        p = self.p
+        k1, kN = p.k + 1, p.k * p.N
+        d = {"lwe_s": np.zeros(p.n, np.int32), "rlwe_s": np.zeros(kN, np.int32),
+             "bsk_noise": np.zeros((p.n, p.l_approx, k1, p.N), np.int32),
+             "bsk_mask": np.zeros((p.n, p.l_approx, k1, p.k, p.N), np.uint64),
+             "ksk_mask": np.zeros((kN, p.ks_level, p.n), np.int32),
+             "ksk_noise": np.zeros((kN, p.ks_level), np.int32)}
+        self._call("keygen_samples", ctypes.c_uint64(seed), _ptr(d["lwe_s"], _i32p), _ptr(d["rlwe_s"], _i32p),
+                   _ptr(d["bsk_noise"], _i32p), _ptr(d["bsk_mask"], _u64p), _ptr(d["ksk_mask"], _i32p),
+                   _ptr(d["ksk_noise"], _i32p))
+        return d
+
     def set_wwl24(self, cprime, s2) -> None:
         a = np.ascontiguousarray(cprime, np.uint64)
         b = np.ascontiguousarray(s2, np.uint64)

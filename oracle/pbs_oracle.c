@@ -151,6 +151,11 @@ struct po_ctx {
     int32_t* ksk;        /* [k*N][t][n+1] */
     uint64_t* wwl_cprime;/* WWL+24 key: [n][L][k+1][N] (allocated on first use) */
     uint64_t* wwl_s2;    /* [l][k+1][N] */
+    /* when set, po_keygen also records its random samples here (po_keygen_samples) */
+    int32_t* rec_bsk_noise;   /* [n][L][k+1][N] */
+    uint64_t* rec_bsk_mask;   /* [n][L][k+1][k][N] */
+    int32_t* rec_ksk_mask;    /* [kN][t][n] */
+    int32_t* rec_ksk_noise;   /* [kN][t] */
     char err[256];
 };
 
@@ -301,14 +306,20 @@ static int log2i(int x) {
 /* NTT-domain RLWE encryption: initTrlweMultiSampleSimple / initTrlweSingleSampleSimple
  * (yatfhe/src/trlwe.cpp:24-46) then symEncTrlweNttSimple (:58-60).  `mu` holds the N
  * torus plaintext coefficients; out = [a_0..a_{k-1}, b] NTT polys. */
-static void enc_trlwe_ntt(po_ctx* c, uint64_t* out, const int64_t* mu, int64_t* tmpT) {
+static void enc_trlwe_ntt(po_ctx* c, uint64_t* out, const int64_t* mu, int64_t* tmpT, int32_t* rec_noise,
+                          uint64_t* rec_mask) {
     const int N = c->p.N, k = c->p.k;
     const uint64_t q = c->q;
     uint64_t* b = out + (size_t)k * N;
-    for (int j = 0; j < N; j++) tmpT[j] = sext(mu[j] + rng_tuniform(&c->rng, c->p.rlwe_noise_b), c->T);
+    for (int j = 0; j < N; j++) {
+        const int64_t e = rng_tuniform(&c->rng, c->p.rlwe_noise_b);
+        if (rec_noise) rec_noise[j] = (int32_t)e;
+        tmpT[j] = sext(mu[j] + e, c->T);
+    }
     ntt_from_torus(c, b, tmpT);
     for (int r = 0; r < k; r++)
         for (int j = 0; j < N; j++) out[(size_t)r * N + j] = rng_urange(&c->rng, q - 1);
+    if (rec_mask) memcpy(rec_mask, out, sizeof(uint64_t) * (size_t)k * N);
     for (int r = 0; r < k; r++)
         for (int j = 0; j < N; j++)
             b[j] = addmod(b[j], nq_mulmod(&c->plan.br, out[(size_t)r * N + j], c->rlwe_s_ntt[(size_t)r * N + j]), q);
@@ -316,14 +327,16 @@ static void enc_trlwe_ntt(po_ctx* c, uint64_t* out, const int64_t* mu, int64_t* 
 
 /* symEncTlwe (yatfhe/src/tlwe.cpp:21-31) with addTUniformNoise (numeric.cpp:57-60) and
  * addTorus / longModP mod LWE_Q = 2^32 (numeric.h:53-66,163-177). */
-static void enc_tlwe(po_ctx* c, int32_t* out, int64_t message, const int32_t* s, int n) {
+static void enc_tlwe(po_ctx* c, int32_t* out, int64_t message, const int32_t* s, int n, int32_t* rec_noise) {
     int64_t tmp = 0;
     for (int i = 0; i < n; i++) {
         int64_t a = rng_uniform_i64(&c->rng, -((int64_t)1 << 31), ((int64_t)1 << 31) - 1);
         out[i] = (int32_t)a;
         if (s[i]) tmp += a * s[i];
     }
-    int64_t muE = sext(message + rng_tuniform(&c->rng, c->p.lwe_noise_b), 32);
+    const int64_t e = rng_tuniform(&c->rng, c->p.lwe_noise_b);
+    if (rec_noise) *rec_noise = (int32_t)e;
+    int64_t muE = sext(message + e, 32);
     out[n] = (int32_t)sext(muE + sext(tmp, 32), 32);
 }
 
@@ -356,7 +369,9 @@ static void keygen_ksk(po_ctx* c) {
         for (int j = 0; j < t; j++) {
             const int sh = 32 - (j + 1) * c->p.ks_radix_bits;
             const int64_t m = sext((int64_t)c->rlwe_s[i] << sh, c->T);
-            enc_tlwe(c, c->ksk + ((size_t)i * t + j) * nb, m, c->lwe_s, n);
+            int32_t* row = c->ksk + ((size_t)i * t + j) * nb;
+            enc_tlwe(c, row, m, c->lwe_s, n, c->rec_ksk_noise ? c->rec_ksk_noise + (size_t)i * t + j : NULL);
+            if (c->rec_ksk_mask) memcpy(c->rec_ksk_mask + ((size_t)i * t + j) * n, row, sizeof(int32_t) * n);
         }
     }
 }
@@ -382,12 +397,16 @@ int po_keygen(po_ctx* c, uint64_t seed) {
             uint64_t* g = c->bsk + ((size_t)i * L + lvl) * lvlWords;
             muPoly[0] = sext(mu << (T - (lvl + 1) * c->p.radix_bits), T);
             ntt_from_torus(c, muNtt, muPoly);
+            const size_t rec = ((size_t)i * L + lvl) * k1;  /* recorded row index, row k = cPrime */
             /* cPrime[lvl] = RLWE(mu * g_lvl) */
-            enc_trlwe_ntt(c, g + (size_t)k * rowWords, muPoly, tmpT);
+            enc_trlwe_ntt(c, g + (size_t)k * rowWords, muPoly, tmpT,
+                          c->rec_bsk_noise ? c->rec_bsk_noise + (rec + k) * N : NULL,
+                          c->rec_bsk_mask ? c->rec_bsk_mask + (rec + k) * k * N : NULL);
             /* c[lvl][r] = RLWE(0) with a[r] += NTT(mu * g_lvl) */
             for (int r = 0; r < k; r++) {
                 uint64_t* row = g + (size_t)r * rowWords;
-                enc_trlwe_ntt(c, row, zeroPoly, tmpT);
+                enc_trlwe_ntt(c, row, zeroPoly, tmpT, c->rec_bsk_noise ? c->rec_bsk_noise + (rec + r) * N : NULL,
+                              c->rec_bsk_mask ? c->rec_bsk_mask + (rec + r) * k * N : NULL);
                 for (int j = 0; j < N; j++) row[(size_t)r * N + j] = addmod(row[(size_t)r * N + j], muNtt[j], c->q);
             }
         }
@@ -403,7 +422,7 @@ int po_keygen(po_ctx* c, uint64_t seed) {
 int po_encrypt(po_ctx* c, const int64_t* mu, int count, int32_t* out) {
     if (!c->have_rng) return fail(c, "po_encrypt: no RNG stream (run po_keygen first)");
     const int n = c->p.n;
-    for (int i = 0; i < count; i++) enc_tlwe(c, out + (size_t)i * (n + 1), mu[i], c->lwe_s, n);
+    for (int i = 0; i < count; i++) enc_tlwe(c, out + (size_t)i * (n + 1), mu[i], c->lwe_s, n, NULL);
     return 0;
 }
 
@@ -1083,4 +1102,31 @@ int po_load_wwl24_file(po_ctx* c, const char* path) {
     if (!e) e |= rd_expect_i32(f, n);
     fclose(f);
     return e ? fail(c, "po_load_wwl24_file: %s is not a WWL+24 key for these parameters", path) : 0;
+}
+
+/* ------------------------------------------------------------------ keygen samples */
+
+/*
+ * po_keygen with its random samples written out, in the layout of the GPU's key generation
+ * entry point: lwe_s [n], rlwe_s [kN] (the secrets), bsk_noise [n][L][k+1][N] (the
+ * TUniform noise of each RLWE sample's b, row k = cPrime), bsk_mask [n][L][k+1][k][N] (its
+ * uniform NTT-domain masks), ksk_mask [kN][t][n] and ksk_noise [kN][t] (the key-switching
+ * samples' masks and noise).  The keys themselves are left in the context as po_keygen
+ * leaves them.
+ */
+int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s, int32_t* bsk_noise,
+                      uint64_t* bsk_mask, int32_t* ksk_mask, int32_t* ksk_noise) {
+    c->rec_bsk_noise = bsk_noise;
+    c->rec_bsk_mask = bsk_mask;
+    c->rec_ksk_mask = ksk_mask;
+    c->rec_ksk_noise = ksk_noise;
+    const int rc = po_keygen(c, seed);
+    c->rec_bsk_noise = NULL;
+    c->rec_bsk_mask = NULL;
+    c->rec_ksk_mask = NULL;
+    c->rec_ksk_noise = NULL;
+    if (rc) return rc;
+    memcpy(lwe_s, c->lwe_s, sizeof(int32_t) * c->p.n);
+    memcpy(rlwe_s, c->rlwe_s, sizeof(int32_t) * (size_t)c->p.k * c->p.N);
+    return 0;
 }

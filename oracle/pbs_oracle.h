@@ -67,6 +67,10 @@ int po_wwl24_expand(po_ctx* c);
 int po_save_wwl24_file(po_ctx* c, const char* path);
 int po_load_wwl24_file(po_ctx* c, const char* path);
 
+/* po_keygen that also writes out its random samples (see pbs_oracle.c). */
+int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s, int32_t* bsk_noise,
+                      uint64_t* bsk_mask, int32_t* ksk_mask, int32_t* ksk_noise);
+
 #ifdef __cplusplus
 }
 #endif

@@ -224,3 +224,21 @@ def test_decomposition_properties():
         dn = ora.decompose(-x, L)
         same = np.all(dn == -d, axis=0)
         assert same.mean() > 0.99
+
+
+def test_keygen_samples_reproduce_keygen():
+    """keygen_samples draws the same stream as keygen and reports its samples consistently:
+    the KSK masks and the secrets are the ones inside the keys."""
+    p = small(T32_N1024, 4)
+    a, b = Restatement(p), Restatement(p)
+    a.keygen(17)
+    d = b.keygen_samples(17)
+    np.testing.assert_array_equal(a.bsk_ntt(), b.bsk_ntt())
+    np.testing.assert_array_equal(a.ksk(), b.ksk())
+    s, z = a.keys()
+    np.testing.assert_array_equal(d["lwe_s"], s)
+    np.testing.assert_array_equal(d["rlwe_s"], z.reshape(-1))
+    ksk = a.ksk().reshape(p.k * p.N, p.ks_level, p.n + 1)
+    np.testing.assert_array_equal(d["ksk_mask"], ksk[:, :, :p.n])
+    assert np.abs(d["bsk_noise"]).max() < 1 << (p.rlwe_noise_b + 1)
+    assert (d["bsk_mask"] < p.q_ntt).all()

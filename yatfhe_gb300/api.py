@@ -242,6 +242,34 @@ def blind_rotate_mp21_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: i
     return acc
 
 
+def keygen_from_samples(ctx: Context, samples: dict, return_keys: bool = False):
+    """Key generation on the GPU from caller-drawn random samples (yg_keygen_from_samples):
+    `samples` holds lwe_s [n], rlwe_s [kN], bsk_noise [n][l][k+1][N], bsk_mask
+    [n][l][k+1][k][N], ksk_mask [kN][t][n], ksk_noise [kN][t].  Returns the device key, and
+    with return_keys also the NTT-domain BSK words and the KSK."""
+    p = ctx.params
+    k1, kN = p.k + 1, p.k * p.N
+    shapes = {"lwe_s": (p.n,), "rlwe_s": (kN,), "bsk_noise": (p.n, p.l_approx, k1, p.N),
+              "bsk_mask": (p.n, p.l_approx, k1, p.k, p.N), "ksk_mask": (kN, p.ks_level, p.n),
+              "ksk_noise": (kN, p.ks_level)}
+    arr = {}
+    for name, shape in shapes.items():
+        dt = np.uint64 if name == "bsk_mask" else np.int32
+        x = np.ascontiguousarray(samples[name], dt)
+        if x.size != int(np.prod(shape)):
+            raise ValueError(f"{name}: expected {shape}, got {x.shape}")
+        arr[name] = x
+    words = np.zeros(p.bsk_ntt_words, np.uint64) if return_keys else None
+    ksk = np.zeros(p.ksk_words, np.int32) if return_keys else None
+    h = ctypes.c_void_p()
+    ptr = lambda x: ctypes.c_void_p(x.ctypes.data) if x is not None else None  # noqa: E731
+    _lib.check(_lib.lib().yg_keygen_from_samples(ctx.handle, ptr(arr["lwe_s"]), ptr(arr["rlwe_s"]),
+                                                 ptr(arr["bsk_noise"]), ptr(arr["bsk_mask"]), ptr(arr["ksk_mask"]),
+                                                 ptr(arr["ksk_noise"]), ptr(words), ptr(ksk), ctypes.byref(h)))
+    key = BootstrapKey(ctx, h)
+    return (key, words, ksk) if return_keys else key
+
+
 def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
     """blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412): the blind rotation on a
     WWL+24 key, whose GINX rows were derived on the GPU at upload."""

@@ -345,6 +345,86 @@ void upload_wwl24(yg_ctx* c, yg_key* key, const u64* cprime, const u64* s2, int 
     convert_bsk_words(c, key, d_out, scratch, tw);
 }
 
+// Key generation arithmetic on the GPU from caller-drawn samples (see yg_keygen_from_samples):
+// the NTT of the RLWE secret mod q (host, exact), the BSK samples (keygen_bsk_kernel), the
+// usual conversion of the NTT-domain words, and the KSK samples (keygen_ksk_kernel).
+void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int32_t* rlwe_s, const int32_t* bsk_noise,
+                         const u64* bsk_mask, const int32_t* ksk_mask, const int32_t* ksk_noise, u64* h_words,
+                         int32_t* h_ksk) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->p.l_approx, t = c->p.ks_level, kN = k * N;
+    for (int i = 0; i < n; i++)
+        if (lwe_s[i] != 0 && lwe_s[i] != 1) throw std::invalid_argument("LWE secret must be binary");
+    for (int i = 0; i < kN; i++)
+        if (rlwe_s[i] != 0 && rlwe_s[i] != 1) throw std::invalid_argument("RLWE secret must be binary");
+    const QTables& qt = *c->qtab;
+    const u64 q = c->q;
+    // NTT(s) mod q, the forward transform the kernels use (Cooley-Tukey, psi^brv twiddles)
+    std::vector<u64> s_ntt((size_t)kN), s_ntt_p((size_t)kN);
+    for (int r = 0; r < k; r++) {
+        u64* a = s_ntt.data() + (size_t)r * N;
+        for (int j = 0; j < N; j++) a[j] = (u64)rlwe_s[(size_t)r * N + j];
+        for (int m = 1, span = N / 2; m < N; m <<= 1, span >>= 1)
+            for (int g = 0; g < m; g++)
+                for (int j = 2 * g * span; j < 2 * g * span + span; j++) {
+                    const u64 u = a[j], v = mulmod(a[j + span], qt.wf[m + g], q);
+                    a[j] = u + v >= q ? u + v - q : u + v;
+                    a[j + span] = u >= v ? u - v : u + q - v;
+                }
+        for (int j = 0; j < N; j++) s_ntt_p[(size_t)r * N + j] = (u64)(((u128)a[j] << 64) / q);
+    }
+    const size_t samples = (size_t)n * L * (k + 1), words = samples * (k + 1) * N;
+    const size_t ksk_samples = (size_t)kN * t;
+    DeviceScratch scratch;
+    DeviceQTables tw(scratch, qt);
+    int32_t* d_lwe_s = scratch.alloc<int32_t>(n, "cudaMalloc keygen");
+    int32_t* d_rlwe_s = scratch.alloc<int32_t>(kN, "cudaMalloc keygen");
+    int32_t* d_noise = scratch.alloc<int32_t>(samples * N, "cudaMalloc keygen noise");
+    u64* d_mask = scratch.alloc<u64>(samples * k * N, "cudaMalloc keygen masks");
+    u64* d_s = scratch.alloc<u64>(2 * (size_t)kN, "cudaMalloc keygen secret");
+    u64* d_words = scratch.alloc<u64>(words, "cudaMalloc keygen words");
+    int32_t* d_kmask = scratch.alloc<int32_t>(ksk_samples * n, "cudaMalloc keygen KSK masks");
+    int32_t* d_knoise = scratch.alloc<int32_t>(ksk_samples, "cudaMalloc keygen KSK noise");
+    int* d_bad = scratch.alloc<int>(1, "cudaMalloc flag");
+    ck(cudaMemcpy(d_lwe_s, lwe_s, n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
+    ck(cudaMemcpy(d_rlwe_s, rlwe_s, kN * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
+    ck(cudaMemcpy(d_noise, bsk_noise, samples * N * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen noise");
+    ck(cudaMemcpy(d_mask, bsk_mask, samples * k * N * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen masks");
+    ck(cudaMemcpy(d_s, s_ntt.data(), kN * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen secret");
+    ck(cudaMemcpy(d_s + kN, s_ntt_p.data(), kN * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen secret");
+    ck(cudaMemcpy(d_kmask, ksk_mask, ksk_samples * n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK masks");
+    ck(cudaMemcpy(d_knoise, ksk_noise, ksk_samples * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK noise");
+    ck(cudaMemset(d_bad, 0, sizeof(int)), "clear flag");
+    yg::KeygenBskArgs a{};
+    a.lwe_s = d_lwe_s;
+    a.noise = d_noise;
+    a.mask = d_mask;
+    a.s_ntt = d_s;
+    a.s_ntt_p = d_s + kN;
+    a.wf = tw.wf;
+    a.wfp = tw.wfp;
+    a.words = d_words;
+    a.q = q;
+    a.n = n;
+    a.N = N;
+    a.k = k;
+    a.L = L;
+    a.radix_bits = c->p.radix_bits;
+    a.torus_bits = c->p.torus_bits;
+    a.bad = d_bad;
+    yg::check_launch(yg::launch_keygen_bsk(a, nullptr), "keygen launch");
+    int bad = 0;
+    ck(cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost), "keygen");
+    if (bad) throw std::invalid_argument("BSK mask word not reduced mod q");
+    if (h_words) ck(cudaMemcpy(h_words, d_words, words * sizeof(u64), cudaMemcpyDeviceToHost), "download BSK words");
+    convert_bsk_words(c, key, d_words, scratch, tw);
+    key->ksk_bytes = ksk_samples * (n + 1) * sizeof(int32_t);
+    ck(cudaMalloc(&key->d_ksk, key->ksk_bytes), "cudaMalloc ksk");
+    yg::KeygenKskArgs kk{d_lwe_s, d_rlwe_s, d_kmask, d_knoise, key->d_ksk, n, kN, t, c->p.ks_radix_bits};
+    yg::check_launch(yg::launch_keygen_ksk(kk, nullptr), "keygen KSK launch");
+    if (h_ksk) ck(cudaMemcpy(h_ksk, key->d_ksk, key->ksk_bytes, cudaMemcpyDeviceToHost), "download KSK");
+    ck(cudaDeviceSynchronize(), "keygen");
+}
+
 // deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)
 // (yatfhe/src/ya_serializer.cpp:21-30,87-98,193-218,287-303): native-endian PODs.
 struct Reader {
@@ -585,6 +665,31 @@ int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out) {
         std::vector<u64> cprime, s2;
         const int levels = read_wwl24_file(ctx->p, path, cprime, s2);
         return yg_key_upload_wwl24_ntt(ctx, cprime.data(), s2.data(), levels, out);
+    });
+}
+
+int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h_rlwe_s, const int32_t* h_bsk_noise,
+                           const uint64_t* h_bsk_mask, const int32_t* h_ksk_mask, const int32_t* h_ksk_noise,
+                           uint64_t* h_bsk_words, int32_t* h_ksk, yg_key** out) {
+    if (!ctx || !h_lwe_s || !h_rlwe_s || !h_bsk_noise || !h_bsk_mask || !h_ksk_mask || !h_ksk_noise || !out)
+        return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            keygen_from_samples(ctx, k.get(), h_lwe_s, h_rlwe_s, h_bsk_noise, h_bsk_mask, h_ksk_mask, h_ksk_noise,
+                                h_bsk_words, h_ksk);
+        } catch (...) {
+            if (k->d_bsk) cudaFree(k->d_bsk);
+            if (k->d_ksk) cudaFree(k->d_ksk);
+            k->d_bsk = nullptr;
+            k->d_ksk = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
     });
 }
 

@@ -273,6 +273,74 @@ __global__ void __launch_bounds__(1024) wwl24_expand_kernel(const WwlExpandArgs 
     }
 }
 
+// encryptTrgswMPNtt's samples (yatfhe/src/trgsw.cpp:36-51 with symEncTrlweNttSimple,
+// yatfhe/src/trlwe.cpp:24-46,58-60), one per CTA: b = NTT(sext(mu + e)) + sum_r a_r . NTT(s_r)
+// mod q with the mask a given in the NTT domain; the cPrime row (row k) carries
+// mu = s_i 2^(T - (lvl+1) radix) at coefficient 0, row r < k carries it on its mask a_r as
+// NTT(mu) (a constant polynomial: mu in every slot).
+template <int T>
+__global__ void __launch_bounds__(1024) keygen_bsk_kernel(const KeygenBskArgs a) {
+    extern __shared__ uint64_t sw[];  // [N]
+    const int N = a.N, H = N / 2, k = a.k, t = threadIdx.x;
+    const int row = blockIdx.x % (k + 1);
+    const int lvl = (blockIdx.x / (k + 1)) % a.L;
+    const int i = blockIdx.x / ((k + 1) * a.L);
+    const uint64_t q = a.q;
+    const int32_t* e = a.noise + (size_t)blockIdx.x * N;
+    const uint64_t* msk = a.mask + (size_t)blockIdx.x * k * N;
+    uint64_t* out = a.words + (size_t)blockIdx.x * (k + 1) * N;
+    const int64_t mu = sext<T>((int64_t)a.lwe_s[i] << (T - (lvl + 1) * a.radix_bits));
+    const uint64_t mu_q = mu < 0 ? (uint64_t)(mu + (int64_t)q) : (uint64_t)mu;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j = t + h * H;
+        const int64_t v = sext<T>((row == k && j == 0 ? mu : 0) + (int64_t)e[j]);
+        sw[j] = v < 0 ? (uint64_t)(v + (int64_t)q) : (uint64_t)v;
+    }
+    __syncthreads();
+    q_forward_in_smem(sw, N, a.wf, a.wfp, q);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j = t + h * H;
+        uint64_t b = sw[j];
+        for (int r = 0; r < k; ++r) {
+            uint64_t m = msk[(size_t)r * N + j];
+            if (m >= q) {
+                atomicExch(a.bad, 1);
+                m = 0;
+            }
+            const uint64_t prod = mulshoup64(m, a.s_ntt[(size_t)r * N + j], a.s_ntt_p[(size_t)r * N + j], q);
+            b = b + prod >= q ? b + prod - q : b + prod;
+            if (r == row) m = m + mu_q >= q ? m + mu_q - q : m + mu_q;  // a_r += NTT(mu) on row r
+            out[(size_t)r * N + j] = m;
+        }
+        out[(size_t)k * N + j] = b;
+    }
+}
+
+// genTlweKeySwitchingKey (yatfhe/src/keyswitching.cpp:19-29), one warp per sample:
+// ksk[i][j] = (a, sum a s + s'_i 2^(32 - (j+1) ksRadix) + e) mod 2^32 (symEncTlwe,
+// yatfhe/src/tlwe.cpp:21-31, whose sign extensions are the identity mod 2^32).
+__global__ void __launch_bounds__(256) keygen_ksk_kernel(const KeygenKskArgs a) {
+    const int sample = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (sample >= a.kN * a.t) return;  // whole warps leave together
+    const int i = sample / a.t, j = sample - i * a.t;
+    const int32_t* m = a.mask + (size_t)sample * a.n;
+    int32_t* dst = a.ksk + (size_t)sample * (a.n + 1);
+    uint32_t sum = 0;
+    for (int x = lane; x < a.n; x += 32) {
+        const int32_t v = m[x];
+        dst[x] = v;
+        if (a.lwe_s[x]) sum += (uint32_t)v;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    if (lane == 0) {
+        const uint32_t msg = (uint32_t)a.rlwe_s[i] << (32 - (j + 1) * a.ks_radix_bits);
+        dst[a.n] = (int32_t)(sum + msg + (uint32_t)a.noise[sample]);
+    }
+}
+
 // Teams of one ciphertext slice: one per RNS channel (kLayoutChannel), or one per channel
 // and accumulator row (kLayoutChannelRow).
 template <int SPLIT>
@@ -1074,6 +1142,28 @@ int launch_wwl24_expand(const WwlExpandArgs& a, void* stream) {
         wwl24_expand_kernel<56><<<a.n * a.L, a.N / 2, smem, (cudaStream_t)stream>>>(a);
     else
         return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_keygen_bsk(const KeygenBskArgs& a, void* stream) {
+    if (a.n <= 0) return 0;
+    if ((a.N != 1024 && a.N != 2048) || a.k != 1 || a.L < 1) return -1;
+    const int blocks = a.n * a.L * (a.k + 1);
+    const size_t smem = (size_t)a.N * sizeof(uint64_t);
+    if (a.torus_bits == 32)
+        keygen_bsk_kernel<32><<<blocks, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else if (a.torus_bits == 56)
+        keygen_bsk_kernel<56><<<blocks, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_keygen_ksk(const KeygenKskArgs& a, void* stream) {
+    const long samples = (long)a.kN * a.t;
+    if (samples <= 0) return 0;
+    if (a.ks_radix_bits < 1 || a.t * a.ks_radix_bits > 32) return -1;
+    keygen_ksk_kernel<<<(unsigned)((samples + 7) / 8), 256, 0, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -98,6 +98,32 @@ struct WwlExpandArgs {
     int* bad;                // set to 1 when a word is not reduced mod q
 };
 
+// Key generation from caller-drawn samples: the arithmetic of encryptTrgswMPNtt
+// (yatfhe/src/trgsw.cpp:36-51, per key index of genBootstrappingKeyMP) and of
+// genTlweKeySwitchingKey (yatfhe/src/keyswitching.cpp:19-29).  One CTA per BSK row sample
+// (key index, level, row; row k is cPrime), N/2 threads; one warp per KSK sample.
+struct KeygenBskArgs {
+    const int32_t* lwe_s;     // [n] 0/1
+    const int32_t* noise;     // [n][L][k+1][N] TUniform noise of each sample's b (torus)
+    const uint64_t* mask;     // [n][L][k+1][k][N] uniform NTT-domain masks (< q)
+    const uint64_t* s_ntt;    // [k][N] NTT of the RLWE secret mod q, and Shoup companions
+    const uint64_t* s_ntt_p;
+    const uint64_t* wf;       // [N] psi^brv(k) mod q, and Shoup companions
+    const uint64_t* wfp;
+    uint64_t* words;          // [n][L][k+1][k+1][N] NTT-domain BSK words
+    uint64_t q;
+    int n, N, k, L, radix_bits, torus_bits;
+    int* bad;                 // set to 1 when a mask word is not reduced mod q
+};
+struct KeygenKskArgs {
+    const int32_t* lwe_s;     // [n] 0/1
+    const int32_t* rlwe_s;    // [kN] 0/1
+    const int32_t* mask;      // [kN][t][n]
+    const int32_t* noise;     // [kN][t]
+    int32_t* ksk;             // [kN][t][n+1]
+    int n, kN, t, ks_radix_bits;
+};
+
 // u32 words of one (step, level, row, channel) block of the device key: 2 output polys.
 __host__ __device__ inline size_t key_block_words(int N) { return 2 * (size_t)N; }
 __host__ __device__ inline size_t key_words(int n, int L, int N) {
@@ -150,6 +176,8 @@ int set_twiddle_heads(int logN, int ps, const uint2* heads);
 int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream);
 int launch_key_intt(const KeyInttArgs& a, void* stream);
 int launch_wwl24_expand(const WwlExpandArgs& a, void* stream);
+int launch_keygen_bsk(const KeygenBskArgs& a, void* stream);
+int launch_keygen_ksk(const KeygenKskArgs& a, void* stream);
 int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream);
 // Resident blind-rotation CTAs per SM for these parameters and ciphertexts per CTA
 // (occupancy calculator; 0 if a CTA does not fit), kNoVariant if no such kernel is compiled,
