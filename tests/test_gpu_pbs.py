@@ -188,3 +188,21 @@ def test_key_words_must_be_reduced(built_lib):
         api.BootstrapKey.from_ntt_words(ctx, words)
     words[123] = p.q_ntt - 1
     api.BootstrapKey.from_ntt_words(ctx, words).close()
+
+
+@pytest.mark.parametrize("count", [100, 16384])
+def test_pbs_host_buffers(count, built_lib):
+    """yg_pbs_host (host buffers in and out; from 16,384 ciphertexts on in four chunks on two
+    streams) equals the device-buffer bootstrap and the oracle."""
+    from yatfhe_gb300 import api
+
+    p = small(T32_N1024, 8)
+    ora, ctx, key = _setup(p, 0x5EED0009, built_lib)
+    rng = np.random.default_rng(count)
+    lwe = rng.integers(-(1 << 31), 1 << 31, size=(count, p.n + 1), dtype=np.int64).astype(np.int32)
+    lut = lutmod.sign_lut(p.N, 32)
+    host = api.functional_bootstrapping_mp_ntt_host(ctx, key, lwe, lut)
+    dev = _pbs_gpu(ctx, key, lwe, lut)
+    np.testing.assert_array_equal(host, dev)
+    pick = rng.choice(count, 6, replace=False)
+    np.testing.assert_array_equal(host[pick], ora.pbs(lwe[pick], lut))

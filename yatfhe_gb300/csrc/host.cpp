@@ -558,6 +558,9 @@ namespace {
 using yg::br_args;
 using yg::check_key;
 
+// yg_pbs_host pipelines batches of at least 4 x kPipelineChunk ciphertexts in 4 chunks.
+constexpr int kPipelineChunk = 4096;
+
 int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
            cudaStream_t s) {
     const int N = c->p.N, kN = c->p.k * N;
@@ -608,6 +611,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
 void yg_ctx_destroy(yg_ctx* ctx) {
     if (!ctx) return;
     if (ctx->d_tw) cudaFree(ctx->d_tw);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     delete ctx;
 }
 
@@ -736,24 +740,54 @@ int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_
     return guarded([&] {
         DeviceGuard g(ctx->device);
         cudaStream_t s = (cudaStream_t)stream;
-        const size_t lwe = (size_t)count * (ctx->p.n + 1) * sizeof(int32_t);
+        const size_t n1 = (size_t)ctx->p.n + 1;
+        const size_t lwe = (size_t)count * n1 * sizeof(int32_t);
         const size_t lut = (size_t)ctx->p.N * sizeof(int64_t);
+        // large batches run as chunks alternating between the caller's stream and a side
+        // stream, so one chunk's copies overlap another chunk's kernels
+        const int chunks = count >= 4 * kPipelineChunk ? 4 : 1;
+        cudaStream_t side = s;
+        if (chunks > 1) {
+            std::lock_guard<std::mutex> lk(ctx->side_mu);
+            if (!ctx->side) ck(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking), "side stream");
+            side = ctx->side;
+        }
         char* d = nullptr;
         ck(cudaMallocAsync(&d, 2 * lwe + lut, s), "cudaMallocAsync io");
         int32_t* d_in = reinterpret_cast<int32_t*>(d);
         int32_t* d_out = reinterpret_cast<int32_t*>(d + lwe);
         int64_t* d_lut = reinterpret_cast<int64_t*>(d + 2 * lwe);
+        cudaEvent_t ev[2] = {nullptr, nullptr};
         try {
-            ck(cudaMemcpyAsync(d_in, h_in, lwe, cudaMemcpyHostToDevice, s), "copy in");
             ck(cudaMemcpyAsync(d_lut, h_lut, lut, cudaMemcpyHostToDevice, s), "copy lut");
-            do_pbs(ctx, key, d_in, d_out, count, d_lut, s);
-            ck(cudaMemcpyAsync(h_out, d_out, lwe, cudaMemcpyDeviceToHost, s), "copy out");
+            if (chunks > 1) {
+                for (auto& e : ev) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+                ck(cudaEventRecord(ev[0], s), "event");  // buffers allocated, LUT copied
+                ck(cudaStreamWaitEvent(side, ev[0], 0), "wait");
+            }
+            for (int c = 0; c < chunks; c++) {
+                const int begin = (int)((long long)count * c / chunks), end = (int)((long long)count * (c + 1) / chunks);
+                cudaStream_t cs = c % 2 ? side : s;
+                const size_t off = (size_t)begin * n1, bytes = (size_t)(end - begin) * n1 * sizeof(int32_t);
+                ck(cudaMemcpyAsync(d_in + off, h_in + off, bytes, cudaMemcpyHostToDevice, cs), "copy in");
+                do_pbs(ctx, key, d_in + off, d_out + off, end - begin, d_lut, cs);
+                ck(cudaMemcpyAsync(h_out + off, d_out + off, bytes, cudaMemcpyDeviceToHost, cs), "copy out");
+            }
+            if (chunks > 1) {
+                ck(cudaEventRecord(ev[1], side), "event");
+                ck(cudaStreamWaitEvent(s, ev[1], 0), "wait");  // the buffers are freed after both
+            }
         } catch (...) {
+            if (chunks > 1) cudaStreamSynchronize(side);
             cudaFreeAsync(d, s);
+            for (auto& e : ev)
+                if (e) cudaEventDestroy(e);
             throw;
         }
         ck(cudaFreeAsync(d, s), "cudaFreeAsync io");
         ck(cudaStreamSynchronize(s), "bootstrap");
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
         return YG_OK;
     });
 }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -86,6 +87,8 @@ struct yg_ctx {
     int layout = 0;        // YG_LAYOUT_* of the blind rotation (yg_ctx_set_launch)
     int per_cta = 1;       // ciphertexts per blind-rotation CTA (yg_ctx_set_launch)
     int ctas_per_sm = 0;   // persistent CTAs per SM, 0 = one CTA per ciphertext group
+    cudaStream_t side = nullptr;  // second stream of the pipelined host-buffer bootstrap
+    std::mutex side_mu;           // creates `side` once
 };
 
 struct yg_key {
