@@ -204,8 +204,10 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads):
-    """The CPU oracle (plain-C restatement of the reference path) on `sample` ciphertexts."""
+def run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads, latency=False):
+    """The CPU oracle (plain-C restatement of the reference path) on `sample` ciphertexts:
+    (outputs, bootstraps/s, seconds, and with `latency` the milliseconds of one bootstrap on
+    one thread, else None)."""
     from oracle.oracle import Restatement
 
     ora = Restatement(p)
@@ -214,7 +216,12 @@ def run_cpu_baseline(p, bsk, ksk, lwe, lut, sample, threads):
     t0 = time.perf_counter()
     out = ora.pbs(lwe[:sample], lut, threads=threads)
     dt = time.perf_counter() - t0
-    return out, sample / dt, dt
+    lat = None
+    if latency:
+        t1 = time.perf_counter()
+        ora.pbs(lwe[:1], lut, threads=1)
+        lat = (time.perf_counter() - t1) * 1e3
+    return out, sample / dt, dt, lat
 
 
 def params_config(p) -> dict:
@@ -776,7 +783,8 @@ def main():
     run.step()
     run.stream.synchronize()
     sample = args.cpu_sample or max(16, threads * 48)  # about 10 s of CPU work
-    cpu_out, cpu_bps, cpu_s = run_cpu_baseline(p, run.bsk, run.ksk, run.lwe, run.lut, sample, threads)
+    cpu_out, cpu_bps, cpu_s, cpu_lat = run_cpu_baseline(p, run.bsk, run.ksk, run.lwe, run.lut, sample, threads,
+                                                        latency=True)
     bit_exact = bool(np.array_equal(cpu_out, run.d_out[:sample].cpu().numpy()))
 
     if not args.no_extras:
@@ -805,7 +813,8 @@ def main():
         "roofline": roofline,
         "cpu_baseline": {"value": cpu_bps, "unit": "bootstraps/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} of the step's ciphertexts, plain-C restatement of "
-                                   f"functionalBootstrappingMPNtt on {threads} threads ({cpu_s:.1f} s)"},
+                                   f"functionalBootstrappingMPNtt on {threads} threads ({cpu_s:.1f} s)",
+                         "latency_ms_one_thread": cpu_lat},
         "bit_exact_vs_oracle_sample": bit_exact,
         "key_upload_s": run.key_upload_s,
         "launch_shape": run.tuning,
