@@ -209,9 +209,11 @@ int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm);
  * registered tenants are kept in pinned host memory in the device layout; at most
  * floor(key_budget_bytes / per-tenant key bytes) of them are resident in HBM at a time (an
  * LRU over tenants with no batch in flight), refilled on a miss by an asynchronous copy on
- * a side stream.  One worker thread admits pending requests into batches of up to
- * max_batch ciphertexts while up to max_inflight earlier batches run; a batch bootstraps
- * every request's ciphertexts with its tenant's key and LUT.  Request buffers should be
+ * a side stream.  One worker thread admits pending requests, in arrival order, into
+ * batches of up to max_batch ciphertexts while up to max_inflight earlier batches run (a
+ * request larger than what is left of a batch is split across it and the next; it
+ * completes with its last part); a batch bootstraps every request's ciphertexts with its
+ * tenant's key and LUT.  Request buffers should be
  * pinned host memory (pageable buffers serialise the copies). */
 typedef struct yg_server yg_server;
 typedef struct yg_server_config {

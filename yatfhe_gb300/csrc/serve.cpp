@@ -11,10 +11,12 @@
 // GPU design.  One worker thread owns the device.  Tenant keys are kept, already in the
 // device layout, in pinned host memory; HBM holds `slots` of them (budget / key bytes),
 // refilled on a miss by cudaMemcpyAsync on a copy stream, with an event the batch's stream
-// waits on.  The worker admits pending requests into a batch (up to max_batch ciphertexts)
-// as long as their keys are resident or can be brought in (an LRU slot whose tenant has no
-// batch in flight), groups the batch by tenant, and launches the multi-key blind rotation
-// and key switch.  Up to max_inflight batches are on the GPU at once, each on its own
+// waits on.  The worker admits pending requests into a batch (up to max_batch ciphertexts),
+// in arrival order, as long as their keys are resident or can be brought in (an LRU slot
+// whose tenant has no batch in flight); a request larger than what is left of the batch is
+// split, its first part filling the batch and the rest opening the next one, so batches
+// leave the worker full whenever enough work is queued.  The batch is grouped by tenant and
+// the multi-key blind rotation and key switch are launched.  Up to max_inflight batches are on the GPU at once, each on its own
 // stream, so requests that arrive while one runs are admitted into the next (continuous
 // batching) and the next batch fills the SMs the previous one's last wave leaves idle.
 // Batch completion is signalled by a host callback on the batch's stream.
@@ -54,8 +56,19 @@ struct Request {
     const int32_t* h_in = nullptr;
     int32_t* h_out = nullptr;
     double t_submit = 0, t_start = 0, t_done = 0;
+    int admitted = 0;    // ciphertexts placed in batches so far
+    int parts_open = 0;  // placed parts whose batch has not retired
     std::atomic<bool> done{false};
 };
+
+// A contiguous part of a request inside one batch.
+struct Part {
+    Request* r;
+    int offset, count;
+};
+
+// Smallest part a request is split into to fill a batch (smaller rests close the batch).
+constexpr int kMinPart = 16;
 
 struct Tenant {
     int id = 0;
@@ -80,8 +93,9 @@ struct Batch {
     int32_t* h_key_of = nullptr;   // pinned staging
     int32_t* h_lut_of = nullptr;
     yg::KsTile* h_tiles = nullptr;
-    std::vector<Request*> reqs;
+    std::vector<Part> parts;
     std::vector<Tenant*> tenants;
+    double t_finish = 0;  // stamped by the completion callback
     std::atomic<bool> finished{false};
     bool busy = false;
     struct yg_server* server = nullptr;
@@ -127,8 +141,7 @@ namespace {
 // worker's timed wait picks the flag up.
 void CUDART_CB batch_done_cb(void* p) {
     Batch* b = static_cast<Batch*>(p);
-    const double t = now_s();
-    for (Request* r : b->reqs) r->t_done = t;
+    b->t_finish = now_s();
     b->finished.store(true);
     b->server->cv.notify_all();
 }
@@ -152,13 +165,17 @@ void retire(yg_server* s) {
     for (auto& bp : s->batches) {
         Batch* b = bp.get();
         if (!b->busy || !b->finished.load()) continue;
-        for (Request* r : b->reqs) {
-            r->done.store(true);
-            s->requests_done++;
-            s->ciphertexts_done += r->count;
+        for (const Part& part : b->parts) {
+            Request* r = part.r;
+            r->t_done = std::max(r->t_done, b->t_finish);
+            s->ciphertexts_done += part.count;
+            if (--r->parts_open == 0 && r->admitted == r->count) {
+                r->done.store(true);
+                s->requests_done++;
+            }
         }
         for (Tenant* t : b->tenants) t->pins--;
-        b->reqs.clear();
+        b->parts.clear();
         b->tenants.clear();
         b->busy = false;
         b->finished.store(false);
@@ -188,11 +205,13 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     const yg_params& p = s->ctx->p;
     const int n1 = p.n + 1, kN = p.k * p.N;
     int total = 0;
-    std::vector<Request*> take;
+    std::vector<Part> take;
     std::vector<Tenant*> used;
     while (!pending.empty()) {
         Request* r = pending.front();
-        if (total + r->count > s->cfg.max_batch && total > 0) break;
+        const int rest = r->count - r->admitted, room = s->cfg.max_batch - total;
+        if (room <= 0 || (rest > room && room < kMinPart && total > 0)) break;
+        const int part = std::min(rest, room);
         Tenant* t = s->tenants[r->tenant].get();
         const bool in_batch = std::find(used.begin(), used.end(), t) != used.end();
         if (t->slot < 0) {
@@ -215,26 +234,30 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
             t->pins++;  // from here on the slot cannot be taken by another tenant
         }
         t->last_use = ++s->tick;
-        take.push_back(r);
-        total += r->count;
+        take.push_back(Part{r, r->admitted, part});
+        r->admitted += part;
+        r->parts_open++;
+        total += part;
+        if (r->admitted < r->count) break;  // the batch is full; the rest opens the next one
         pending.pop_front();
     }
     if (take.empty()) return false;
     // group by tenant so the key switch streams one KSK per run of ciphertexts
-    std::stable_sort(take.begin(), take.end(), [](const Request* a, const Request* b) { return a->tenant < b->tenant; });
+    std::stable_sort(take.begin(), take.end(), [](const Part& a, const Part& b) { return a.r->tenant < b.r->tenant; });
     const double t0 = now_s();
     int off = 0, ntiles = 0;
-    for (Request* r : take) {
+    for (const Part& part : take) {
+        Request* r = part.r;
         Tenant* t = s->tenants[r->tenant].get();
-        r->t_start = t0;
-        ck(cudaMemcpyAsync(b->d_in + (size_t)off * n1, r->h_in, (size_t)r->count * n1 * 4, cudaMemcpyHostToDevice,
-                           b->stream),
+        if (part.offset == 0) r->t_start = t0;
+        ck(cudaMemcpyAsync(b->d_in + (size_t)off * n1, r->h_in + (size_t)part.offset * n1, (size_t)part.count * n1 * 4,
+                           cudaMemcpyHostToDevice, b->stream),
            "copy in");
-        for (int c = 0; c < r->count; c++) {
+        for (int c = 0; c < part.count; c++) {
             b->h_key_of[off + c] = t->slot;
             b->h_lut_of[off + c] = t->index;
         }
-        off += r->count;
+        off += part.count;
     }
     for (int c = 0; c < total;) {
         int e = c + 1;
@@ -260,13 +283,13 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     yg::KsArgs k{b->d_big, nullptr, b->d_out, total, kN, p.n, p.ks_level, p.ks_radix_bits, b->d_tiles, ntiles};
     yg::check_launch(yg::launch_keyswitch(k, b->stream), "keyswitch launch");
     off = 0;
-    for (Request* r : take) {
-        ck(cudaMemcpyAsync(r->h_out, b->d_out + (size_t)off * n1, (size_t)r->count * n1 * 4, cudaMemcpyDeviceToHost,
-                           b->stream),
+    for (const Part& part : take) {
+        ck(cudaMemcpyAsync(part.r->h_out + (size_t)part.offset * n1, b->d_out + (size_t)off * n1,
+                           (size_t)part.count * n1 * 4, cudaMemcpyDeviceToHost, b->stream),
            "copy out");
-        off += r->count;
+        off += part.count;
     }
-    b->reqs = std::move(take);
+    b->parts = std::move(take);
     b->tenants = std::move(used);
     b->busy = true;
     b->finished.store(false);
