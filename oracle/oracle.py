@@ -188,6 +188,19 @@ class _Common:
         return out
 
 
+    # Lazy keys: cprime [n][l_approx][k+1][N] coefficient-domain torus values, s2 [l][k+1][N]
+    # NTT-domain words.
+    def keygen_lazy(self, seed: int) -> None:
+        self._call("keygen_lazy", ctypes.c_uint64(seed))
+
+    def lazy_words(self):
+        p = self.p
+        cprime = np.zeros((p.n, p.l_approx, p.k + 1, p.N), np.int64)
+        s2 = np.zeros((p.l, p.k + 1, p.N), np.uint64)
+        self._call("get_lazy" if self.prefix == "po_" else "export_lazy", _ptr(cprime, _i64p), _ptr(s2, _u64p))
+        return cprime, s2
+
+
 class Restatement(_Common):
     """The plain-C oracle for one parameter set."""
 
@@ -278,6 +291,33 @@ class Restatement(_Common):
         self._call("wwl24_expand")
         return self.pbs(lwe, v, threads)
 
+    def set_lazy(self, cprime, s2) -> None:
+        a = np.ascontiguousarray(cprime, np.int64)
+        b = np.ascontiguousarray(s2, np.uint64)
+        self._call("set_lazy", _ptr(a, _i64p), _ptr(b, _u64p))
+
+    def save_lazy_file(self, path) -> None:
+        self._call("save_lazy_file", str(path).encode())
+
+    def load_lazy_file(self, path) -> None:
+        self._call("load_lazy_file", str(path).encode())
+
+    def blind_rotate_lazy(self, lwe, v) -> np.ndarray:
+        """The accumulator [(k+1) N] after the lazy blind rotation of one ciphertext."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
+        self._call("blind_rotate_lazy", _ptr(lwe, _i32p), _ptr(v, _i64p), _ptr(acc, _i64p))
+        return acc
+
+    def pbs_lazy(self, lwe, v, threads: int = 1) -> np.ndarray:
+        """The bootstrap with blindRotateLazyPipeAltNtt on the lazy key."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        self._call("pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), threads)
+        return out
+
     @property
     def q(self) -> int:
         return int(Restatement._lib.po_qntt(self._h))
@@ -333,6 +373,22 @@ class Reference(_Common):
         out = np.zeros_like(lwe)
         acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
         self._call("pbs_wwl24", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
+        return (out, acc) if with_acc else out
+
+    def save_lazy_file(self, path) -> None:
+        self._call("save_lazy", str(path).encode())
+
+    def load_lazy_file(self, path) -> None:
+        self._call("load_lazy", str(path).encode())
+
+    def pbs_lazy(self, lwe, v, with_acc: bool = False):
+        """functionalBootstrappingMPNtt's composition around blindRotateLazyPipeAltNtt; with_acc
+        also returns ciphertext 0's accumulator after the blind rotation."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
+        self._call("pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
         return (out, acc) if with_acc else out
 
     def set_keys(self, lwe_s, rlwe_s) -> None:

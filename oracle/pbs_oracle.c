@@ -150,7 +150,8 @@ struct po_ctx {
     uint64_t* bsk;       /* [n][L][k+1][k+1][N] */
     int32_t* ksk;        /* [k*N][t][n+1] */
     uint64_t* wwl_cprime;/* WWL+24 key: [n][L][k+1][N] (allocated on first use) */
-    uint64_t* wwl_s2;    /* [l][k+1][N] */
+    uint64_t* wwl_s2;    /* [l][k+1][N] (also the s2 key of the lazy family) */
+    int64_t* lazy_cprime;/* lazy key: [n][L][k+1][N] coefficient-domain torus (allocated on first use) */
     /* when set, po_keygen also records its random samples here (po_keygen_samples) */
     int32_t* rec_bsk_noise;   /* [n][L][k+1][N] */
     uint64_t* rec_bsk_mask;   /* [n][L][k+1][k][N] */
@@ -212,6 +213,7 @@ void po_destroy(po_ctx* c) {
     free(c->ksk);
     free(c->wwl_cprime);
     free(c->wwl_s2);
+    free(c->lazy_cprime);
     free(c);
 }
 
@@ -806,8 +808,11 @@ typedef struct {
     const int64_t* v;
     int32_t* out;
     int begin, end;
+    int lazy;  /* 1: blindRotateLazyPipeAltNtt on the lazy key */
     int rc;
 } pbs_job;
+
+static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc);
 
 /* functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:71-80). */
 static void* pbs_worker(void* arg) {
@@ -822,20 +827,24 @@ static void* pbs_worker(void* arg) {
     if (ep_alloc(c, &s) || !scaled || !acc || !ext || !delta) {
         j->rc = -1;
     } else {
+        j->rc = 0;
         for (int i = j->begin; i < j->end; i++) {
             po_modswitch(c, j->in + (size_t)i * nb, scaled);
-            blind_rotate(c, &s, scaled, j->v, acc, NULL, 0, NULL);
+            if (j->lazy) {
+                if (blind_rotate_lazy(c, &s, scaled, j->v, acc)) { j->rc = -1; break; }
+            } else {
+                blind_rotate(c, &s, scaled, j->v, acc, NULL, 0, NULL);
+            }
             extract(c, acc, ext);
             keyswitch(c, ext, j->out + (size_t)i * nb, delta);
         }
-        j->rc = 0;
     }
     ep_free(&s);
     free(scaled); free(acc); free(ext); free(delta);
     return NULL;
 }
 
-int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+static int pbs_run(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads, int lazy) {
     if (threads < 1) threads = 1;
     if (threads > count) threads = count > 0 ? count : 1;
     pbs_job* jobs = (pbs_job*)calloc((size_t)threads, sizeof(pbs_job));
@@ -843,7 +852,7 @@ int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* o
     if (!jobs || !tids) { free(jobs); free(tids); return fail(c, "po_pbs: out of memory"); }
     int rc = 0;
     for (int t = 0; t < threads; t++) {
-        jobs[t].c = c; jobs[t].in = in; jobs[t].v = v; jobs[t].out = out;
+        jobs[t].c = c; jobs[t].in = in; jobs[t].v = v; jobs[t].out = out; jobs[t].lazy = lazy;
         jobs[t].begin = (int)((long long)count * t / threads);
         jobs[t].end = (int)((long long)count * (t + 1) / threads);
         if (threads == 1) pbs_worker(&jobs[t]);
@@ -856,6 +865,10 @@ int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* o
     free(jobs);
     free(tids);
     return rc ? fail(c, "po_pbs: worker failed") : 0;
+}
+
+int po_pbs(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+    return pbs_run(c, in, count, v, out, threads, 0);
 }
 
 /* ------------------------------------------------------------------ WWL+24 keys */
@@ -1129,4 +1142,275 @@ int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s,
     memcpy(lwe_s, c->lwe_s, sizeof(int32_t) * c->p.n);
     memcpy(rlwe_s, c->rlwe_s, sizeof(int32_t) * (size_t)c->p.k * c->p.N);
     return 0;
+}
+
+/* ------------------------------------------------------------------ lazy ("OURS") keys */
+
+/*
+ * The key of blindRotateLazyPipeAltNtt (BootstrappingKeyMPLazyPipeAlt,
+ * yatfhe/include/yatfhe/bootstrapping.h:284-307): per key index i and level lvl the half
+ * TRGSW row bskPrime[i].cPrime[lvl] = RLWE(s_i g_lvl) kept in the coefficient domain (TrgswMP,
+ * torus words), and the s2 key RLev(-s . s) in the NTT domain (held in c->wwl_s2).
+ * genBootstrappingKeyMPLazyPipeAlt (yatfhe/src/bootstrapping.cpp:322-339) encrypts each row
+ * with encryptTrgswMP (yatfhe/src/trgsw.cpp:18-34), whose symEncTrlweMultiSampleNtt
+ * (yatfhe/src/trlwe.cpp:56-60,103-106) draws the samples of the WWL+24 key generation in the
+ * same order and keeps the coefficient-domain sample (a, applyIntt(NTT(b) + NTT(a) . NTT(s)));
+ * the mask a equals applyIntt(NTT(a)).  So the lazy key of a seed is the WWL+24 key of that
+ * seed with its cPrime rows taken back to the torus.
+ */
+static int lazy_alloc(po_ctx* c) {
+    if (!c->lazy_cprime) c->lazy_cprime = (int64_t*)calloc(wwl_cprime_words(c), sizeof(int64_t));
+    if (!c->wwl_s2) c->wwl_s2 = (uint64_t*)calloc(wwl_s2_words(c), sizeof(uint64_t));
+    return c->lazy_cprime && c->wwl_s2 ? 0 : -1;
+}
+
+int po_keygen_lazy(po_ctx* c, uint64_t seed) {
+    if (po_keygen_wwl24(c, seed)) return -1;
+    const int N = c->p.N;
+    uint64_t* scratch = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    if (lazy_alloc(c) || !scratch) {
+        free(scratch);
+        return fail(c, "po_keygen_lazy: out of memory");
+    }
+    const size_t polys = wwl_cprime_words(c) / N;
+    for (size_t p = 0; p < polys; p++) {
+        memcpy(scratch, c->wwl_cprime + p * N, sizeof(uint64_t) * N);
+        intt_to_torus(c, c->lazy_cprime + p * N, scratch);
+    }
+    free(scratch);
+    return 0;
+}
+
+int po_get_lazy(po_ctx* c, int64_t* cprime, uint64_t* s2) {
+    if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_get_lazy: no lazy key");
+    memcpy(cprime, c->lazy_cprime, sizeof(int64_t) * wwl_cprime_words(c));
+    memcpy(s2, c->wwl_s2, sizeof(uint64_t) * wwl_s2_words(c));
+    return 0;
+}
+
+int po_set_lazy(po_ctx* c, const int64_t* cprime, const uint64_t* s2) {
+    if (lazy_alloc(c)) return fail(c, "po_set_lazy: out of memory");
+    const size_t words = wwl_cprime_words(c);
+    for (size_t j = 0; j < words; j++) c->lazy_cprime[j] = sext(cprime[j], c->T);
+    memcpy(c->wwl_s2, s2, sizeof(uint64_t) * wwl_s2_words(c));
+    return 0;
+}
+
+/* serialize(TorusPolynomial) (yatfhe/src/ya_serializer.cpp:33-36): [int N] + N Torus words
+ * (int32 for T = 32, int64 for T = 56). */
+static int wr_torus_poly(FILE* f, const int64_t* v, int N, int T) {
+    int32_t nn = N;
+    int e = wr(f, &nn, 4);
+    for (int j = 0; j < N && !e; j++) {
+        if (T == 32) {
+            int32_t w = (int32_t)v[j];
+            e |= wr(f, &w, 4);
+        } else {
+            e |= wr(f, &v[j], 8);
+        }
+    }
+    return e;
+}
+
+static int rd_torus_poly(FILE* f, int64_t* v, int N, int T) {
+    int e = rd_expect_i32(f, N);
+    for (int j = 0; j < N && !e; j++) {
+        if (T == 32) {
+            int32_t w;
+            e |= rd(f, &w, 4);
+            v[j] = w;
+        } else {
+            e |= rd(f, &v[j], 8);
+            v[j] = sext(v[j], T);
+        }
+    }
+    return e;
+}
+
+/*
+ * serializeBskLazyPipeAlt / deserializeBskLazyPipeAlt (yatfhe/src/ya_serializer.cpp:445-481):
+ * the TrlevDft s2 (`[int l][int l]` + l TrlweDft, :101-115), then n half TrgswMP
+ * (`[int L][int k][bool isHalf = 1][int L]` + L Trlwe, :131-146; a Trlwe is
+ * `[int k][int N]` + b + `[int k]` + a_0..a_{k-1}, each a TorusPolynomial, :57-63), then
+ * `[int level = L][int group = 1]`.
+ */
+int po_save_lazy_file(po_ctx* c, const char* path) {
+    if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_save_lazy_file: no lazy key");
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, "po_save_lazy_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, Ls = c->p.l, T = c->T;
+    const size_t row = (size_t)(k + 1) * N;
+    int32_t ls = Ls, l32 = L, k32 = k, n32 = N;
+    int e = wr(f, &ls, 4) | wr(f, &ls, 4);
+    for (int lv = 0; lv < Ls; lv++) e |= wr_trlwe_dft(f, c->wwl_s2 + (size_t)lv * row, k, N);
+    for (int i = 0; i < n && !e; i++) {
+        uint8_t half = 1;
+        e |= wr(f, &l32, 4) | wr(f, &k32, 4) | wr(f, &half, 1) | wr(f, &l32, 4);
+        for (int lvl = 0; lvl < L && !e; lvl++) {
+            const int64_t* t = c->lazy_cprime + ((size_t)i * L + lvl) * row;
+            e |= wr(f, &k32, 4) | wr(f, &n32, 4);
+            e |= wr_torus_poly(f, t + (size_t)k * N, N, T);
+            e |= wr(f, &k32, 4);
+            for (int r = 0; r < k; r++) e |= wr_torus_poly(f, t + (size_t)r * N, N, T);
+        }
+    }
+    int32_t group = 1;
+    e |= wr(f, &l32, 4) | wr(f, &group, 4);
+    if (fclose(f) != 0) e = -1;
+    return e ? fail(c, "po_save_lazy_file: write failed") : 0;
+}
+
+int po_load_lazy_file(po_ctx* c, const char* path) {
+    if (lazy_alloc(c)) return fail(c, "po_load_lazy_file: out of memory");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(c, "po_load_lazy_file: cannot open %s", path);
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->L, Ls = c->p.l, T = c->T;
+    const size_t row = (size_t)(k + 1) * N;
+    int e = rd_expect_i32(f, Ls) | rd_expect_i32(f, Ls);
+    for (int lv = 0; lv < Ls && !e; lv++) e |= rd_trlwe_dft(f, c->wwl_s2 + (size_t)lv * row, k, N);
+    for (int i = 0; i < n && !e; i++) {
+        uint8_t half = 0;
+        e |= rd_expect_i32(f, L) | rd_expect_i32(f, k) | rd(f, &half, 1);
+        if (e || half != 1) { e = -1; break; }
+        e |= rd_expect_i32(f, L);
+        for (int lvl = 0; lvl < L && !e; lvl++) {
+            int64_t* t = c->lazy_cprime + ((size_t)i * L + lvl) * row;
+            e |= rd_expect_i32(f, k) | rd_expect_i32(f, N);
+            if (!e) e |= rd_torus_poly(f, t + (size_t)k * N, N, T);
+            if (!e) e |= rd_expect_i32(f, k);
+            for (int r = 0; r < k && !e; r++) e |= rd_torus_poly(f, t + (size_t)r * N, N, T);
+        }
+    }
+    if (!e) e |= rd_expect_i32(f, L) | rd_expect_i32(f, 1);
+    fclose(f);
+    return e ? fail(c, "po_load_lazy_file: %s is not a lazy key for these parameters", path) : 0;
+}
+
+/*
+ * blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-1135; its split of the work into
+ * pipelined stages and threads does not change a result) for one ciphertext, scaled = its
+ * mask and body switched to mod 2N:
+ *   derived = RLWE(v s_0) = INTT(sum_lvl gdV[lvl] . NTT(bskPrime[0].cPrime[lvl]))
+ *     (deriveFirstComponentNtt, yatfhe/src/trgsw.cpp:929-955; gdV[lvl] = NTT of digit lvl of
+ *     v, prepareGdV, :911-927),
+ *   acc = X^(-b) ((X^(a_0) - 1) derived + (0, v))                       (:1117-1124),
+ *   for i = 1 .. n-1 with a_i != 0: acc = acc [x] TRGSW_i in place
+ *     (externalProductTrgswMPNttInPlace, yatfhe/src/trgsw.cpp:774-776).
+ * TRGSW_i is built from bskPrime[i] for this ciphertext (stageA and stageB, :1036-1085): each
+ * level's row is rotated, cP = (X^(a_i) - 1) cPrime[lvl] with cP.b[0] += g_lvl
+ * (rotateTrlweMinusOneBPlusOne, yatfhe/src/trlwe.cpp:291-297), the masks go into l digit
+ * polynomials (gadgetDecomposeTrlweA, yatfhe/src/trlwe.cpp:200-211), and with D_l' = NTT of
+ * digit l' of cP.a_k1
+ *   cPrime[lvl].a[k1] = sum_l' D_l' . NTT(2^(T - (l'+1) radix))   (the gadget recomposer)
+ *   cPrime[lvl].b     = NTT(cP.b)
+ *   c[lvl][k1].a[k2]  = sum_l' D_l' . s2[l'].a[k2] + NTT(cP.b)
+ *   c[lvl][k1].b      = sum_l' D_l' . s2[l'].b                       (all mod q).
+ */
+static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, k1 = k + 1, L = c->L, Ls = c->p.l, T = c->T;
+    const int rb = c->p.radix_bits;
+    const uint64_t q = c->q;
+    const nq_barrett* br = &c->plan.br;
+    const size_t row = (size_t)k1 * N, lvlWords = (size_t)k1 * row;
+    if (!c->lazy_cprime || !c->wwl_s2 || n < 2 || L > 64 || Ls > 64) return -1;
+    uint64_t* rows = (uint64_t*)malloc(sizeof(uint64_t) * L * lvlWords);  /* [lvl][r][o][N] */
+    uint64_t* recomp = (uint64_t*)malloc(sizeof(uint64_t) * Ls * N);      /* NTT(2^(T-(l'+1) radix)) */
+    uint64_t* gdv = (uint64_t*)malloc(sizeof(uint64_t) * L * N);
+    uint64_t* hat = (uint64_t*)malloc(sizeof(uint64_t) * row);
+    uint64_t* t1 = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    uint64_t* bh = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    int64_t* hold = (int64_t*)malloc(sizeof(int64_t) * row);
+    int64_t* tmp = (int64_t*)malloc(sizeof(int64_t) * row);
+    int64_t* dig = (int64_t*)malloc(sizeof(int64_t) * (size_t)(L > Ls ? L : Ls) * N);
+    int64_t dg[64];
+    int rc = -1;
+    if (!rows || !recomp || !gdv || !hat || !t1 || !bh || !hold || !tmp || !dig) goto out;
+
+    for (int gl = 0; gl < Ls; gl++) {
+        memset(tmp, 0, sizeof(int64_t) * N);
+        tmp[0] = sext((int64_t)1 << (T - (gl + 1) * rb), T);
+        ntt_from_torus(c, recomp + (size_t)gl * N, tmp);
+    }
+    for (int j = 0; j < N; j++) {
+        zero_mean_digits((uint64_t)v[j], L, rb, T, dg);
+        for (int l = 0; l < L; l++) dig[(size_t)l * N + j] = dg[l];
+    }
+    for (int l = 0; l < L; l++) ntt_from_torus(c, gdv + (size_t)l * N, dig + (size_t)l * N);
+
+    /* first component */
+    memset(hat, 0, sizeof(uint64_t) * row);
+    for (int lvl = 0; lvl < L; lvl++) {
+        const int64_t* cp = c->lazy_cprime + (size_t)lvl * row;  /* i = 0 */
+        for (int o = 0; o < k1; o++) {
+            ntt_from_torus(c, t1, cp + (size_t)o * N);
+            uint64_t* h = hat + (size_t)o * N;
+            for (int j = 0; j < N; j++) h[j] = addmod(h[j], nq_mulmod(br, gdv[(size_t)lvl * N + j], t1[j]), q);
+        }
+    }
+    for (int o = 0; o < k1; o++) intt_to_torus(c, hold + (size_t)o * N, hat + (size_t)o * N);
+    for (int o = 0; o < k1; o++) rotate_poly(c, tmp + (size_t)o * N, hold + (size_t)o * N, scaled[0], 1);
+    for (int j = 0; j < N; j++) tmp[(size_t)k * N + j] = sext(tmp[(size_t)k * N + j] + v[j], T);
+    for (int o = 0; o < k1; o++) rotate_poly(c, acc + (size_t)o * N, tmp + (size_t)o * N, -scaled[n], 0);
+
+    for (int i = 1; i < n; i++) {
+        const int a = scaled[i];
+        if (a == 0) continue;
+        for (int lvl = 0; lvl < L; lvl++) {
+            const int64_t* cp = c->lazy_cprime + ((size_t)i * L + lvl) * row;
+            uint64_t* R = rows + (size_t)lvl * lvlWords;  /* R[r][o]: r < k c[lvl][r], r = k cPrime[lvl] */
+            for (int o = 0; o < k1; o++) rotate_poly(c, hold + (size_t)o * N, cp + (size_t)o * N, a, 1);
+            hold[(size_t)k * N] = sext(hold[(size_t)k * N] + ((int64_t)1 << (T - (lvl + 1) * rb)), T);
+            memset(R, 0, sizeof(uint64_t) * lvlWords);
+            ntt_from_torus(c, bh, hold + (size_t)k * N);
+            for (int r = 0; r < k; r++) {
+                for (int j = 0; j < N; j++) {
+                    zero_mean_digits((uint64_t)hold[(size_t)r * N + j], Ls, rb, T, dg);
+                    for (int gl = 0; gl < Ls; gl++) dig[(size_t)gl * N + j] = dg[gl];
+                }
+                for (int gl = 0; gl < Ls; gl++) {
+                    ntt_from_torus(c, t1, dig + (size_t)gl * N);
+                    const uint64_t* s2 = c->wwl_s2 + (size_t)gl * row;
+                    uint64_t* cpa = R + (size_t)k * row + (size_t)r * N;
+                    for (int j = 0; j < N; j++)
+                        cpa[j] = addmod(cpa[j], nq_mulmod(br, t1[j], recomp[(size_t)gl * N + j]), q);
+                    for (int o = 0; o < k1; o++) {
+                        uint64_t* cr = R + (size_t)r * row + (size_t)o * N;
+                        for (int j = 0; j < N; j++) cr[j] = addmod(cr[j], nq_mulmod(br, t1[j], s2[(size_t)o * N + j]), q);
+                    }
+                }
+                for (int k2 = 0; k2 < k; k2++) {
+                    uint64_t* cr = R + (size_t)r * row + (size_t)k2 * N;
+                    for (int j = 0; j < N; j++) cr[j] = addmod(cr[j], bh[j], q);
+                }
+            }
+            memcpy(R + (size_t)k * row + (size_t)k * N, bh, sizeof(uint64_t) * N);
+        }
+        external_product(c, s, rows, acc, acc);
+    }
+    rc = 0;
+out:
+    free(rows); free(recomp); free(gdv); free(hat); free(t1); free(bh); free(hold); free(tmp); free(dig);
+    return rc;
+}
+
+int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out) {
+    ep_scratch s;
+    int32_t* scaled = (int32_t*)malloc(sizeof(int32_t) * (c->p.n + 1));
+    if (ep_alloc(c, &s) || !scaled) {
+        ep_free(&s);
+        free(scaled);
+        return fail(c, "po_blind_rotate_lazy: out of memory");
+    }
+    po_modswitch(c, in, scaled);
+    const int rc = blind_rotate_lazy(c, &s, scaled, v, acc_out);
+    ep_free(&s);
+    free(scaled);
+    return rc ? fail(c, "po_blind_rotate_lazy: no lazy key, or n < 2") : 0;
+}
+
+/* functionalBootstrappingMPNtt's composition (yatfhe/src/bootstrapping.cpp:71-80) with
+ * blindRotateLazyPipeAltNtt in place of blindRotateMP21Ntt. */
+int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+    if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_pbs_lazy: no lazy key");
+    return pbs_run(c, in, count, v, out, threads, 1);
 }

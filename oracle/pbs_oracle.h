@@ -67,6 +67,16 @@ int po_wwl24_expand(po_ctx* c);
 int po_save_wwl24_file(po_ctx* c, const char* path);
 int po_load_wwl24_file(po_ctx* c, const char* path);
 
+/* Lazy ("OURS") keys of blindRotateLazyPipeAltNtt: half TRGSW rows in the coefficient domain
+ * cprime [n][l_approx][k+1][N] (torus values) + the s2 key [l][k+1][N] (NTT domain). */
+int po_keygen_lazy(po_ctx* c, uint64_t seed);
+int po_get_lazy(po_ctx* c, int64_t* cprime, uint64_t* s2);
+int po_set_lazy(po_ctx* c, const int64_t* cprime, const uint64_t* s2);
+int po_save_lazy_file(po_ctx* c, const char* path);
+int po_load_lazy_file(po_ctx* c, const char* path);
+int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out);
+int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
+
 /* po_keygen that also writes out its random samples (see pbs_oracle.c). */
 int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s, int32_t* bsk_noise,
                       uint64_t* bsk_mask, int32_t* ksk_mask, int32_t* ksk_noise);

@@ -42,6 +42,7 @@ struct RefState {
     std::unique_ptr<TrgswKey> trgswKey;
     std::unique_ptr<BootstrappingKeyMP> bsk;
     std::unique_ptr<BootstrappingKeyWWL24> wwl;
+    std::unique_ptr<BootstrappingKeyMPLazyPipeAlt> lazy;
     std::unique_ptr<TlweKeySwitchingKey> ksk;
     std::string lastError;
 };
@@ -593,6 +594,103 @@ int ref_pbs_wwl24(const int32_t* in, int count, const int64_t* v, int32_t* out, 
             rescaleTlweToNewMod(sc, x);
             genNoiselessTrlweSample(acc, vp, sc);
             blindRotateWWL24Ntt(acc, *s.wwl, sc, p);
+            if (c == 0 && acc0) {
+                for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
+                fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);
+            }
+            extractTlweFromTrlwe(big, acc, p.driftPhase);
+            switchKeyForTlwe(y, *s.ksk, big, p);
+            fromTlwe(out + static_cast<size_t>(c) * (n + 1), y, n);
+        }
+    });
+}
+
+// ---------------------------------------------------------------- lazy ("OURS") keys
+// genBootstrappingKeyMPLazyPipeAlt (yatfhe/src/bootstrapping.cpp:322-339) with its per-i
+// encryptTrgswMP calls (yatfhe/src/trgsw.cpp:18-34) run in order on the calling thread, after
+// genTlweKey and genTrlweKey and before genTlweKeySwitchingKey, as ref_keygen_wwl24 does.
+int ref_keygen_lazy(uint64_t seed) {
+    if (!st().ready) return fail("ref_keygen_lazy: ref_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        auto& p = s.param;
+        (void)rng();
+        yatfhe_oracle_set_seed(seed);
+        rng = ChaCha20Rng();
+        s.lweKey = std::make_unique<TlweKey>(p);
+        s.trgswKey = std::make_unique<TrgswKey>(p);
+        s.lazy = std::make_unique<BootstrappingKeyMPLazyPipeAlt>(p, p.lApprox, true);
+        s.ksk = std::make_unique<TlweKeySwitchingKey>(p);
+        genTlweKey(*s.lweKey);
+        genTrlweKey(s.trgswKey->trlweKey);
+        for (int i = 0; i < s.lazy->n; i++) encryptTrgswMP(s.lazy->bskPrime[i], s.lweKey->s[i], *s.trgswKey, 0, p);
+        symEncTrlevWithKeyNtt(s.lazy->s2Dft, s.trgswKey->trlweKey, s.trgswKey->trlweKey.s, true, p);
+        TlweKey ksTarget = *s.lweKey;
+        genTlweKeySwitchingKey(*s.ksk, s.trgswKey->trlweKey, ksTarget, p);
+    });
+}
+
+// The lazy key's words: cprime = [i][lvl][poly][N] torus values (poly = a[0..k-1] then b of
+// bskPrime[i].cPrime[lvl]), s2 = [lvl][poly][N] NTT-domain words of s2Dft.
+int ref_export_lazy(int64_t* cprime, uint64_t* s2) {
+    auto& s = st();
+    if (!s.lazy) return fail("ref_export_lazy: no lazy key");
+    const int k = s.param.k, N = s.param.N;
+    int64_t* o = cprime;
+    for (const auto& g : s.lazy->bskPrime)
+        for (const auto& t : g.cPrime)
+            for (int poly = 0; poly <= k; poly++) {
+                fromPoly(o, poly < k ? t.a[poly] : t.b, N);
+                o += N;
+            }
+    uint64_t* w = s2;
+    for (const auto& t : s.lazy->s2Dft.trlweDfts)
+        for (int poly = 0; poly <= k; poly++) {
+            const NttPolynomial& P = poly < k ? t.a[poly] : t.b;
+            std::memcpy(w, P.coeffs.data(), sizeof(uint64_t) * N);
+            w += N;
+        }
+    return 0;
+}
+
+// serializeBskLazyPipeAlt / deserializeBskLazyPipeAlt (yatfhe/src/ya_serializer.cpp:445-481).
+int ref_save_lazy(const char* path) {
+    if (!st().lazy) return fail("ref_save_lazy: no lazy key");
+    return guarded([&] { serializeBskLazyPipeAlt(*st().lazy, path); });
+}
+
+int ref_load_lazy(const char* path) {
+    if (!st().ready) return fail("ref_load_lazy: ref_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        s.lazy = std::make_unique<BootstrappingKeyMPLazyPipeAlt>();
+        deserializeBskLazyPipeAlt(*s.lazy, path, s.param.n);
+    });
+}
+
+// functionalBootstrappingMPNtt's composition (yatfhe/src/bootstrapping.cpp:71-80) with
+// blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-999) in place of the MP21 blind
+// rotation: prepareGdV once (yatfhe/src/trgsw.cpp:911-927), then per ciphertext the lazy blind
+// rotation (which builds the accumulator from v itself), extraction and key switching.  acc0
+// (may be null) receives ciphertext 0's accumulator after the blind rotation.
+int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
+    auto& s = st();
+    if (!s.lazy || !s.ksk) return fail("ref_pbs_lazy: keys not loaded");
+    return guarded([&] {
+        const auto& p = s.param;
+        const int n = p.n, N = p.N, k = p.k;
+        TorusPolynomial vp{N};
+        toPoly(vp, v, N);
+        std::vector<NttPolynomial> gdV;
+        prepareGdV(gdV, vp, p);
+        for (int c = 0; c < count; c++) {
+            Tlwe x{n}, y{n};
+            toTlwe(x, in + static_cast<size_t>(c) * (n + 1), n);
+            ScaledTlwe sc{2 * N, n};
+            Trlwe acc{k, N};
+            Tlwe big{s.ksk->nCurrKey};
+            rescaleTlweToNewMod(sc, x);
+            blindRotateLazyPipeAltNtt(acc, *s.lazy, sc, vp, gdV, p);
             if (c == 0 && acc0) {
                 for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
                 fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);

@@ -10,7 +10,7 @@ parameter set and key seed:
     the test polynomial, the reference's outputs of functionalBootstrappingMPNtt, its
     decryptions, and the blind-rotation accumulator of ciphertext 0 after a few CMux steps.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [ginx] [wwl24] [lazy]
 """
 from __future__ import annotations
 
@@ -38,6 +38,14 @@ WWL24_CASES = {
     # name: (params, key seed, number of ciphertexts, message seed); sign bootstrap
     "wwl24_t32_n2048_seed5eed0005": (WWL24_T32_N2048, 0x5EED0005, 8, 14),
     "wwl24_t56_n2048_seed5eed0006": (WWL24_T56_N2048, 0x5EED0006, 8, 15),
+}
+
+LAZY_CASES = {
+    # name: (params, key seed, number of ciphertexts, message seed); sign bootstrap through
+    # blindRotateLazyPipeAltNtt on the reference's default sets.  (On the n=630, N=1024 set
+    # the reference's own lazy outputs do not decrypt: its s2 key has 3 levels of 7 bits.)
+    "lazy_t32_n2048_seed5eed0007": (WWL24_T32_N2048, 0x5EED0007, 8, 16),
+    "lazy_t56_n2048_seed5eed0008": (WWL24_T56_N2048, 0x5EED0008, 8, 17),
 }
 
 
@@ -110,8 +118,42 @@ def make_wwl24(name, p, seed, count, mseed):
     print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
 
 
+def make_lazy(name, p, seed, count, mseed):
+    ref = Reference(p)
+    ref.keygen_lazy(seed)
+    s, z = ref.keys()
+    cprime, s2 = ref.lazy_words()
+    ksk = ref.ksk()
+    rng = np.random.default_rng(mseed)
+    bits = rng.integers(0, 2, count)
+    mu = np.where(bits == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    lut = lutmod.sign_lut(p.N, p.torus_bits)
+    lwe = ref.encrypt(mu)
+    out, acc0 = ref.pbs_lazy(lwe, lut, with_acc=True)
+    dec = ref.decrypt(out, 8)
+    expect = np.where(bits == 1, 1, -1)
+    if not np.array_equal(dec, expect):
+        raise SystemExit(f"{name}: the reference's own decryptions {dec} differ from the messages {expect}")
+    np.savez_compressed(
+        HERE / f"{name}.npz",
+        params=np.array([p.n, p.N, p.k, p.radix_bits, p.l, p.l_approx, p.ks_radix_bits, p.ks_level, p.lwe_noise_b,
+                         p.rlwe_noise_b, p.torus_base, p.torus_bits], np.int64),
+        seed=np.array([seed], np.uint64),
+        sha_lwe_s=digest(s), sha_rlwe_s=digest(z), sha_cprime=digest(cprime), sha_s2=digest(s2),
+        sha_ksk=digest(ksk),
+        mu=mu, lwe_in=lwe, lut=lut, lwe_out=out, decrypted=dec, base=np.array([8]), acc0=acc0)
+    print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
+
+
 if __name__ == "__main__":
-    for name, (p, seed, count, mseed) in CASES.items():
-        make(name, p, seed, count, mseed)
-    for name, (p, seed, count, mseed) in WWL24_CASES.items():
-        make_wwl24(name, p, seed, count, mseed)
+    # optional arguments: the families to (re)generate, of "ginx", "wwl24", "lazy" (default all)
+    families = set(sys.argv[1:]) or {"ginx", "wwl24", "lazy"}
+    if "ginx" in families:
+        for name, (p, seed, count, mseed) in CASES.items():
+            make(name, p, seed, count, mseed)
+    if "wwl24" in families:
+        for name, (p, seed, count, mseed) in WWL24_CASES.items():
+            make_wwl24(name, p, seed, count, mseed)
+    if "lazy" in families:
+        for name, (p, seed, count, mseed) in LAZY_CASES.items():
+            make_lazy(name, p, seed, count, mseed)
