@@ -111,6 +111,25 @@ int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h
  * by serializeBskWWL24 (:220-229) and uploads it as above. */
 int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);
 
+/* Lazy ("OURS") keys (BootstrappingKeyMPLazyPipeAlt, yatfhe/include/yatfhe/bootstrapping.h:284-307):
+ * the half TRGSW rows bskPrime[i].cPrime of every key index in the coefficient domain,
+ * [n][l_approx][k+1][N] torus values sign-extended to int64 (poly p < k is a[p], poly k is
+ * b), and the s2 key s2Dft with s2_levels (the reference's param.l) levels,
+ * [s2_levels][k+1][N] NTT-domain words mod q.  The device keeps the rows as they are, in the
+ * torus word size (4 bytes at T = 32, a quarter of the GINX rows' bytes), and every
+ * bootstrap rebuilds each CMux step's TRGSW from them as blindRotateLazyPipeAltNtt
+ * (yatfhe/src/blind_rotate.cpp:995-1135) does.  Such a key runs yg_pbs, yg_pbs_host,
+ * yg_blind_rotate (steps = n) and yg_blind_rotate_extract with the lazy blind rotation; the
+ * batch plans, the serving loop, yg_pbs_noalloc and yg_blind_rotate_acc reject it with
+ * YG_ERR_INVALID.  Requires n >= 2, l_approx <= 8, radix_bits <= 15, s2_levels <= 8 and
+ * s2_levels * radix_bits <= torus_bits; an unreduced s2 word or a row value that is not a
+ * sign-extended torus value is rejected with YG_ERR_INVALID.  Synchronizes the device. */
+int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s2, int s2_levels, yg_key** out);
+
+/* Replaces deserializeBskLazyPipeAlt (yatfhe/src/ya_serializer.cpp:462-481): reads a file
+ * written by serializeBskLazyPipeAlt (:445-460) and uploads it as above. */
+int yg_key_load_lazy_file(yg_ctx* ctx, const char* path, yg_key** out);
+
 /* Attaches the key-switching key (TlweKeySwitchingKey::decomposedKsk,
  * yatfhe/include/yatfhe/keyswitching.h:14-31) as int32 words [k N][t][n + 1]. */
 int yg_key_set_ksk(yg_key* key, const int32_t* h_ksk);
@@ -142,7 +161,8 @@ size_t yg_pbs_noalloc_max_count(const yg_ctx* ctx);
 
 /* rescaleTlweToNewMod + genNoiselessTrlweSample + the first `steps` iterations of
  * blindRotateMP21Ntt (yatfhe/src/blind_rotate.cpp:1538-1565; steps = n is the whole
- * rotation).  d_acc receives [count][(k+1) N] int64 torus words, a then b. */
+ * rotation).  d_acc receives [count][(k+1) N] int64 torus words, a then b.  With a lazy key:
+ * rescaleTlweToNewMod + blindRotateLazyPipeAltNtt, steps = n only. */
 int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut, int64_t* d_acc,
                     int count, int steps, void* stream);
 

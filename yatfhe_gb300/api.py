@@ -74,7 +74,8 @@ class BootstrapKey:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self._h = handle
-        self.family = "ginx"  # key format it was made from: "ginx" (BootstrappingKeyMP) or "wwl24"
+        # key format it was made from: "ginx" (BootstrappingKeyMP), "wwl24" or "lazy"
+        self.family = "ginx"
 
     @classmethod
     def from_file(cls, ctx: Context, path) -> "BootstrapKey":
@@ -118,6 +119,36 @@ class BootstrapKey:
         _lib.check(_lib.lib().yg_key_load_wwl24_file(ctx.handle, str(path).encode(), ctypes.byref(h)))
         key = cls(ctx, h)
         key.family = "wwl24"
+        return key
+
+    @classmethod
+    def from_lazy_words(cls, ctx: Context, cprime: np.ndarray, s2: np.ndarray) -> "BootstrapKey":
+        """A lazy ("OURS") key (BootstrappingKeyMPLazyPipeAlt: half rows bskPrime[i].cPrime
+        [n][l_approx][k+1][N] as torus values, the s2 key [levels][k+1][N] as NTT-domain words
+        mod q).  The device keeps the rows in the torus word size; every bootstrap rebuilds each
+        step's TRGSW from them (blindRotateLazyPipeAltNtt)."""
+        p = ctx.params
+        c = np.ascontiguousarray(cprime, np.int64)
+        s = np.ascontiguousarray(s2, np.uint64)
+        row = (p.k + 1) * p.N
+        if c.size != p.n * p.l_approx * row:
+            raise ValueError(f"expected {p.n * p.l_approx * row} half-row words, got {c.size}")
+        if s.size == 0 or s.size % row:
+            raise ValueError(f"the s2 key must be a whole number of [{p.k + 1}][{p.N}] levels")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_upload_lazy(ctx.handle, ctypes.c_void_p(c.ctypes.data),
+                                                  ctypes.c_void_p(s.ctypes.data), s.size // row, ctypes.byref(h)))
+        key = cls(ctx, h)
+        key.family = "lazy"
+        return key
+
+    @classmethod
+    def from_lazy_file(cls, ctx: Context, path) -> "BootstrapKey":
+        """A lazy key file written by serializeBskLazyPipeAlt."""
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_load_lazy_file(ctx.handle, str(path).encode(), ctypes.byref(h)))
+        key = cls(ctx, h)
+        key.family = "lazy"
         return key
 
     def set_ksk(self, ksk: np.ndarray) -> "BootstrapKey":
@@ -276,6 +307,15 @@ def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: 
     if key.family != "wwl24":
         raise ValueError("blind_rotate_wwl24_ntt needs a key made by BootstrapKey.from_wwl24_words/_file")
     return blind_rotate_mp21_ntt(ctx, key, lwe_in, lut, steps=steps, stream=stream)
+
+
+def blind_rotate_lazy_pipe_alt_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, stream=None):
+    """blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-1135) on a lazy key:
+    accumulators [count, (k+1) N] (int64 torus words) after the whole rotation.  The
+    reference's gdVntt argument (prepareGdV of the test polynomial) is computed on the GPU."""
+    if key.family != "lazy":
+        raise ValueError("blind_rotate_lazy_pipe_alt_ntt needs a key made by BootstrapKey.from_lazy_words/_file")
+    return blind_rotate_mp21_ntt(ctx, key, lwe_in, lut, stream=stream)
 
 
 def switch_key_for_tlwe(ctx: Context, key: BootstrapKey, big, stream=None):

@@ -345,6 +345,53 @@ void upload_wwl24(yg_ctx* c, yg_key* key, const u64* cprime, const u64* s2, int 
     convert_bsk_words(c, key, d_out, scratch, tw);
 }
 
+int64_t sext_host(int64_t x, int bits) { return (int64_t)((uint64_t)x << (64 - bits)) >> (64 - bits); }
+
+// Lazy key -> the device: the half rows ([n][L][2][N] torus values) in the torus word size,
+// and the mod-q transform tables with the s2 key ([Ls][2][N] NTT-domain words) and their
+// Shoup companions.  The blind rotation rebuilds each step's rows from these
+// (lazy_blind_rotate_kernel); no other conversion runs at upload.
+void upload_lazy(yg_ctx* c, yg_key* key, const int64_t* cprime, const u64* s2, int Ls) {
+    const int n = c->p.n, N = c->p.N, L = c->p.l_approx, T = c->p.torus_bits, rb = c->p.radix_bits;
+    if (n < 2) throw std::invalid_argument("lazy key: the blind rotation needs n >= 2");
+    if (L > yg::kLazyMaxLevels) throw std::invalid_argument("lazy key: l_approx <= 8");
+    if (rb > 15) throw std::invalid_argument("lazy key: radix_bits <= 15");
+    if (Ls < 1 || Ls > yg::kLazyMaxLevels || Ls * rb > T)
+        throw std::invalid_argument("lazy s2 key: 1 <= levels <= 8 and levels * radix_bits <= torus_bits");
+    const u64 q = c->q;
+    const QTables& qt = *c->qtab;
+    const size_t s2_words = (size_t)Ls * 2 * N, cp_words = (size_t)n * L * 2 * N;
+    std::vector<u64> tab(4 * (size_t)N + 2 * s2_words);
+    std::copy(qt.w.begin(), qt.w.end(), tab.begin());
+    std::copy(qt.wp.begin(), qt.wp.end(), tab.begin() + N);
+    std::copy(qt.wf.begin(), qt.wf.end(), tab.begin() + 2 * (size_t)N);
+    std::copy(qt.wfp.begin(), qt.wfp.end(), tab.begin() + 3 * (size_t)N);
+    u64* t2 = tab.data() + 4 * (size_t)N;
+    for (size_t j = 0; j < s2_words; j++) {
+        if (s2[j] >= q) throw std::invalid_argument("lazy s2 key word not reduced mod q");
+        t2[j] = s2[j];
+        t2[s2_words + j] = (u64)(((u128)s2[j] << 64) / q);
+    }
+    const size_t wb = T == 32 ? 4 : 8;
+    std::vector<unsigned char> words(cp_words * wb);
+    for (size_t j = 0; j < cp_words; j++) {
+        const int64_t v = cprime[j];
+        if (sext_host(v, T) != v) throw std::invalid_argument("lazy key word is not a sign-extended torus value");
+        if (T == 32) {
+            const int32_t w = (int32_t)v;
+            std::memcpy(words.data() + j * 4, &w, 4);
+        } else {
+            std::memcpy(words.data() + j * 8, &v, 8);
+        }
+    }
+    ck(cudaMalloc(&key->d_lazy_tab, tab.size() * sizeof(u64)), "cudaMalloc lazy tables");
+    ck(cudaMalloc(&key->d_lazy_cprime, words.size()), "cudaMalloc lazy key");
+    ck(cudaMemcpy(key->d_lazy_tab, tab.data(), tab.size() * sizeof(u64), cudaMemcpyHostToDevice), "upload lazy tables");
+    ck(cudaMemcpy(key->d_lazy_cprime, words.data(), words.size(), cudaMemcpyHostToDevice), "upload lazy key");
+    key->lazy_ls = Ls;
+    key->bsk_bytes = tab.size() * sizeof(u64) + words.size();
+}
+
 // Key generation arithmetic on the GPU from caller-drawn samples (see yg_keygen_from_samples):
 // the NTT of the RLWE secret mod q (host, exact), the BSK samples (keygen_bsk_kernel), the
 // usual conversion of the NTT-domain words, and the KSK samples (keygen_ksk_kernel).
@@ -528,6 +575,93 @@ int read_wwl24_file(const yg_params& p, const char* path, std::vector<u64>& cpri
     return Ls;
 }
 
+// deserializeBskLazyPipeAlt (yatfhe/src/ya_serializer.cpp:462-481): the TrlevDft s2
+// (`[int l][int l]` + l TrlweDft), n half TrgswMP (`[int L][int k][bool 1][int L]` + L Trlwe,
+// :148-174; a Trlwe is `[int k][int N]`, b, `[int k]`, a_0..a_{k-1}, each a TorusPolynomial
+// `[int N]` + N Torus words, :33-42,65-74), then `[int level][int group]`.  Torus words are
+// int32 in the reference's 32-bit build, int64 in its 56-bit build.
+int read_lazy_file(const yg_params& p, const char* path, std::vector<int64_t>& cprime, std::vector<u64>& s2) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    Reader r{f, path};
+    const int n = p.n, N = p.N, k = p.k, L = p.l_approx;
+    const size_t row = (size_t)(k + 1) * N;
+    auto torus_poly = [&](int64_t* dst) {
+        r.expect(N, "TorusPolynomial N");
+        if (p.torus_bits == 32) {
+            std::vector<int32_t> w(N);
+            r.raw(w.data(), 4 * (size_t)N);
+            for (int j = 0; j < N; j++) dst[j] = w[j];
+        } else {
+            r.raw(dst, 8 * (size_t)N);
+        }
+    };
+    int Ls = 0;
+    try {
+        Ls = r.i32();
+        if (Ls < 1 || Ls > yg::kLazyMaxLevels) throw std::runtime_error(std::string(path) + ": s2 key levels out of range");
+        r.expect(Ls, "TrlevDft size");
+        s2.assign((size_t)Ls * row, 0);
+        for (int l = 0; l < Ls; l++) read_trlwe_dft(r, s2.data() + (size_t)l * row, k, N);
+        cprime.assign((size_t)n * L * row, 0);
+        for (int i = 0; i < n; i++) {
+            r.expect(L, "TrgswMP l");
+            r.expect(k, "TrgswMP k");
+            if (r.b8() != 1) throw std::runtime_error(std::string(path) + ": full TRGSW rows are not a lazy key");
+            r.expect(L, "cPrime size");
+            for (int l = 0; l < L; l++) {
+                int64_t* t = cprime.data() + ((size_t)i * L + l) * row;
+                r.expect(k, "Trlwe k");
+                r.expect(N, "Trlwe N");
+                torus_poly(t + (size_t)k * N);
+                r.expect(k, "Trlwe a size");
+                for (int a = 0; a < k; a++) torus_poly(t + (size_t)a * N);
+            }
+        }
+        r.expect(L, "key level");
+        r.expect(1, "key group");
+    } catch (...) {
+        std::fclose(f);
+        throw;
+    }
+    std::fclose(f);
+    return Ls;
+}
+
+// The lazy blind rotation's launch arguments for a context and lazy key (buffers and count
+// left empty).
+yg::LazyBrArgs lazy_args(const yg_ctx* c, const yg_key* key) {
+    yg::LazyBrArgs a{};
+    const int N = c->p.N, T = c->p.torus_bits, rb = c->p.radix_bits, Ls = key->lazy_ls;
+    const u64 q = c->q;
+    const u64* tab = key->d_lazy_tab;
+    a.cprime = key->d_lazy_cprime;
+    a.wi = tab;
+    a.wip = tab + N;
+    a.wf = tab + 2 * (size_t)N;
+    a.wfp = tab + 3 * (size_t)N;
+    a.s2 = tab + 4 * (size_t)N;
+    a.s2p = a.s2 + (size_t)Ls * 2 * N;
+    a.q = q;
+    u64 inv = q;  // Newton: each step doubles the bits of q^-1 mod 2^64 that are right
+    for (int i = 0; i < 6; i++) inv *= 2 - q * inv;
+    a.qinv = inv;
+    a.post = mulmod(c->qtab->ninv, (u64)(((u128)1 << 64) % q), q);
+    a.postp = (u64)(((u128)a.post << 64) / q);
+    for (int gl = 0; gl < Ls; gl++) {
+        const int64_t g = sext_host((int64_t)1 << (T - (gl + 1) * rb), T);
+        a.recomp[gl] = g < 0 ? (u64)(g + (int64_t)q) : (u64)g;
+        a.recompp[gl] = (u64)(((u128)a.recomp[gl] << 64) / q);
+    }
+    a.n = c->p.n;
+    a.N = N;
+    a.L = c->p.l_approx;
+    a.Ls = Ls;
+    a.radix_bits = rb;
+    a.torus_bits = T;
+    return a;
+}
+
 }  // namespace
 
 yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
@@ -545,10 +679,13 @@ yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     return a;
 }
 
-int yg::check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk) {
+int yg::check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bool lazy_ok) {
     if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
     if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
-    if (need_bsk && !k->d_bsk) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
+    if (need_bsk && k->lazy() && !lazy_ok)
+        return set_err(YG_ERR_INVALID,
+                       "lazy keys run through yg_pbs, yg_pbs_host, yg_blind_rotate and yg_blind_rotate_extract");
+    if (need_bsk && !k->d_bsk && !k->lazy()) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
     if (need_ksk && !k->d_ksk) return set_err(YG_ERR_STATE, "key has no key-switching key (yg_key_set_ksk)");
     return YG_OK;
 }
@@ -566,12 +703,22 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
     const int N = c->p.N, kN = c->p.k * N;
     int32_t* big = nullptr;
     ck(cudaMallocAsync(&big, (size_t)count * (kN + 1) * sizeof(int32_t), s), "cudaMallocAsync extract buffer");
-    yg::BrArgs a = br_args(c, key);
-    a.lwe_in = d_in;
-    a.lut = d_lut;
-    a.big_out = big;
-    a.count = count;
-    int rc = yg::launch_blind_rotate(c->logN, c->p.torus_bits, a, s);
+    int rc;
+    if (key->lazy()) {
+        yg::LazyBrArgs a = lazy_args(c, key);
+        a.lwe_in = d_in;
+        a.lut = d_lut;
+        a.big_out = big;
+        a.count = count;
+        rc = yg::launch_lazy_blind_rotate(a, s);
+    } else {
+        yg::BrArgs a = br_args(c, key);
+        a.lwe_in = d_in;
+        a.lut = d_lut;
+        a.big_out = big;
+        a.count = count;
+        rc = yg::launch_blind_rotate(c->logN, c->p.torus_bits, a, s);
+    }
     if (rc == 0) {
         yg::KsArgs k{big, key->d_ksk, d_out, count, kN, c->p.n, c->p.ks_level, c->p.ks_radix_bits};
         rc = yg::launch_keyswitch(k, s);
@@ -672,6 +819,38 @@ int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out) {
     });
 }
 
+int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s2, int s2_levels, yg_key** out) {
+    if (!ctx || !h_cprime || !h_s2 || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            upload_lazy(ctx, k.get(), h_cprime, h_s2, s2_levels);
+        } catch (...) {
+            if (k->d_lazy_cprime) cudaFree(k->d_lazy_cprime);
+            if (k->d_lazy_tab) cudaFree(k->d_lazy_tab);
+            k->d_lazy_cprime = nullptr;
+            k->d_lazy_tab = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_key_load_lazy_file(yg_ctx* ctx, const char* path, yg_key** out) {
+    if (!ctx || !path || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<int64_t> cprime;
+        std::vector<u64> s2;
+        const int levels = read_lazy_file(ctx->p, path, cprime, s2);
+        return yg_key_upload_lazy(ctx, cprime.data(), s2.data(), levels, out);
+    });
+}
+
 int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h_rlwe_s, const int32_t* h_bsk_noise,
                            const uint64_t* h_bsk_mask, const int32_t* h_ksk_mask, const int32_t* h_ksk_noise,
                            uint64_t* h_bsk_words, int32_t* h_ksk, yg_key** out) {
@@ -716,6 +895,8 @@ void yg_key_destroy(yg_key* key) {
     if (!key) return;
     if (key->d_bsk) cudaFree(key->d_bsk);
     if (key->d_ksk) cudaFree(key->d_ksk);
+    if (key->d_lazy_cprime) cudaFree(key->d_lazy_cprime);
+    if (key->d_lazy_tab) cudaFree(key->d_lazy_tab);
     delete key;
 }
 
@@ -723,7 +904,7 @@ size_t yg_key_device_bytes(const yg_key* key) { return key ? key->bsk_bytes + ke
 
 int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, int count, const int64_t* d_lut,
            void* stream) {
-    if (int rc = check_key(ctx, key, true, true)) return rc;
+    if (int rc = check_key(ctx, key, true, true, true)) return rc;
     if (count < 0 || (count > 0 && (!d_in || !d_out || !d_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
     if (count == 0) return YG_OK;
     return guarded([&] {
@@ -734,7 +915,7 @@ int yg_pbs(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, int32_t* d_out, 
 
 int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_out, int count, const int64_t* h_lut,
                 void* stream) {
-    if (int rc = check_key(ctx, key, true, true)) return rc;
+    if (int rc = check_key(ctx, key, true, true, true)) return rc;
     if (count < 0 || (count > 0 && (!h_in || !h_out || !h_lut))) return set_err(YG_ERR_INVALID, "bad buffers");
     if (count == 0) return YG_OK;
     return guarded([&] {
@@ -794,10 +975,23 @@ int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_
 
 int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut, int64_t* d_acc,
                     int count, int steps, void* stream) {
-    if (int rc = check_key(ctx, key, true, false)) return rc;
+    if (int rc = check_key(ctx, key, true, false, true)) return rc;
     if (count < 0 || steps < 0 || steps > ctx->p.n) return set_err(YG_ERR_INVALID, "bad count or steps");
+    if (key->lazy() && steps != ctx->p.n) return set_err(YG_ERR_INVALID, "a lazy key runs the whole rotation: steps = n");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (key->lazy()) {
+        return guarded([&] {
+            DeviceGuard g(ctx->device);
+            yg::LazyBrArgs a = lazy_args(ctx, key);
+            a.lwe_in = d_in;
+            a.lut = d_lut;
+            a.acc_out = d_acc;
+            a.count = count;
+            yg::check_launch(yg::launch_lazy_blind_rotate(a, stream), "lazy blind rotate launch");
+            return YG_OK;
+        });
+    }
     return guarded([&] {
         DeviceGuard g(ctx->device);
         yg::BrArgs a = br_args(ctx, key);
@@ -813,10 +1007,22 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
 
 int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const int64_t* d_lut,
                             int32_t* d_big, int count, void* stream) {
-    if (int rc = check_key(ctx, key, true, false)) return rc;
+    if (int rc = check_key(ctx, key, true, false, true)) return rc;
     if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_big) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (key->lazy()) {
+        return guarded([&] {
+            DeviceGuard g(ctx->device);
+            yg::LazyBrArgs a = lazy_args(ctx, key);
+            a.lwe_in = d_in;
+            a.lut = d_lut;
+            a.big_out = d_big;
+            a.count = count;
+            yg::check_launch(yg::launch_lazy_blind_rotate(a, stream), "lazy blind rotate launch");
+            return YG_OK;
+        });
+    }
     return guarded([&] {
         DeviceGuard g(ctx->device);
         yg::BrArgs a = br_args(ctx, key);

@@ -96,11 +96,18 @@ struct yg_key {
     uint32_t* d_bsk = nullptr;
     int32_t* d_ksk = nullptr;
     size_t bsk_bytes = 0, ksk_bytes = 0;
+    // A lazy ("OURS") key instead of GINX rows: the half rows [n][L][2][N] in the torus word
+    // size, and one block of [wi | wip | wf | wfp] (N each) + [s2 | s2p] ([Ls][2][N] each).
+    void* d_lazy_cprime = nullptr;
+    uint64_t* d_lazy_tab = nullptr;
+    int lazy_ls = 0;
+    bool lazy() const { return d_lazy_cprime != nullptr; }
 };
 
 namespace yg {
 
-int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk);
+// need_bsk: the key must hold GINX rows, or (lazy_ok) GINX rows or a lazy key.
+int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bool lazy_ok = false);
 
 // Blind-rotation launch arguments of a context and key (buffers and count left empty).
 BrArgs br_args(const yg_ctx* c, const yg_key* key);

@@ -341,6 +341,262 @@ __global__ void __launch_bounds__(256) keygen_ksk_kernel(const KeygenKskArgs a) 
     }
 }
 
+// torus a + b reduced to T bits.
+template <int T>
+__device__ __forceinline__ typename TorusOf<T>::type tadd(typename TorusOf<T>::type a, typename TorusOf<T>::type b) {
+    using U = typename TorusOf<T>::utype;
+    if constexpr (T == 32) return (int32_t)((U)a + (U)b);
+    else return sext<56>((int64_t)((U)a + (U)b));
+}
+
+// x y 2^-64 mod q for x, y < q < 2^62 (Montgomery; qinv = q^-1 mod 2^64): x y - m q with
+// m = (x y) qinv mod 2^64 has zero low word, so the high words' difference is exact.
+__device__ __forceinline__ uint64_t montmul64(uint64_t x, uint64_t y, uint64_t q, uint64_t qinv) {
+    const uint64_t lo = x * y, hi = __umul64hi(x, y);
+    const uint64_t mh = __umul64hi(lo * qinv, q);
+    return hi >= mh ? hi - mh : hi + q - mh;
+}
+
+// blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-1135) and the extraction, one
+// ciphertext per CTA of N/2 threads; thread t owns coefficients and transform slots t and
+// t + N/2.  The arithmetic is the reference's: words mod q, transformed in shared memory by
+// q_forward_in_smem / q_inverse_in_smem (HEXL's negacyclic convention), products with key
+// words or constants by Shoup multiplication, products of two computed words by Montgomery
+// multiplication (whose 2^-64 the final N^-1 2^64 scaling removes).
+//   first component: acc = X^(-b) ((X^(a_0) - 1) derived + (0, v)), derived =
+//     INTT(sum_lvl NTT(digit lvl of v) . NTT(cPrime_0[lvl]))        (:1117-1124)
+//   step i (a_i != 0): acc = acc [x] TRGSW_i (externalProductTrgswMPNttInPlace), where level
+//     lvl of TRGSW_i comes from the rotated half row cP = (X^(a_i) - 1) cPrime_i[lvl],
+//     cP.b[0] += 2^(T - (lvl+1) radix), and its mask digits D_l' (l' < Ls, transformed):
+//       cPrime.a = sum D_l' . 2^(T - (l'+1) radix),  cPrime.b = NTT(cP.b),
+//       c.a = sum D_l' . s2[l'].a + NTT(cP.b),       c.b = sum D_l' . s2[l'].b
+//     (stageA / stageB, :1036-1085).  Each level is built in registers and multiplied into the
+//     product at once: nothing of TRGSW_i is stored.
+template <int T>
+__global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBrArgs a) {
+    using TT = typename TorusOf<T>::type;
+    using U = typename TorusOf<T>::utype;
+    extern __shared__ __align__(16) unsigned char lz_smem[];
+    const int N = a.N, H = N >> 1, t = threadIdx.x, n = a.n, L = a.L, Ls = a.Ls, rb = a.radix_bits;
+    const int logN = 31 - __clz(N);
+    const int ct = blockIdx.x;
+    const uint64_t q = a.q, qinv = a.qinv;
+    uint64_t* sw = reinterpret_cast<uint64_t*>(lz_smem);                  // [N]
+    TT* acc = reinterpret_cast<TT*>(sw + N);                              // [2][N]
+    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);               // [max(L, Ls)][N]
+    int16_t* sa = dig + (size_t)(L > Ls ? L : Ls) * N;                    // [n + 1]
+    const TT* cpr = static_cast<const TT*>(a.cprime);
+    const int jj[2] = {t, t + H};
+
+    auto lift = [q](int64_t x) -> uint64_t { return x < 0 ? (uint64_t)(x + (int64_t)q) : (uint64_t)x; };
+    auto addq = [q](uint64_t x, uint64_t y) -> uint64_t {
+        const uint64_t s = x + y;
+        return s >= q ? s - q : s;
+    };
+    // applyIntt's last steps (yatfhe/src/ntt_hexl.cpp:153-175): scale, centre, low T bits.
+    auto to_torus = [&](uint64_t v) -> TT {
+        v = mulshoup64(v, a.post, a.postp, q);
+        const int64_t c = v >= (q + 1) / 2 ? (int64_t)(v - q) : (int64_t)v;
+        if constexpr (T == 32) return (int32_t)(uint32_t)(uint64_t)c;
+        else return sext<56>(c);
+    };
+    // (X^r p)[j] for r in [0, 2N) (rotateTorusPolynomial, yatfhe/src/polynomial.cpp:184-193)
+    auto rot_at = [N](const TT* p, int r, int j) -> TT {
+        int x = j - r;
+        bool neg = false;
+        if (x < 0) {
+            x += N;
+            neg = true;
+        }
+        if (x < 0) {
+            x += N;
+            neg = false;
+        }
+        const TT v = p[x];
+        return neg ? tneg<T>(v) : v;
+    };
+    auto norm = [N](int r) {
+        r %= 2 * N;
+        return r < 0 ? r + 2 * N : r;
+    };
+    auto forward = [&]() { q_forward_in_smem(sw, N, a.wf, a.wfp, q); };
+    auto inverse = [&]() { q_inverse_in_smem(sw, N, a.wi, a.wip, q); };
+
+    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81)
+    const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+    for (int i = t; i <= n; i += H) sa[i] = (int16_t)modswitch_down(in[i], 31 - logN, logN + 1);
+    // digits of v, L levels (prepareGdV, yatfhe/src/trgsw.cpp:911-927)
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int j = jj[e];
+        zero_mean_digits<U, T>((U)(TT)a.lut[j], L, rb, [&](int level, int d) { dig[level * N + j] = (int16_t)d; });
+    }
+
+    // first component (deriveFirstComponentNtt, yatfhe/src/trgsw.cpp:929-955)
+    {
+        uint64_t h[2][2] = {{0, 0}, {0, 0}};
+        for (int lvl = 0; lvl < L; ++lvl) {
+            uint64_t V[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[jj[e]] = lift(dig[lvl * N + jj[e]]);
+            __syncthreads();
+            forward();
+#pragma unroll
+            for (int e = 0; e < 2; ++e) V[e] = sw[jj[e]];
+#pragma unroll
+            for (int poly = 0; poly < 2; ++poly) {
+                __syncthreads();
+                const TT* src = cpr + ((size_t)lvl * 2 + poly) * N;  // key index 0
+#pragma unroll
+                for (int e = 0; e < 2; ++e) sw[jj[e]] = lift((int64_t)src[jj[e]]);
+                __syncthreads();
+                forward();
+#pragma unroll
+                for (int e = 0; e < 2; ++e) h[poly][e] = addq(h[poly][e], montmul64(V[e], sw[jj[e]], q, qinv));
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly) {
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[jj[e]] = h[poly][e];
+            __syncthreads();
+            inverse();
+#pragma unroll
+            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = to_torus(sw[jj[e]]);
+            __syncthreads();
+        }
+        TT tv[2][2];
+        const int r0 = norm(sa[0]);
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int j = jj[e];
+                TT x = tsub<T>(rot_at(acc + poly * N, r0, j), acc[poly * N + j]);
+                if (poly == 1) x = tadd<T>(x, (TT)a.lut[j]);
+                tv[poly][e] = x;
+            }
+        __syncthreads();
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = tv[poly][e];
+        __syncthreads();
+        const int rb0 = norm(-(int)sa[n]);
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) tv[poly][e] = rot_at(acc + poly * N, rb0, jj[e]);
+        __syncthreads();
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = tv[poly][e];
+        __syncthreads();
+    }
+
+    for (int i = 1; i < n; ++i) {
+        const int ai = sa[i];
+        if (ai == 0) continue;  // the same for every thread of the CTA
+        const int r = norm(ai);
+        uint64_t acch[2][2] = {{0, 0}, {0, 0}};
+        for (int lvl = 0; lvl < L; ++lvl) {
+            const TT* cp = cpr + ((size_t)i * L + lvl) * 2 * N;
+            const int sh = T - (lvl + 1) * rb;
+            TT one;
+            if constexpr (T == 32) one = (int32_t)((uint32_t)1 << sh);
+            else one = sext<56>((int64_t)1 << sh);
+            TT bp[2];
+            // stageA: rotateTrlweMinusOneBPlusOne, then the mask's Ls digits (decomposeRow)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int j = jj[e];
+                const TT ra = tsub<T>(rot_at(cp, r, j), cp[j]);
+                TT rbv = tsub<T>(rot_at(cp + N, r, j), cp[N + j]);
+                if (j == 0) rbv = tadd<T>(rbv, one);
+                bp[e] = rbv;
+                zero_mean_digits<U, T>((U)ra, Ls, rb, [&](int level, int d) { dig[level * N + j] = (int16_t)d; });
+            }
+            // stageB: the level's rows, slot by slot in registers
+            uint64_t ca[2] = {0, 0}, cb[2] = {0, 0}, cpa[2] = {0, 0}, bh[2];
+            for (int gl = 0; gl < Ls; ++gl) {
+#pragma unroll
+                for (int e = 0; e < 2; ++e) sw[jj[e]] = lift(dig[gl * N + jj[e]]);
+                __syncthreads();
+                forward();
+                const uint64_t* s2a = a.s2 + (size_t)gl * 2 * N;
+                const uint64_t* s2pa = a.s2p + (size_t)gl * 2 * N;
+                const uint64_t rc = a.recomp[gl], rcp = a.recompp[gl];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int j = jj[e];
+                    const uint64_t D = sw[j];
+                    ca[e] = addq(ca[e], mulshoup64(D, s2a[j], s2pa[j], q));
+                    cb[e] = addq(cb[e], mulshoup64(D, s2a[N + j], s2pa[N + j], q));
+                    cpa[e] = addq(cpa[e], mulshoup64(D, rc, rcp, q));
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[jj[e]] = lift((int64_t)bp[e]);
+            __syncthreads();
+            forward();
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                bh[e] = sw[jj[e]];
+                ca[e] = addq(ca[e], bh[e]);
+            }
+            // the accumulator's digits of this level against the level's rows
+#pragma unroll
+            for (int poly = 0; poly < 2; ++poly) {
+                __syncthreads();
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    int d = 0;
+                    zero_mean_digits<U, T>((U)acc[poly * N + jj[e]], L, rb, [&](int level, int x) {
+                        if (level == lvl) d = x;
+                    });
+                    sw[jj[e]] = lift(d);
+                }
+                __syncthreads();
+                forward();
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const uint64_t X = sw[jj[e]];
+                    acch[0][e] = addq(acch[0][e], montmul64(X, poly == 0 ? ca[e] : cpa[e], q, qinv));
+                    acch[1][e] = addq(acch[1][e], montmul64(X, poly == 0 ? cb[e] : bh[e], q, qinv));
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly) {
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[jj[e]] = acch[poly][e];
+            __syncthreads();
+            inverse();
+#pragma unroll
+            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = to_torus(sw[jj[e]]);
+            __syncthreads();
+        }
+    }
+
+    if (a.acc_out) {
+        int64_t* dst = a.acc_out + (size_t)ct * 2 * N;
+        for (int idx = t; idx < 2 * N; idx += H) dst[idx] = (int64_t)acc[idx];
+    }
+    if (a.big_out) {
+        // extractTlweFromTrlwe(out, acc, 0): a'[j] = j ? -a[N-j] : a[0], b' = b[0], rescaled 2^T -> 2^32
+        int32_t* dst = a.big_out + (size_t)ct * (N + 1);
+        for (int j = t; j <= N; j += H) {
+            const TT x = j == N ? acc[N] : (j == 0 ? acc[0] : tneg<T>(acc[N - j]));
+            if constexpr (T == 32) dst[j] = (int32_t)x;
+            else dst[j] = (int32_t)modswitch_down((int64_t)x, T - 32, 32);
+        }
+    }
+}
+
 // Teams of one ciphertext slice: one per RNS channel (kLayoutChannel), or one per channel
 // and accumulator row (kLayoutChannelRow).
 template <int SPLIT>
@@ -1165,6 +1421,22 @@ int launch_keygen_ksk(const KeygenKskArgs& a, void* stream) {
     if (a.ks_radix_bits < 1 || a.t * a.ks_radix_bits > 32) return -1;
     keygen_ksk_kernel<<<(unsigned)((samples + 7) / 8), 256, 0, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream) {
+    if (a.count <= 0) return 0;
+    if ((a.N != 1024 && a.N != 2048) || a.n < 2 || a.L < 1 || a.L > kLazyMaxLevels || a.Ls < 1 ||
+        a.Ls > kLazyMaxLevels)
+        return -1;
+    const size_t smem = lazy_br_smem_bytes(a.N, a.torus_bits, a.n, a.L, a.Ls);
+    auto go = [&](auto kern) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+        kern<<<a.count, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    };
+    if (a.torus_bits == 32) return go(lazy_blind_rotate_kernel<32>);
+    if (a.torus_bits == 56) return go(lazy_blind_rotate_kernel<56>);
+    return -1;
 }
 
 int launch_keyswitch(const KsArgs& a, void* stream) {

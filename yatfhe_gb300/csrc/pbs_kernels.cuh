@@ -124,6 +124,40 @@ struct KeygenKskArgs {
     int n, kN, t, ks_radix_bits;
 };
 
+// The lazy ("OURS") blind rotation of blindRotateLazyPipeAltNtt with its extraction, one
+// ciphertext per CTA of N/2 threads, k = 1.  The key stays as the reference keeps it: the
+// half TRGSW rows in the coefficient domain (torus words) and the NTT-domain s2 key; every
+// CMux step rebuilds the rows of its TRGSW for the ciphertext from them.
+constexpr int kLazyMaxLevels = 8;  // levels of the half rows (l_approx) and of the s2 key
+struct LazyBrArgs {
+    const int32_t* lwe_in;   // [count][n+1]
+    const int64_t* lut;      // [N] test polynomial v (torus, sign-extended)
+    const void* cprime;      // [n][L][2][N] half rows (a, b): int32 words at T = 32, int64 at T = 56
+    const uint64_t* s2;      // [Ls][2][N] NTT-domain s2 key mod q
+    const uint64_t* s2p;     // [Ls][2][N] floor(s2 2^64 / q)
+    const uint64_t* wf;      // [N] psi^brv(k) mod q, and Shoup companions
+    const uint64_t* wfp;
+    const uint64_t* wi;      // [N] psi^-brv(k) mod q, and Shoup companions
+    const uint64_t* wip;
+    uint64_t q;
+    uint64_t qinv;           // q^-1 mod 2^64 (Montgomery products)
+    uint64_t post, postp;    // N^-1 2^64 mod q and its Shoup companion
+    uint64_t recomp[kLazyMaxLevels];   // 2^(T - (l'+1) radix) as a torus value, lifted mod q
+    uint64_t recompp[kLazyMaxLevels];  // Shoup companions
+    int32_t* big_out;        // [count][N + 1] extracted LWE, or null
+    int64_t* acc_out;        // [count][2 N] accumulator, or null
+    int count, n, N, L, Ls, radix_bits, torus_bits;
+};
+// Shared memory of one CTA: the transform buffer, the accumulator, int16 digits of
+// max(L, Ls) levels and the mod-2N input.
+__host__ __device__ inline size_t lazy_br_smem_bytes(int N, int torus_bits, int n, int L, int Ls) {
+    size_t b = (size_t)N * 8;
+    b += 2 * (size_t)N * (torus_bits == 32 ? 4 : 8);
+    b += (size_t)(L > Ls ? L : Ls) * N * 2;
+    b += ((size_t)n + 1) * 2;
+    return (b + 15) & ~(size_t)15;
+}
+
 // u32 words of one (step, level, row, channel) block of the device key: 2 output polys.
 __host__ __device__ inline size_t key_block_words(int N) { return 2 * (size_t)N; }
 __host__ __device__ inline size_t key_words(int n, int L, int N) {
@@ -185,5 +219,6 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 constexpr int kNoVariant = -2;
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
 int launch_keyswitch(const KsArgs& a, void* stream);
+int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream);
 
 }  // namespace yg
