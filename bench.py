@@ -412,6 +412,97 @@ def leg_wwl24(dev, steps=2, warmup=1, count=16384):
             "key_device_bytes": key.device_bytes}
 
 
+def leg_lazy(dev, steps=3, warmup=1, count=1216, cpu_sample=16):
+    """Lazy ("OURS") keys on the reference's default TORUS=32 set (n=680, N=2048, B=2^4,
+    lApprox=4, s2 key with l=8 levels, KS 2^2 x 16): seeded synthetic half rows (uniform torus
+    words, like a real key's coefficient-domain rows) and s2 key (uniform mod q), uploaded
+    through yg_key_upload_lazy, then `count` bootstraps per step through
+    yg_blind_rotate_extract (lazy_blind_rotate_kernel) and yg_keyswitch.  Reports the device
+    key bytes beside the GINX key's, the upload time, the throughput, and the CPU restatement
+    of blindRotateLazyPipeAltNtt on a `cpu_sample`-ciphertext sample with all host threads
+    (also the bit-exact check of that sample)."""
+    import torch
+
+    from yatfhe_gb300 import _lib, api
+    from yatfhe_gb300.params import WWL24_T32_N2048 as p
+
+    rng = np.random.default_rng(0x5EED000A)
+    row = (p.k + 1) * p.N
+    cprime = rng.integers(-(1 << 31), 1 << 31, size=p.n * p.l_approx * row, dtype=np.int64)
+    s2 = rng.integers(0, p.q_ntt, size=p.l * row, dtype=np.uint64)
+    ksk = rng.integers(-(1 << 31), 1 << 31, size=p.ksk_words, dtype=np.int64).astype(np.int32)
+    ctx = api.Context(p, dev)
+    uploads = []
+    for _ in range(3):  # the first call also pays one-time setup; the best of three is reported
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        key = api.BootstrapKey.from_lazy_words(ctx, cprime, s2)
+        uploads.append(time.perf_counter() - t0)
+        key.close()
+    key = api.BootstrapKey.from_lazy_words(ctx, cprime, s2).set_ksk(ksk)
+    lwe = synthetic_lwe(p, count, 0x5EED000B)
+    lut = workload_lut(p)
+    d_in = torch.from_numpy(lwe).to(f"cuda:{dev}")
+    d_lut = torch.from_numpy(lut).to(f"cuda:{dev}")
+    d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
+    d_out = torch.empty_like(d_in)
+    L = _lib.lib()
+    stream = torch.cuda.Stream(device=dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps + 2)]
+
+    def step(e0=None, e1=None):
+        _lib.check(L.yg_blind_rotate_extract(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
+                                             ctypes.c_void_p(d_lut.data_ptr()), ctypes.c_void_p(d_big.data_ptr()),
+                                             count, sh))
+        if e1 is not None:
+            e1.record(stream)
+        _lib.check(L.yg_keyswitch(ctx.handle, key.handle, ctypes.c_void_p(d_big.data_ptr()),
+                                  ctypes.c_void_p(d_out.data_ptr()), count, sh))
+
+    for _ in range(warmup):
+        step()
+    stream.synchronize()
+    ev[0].record(stream)
+    marks = []
+    for i in range(steps):
+        b0 = ev[2 + 2 * i]
+        b0.record(stream)
+        step(e1=ev[3 + 2 * i])
+        marks.append((b0, ev[3 + 2 * i]))
+    ev[1].record(stream)
+    stream.synchronize()
+    ms = ev[0].elapsed_time(ev[1])
+    br_ms = sum(x.elapsed_time(y) for x, y in marks) / steps
+    value = count * steps / (ms / 1e3)
+    # CPU baseline: the restatement of the lazy bootstrap, all host threads, on a sample
+    from oracle.oracle import Restatement
+
+    threads = os.cpu_count() or 1
+    ora = Restatement(p)
+    ora.set_lazy(cprime.reshape(p.n, p.l_approx, p.k + 1, p.N), s2.reshape(p.l, p.k + 1, p.N))
+    ora.set_ksk(ksk)
+    t0 = time.perf_counter()
+    cpu_out = ora.pbs_lazy(lwe[:cpu_sample], lut, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    bit_exact = bool(np.array_equal(cpu_out, d_out[:cpu_sample].cpu().numpy()))
+    # butterflies of the kernel's transforms per bootstrap: per CMux step L batches of Ls + 3
+    # forward transforms and one batch of 2 inverse ones, N/2 log2 N butterflies each
+    logn = p.N.bit_length() - 1
+    bfly = (p.n - 1) * (p.l_approx * (p.l + 3) + 2) * (p.N // 2) * logn
+    return {"workload": f"lazy_t32_n2048_batch{count}", "params": dict(params_config(p), s2_levels=p.l),
+            "ciphertexts_per_step": count, "value": value, "unit": "bootstraps/s", "steps": steps,
+            "ms_per_step": ms / steps, "blind_rotate_ms_per_step": br_ms,
+            "transform_butterflies_per_bootstrap": bfly,
+            "butterflies_per_s": bfly * count / (br_ms / 1e3),
+            "key_upload_s": min(uploads), "key_upload_s_all": uploads,
+            "key_device_bytes": key.device_bytes, "ginx_key_device_bytes_same_set": p.n * p.l_approx * 4 * 3 * p.N * 4,
+            "cpu_baseline": {"value": cpu_sample / cpu_s, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+                             "sample": f"{cpu_sample} of the step's ciphertexts, restatement of "
+                                       "blindRotateLazyPipeAltNtt + extraction + key switching"},
+            "sample_bit_exact": bit_exact}
+
+
 def leg_keygen(dev, reps=3):
     """Key generation on the GPU for the TORUS=32 set (n=630, N=1024): seeded synthetic
     samples with the distributions of real ones (binary secrets, TUniform(2^8) / (2^18)
@@ -792,6 +883,7 @@ def main():
             "t56_n2048_batch16384": _safe(leg_t56, dev),
             "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
             "keygen_t32_n1024": _safe(leg_keygen, dev),
+            "lazy_t32_n2048_batch1216": _safe(leg_lazy, dev),
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
             "serving_t32_128tenants_4GB": _safe(
                 leg_serving, dev, requests=args.serving_requests,

@@ -15,6 +15,7 @@
 //   blindRotateMP21Ntt             yatfhe/include/yatfhe/blind_rotate.h:69
 //   blindRotateJP22Ntt             yatfhe/include/yatfhe/blind_rotate.h:65 (binary keys)
 //   blindRotateWWL24Ntt            yatfhe/include/yatfhe/blind_rotate.h:61
+//   blindRotateLazyPipeAltNtt      yatfhe/include/yatfhe/blind_rotate.h:44-45
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
 // plus a batched form of the first, which the reference does not have.
 #ifndef YATFHE_GB300_REFERENCE_HPP
@@ -144,6 +145,32 @@ inline yg_key* device_key_wwl24(yg_ctx* c, const BootstrappingKeyWWL24& bsk, int
     return key;
 }
 
+// BootstrappingKeyMPLazyPipeAlt (yatfhe/include/yatfhe/bootstrapping.h:284-307) -> device key:
+// the half rows bskPrime[i].cPrime [n][l][k+1][N] as torus values and the s2 key
+// [levels][k+1][N]; the device keeps both as they are.
+inline yg_key* device_key_lazy(yg_ctx* c, const BootstrappingKeyMPLazyPipeAlt& bsk, int k, int N) {
+    auto& r = reg();
+    auto it = r.keys.find(&bsk);
+    if (it != r.keys.end()) return it->second;
+    std::vector<int64_t> cprime;
+    std::vector<uint64_t> s2;
+    for (const auto& g : bsk.bskPrime)
+        for (const auto& t : g.cPrime)
+            for (int poly = 0; poly <= k; poly++) {
+                const auto& P = poly < k ? t.a[poly] : t.b;
+                for (int j = 0; j < N; j++) cprime.push_back(static_cast<int64_t>(P.coeffs[j]));
+            }
+    for (const auto& t : bsk.s2Dft.trlweDfts)
+        for (int poly = 0; poly <= k; poly++) {
+            const auto& P = poly < k ? t.a[poly] : t.b;
+            s2.insert(s2.end(), P.coeffs.begin(), P.coeffs.begin() + N);
+        }
+    yg_key* key = nullptr;
+    check(yg_key_upload_lazy(c, cprime.data(), s2.data(), static_cast<int>(bsk.s2Dft.trlweDfts.size()), &key));
+    r.keys[&bsk] = key;
+    return key;
+}
+
 template <typename T>
 struct DeviceBuf {
     T* p = nullptr;
@@ -236,6 +263,39 @@ inline void blindRotateWWL24Ntt(Trlwe& accum, const BootstrappingKeyWWL24& bsk, 
     yg_ctx* c = detail::context(detail::params_of(param, levels));
     yg_key* key = detail::device_key_wwl24(c, bsk, param.k, param.N);
     detail::rotate_accumulator(c, key, accum, input, param);
+}
+
+// blindRotateLazyPipeAltNtt: accum receives the lazy blind rotation of input with test
+// polynomial v (the rotation builds its accumulator from v, as the reference's does).
+// gdVntt, prepareGdV(v) in the reference, is derived from v on the GPU and not read.
+inline void blindRotateLazyPipeAltNtt(Trlwe& accum, const BootstrappingKeyMPLazyPipeAlt& bsk, const ScaledTlwe& input,
+                                      const TorusPolynomial& v, const std::vector<NttPolynomial>& gdVntt,
+                                      const YatfheParameters& param) {
+    (void)gdVntt;
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    const int n = param.n, N = param.N, k = param.k;
+    const int levels = bsk.bskPrime.empty() ? param.lApprox : bsk.bskPrime[0].l;
+    yg_ctx* c = detail::context(detail::params_of(param, levels));
+    yg_key* key = detail::device_key_lazy(c, bsk, k, N);
+    // the mod-2N input as 32-bit words that switch back to the same values: x 2^(32 - log2(2N))
+    int sh = 32;
+    for (int m = 2 * N; m > 1; m >>= 1) sh--;
+    std::vector<int32_t> words(static_cast<size_t>(n) + 1);
+    for (int i = 0; i < n; i++) words[i] = static_cast<int32_t>(static_cast<uint32_t>(input.a[i]) << sh);
+    words[n] = static_cast<int32_t>(static_cast<uint32_t>(input.b) << sh);
+    std::vector<int64_t> lut(N), acc(static_cast<size_t>(k + 1) * N);
+    for (int j = 0; j < N; j++) lut[j] = static_cast<int64_t>(v.coeffs[j]);
+    detail::DeviceBuf<int32_t> d_in(words.size());
+    detail::DeviceBuf<int64_t> d_lut(lut.size());
+    detail::DeviceBuf<int64_t> d_acc(acc.size());
+    detail::cuda(cudaMemcpy(d_in.p, words.data(), words.size() * 4, cudaMemcpyHostToDevice));
+    detail::cuda(cudaMemcpy(d_lut.p, lut.data(), lut.size() * 8, cudaMemcpyHostToDevice));
+    detail::check(yg_blind_rotate(c, key, d_in.p, d_lut.p, d_acc.p, 1, n, nullptr));
+    detail::cuda(cudaMemcpy(acc.data(), d_acc.p, acc.size() * 8, cudaMemcpyDeviceToHost));
+    for (int p = 0; p < k; p++)
+        for (int j = 0; j < N; j++) accum.a[p].coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(p) * N + j]);
+    for (int j = 0; j < N; j++) accum.b.coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(k) * N + j]);
 }
 
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,

@@ -357,11 +357,54 @@ __device__ __forceinline__ uint64_t montmul64(uint64_t x, uint64_t y, uint64_t q
     return hi >= mh ? hi - mh : hi + q - mh;
 }
 
+// M forward transforms mod q of the polynomials sw[k N .. k N + N), k < M, in the convention
+// of q_forward_in_smem, sharing each stage's twiddle loads and barrier.  Ends synchronised.
+__device__ void q_forward_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
+                                uint64_t q) {
+    for (int s = 0; s < logN; ++s) {
+        const int m = 1 << s, lt = logN - 1 - s, t = 1 << lt;
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int i = b >> lt, j = b & (t - 1);
+            const int xi = (i << (lt + 1)) + j;
+            const uint64_t W = w[m + i], Wp = wp[m + i];
+            for (int k = 0; k < M; ++k) {
+                uint64_t* p = sw + (size_t)k * N;
+                const uint64_t u = p[xi], v = mulshoup64(p[xi + t], W, Wp, q);
+                const uint64_t sum = u + v;
+                p[xi] = sum >= q ? sum - q : sum;
+                p[xi + t] = u >= v ? u - v : u + q - v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// M inverse transforms mod q (the convention of q_inverse_in_smem, no N^-1), batched as above.
+__device__ void q_inverse_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
+                                uint64_t q) {
+    for (int lt = 0; lt < logN; ++lt) {
+        const int t = 1 << lt, h = N >> (lt + 1);
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int i = b >> lt, j = b & (t - 1);
+            const int xi = (i << (lt + 1)) + j;
+            const uint64_t W = w[h + i], Wp = wp[h + i];
+            for (int k = 0; k < M; ++k) {
+                uint64_t* p = sw + (size_t)k * N;
+                const uint64_t u = p[xi], v = p[xi + t];
+                const uint64_t sum = u + v;
+                p[xi] = sum >= q ? sum - q : sum;
+                p[xi + t] = mulshoup64(u >= v ? u - v : u + q - v, W, Wp, q);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-1135) and the extraction, one
 // ciphertext per CTA of N/2 threads; thread t owns coefficients and transform slots t and
-// t + N/2.  The arithmetic is the reference's: words mod q, transformed in shared memory by
-// q_forward_in_smem / q_inverse_in_smem (HEXL's negacyclic convention), products with key
-// words or constants by Shoup multiplication, products of two computed words by Montgomery
+// t + N/2.  The arithmetic is the reference's: words mod q, transformed in shared memory in
+// HEXL's negacyclic convention (q_forward_batch / q_inverse_batch), products with key words
+// or constants by Shoup multiplication, products of two computed words by Montgomery
 // multiplication (whose 2^-64 the final N^-1 2^64 scaling removes).
 //   first component: acc = X^(-b) ((X^(a_0) - 1) derived + (0, v)), derived =
 //     INTT(sum_lvl NTT(digit lvl of v) . NTT(cPrime_0[lvl]))        (:1117-1124)
@@ -370,8 +413,10 @@ __device__ __forceinline__ uint64_t montmul64(uint64_t x, uint64_t y, uint64_t q
 //     cP.b[0] += 2^(T - (lvl+1) radix), and its mask digits D_l' (l' < Ls, transformed):
 //       cPrime.a = sum D_l' . 2^(T - (l'+1) radix),  cPrime.b = NTT(cP.b),
 //       c.a = sum D_l' . s2[l'].a + NTT(cP.b),       c.b = sum D_l' . s2[l'].b
-//     (stageA / stageB, :1036-1085).  Each level is built in registers and multiplied into the
-//     product at once: nothing of TRGSW_i is stored.
+//     (stageA / stageB, :1036-1085).  Per level the Ls digit polynomials, cP.b and the
+//     accumulator's two digit polynomials of that level go through one batch of Ls + 3
+//     transforms; the level's rows are then formed slot by slot in registers and multiplied
+//     into the product at once, so nothing of TRGSW_i is stored.
 template <int T>
 __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBrArgs a) {
     using TT = typename TorusOf<T>::type;
@@ -381,10 +426,10 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
     const int logN = 31 - __clz(N);
     const int ct = blockIdx.x;
     const uint64_t q = a.q, qinv = a.qinv;
-    uint64_t* sw = reinterpret_cast<uint64_t*>(lz_smem);                  // [N]
-    TT* acc = reinterpret_cast<TT*>(sw + N);                              // [2][N]
-    int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);               // [max(L, Ls)][N]
-    int16_t* sa = dig + (size_t)(L > Ls ? L : Ls) * N;                    // [n + 1]
+    const int M = Ls + 3;
+    uint64_t* sw = reinterpret_cast<uint64_t*>(lz_smem);                  // [Ls + 3][N]
+    TT* acc = reinterpret_cast<TT*>(sw + (size_t)M * N);                  // [2][N]
+    int16_t* sa = reinterpret_cast<int16_t*>(acc + 2 * N);                // [n + 1]
     const TT* cpr = static_cast<const TT*>(a.cprime);
     const int jj[2] = {t, t + H};
 
@@ -419,53 +464,57 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
         r %= 2 * N;
         return r < 0 ? r + 2 * N : r;
     };
-    auto forward = [&]() { q_forward_in_smem(sw, N, a.wf, a.wfp, q); };
-    auto inverse = [&]() { q_inverse_in_smem(sw, N, a.wi, a.wip, q); };
+    // digit `lvl` of the zero-mean decomposition of x into `levels` digits
+    auto digit_at = [rb](TT x, int levels, int lvl) {
+        int d = 0;
+        zero_mean_digits<U, T>((U)x, levels, rb, [&](int level, int v) {
+            if (level == lvl) d = v;
+        });
+        return d;
+    };
+    // both accumulator polynomials from the transform slots of sw[0..2N), scaled to the torus
+    auto inverse_to_acc = [&](const uint64_t (&h)[2][2]) {
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[poly * N + jj[e]] = h[poly][e];
+        __syncthreads();
+        q_inverse_batch(sw, 2, N, logN, a.wi, a.wip, q);
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = to_torus(sw[poly * N + jj[e]]);
+        __syncthreads();
+    };
 
     // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81)
     const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
     for (int i = t; i <= n; i += H) sa[i] = (int16_t)modswitch_down(in[i], 31 - logN, logN + 1);
-    // digits of v, L levels (prepareGdV, yatfhe/src/trgsw.cpp:911-927)
-#pragma unroll
-    for (int e = 0; e < 2; ++e) {
-        const int j = jj[e];
-        zero_mean_digits<U, T>((U)(TT)a.lut[j], L, rb, [&](int level, int d) { dig[level * N + j] = (int16_t)d; });
-    }
 
-    // first component (deriveFirstComponentNtt, yatfhe/src/trgsw.cpp:929-955)
+    // first component (deriveFirstComponentNtt, yatfhe/src/trgsw.cpp:929-955, with the digits
+    // of v that prepareGdV transforms, :911-927)
     {
         uint64_t h[2][2] = {{0, 0}, {0, 0}};
         for (int lvl = 0; lvl < L; ++lvl) {
-            uint64_t V[2];
+            const TT* src = cpr + (size_t)lvl * 2 * N;  // key index 0
 #pragma unroll
-            for (int e = 0; e < 2; ++e) sw[jj[e]] = lift(dig[lvl * N + jj[e]]);
+            for (int e = 0; e < 2; ++e) {
+                const int j = jj[e];
+                sw[j] = lift(digit_at((TT)a.lut[j], L, lvl));
+                sw[N + j] = lift((int64_t)src[j]);
+                sw[2 * N + j] = lift((int64_t)src[N + j]);
+            }
             __syncthreads();
-            forward();
+            q_forward_batch(sw, 3, N, logN, a.wf, a.wfp, q);
 #pragma unroll
-            for (int e = 0; e < 2; ++e) V[e] = sw[jj[e]];
-#pragma unroll
-            for (int poly = 0; poly < 2; ++poly) {
-                __syncthreads();
-                const TT* src = cpr + ((size_t)lvl * 2 + poly) * N;  // key index 0
-#pragma unroll
-                for (int e = 0; e < 2; ++e) sw[jj[e]] = lift((int64_t)src[jj[e]]);
-                __syncthreads();
-                forward();
-#pragma unroll
-                for (int e = 0; e < 2; ++e) h[poly][e] = addq(h[poly][e], montmul64(V[e], sw[jj[e]], q, qinv));
+            for (int e = 0; e < 2; ++e) {
+                const int j = jj[e];
+                h[0][e] = addq(h[0][e], montmul64(sw[j], sw[N + j], q, qinv));
+                h[1][e] = addq(h[1][e], montmul64(sw[j], sw[2 * N + j], q, qinv));
             }
             __syncthreads();
         }
-#pragma unroll
-        for (int poly = 0; poly < 2; ++poly) {
-#pragma unroll
-            for (int e = 0; e < 2; ++e) sw[jj[e]] = h[poly][e];
-            __syncthreads();
-            inverse();
-#pragma unroll
-            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = to_torus(sw[jj[e]]);
-            __syncthreads();
-        }
+        inverse_to_acc(h);
         TT tv[2][2];
         const int r0 = norm(sa[0]);
 #pragma unroll
@@ -507,79 +556,42 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
             TT one;
             if constexpr (T == 32) one = (int32_t)((uint32_t)1 << sh);
             else one = sext<56>((int64_t)1 << sh);
-            TT bp[2];
-            // stageA: rotateTrlweMinusOneBPlusOne, then the mask's Ls digits (decomposeRow)
+            // stageA (rotateTrlweMinusOneBPlusOne, then the mask's Ls digits, decomposeRow) and
+            // the accumulator's digits of this level: the inputs of the level's transforms
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int j = jj[e];
                 const TT ra = tsub<T>(rot_at(cp, r, j), cp[j]);
                 TT rbv = tsub<T>(rot_at(cp + N, r, j), cp[N + j]);
                 if (j == 0) rbv = tadd<T>(rbv, one);
-                bp[e] = rbv;
-                zero_mean_digits<U, T>((U)ra, Ls, rb, [&](int level, int d) { dig[level * N + j] = (int16_t)d; });
+                zero_mean_digits<U, T>((U)ra, Ls, rb, [&](int level, int d) { sw[(size_t)level * N + j] = lift(d); });
+                sw[(size_t)Ls * N + j] = lift((int64_t)rbv);
+                sw[(size_t)(Ls + 1) * N + j] = lift(digit_at(acc[j], L, lvl));
+                sw[(size_t)(Ls + 2) * N + j] = lift(digit_at(acc[N + j], L, lvl));
             }
-            // stageB: the level's rows, slot by slot in registers
-            uint64_t ca[2] = {0, 0}, cb[2] = {0, 0}, cpa[2] = {0, 0}, bh[2];
-            for (int gl = 0; gl < Ls; ++gl) {
-#pragma unroll
-                for (int e = 0; e < 2; ++e) sw[jj[e]] = lift(dig[gl * N + jj[e]]);
-                __syncthreads();
-                forward();
-                const uint64_t* s2a = a.s2 + (size_t)gl * 2 * N;
-                const uint64_t* s2pa = a.s2p + (size_t)gl * 2 * N;
-                const uint64_t rc = a.recomp[gl], rcp = a.recompp[gl];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int j = jj[e];
-                    const uint64_t D = sw[j];
-                    ca[e] = addq(ca[e], mulshoup64(D, s2a[j], s2pa[j], q));
-                    cb[e] = addq(cb[e], mulshoup64(D, s2a[N + j], s2pa[N + j], q));
-                    cpa[e] = addq(cpa[e], mulshoup64(D, rc, rcp, q));
-                }
-                __syncthreads();
-            }
-#pragma unroll
-            for (int e = 0; e < 2; ++e) sw[jj[e]] = lift((int64_t)bp[e]);
             __syncthreads();
-            forward();
+            q_forward_batch(sw, M, N, logN, a.wf, a.wfp, q);
+            // stageB slot by slot, and the level's share of the external product
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                bh[e] = sw[jj[e]];
-                ca[e] = addq(ca[e], bh[e]);
-            }
-            // the accumulator's digits of this level against the level's rows
-#pragma unroll
-            for (int poly = 0; poly < 2; ++poly) {
-                __syncthreads();
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    int d = 0;
-                    zero_mean_digits<U, T>((U)acc[poly * N + jj[e]], L, rb, [&](int level, int x) {
-                        if (level == lvl) d = x;
-                    });
-                    sw[jj[e]] = lift(d);
+                const int j = jj[e];
+                uint64_t ca = 0, cb = 0, cpa = 0;
+                for (int gl = 0; gl < Ls; ++gl) {
+                    const uint64_t D = sw[(size_t)gl * N + j];
+                    const size_t o = (size_t)gl * 2 * N + j;
+                    ca = addq(ca, mulshoup64(D, a.s2[o], a.s2p[o], q));
+                    cb = addq(cb, mulshoup64(D, a.s2[o + N], a.s2p[o + N], q));
+                    cpa = addq(cpa, mulshoup64(D, a.recomp[gl], a.recompp[gl], q));
                 }
-                __syncthreads();
-                forward();
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const uint64_t X = sw[jj[e]];
-                    acch[0][e] = addq(acch[0][e], montmul64(X, poly == 0 ? ca[e] : cpa[e], q, qinv));
-                    acch[1][e] = addq(acch[1][e], montmul64(X, poly == 0 ? cb[e] : bh[e], q, qinv));
-                }
+                const uint64_t bh = sw[(size_t)Ls * N + j];
+                ca = addq(ca, bh);
+                const uint64_t xa = sw[(size_t)(Ls + 1) * N + j], xb = sw[(size_t)(Ls + 2) * N + j];
+                acch[0][e] = addq(acch[0][e], addq(montmul64(xa, ca, q, qinv), montmul64(xb, cpa, q, qinv)));
+                acch[1][e] = addq(acch[1][e], addq(montmul64(xa, cb, q, qinv), montmul64(xb, bh, q, qinv)));
             }
             __syncthreads();
         }
-#pragma unroll
-        for (int poly = 0; poly < 2; ++poly) {
-#pragma unroll
-            for (int e = 0; e < 2; ++e) sw[jj[e]] = acch[poly][e];
-            __syncthreads();
-            inverse();
-#pragma unroll
-            for (int e = 0; e < 2; ++e) acc[poly * N + jj[e]] = to_torus(sw[jj[e]]);
-            __syncthreads();
-        }
+        inverse_to_acc(acch);
     }
 
     if (a.acc_out) {

@@ -148,12 +148,12 @@ struct LazyBrArgs {
     int64_t* acc_out;        // [count][2 N] accumulator, or null
     int count, n, N, L, Ls, radix_bits, torus_bits;
 };
-// Shared memory of one CTA: the transform buffer, the accumulator, int16 digits of
-// max(L, Ls) levels and the mod-2N input.
+// Shared memory of one CTA: Ls + 3 polynomials of transform words (a level's batch), the
+// accumulator and the mod-2N input (193 KB at N = 2048, T = 32, Ls = 8).
 __host__ __device__ inline size_t lazy_br_smem_bytes(int N, int torus_bits, int n, int L, int Ls) {
-    size_t b = (size_t)N * 8;
+    (void)L;
+    size_t b = (size_t)(Ls + 3) * N * 8;
     b += 2 * (size_t)N * (torus_bits == 32 ? 4 : 8);
-    b += (size_t)(L > Ls ? L : Ls) * N * 2;
     b += ((size_t)n + 1) * 2;
     return (b + 15) & ~(size_t)15;
 }
