@@ -357,10 +357,19 @@ __device__ __forceinline__ uint64_t montmul64(uint64_t x, uint64_t y, uint64_t q
     return hi >= mh ? hi - mh : hi + q - mh;
 }
 
+// x w mod q up to one multiple of q: x w - floor(x wp / 2^64) q is in [0, 2q) for any
+// 64-bit x, w < q, wp = floor(w 2^64 / q) (Shoup without the final correction).
+__device__ __forceinline__ uint64_t mulshoup64_lazy(uint64_t x, uint64_t w, uint64_t wp, uint64_t q) {
+    return x * w - __umul64hi(x, wp) * q;
+}
+
 // M forward transforms mod q of the polynomials sw[k N .. k N + N), k < M, in the convention
-// of q_forward_in_smem, sharing each stage's twiddle loads and barrier.  Ends synchronised.
+// of q_forward_in_smem, sharing each stage's twiddle loads and barrier.  Harvey's lazy
+// butterflies: words in [0, 4q) in and out (4q < 2^64 for both moduli), so the results are
+// the transform's values up to multiples of q.  Ends synchronised.
 __device__ void q_forward_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
                                 uint64_t q) {
+    const uint64_t q2 = 2 * q;
     for (int s = 0; s < logN; ++s) {
         const int m = 1 << s, lt = logN - 1 - s, t = 1 << lt;
         for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
@@ -369,19 +378,22 @@ __device__ void q_forward_batch(uint64_t* sw, int M, int N, int logN, const uint
             const uint64_t W = w[m + i], Wp = wp[m + i];
             for (int k = 0; k < M; ++k) {
                 uint64_t* p = sw + (size_t)k * N;
-                const uint64_t u = p[xi], v = mulshoup64(p[xi + t], W, Wp, q);
-                const uint64_t sum = u + v;
-                p[xi] = sum >= q ? sum - q : sum;
-                p[xi + t] = u >= v ? u - v : u + q - v;
+                uint64_t u = p[xi];
+                u = u >= q2 ? u - q2 : u;
+                const uint64_t v = mulshoup64_lazy(p[xi + t], W, Wp, q);
+                p[xi] = u + v;
+                p[xi + t] = u + q2 - v;
             }
         }
         __syncthreads();
     }
 }
 
-// M inverse transforms mod q (the convention of q_inverse_in_smem, no N^-1), batched as above.
+// M inverse transforms mod q (the convention of q_inverse_in_smem, no N^-1), batched as above,
+// with lazy butterflies on words in [0, 2q) in and out.
 __device__ void q_inverse_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
                                 uint64_t q) {
+    const uint64_t q2 = 2 * q;
     for (int lt = 0; lt < logN; ++lt) {
         const int t = 1 << lt, h = N >> (lt + 1);
         for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
@@ -392,8 +404,8 @@ __device__ void q_inverse_batch(uint64_t* sw, int M, int N, int logN, const uint
                 uint64_t* p = sw + (size_t)k * N;
                 const uint64_t u = p[xi], v = p[xi + t];
                 const uint64_t sum = u + v;
-                p[xi] = sum >= q ? sum - q : sum;
-                p[xi + t] = mulshoup64(u >= v ? u - v : u + q - v, W, Wp, q);
+                p[xi] = sum >= q2 ? sum - q2 : sum;
+                p[xi + t] = mulshoup64_lazy(u + q2 - v, W, Wp, q);
             }
         }
         __syncthreads();
@@ -438,7 +450,14 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
         const uint64_t s = x + y;
         return s >= q ? s - q : s;
     };
-    // applyIntt's last steps (yatfhe/src/ntt_hexl.cpp:153-175): scale, centre, low T bits.
+    const uint64_t q2 = 2 * q;
+    // a forward transform's word (in [0, 4q)) reduced to [0, q)
+    auto red4 = [q, q2](uint64_t x) -> uint64_t {
+        x = x >= q2 ? x - q2 : x;
+        return x >= q ? x - q : x;
+    };
+    // applyIntt's last steps (yatfhe/src/ntt_hexl.cpp:153-175): scale, centre, low T bits
+    // (the word, in [0, 2q) after the lazy inverse transform, is reduced by the product).
     auto to_torus = [&](uint64_t v) -> TT {
         v = mulshoup64(v, a.post, a.postp, q);
         const int64_t c = v >= (q + 1) / 2 ? (int64_t)(v - q) : (int64_t)v;
@@ -509,8 +528,9 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int j = jj[e];
-                h[0][e] = addq(h[0][e], montmul64(sw[j], sw[N + j], q, qinv));
-                h[1][e] = addq(h[1][e], montmul64(sw[j], sw[2 * N + j], q, qinv));
+                const uint64_t V = red4(sw[j]);
+                h[0][e] = addq(h[0][e], montmul64(V, red4(sw[N + j]), q, qinv));
+                h[1][e] = addq(h[1][e], montmul64(V, red4(sw[2 * N + j]), q, qinv));
             }
             __syncthreads();
         }
@@ -575,17 +595,24 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int j = jj[e];
+                // sums kept in [0, 2q): lazy products of the raw [0, 4q) words
+                auto add2 = [q2](uint64_t x, uint64_t y) -> uint64_t {
+                    const uint64_t s = x + y;
+                    return s >= q2 ? s - q2 : s;
+                };
                 uint64_t ca = 0, cb = 0, cpa = 0;
                 for (int gl = 0; gl < Ls; ++gl) {
                     const uint64_t D = sw[(size_t)gl * N + j];
                     const size_t o = (size_t)gl * 2 * N + j;
-                    ca = addq(ca, mulshoup64(D, a.s2[o], a.s2p[o], q));
-                    cb = addq(cb, mulshoup64(D, a.s2[o + N], a.s2p[o + N], q));
-                    cpa = addq(cpa, mulshoup64(D, a.recomp[gl], a.recompp[gl], q));
+                    ca = add2(ca, mulshoup64_lazy(D, a.s2[o], a.s2p[o], q));
+                    cb = add2(cb, mulshoup64_lazy(D, a.s2[o + N], a.s2p[o + N], q));
+                    cpa = add2(cpa, mulshoup64_lazy(D, a.recomp[gl], a.recompp[gl], q));
                 }
-                const uint64_t bh = sw[(size_t)Ls * N + j];
-                ca = addq(ca, bh);
-                const uint64_t xa = sw[(size_t)(Ls + 1) * N + j], xb = sw[(size_t)(Ls + 2) * N + j];
+                const uint64_t bh = red4(sw[(size_t)Ls * N + j]);
+                ca = addq(ca >= q ? ca - q : ca, bh);
+                cb = cb >= q ? cb - q : cb;
+                cpa = cpa >= q ? cpa - q : cpa;
+                const uint64_t xa = red4(sw[(size_t)(Ls + 1) * N + j]), xb = red4(sw[(size_t)(Ls + 2) * N + j]);
                 acch[0][e] = addq(acch[0][e], addq(montmul64(xa, ca, q, qinv), montmul64(xb, cpa, q, qinv)));
                 acch[1][e] = addq(acch[1][e], addq(montmul64(xa, cb, q, qinv), montmul64(xb, bh, q, qinv)));
             }
