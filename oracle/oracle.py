@@ -201,6 +201,21 @@ class _Common:
         return cprime, s2
 
 
+    # Group-g keys of blindRotateNtt: TrgswDft words [keys][l][k+1][k+1][N].
+    def group_key_count(self, group: int) -> int:
+        return self.p.n if group == 1 else (self.p.n // group) << group
+
+    def keygen_group(self, seed: int, group: int) -> None:
+        self._call("keygen_group", ctypes.c_uint64(seed), group)
+        self._group = group
+
+    def group_words(self) -> np.ndarray:
+        p, g = self.p, self._group
+        out = np.zeros((self.group_key_count(g), p.l, p.k + 1, p.k + 1, p.N), np.uint64)
+        self._call("get_group" if self.prefix == "po_" else "export_group", _ptr(out, _u64p))
+        return out
+
+
 class Restatement(_Common):
     """The plain-C oracle for one parameter set."""
 
@@ -296,6 +311,27 @@ class Restatement(_Common):
         b = np.ascontiguousarray(s2, np.uint64)
         self._call("set_lazy", _ptr(a, _i64p), _ptr(b, _u64p))
 
+    def set_group(self, words, group: int) -> None:
+        a = np.ascontiguousarray(words, np.uint64)
+        self._call("set_group", _ptr(a, _u64p), group)
+        self._group = group
+
+    def blind_rotate_group(self, lwe, v) -> np.ndarray:
+        """The accumulator [(k+1) N] after blindRotateNtt on the group key, one ciphertext."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
+        self._call("blind_rotate_group", _ptr(lwe, _i32p), _ptr(v, _i64p), _ptr(acc, _i64p))
+        return acc
+
+    def pbs_group(self, lwe, v, threads: int = 1) -> np.ndarray:
+        """functionalBootstrappingNtt on the group key."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        self._call("pbs_group", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), threads)
+        return out
+
     def save_lazy_file(self, path) -> None:
         self._call("save_lazy_file", str(path).encode())
 
@@ -373,6 +409,16 @@ class Reference(_Common):
         out = np.zeros_like(lwe)
         acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
         self._call("pbs_wwl24", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
+        return (out, acc) if with_acc else out
+
+    def pbs_group(self, lwe, v, with_acc: bool = False):
+        """functionalBootstrappingNtt's composition on the group key; with_acc also returns
+        ciphertext 0's accumulator after blindRotateNtt."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
+        self._call("pbs_group", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
         return (out, acc) if with_acc else out
 
     def save_lazy_file(self, path) -> None:

@@ -152,6 +152,8 @@ struct po_ctx {
     uint64_t* wwl_cprime;/* WWL+24 key: [n][L][k+1][N] (allocated on first use) */
     uint64_t* wwl_s2;    /* [l][k+1][N] (also the s2 key of the lazy family) */
     int64_t* lazy_cprime;/* lazy key: [n][L][k+1][N] coefficient-domain torus (allocated on first use) */
+    uint64_t* grp_bsk;   /* group-g key: [keys][l][k+1][k+1][N] NTT domain (allocated on first use) */
+    int grp;             /* its group g (0: none) */
     /* when set, po_keygen also records its random samples here (po_keygen_samples) */
     int32_t* rec_bsk_noise;   /* [n][L][k+1][N] */
     uint64_t* rec_bsk_mask;   /* [n][L][k+1][k][N] */
@@ -214,6 +216,7 @@ void po_destroy(po_ctx* c) {
     free(c->wwl_cprime);
     free(c->wwl_s2);
     free(c->lazy_cprime);
+    free(c->grp_bsk);
     free(c);
 }
 
@@ -808,11 +811,12 @@ typedef struct {
     const int64_t* v;
     int32_t* out;
     int begin, end;
-    int lazy;  /* 1: blindRotateLazyPipeAltNtt on the lazy key */
+    int lazy;  /* 1: blindRotateLazyPipeAltNtt on the lazy key, 2: blindRotateNtt on the group key */
     int rc;
 } pbs_job;
 
 static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc);
+static int blind_rotate_group(const po_ctx* c, const int32_t* scaled, const int64_t* v, int64_t* acc);
 
 /* functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:71-80). */
 static void* pbs_worker(void* arg) {
@@ -830,7 +834,9 @@ static void* pbs_worker(void* arg) {
         j->rc = 0;
         for (int i = j->begin; i < j->end; i++) {
             po_modswitch(c, j->in + (size_t)i * nb, scaled);
-            if (j->lazy) {
+            if (j->lazy == 2) {
+                if (blind_rotate_group(c, scaled, j->v, acc)) { j->rc = -1; break; }
+            } else if (j->lazy) {
                 if (blind_rotate_lazy(c, &s, scaled, j->v, acc)) { j->rc = -1; break; }
             } else {
                 blind_rotate(c, &s, scaled, j->v, acc, NULL, 0, NULL);
@@ -1413,4 +1419,205 @@ int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t
 int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
     if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_pbs_lazy: no lazy key");
     return pbs_run(c, in, count, v, out, threads, 1);
+}
+
+/* ------------------------------------------------------------------ group keys */
+
+/*
+ * The key family of blindRotateNtt (BootstrappingKey, yatfhe/include/yatfhe/bootstrapping.h:16-45):
+ * TrgswDft rows [lvl < l][row <= k] (trgsw.h:121-135), one TRGSW per LWE coefficient for
+ * group 1, else 2^g per group of g coefficients, TRGSW k2 of a group encrypting
+ * [combined == k2] with combined = sum_i2 s_(i+i2) 2^(g-1-i2) (genBootstrappingKeyGroup,
+ * yatfhe/src/bootstrapping.cpp:16-38).
+ */
+static size_t grp_keys(const po_ctx* c, int g) {
+    return g == 1 ? (size_t)c->p.n : (size_t)(c->p.n / g) << g;
+}
+static size_t grp_trgsw_words(const po_ctx* c) {
+    const size_t k1 = (size_t)c->p.k + 1;
+    return (size_t)c->p.l * k1 * k1 * c->p.N;
+}
+
+static int grp_alloc(po_ctx* c, int g) {
+    if (g < 1 || g > 3 || c->p.n % g) return -1;
+    free(c->grp_bsk);
+    c->grp_bsk = (uint64_t*)calloc(grp_keys(c, g) * grp_trgsw_words(c), sizeof(uint64_t));
+    c->grp = c->grp_bsk ? g : 0;
+    return c->grp_bsk ? 0 : -1;
+}
+
+/* encryptTrgswNtt (yatfhe/src/trgsw.cpp:281-284): encZeroTrgswNtt (:185-191), one
+ * symEncTrlweSingleSampleNtt of 0 per (lvl, row) (yatfhe/src/trlwe.cpp:88-91: noise b, uniform
+ * masks, NTT-domain b + a . s), then addIntegerToTrgswNtt (:227-246): mu 2^(T-(lvl+1) radix)
+ * added to coefficient 0 of a[row] (row < k) or of b (row k) in the torus domain, that
+ * polynomial transformed again (its b comes back from applyIntt, reduced to T bits). */
+static void enc_trgsw_group(po_ctx* c, uint64_t* out, int mu, int64_t* tmpT, int64_t* zero) {
+    const int N = c->p.N, k = c->p.k, l = c->p.l, T = c->T;
+    const size_t row = (size_t)(k + 1) * N;
+    for (int lvl = 0; lvl < l; lvl++)
+        for (int r = 0; r <= k; r++) enc_trlwe_coef_ntt(c, out + ((size_t)lvl * (k + 1) + r) * row, zero, tmpT);
+    uint64_t* scratch = (uint64_t*)tmpT + 0;  /* reuses tmpT's storage as transform scratch */
+    for (int lvl = 0; lvl < l; lvl++) {
+        const int64_t g = sext((int64_t)mu << (T - (lvl + 1) * c->p.radix_bits), T);
+        for (int r = 0; r <= k; r++) {
+            uint64_t* poly = out + ((size_t)lvl * (k + 1) + r) * row + (size_t)r * N;  /* a[r], or b for r = k */
+            memcpy(scratch, poly, sizeof(uint64_t) * N);
+            intt_to_torus(c, zero, scratch);
+            zero[0] = sext(zero[0] + g, T);
+            ntt_from_torus(c, poly, zero);
+            memset(zero, 0, sizeof(int64_t) * N);
+        }
+    }
+}
+
+int po_keygen_group(po_ctx* c, uint64_t seed, int group) {
+    const int n = c->p.n, N = c->p.N;
+    if (grp_alloc(c, group)) return fail(c, "po_keygen_group: group must be 1, 2 or 3 and divide n");
+    int64_t* tmpT = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    int64_t* zero = (int64_t*)calloc((size_t)N, sizeof(int64_t));
+    if (!tmpT || !zero) {
+        free(tmpT); free(zero);
+        return fail(c, "po_keygen_group: out of memory");
+    }
+    keygen_secrets(c, seed, tmpT);
+    const size_t tw = grp_trgsw_words(c);
+    if (group == 1) {
+        for (int i = 0; i < n; i++) enc_trgsw_group(c, c->grp_bsk + (size_t)i * tw, c->lwe_s[i], tmpT, zero);
+    } else {
+        size_t j = 0;
+        for (int i = 0; i < n; i += group) {
+            int combined = 0;
+            for (int i2 = 0; i2 < group; i2++) combined |= c->lwe_s[i + i2] << (group - 1 - i2);
+            for (int k2 = 0; k2 < (1 << group); k2++, j++)
+                enc_trgsw_group(c, c->grp_bsk + j * tw, combined == k2, tmpT, zero);
+        }
+    }
+    free(tmpT);
+    free(zero);
+    keygen_ksk(c);
+    return 0;
+}
+
+int po_get_group(po_ctx* c, uint64_t* out) {
+    if (!c->grp_bsk) return fail(c, "po_get_group: no group key");
+    memcpy(out, c->grp_bsk, sizeof(uint64_t) * grp_keys(c, c->grp) * grp_trgsw_words(c));
+    return 0;
+}
+
+int po_set_group(po_ctx* c, const uint64_t* words, int group) {
+    if (grp_alloc(c, group)) return fail(c, "po_set_group: group must be 1, 2 or 3 and divide n");
+    memcpy(c->grp_bsk, words, sizeof(uint64_t) * grp_keys(c, group) * grp_trgsw_words(c));
+    return 0;
+}
+
+/* externalProductTrgswNtt (yatfhe/src/trgsw.cpp:550-576): every input polynomial decomposed
+ * into l digit polynomials (gadgetDecomposeTrlwe), the first `level` of them transformed and
+ * multiplied with key rows [lvl][col][col2], summed mod q, inverse transform.  key =
+ * [l][k+1][k+1][N]; in/out = [a_0..a_{k-1}, b], may alias. */
+static void ep_group(const po_ctx* c, const uint64_t* key, const int64_t* in, int64_t* out, int level,
+                     int64_t* digits, uint64_t* dntt, uint64_t* acc) {
+    const int N = c->p.N, k1 = c->p.k + 1, l = c->p.l;
+    const uint64_t q = c->q;
+    const size_t row = (size_t)k1 * N;
+    int64_t dg[64];
+    memset(acc, 0, sizeof(uint64_t) * row);
+    for (int col = 0; col < k1; col++) {
+        for (int j = 0; j < N; j++) {
+            zero_mean_digits((uint64_t)in[(size_t)col * N + j], l, c->p.radix_bits, c->T, dg);
+            for (int lv = 0; lv < level; lv++) digits[(size_t)lv * N + j] = dg[lv];
+        }
+        for (int lv = 0; lv < level; lv++) {
+            ntt_from_torus(c, dntt, digits + (size_t)lv * N);
+            const uint64_t* kr = key + ((size_t)lv * k1 + col) * row;
+            for (int o = 0; o < k1; o++)
+                for (int j = 0; j < N; j++)
+                    acc[(size_t)o * N + j] = addmod(acc[(size_t)o * N + j],
+                                                    nq_mulmod(&c->plan.br, dntt[j], kr[(size_t)o * N + j]), q);
+        }
+    }
+    for (int o = 0; o < k1; o++) intt_to_torus(c, out + (size_t)o * N, acc + (size_t)o * N);
+}
+
+/*
+ * blindRotateNtt (yatfhe/src/blind_rotate.cpp:549-560) on the group key, after
+ * genNoiselessTrlweSample:
+ *   group 1 (blindRotateNormalNtt, :202-212): for a_i != 0, acc += EP(K_i, X^(a_i) acc - acc)
+ *     (controlMuxNtt, yatfhe/src/cmux.cpp:16-21);
+ *   group g > 1 (blindRotateGroup2Ntt :264-324, blindRotateGroup3Ntt :398-488): per group of g
+ *     coefficients acc = EP(sum_k2 rotateTrgswNtt(K_k2, r_k2), acc), r_k2 the sum of the a's whose
+ *     bit is set in k2 (k2 = 1 is the last coefficient of the group); rotateTrgswNtt multiplies
+ *     each polynomial by NTT(+-X^r') (rotateNttPolynomial, yatfhe/src/polynomial.cpp:405-412,
+ *     with validateRotator's r' and sign; unchanged when r = 0 mod 2N).
+ * The external products use lApprox of the key's l levels.
+ */
+static int blind_rotate_group(const po_ctx* c, const int32_t* scaled, const int64_t* v, int64_t* acc) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, k1 = k + 1, l = c->p.l, L = c->L, g = c->grp;
+    const uint64_t q = c->q;
+    const size_t row = (size_t)k1 * N, tw = grp_trgsw_words(c), lvw = (size_t)k1 * row;
+    if (!c->grp_bsk || g < 1 || L > l || l > 64) return -1;
+    int64_t* digits = (int64_t*)malloc(sizeof(int64_t) * (size_t)L * N);
+    uint64_t* dntt = (uint64_t*)malloc(sizeof(uint64_t) * N);
+    uint64_t* hat = (uint64_t*)malloc(sizeof(uint64_t) * row);
+    int64_t* tmp = (int64_t*)malloc(sizeof(int64_t) * row);
+    int64_t* mono = (int64_t*)malloc(sizeof(int64_t) * N);
+    uint64_t* rot = (uint64_t*)malloc(sizeof(uint64_t) * N * 8);
+    uint64_t* comb = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)L * lvw);
+    int rc = -1;
+    if (!digits || !dntt || !hat || !tmp || !mono || !rot || !comb) goto out;
+    memset(acc, 0, sizeof(int64_t) * (size_t)k * N);
+    rotate_poly(c, acc + (size_t)k * N, v, -scaled[n], 0);
+    if (g == 1) {
+        for (int i = 0; i < n; i++) {
+            const int a = scaled[i];
+            if (a == 0) continue;
+            for (int r = 0; r < k1; r++) rotate_poly(c, tmp + (size_t)r * N, acc + (size_t)r * N, a, 1);
+            ep_group(c, c->grp_bsk + (size_t)i * tw, tmp, tmp, L, digits, dntt, hat);
+            for (size_t j = 0; j < row; j++) acc[j] = sext(acc[j] + tmp[j], c->T);
+        }
+    } else {
+        for (int i = 0; i < n; i += g) {
+            const uint64_t* keys = c->grp_bsk + (size_t)(i / g) * ((size_t)1 << g) * tw;
+            for (int k2 = 0; k2 < (1 << g); k2++) {
+                int r = 0;
+                for (int i2 = 0; i2 < g; i2++)
+                    if ((k2 >> (g - 1 - i2)) & 1) r += scaled[i + i2];
+                int t = r % (2 * N);
+                if (t < 0) t += 2 * N;
+                memset(mono, 0, sizeof(int64_t) * N);
+                if (t < N) mono[t] = 1; else mono[t - N] = -1;
+                ntt_from_torus(c, rot + (size_t)k2 * N, mono);
+            }
+            for (int lv = 0; lv < L; lv++)
+                for (size_t x = 0; x < lvw; x++) {
+                    const size_t j = x % N;
+                    uint64_t s = 0;
+                    for (int k2 = 0; k2 < (1 << g); k2++) {
+                        const uint64_t w = keys[(size_t)k2 * tw + (size_t)lv * lvw + x];
+                        s = addmod(s, k2 == 0 ? w : nq_mulmod(&c->plan.br, w, rot[(size_t)k2 * N + j]), q);
+                    }
+                    comb[(size_t)lv * lvw + x] = s;
+                }
+            /* comb has the key's [lvl][col][col2] layout for its first L levels */
+            ep_group(c, comb, acc, acc, L, digits, dntt, hat);
+        }
+    }
+    rc = 0;
+out:
+    free(digits); free(dntt); free(hat); free(tmp); free(mono); free(rot); free(comb);
+    return rc;
+}
+
+int po_blind_rotate_group(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out) {
+    int32_t* scaled = (int32_t*)malloc(sizeof(int32_t) * (c->p.n + 1));
+    if (!scaled) return fail(c, "po_blind_rotate_group: out of memory");
+    po_modswitch(c, in, scaled);
+    const int rc = blind_rotate_group(c, scaled, v, acc_out);
+    free(scaled);
+    return rc ? fail(c, "po_blind_rotate_group: no group key") : 0;
+}
+
+/* functionalBootstrappingNtt (yatfhe/src/bootstrapping.cpp:60-68) on the group key. */
+int po_pbs_group(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+    if (!c->grp_bsk) return fail(c, "po_pbs_group: no group key");
+    return pbs_run(c, in, count, v, out, threads, 2);
 }

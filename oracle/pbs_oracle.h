@@ -77,6 +77,14 @@ int po_load_lazy_file(po_ctx* c, const char* path);
 int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out);
 int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
 
+/* Group-g keys of blindRotateNtt (BootstrappingKey, TrgswDft rows [keys][l][k+1][k+1][N] in the
+ * NTT domain; keys = n for g = 1, n / g * 2^g otherwise; g divides n). */
+int po_keygen_group(po_ctx* c, uint64_t seed, int group);
+int po_get_group(po_ctx* c, uint64_t* out);
+int po_set_group(po_ctx* c, const uint64_t* words, int group);
+int po_blind_rotate_group(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out);
+int po_pbs_group(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
+
 /* po_keygen that also writes out its random samples (see pbs_oracle.c). */
 int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s, int32_t* bsk_noise,
                       uint64_t* bsk_mask, int32_t* ksk_mask, int32_t* ksk_noise);

@@ -43,6 +43,7 @@ struct RefState {
     std::unique_ptr<BootstrappingKeyMP> bsk;
     std::unique_ptr<BootstrappingKeyWWL24> wwl;
     std::unique_ptr<BootstrappingKeyMPLazyPipeAlt> lazy;
+    std::unique_ptr<BootstrappingKey> gbsk;  // the group-g key family (TrgswDft rows)
     std::unique_ptr<TlweKeySwitchingKey> ksk;
     std::string lastError;
 };
@@ -121,6 +122,8 @@ int ref_setup(const ref_params* p) {
         s.trgswKey.reset();
         s.bsk.reset();
         s.wwl.reset();
+        s.lazy.reset();
+        s.gbsk.reset();
         s.ksk.reset();
         s.ready = true;
     });
@@ -691,6 +694,84 @@ int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, i
             Tlwe big{s.ksk->nCurrKey};
             rescaleTlweToNewMod(sc, x);
             blindRotateLazyPipeAltNtt(acc, *s.lazy, sc, vp, gdV, p);
+            if (c == 0 && acc0) {
+                for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
+                fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);
+            }
+            extractTlweFromTrlwe(big, acc, p.driftPhase);
+            switchKeyForTlwe(y, *s.ksk, big, p);
+            fromTlwe(out + static_cast<size_t>(c) * (n + 1), y, n);
+        }
+    });
+}
+
+// ---------------------------------------------------------------- group keys (BootstrappingKey)
+// genTlweKey, genTrlweKey, genBootstrappingKey with param.group = group
+// (yatfhe/src/bootstrapping.cpp:98-104: genBootstrappingKeyNormal for group 1,
+// genBootstrappingKeyGroup :16-38 otherwise; both run in order on the calling thread), then
+// genTlweKeySwitchingKey.
+int ref_keygen_group(uint64_t seed, int group) {
+    if (!st().ready) return fail("ref_keygen_group: ref_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        auto& p = s.param;
+        p.group = group;
+        (void)rng();
+        yatfhe_oracle_set_seed(seed);
+        rng = ChaCha20Rng();
+        s.lweKey = std::make_unique<TlweKey>(p);
+        s.trgswKey = std::make_unique<TrgswKey>(p);
+        s.gbsk = std::make_unique<BootstrappingKey>(p);
+        s.ksk = std::make_unique<TlweKeySwitchingKey>(p);
+        genTlweKey(*s.lweKey);
+        genTrlweKey(s.trgswKey->trlweKey);
+        genBootstrappingKey(*s.gbsk, *s.trgswKey, *s.lweKey, p);
+        TlweKey ksTarget = *s.lweKey;
+        genTlweKeySwitchingKey(*s.ksk, s.trgswKey->trlweKey, ksTarget, p);
+    });
+}
+
+// The group key's NTT-domain words, [j][lvl][row][poly][N] of bskDft[j].trlweDftSamples[lvl][row]
+// (poly = a[0..k-1] then b), j < n / group * 2^group (n for group 1), lvl < param.l.
+int ref_export_group(uint64_t* out) {
+    auto& s = st();
+    if (!s.gbsk) return fail("ref_export_group: no group key");
+    const int k = s.param.k, N = s.param.N;
+    uint64_t* o = out;
+    for (const auto& g : s.gbsk->bskDft)
+        for (const auto& lv : g.trlweDftSamples)
+            for (const auto& t : lv)
+                for (int poly = 0; poly <= k; poly++) {
+                    const NttPolynomial& P = poly < k ? t.a[poly] : t.b;
+                    std::memcpy(o, P.coeffs.data(), sizeof(uint64_t) * N);
+                    o += N;
+                }
+    return 0;
+}
+
+// functionalBootstrappingNtt (yatfhe/src/bootstrapping.cpp:60-68) on the group key, one
+// ciphertext after the other: rescaleTlweToNewMod, genNoiselessTrlweSample, blindRotateNtt
+// (yatfhe/src/blind_rotate.cpp:549-560: blindRotateNormalNtt, blindRotateGroup2Ntt or
+// blindRotateGroup3Ntt by the key's group), extraction, key switching.  acc0 (may be null)
+// receives ciphertext 0's accumulator after the blind rotation.
+int ref_pbs_group(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
+    auto& s = st();
+    if (!s.gbsk || !s.ksk) return fail("ref_pbs_group: keys not loaded");
+    return guarded([&] {
+        YatfheParameters p = s.param;
+        p.group = s.gbsk->group;
+        const int n = p.n, N = p.N, k = p.k;
+        TorusPolynomial vp{N};
+        toPoly(vp, v, N);
+        for (int c = 0; c < count; c++) {
+            Tlwe x{n}, y{n};
+            toTlwe(x, in + static_cast<size_t>(c) * (n + 1), n);
+            ScaledTlwe sc{2 * N, n};
+            Trlwe acc{k, N};
+            Tlwe big{s.ksk->nCurrKey};
+            rescaleTlweToNewMod(sc, x);
+            genNoiselessTrlweSample(acc, vp, sc);
+            blindRotateNtt(acc, s.gbsk->bskDft, sc, p);
             if (c == 0 && acc0) {
                 for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
                 fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);

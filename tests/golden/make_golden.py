@@ -10,7 +10,7 @@ parameter set and key seed:
     the test polynomial, the reference's outputs of functionalBootstrappingMPNtt, its
     decryptions, and the blind-rotation accumulator of ciphertext 0 after a few CMux steps.
 
-    python tests/golden/make_golden.py [ginx] [wwl24] [lazy]
+    python tests/golden/make_golden.py [ginx] [wwl24] [lazy] [group]
 """
 from __future__ import annotations
 
@@ -46,6 +46,15 @@ LAZY_CASES = {
     # the reference's own lazy outputs do not decrypt: its s2 key has 3 levels of 7 bits.)
     "lazy_t32_n2048_seed5eed0007": (WWL24_T32_N2048, 0x5EED0007, 8, 16),
     "lazy_t56_n2048_seed5eed0008": (WWL24_T56_N2048, 0x5EED0008, 8, 17),
+}
+
+GROUP_CASES = {
+    # name: (params, group, key seed, number of ciphertexts, message seed); sign bootstrap
+    # through functionalBootstrappingNtt / blindRotateNtt with the group-g key family
+    "group2_t32_n1024_seed5eed000c": (T32_N1024, 2, 0x5EED000C, 8, 19),
+    "group3_t32_n1024_seed5eed000d": (T32_N1024, 3, 0x5EED000D, 8, 20),
+    "group1_t32_n1024_seed5eed000e": (T32_N1024, 1, 0x5EED000E, 8, 21),
+    "group2_t56_n2048_seed5eed000f": (T56_N2048, 2, 0x5EED000F, 8, 22),
 }
 
 
@@ -145,9 +154,36 @@ def make_lazy(name, p, seed, count, mseed):
     print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
 
 
+def make_group(name, p, group, seed, count, mseed):
+    ref = Reference(p)
+    ref.keygen_group(seed, group)
+    s, z = ref.keys()
+    words = ref.group_words()
+    ksk = ref.ksk()
+    rng = np.random.default_rng(mseed)
+    bits = rng.integers(0, 2, count)
+    mu = np.where(bits == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    lut = lutmod.sign_lut(p.N, p.torus_bits)
+    lwe = ref.encrypt(mu)
+    out, acc0 = ref.pbs_group(lwe, lut, with_acc=True)
+    dec = ref.decrypt(out, 8)
+    expect = np.where(bits == 1, 1, -1)
+    if not np.array_equal(dec, expect):
+        raise SystemExit(f"{name}: the reference's own decryptions {dec} differ from the messages {expect}")
+    np.savez_compressed(
+        HERE / f"{name}.npz",
+        params=np.array([p.n, p.N, p.k, p.radix_bits, p.l, p.l_approx, p.ks_radix_bits, p.ks_level, p.lwe_noise_b,
+                         p.rlwe_noise_b, p.torus_base, p.torus_bits], np.int64),
+        group=np.array([group]), seed=np.array([seed], np.uint64),
+        sha_lwe_s=digest(s), sha_rlwe_s=digest(z), sha_key=digest(words), sha_ksk=digest(ksk),
+        mu=mu, lwe_in=lwe, lut=lut, lwe_out=out, decrypted=dec, base=np.array([8]), acc0=acc0)
+    print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
+
+
 if __name__ == "__main__":
-    # optional arguments: the families to (re)generate, of "ginx", "wwl24", "lazy" (default all)
-    families = set(sys.argv[1:]) or {"ginx", "wwl24", "lazy"}
+    # optional arguments: the families to (re)generate, of "ginx", "wwl24", "lazy", "group"
+    # (default all)
+    families = set(sys.argv[1:]) or {"ginx", "wwl24", "lazy", "group"}
     if "ginx" in families:
         for name, (p, seed, count, mseed) in CASES.items():
             make(name, p, seed, count, mseed)
@@ -157,3 +193,6 @@ if __name__ == "__main__":
     if "lazy" in families:
         for name, (p, seed, count, mseed) in LAZY_CASES.items():
             make_lazy(name, p, seed, count, mseed)
+    if "group" in families:
+        for name, (p, group, seed, count, mseed) in GROUP_CASES.items():
+            make_group(name, p, group, seed, count, mseed)
