@@ -126,6 +126,19 @@ int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);
  * sign-extended torus value is rejected with YG_ERR_INVALID.  Synchronizes the device. */
 int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s2, int s2_levels, yg_key** out);
 
+/* Group-g keys (BootstrappingKey, yatfhe/include/yatfhe/bootstrapping.h:16-45, made by
+ * genBootstrappingKey with param.group = group, yatfhe/src/bootstrapping.cpp:16-38,98-104): the
+ * NTT-domain TrgswDft words of every key, [keys][key_levels][k+1][k+1][N] (trlweDftSamples[lvl][row],
+ * poly p < k is a[p], poly k is b; keys = n for group 1, n / group * 2^group otherwise),
+ * key_levels the reference's param.l.  The key handle runs blindRotateNtt
+ * (yatfhe/src/blind_rotate.cpp:549-560: blindRotateNormalNtt, blindRotateGroup2Ntt or
+ * blindRotateGroup3Ntt) in yg_pbs (then functionalBootstrappingNtt,
+ * yatfhe/src/bootstrapping.cpp:60-68), yg_pbs_host, yg_blind_rotate (steps = n) and
+ * yg_blind_rotate_extract; the other entry points refuse it like a lazy key.  Requires group
+ * 1, 2 or 3 dividing n, l_approx <= key_levels <= 8, key_levels * radix_bits <= torus_bits;
+ * an unreduced word is rejected with YG_ERR_INVALID.  Synchronizes the device. */
+int yg_key_upload_group(yg_ctx* ctx, const uint64_t* h_words, int group, int key_levels, yg_key** out);
+
 /* Replaces deserializeBskLazyPipeAlt (yatfhe/src/ya_serializer.cpp:462-481): reads a file
  * written by serializeBskLazyPipeAlt (:445-460) and uploads it as above. */
 int yg_key_load_lazy_file(yg_ctx* ctx, const char* path, yg_key** out);

@@ -75,6 +75,7 @@ def test_null_arguments_are_rejected(built_lib):
     assert L.yg_key_load_wwl24_file(None, None, None) == -1
     assert L.yg_key_upload_lazy(None, None, None, 1, None) == -1
     assert L.yg_key_load_lazy_file(None, None, None) == -1
+    assert L.yg_key_upload_group(None, None, 2, 3, None) == -1
     assert L.yg_key_device_bytes(None) == 0
     L.yg_ctx_destroy(None)
     L.yg_key_destroy(None)

@@ -75,6 +75,7 @@ _SIGNATURES = {
     "yg_key_load_wwl24_file": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "yg_key_upload_lazy": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(_vp)]),
     "yg_key_load_lazy_file": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "yg_key_upload_group": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
     "yg_keygen_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "yg_key_set_ksk": (ctypes.c_int, [_vp, _vp]),
     "yg_key_destroy": (None, [_vp]),

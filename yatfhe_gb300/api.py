@@ -74,7 +74,8 @@ class BootstrapKey:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self._h = handle
-        # key format it was made from: "ginx" (BootstrappingKeyMP), "wwl24" or "lazy"
+        # key format it was made from: "ginx" (BootstrappingKeyMP), "wwl24", "lazy" or
+        # "group<g>" (BootstrappingKey with param.group = g)
         self.family = "ginx"
 
     @classmethod
@@ -149,6 +150,23 @@ class BootstrapKey:
         _lib.check(_lib.lib().yg_key_load_lazy_file(ctx.handle, str(path).encode(), ctypes.byref(h)))
         key = cls(ctx, h)
         key.family = "lazy"
+        return key
+
+    @classmethod
+    def from_group_words(cls, ctx: Context, words: np.ndarray, group: int) -> "BootstrapKey":
+        """A group-g key of blindRotateNtt (BootstrappingKey: TrgswDft words [keys][l][k+1][k+1][N],
+        NTT domain mod q; keys = n for group 1, n / g * 2^g otherwise)."""
+        p = ctx.params
+        w = np.ascontiguousarray(words, np.uint64)
+        keys = p.n if group == 1 else (p.n // group) << group
+        per = (p.k + 1) ** 2 * p.N
+        if w.size % (keys * per):
+            raise ValueError(f"expected {keys} keys of [l][{p.k + 1}][{p.k + 1}][{p.N}] words")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_key_upload_group(ctx.handle, ctypes.c_void_p(w.ctypes.data), group,
+                                                  w.size // (keys * per), ctypes.byref(h)))
+        key = cls(ctx, h)
+        key.family = f"group{group}"
         return key
 
     def set_ksk(self, ksk: np.ndarray) -> "BootstrapKey":
@@ -316,6 +334,21 @@ def blind_rotate_lazy_pipe_alt_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut,
     if key.family != "lazy":
         raise ValueError("blind_rotate_lazy_pipe_alt_ntt needs a key made by BootstrapKey.from_lazy_words/_file")
     return blind_rotate_mp21_ntt(ctx, key, lwe_in, lut, stream=stream)
+
+
+def blind_rotate_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, stream=None):
+    """blindRotateNtt (yatfhe/src/blind_rotate.cpp:549-560) after genNoiselessTrlweSample, on a
+    group key: accumulators [count, (k+1) N] (int64 torus words) after the whole rotation."""
+    if not key.family.startswith("group"):
+        raise ValueError("blind_rotate_ntt needs a key made by BootstrapKey.from_group_words")
+    return blind_rotate_mp21_ntt(ctx, key, lwe_in, lut, stream=stream)
+
+
+def functional_bootstrapping_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, out=None, stream=None):
+    """functionalBootstrappingNtt (yatfhe/src/bootstrapping.cpp:60-68) on a group key."""
+    if not key.family.startswith("group"):
+        raise ValueError("functional_bootstrapping_ntt needs a key made by BootstrapKey.from_group_words")
+    return functional_bootstrapping_mp_ntt(ctx, key, lwe_in, lut, out=out, stream=stream)
 
 
 def switch_key_for_tlwe(ctx: Context, key: BootstrapKey, big, stream=None):

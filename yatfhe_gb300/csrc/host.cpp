@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -392,6 +393,64 @@ void upload_lazy(yg_ctx* c, yg_key* key, const int64_t* cprime, const u64* s2, i
     key->bsk_bytes = tab.size() * sizeof(u64) + words.size();
 }
 
+// Group-g key (TrgswDft words [keys][key_levels][2][2][N]) -> the device: the levels the
+// external product uses (l_approx of them), the mod-q transform tables, psi^j 2^64 mod q for
+// j < 2N and the exponent e_s of every transform slot (slot s of NTT(X^r) is psi^(r e_s)),
+// found by transforming X on the host with the kernels' forward transform.
+void upload_group(yg_ctx* c, yg_key* key, const u64* words, int group, int key_levels) {
+    const int n = c->p.n, N = c->p.N, L = c->p.l_approx, rb = c->p.radix_bits, T = c->p.torus_bits;
+    if (group < 1 || group > 3 || n % group) throw std::invalid_argument("group key: group 1, 2 or 3, dividing n");
+    if (key_levels < L || key_levels > yg::kGroupMaxLevels || key_levels * rb > T)
+        throw std::invalid_argument("group key: l_approx <= key levels <= 8 and key levels * radix_bits <= torus_bits");
+    const u64 q = c->q;
+    const QTables& qt = *c->qtab;
+    const size_t keys = group == 1 ? (size_t)n : (size_t)(n / group) << group;
+    const size_t used = (size_t)L * 4 * N, full = (size_t)key_levels * 4 * N;
+    std::vector<u64> w(keys * used);
+    for (size_t j = 0; j < keys; j++)
+        for (size_t x = 0; x < used; x++) {
+            const u64 v = words[j * full + x];
+            if (v >= q) throw std::invalid_argument("group key word not reduced mod q");
+            w[j * used + x] = v;
+        }
+    // slot exponents: the forward transform of X, then each slot's power of psi
+    std::vector<u64> x(N, 0);
+    x[1] = 1;
+    for (int m = 1, t = N / 2; m < N; m <<= 1, t >>= 1)
+        for (int b = 0; b < N / 2; b++) {
+            const int i = b / t, j = b - i * t, xi = 2 * i * t + j, yi = xi + t;
+            const u64 u = x[xi], v = mulmod(x[yi], qt.wf[m + i], q);
+            x[xi] = (u + v) % q;
+            x[yi] = (u + q - v) % q;
+        }
+    const u64 psi = minimal_root(N, q);
+    std::map<u64, int> expo;
+    std::vector<u64> tab(7 * (size_t)N);
+    u64 pw = 1;
+    const u64 r64 = (u64)(((u128)1 << 64) % q);
+    for (int j = 0; j < 2 * N; j++) {
+        expo[pw] = j;
+        tab[4 * (size_t)N + j] = mulmod(pw, r64, q);
+        pw = mulmod(pw, psi, q);
+    }
+    for (int s = 0; s < N; s++) {
+        auto it = expo.find(x[s]);
+        if (it == expo.end() || !(it->second & 1)) throw std::runtime_error("slot exponent not found");
+        tab[6 * (size_t)N + s] = (u64)it->second;
+    }
+    std::copy(qt.w.begin(), qt.w.end(), tab.begin());
+    std::copy(qt.wp.begin(), qt.wp.end(), tab.begin() + N);
+    std::copy(qt.wf.begin(), qt.wf.end(), tab.begin() + 2 * (size_t)N);
+    std::copy(qt.wfp.begin(), qt.wfp.end(), tab.begin() + 3 * (size_t)N);
+    ck(cudaMalloc(&key->d_group_tab, tab.size() * sizeof(u64)), "cudaMalloc group tables");
+    ck(cudaMalloc(&key->d_group, w.size() * sizeof(u64)), "cudaMalloc group key");
+    ck(cudaMemcpy(key->d_group_tab, tab.data(), tab.size() * sizeof(u64), cudaMemcpyHostToDevice), "upload group tables");
+    ck(cudaMemcpy(key->d_group, w.data(), w.size() * sizeof(u64), cudaMemcpyHostToDevice), "upload group key");
+    key->group = group;
+    key->group_levels = key_levels;
+    key->bsk_bytes = (tab.size() + w.size()) * sizeof(u64);
+}
+
 // Key generation arithmetic on the GPU from caller-drawn samples (see yg_keygen_from_samples):
 // the NTT of the RLWE secret mod q (host, exact), the BSK samples (keygen_bsk_kernel), the
 // usual conversion of the NTT-domain words, and the KSK samples (keygen_ksk_kernel).
@@ -628,6 +687,36 @@ int read_lazy_file(const yg_params& p, const char* path, std::vector<int64_t>& c
     return Ls;
 }
 
+// The group blind rotation's launch arguments for a context and group key (buffers and count
+// left empty).
+yg::GroupBrArgs group_args(const yg_ctx* c, const yg_key* key) {
+    yg::GroupBrArgs a{};
+    const int N = c->p.N;
+    const u64 q = c->q;
+    const u64* tab = key->d_group_tab;
+    a.key = key->d_group;
+    a.wi = tab;
+    a.wip = tab + N;
+    a.wf = tab + 2 * (size_t)N;
+    a.wfp = tab + 3 * (size_t)N;
+    a.psi_m = tab + 4 * (size_t)N;
+    a.slot_exp = tab + 6 * (size_t)N;
+    a.q = q;
+    u64 inv = q;
+    for (int i = 0; i < 6; i++) inv *= 2 - q * inv;
+    a.qinv = inv;
+    a.post = mulmod(c->qtab->ninv, (u64)(((u128)1 << 64) % q), q);
+    a.postp = (u64)(((u128)a.post << 64) / q);
+    a.n = c->p.n;
+    a.N = N;
+    a.L = c->p.l_approx;
+    a.l_full = key->group_levels;
+    a.group = key->group;
+    a.radix_bits = c->p.radix_bits;
+    a.torus_bits = c->p.torus_bits;
+    return a;
+}
+
 // The lazy blind rotation's launch arguments for a context and lazy key (buffers and count
 // left empty).
 yg::LazyBrArgs lazy_args(const yg_ctx* c, const yg_key* key) {
@@ -682,10 +771,11 @@ yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
 int yg::check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bool lazy_ok) {
     if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
     if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
-    if (need_bsk && k->lazy() && !lazy_ok)
+    if (need_bsk && (k->lazy() || k->grouped()) && !lazy_ok)
         return set_err(YG_ERR_INVALID,
-                       "lazy keys run through yg_pbs, yg_pbs_host, yg_blind_rotate and yg_blind_rotate_extract");
-    if (need_bsk && !k->d_bsk && !k->lazy()) return set_err(YG_ERR_STATE, "key has no bootstrapping key");
+                       "lazy and group keys run through yg_pbs, yg_pbs_host, yg_blind_rotate and yg_blind_rotate_extract");
+    if (need_bsk && !k->d_bsk && !k->lazy() && !k->grouped())
+        return set_err(YG_ERR_STATE, "key has no bootstrapping key");
     if (need_ksk && !k->d_ksk) return set_err(YG_ERR_STATE, "key has no key-switching key (yg_key_set_ksk)");
     return YG_OK;
 }
@@ -704,7 +794,14 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
     int32_t* big = nullptr;
     ck(cudaMallocAsync(&big, (size_t)count * (kN + 1) * sizeof(int32_t), s), "cudaMallocAsync extract buffer");
     int rc;
-    if (key->lazy()) {
+    if (key->grouped()) {
+        yg::GroupBrArgs a = group_args(c, key);
+        a.lwe_in = d_in;
+        a.lut = d_lut;
+        a.big_out = big;
+        a.count = count;
+        rc = yg::launch_group_blind_rotate(a, s);
+    } else if (key->lazy()) {
         yg::LazyBrArgs a = lazy_args(c, key);
         a.lwe_in = d_in;
         a.lut = d_lut;
@@ -840,6 +937,27 @@ int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s
     });
 }
 
+int yg_key_upload_group(yg_ctx* ctx, const uint64_t* h_words, int group, int key_levels, yg_key** out) {
+    if (!ctx || !h_words || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            upload_group(ctx, k.get(), h_words, group, key_levels);
+        } catch (...) {
+            if (k->d_group) cudaFree(k->d_group);
+            if (k->d_group_tab) cudaFree(k->d_group_tab);
+            k->d_group = nullptr;
+            k->d_group_tab = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
 int yg_key_load_lazy_file(yg_ctx* ctx, const char* path, yg_key** out) {
     if (!ctx || !path || !out) return set_err(YG_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -897,6 +1015,8 @@ void yg_key_destroy(yg_key* key) {
     if (key->d_ksk) cudaFree(key->d_ksk);
     if (key->d_lazy_cprime) cudaFree(key->d_lazy_cprime);
     if (key->d_lazy_tab) cudaFree(key->d_lazy_tab);
+    if (key->d_group) cudaFree(key->d_group);
+    if (key->d_group_tab) cudaFree(key->d_group_tab);
     delete key;
 }
 
@@ -977,9 +1097,22 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
                     int count, int steps, void* stream) {
     if (int rc = check_key(ctx, key, true, false, true)) return rc;
     if (count < 0 || steps < 0 || steps > ctx->p.n) return set_err(YG_ERR_INVALID, "bad count or steps");
-    if (key->lazy() && steps != ctx->p.n) return set_err(YG_ERR_INVALID, "a lazy key runs the whole rotation: steps = n");
+    if ((key->lazy() || key->grouped()) && steps != ctx->p.n)
+        return set_err(YG_ERR_INVALID, "a lazy or group key runs the whole rotation: steps = n");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (key->grouped()) {
+        return guarded([&] {
+            DeviceGuard g(ctx->device);
+            yg::GroupBrArgs a = group_args(ctx, key);
+            a.lwe_in = d_in;
+            a.lut = d_lut;
+            a.acc_out = d_acc;
+            a.count = count;
+            yg::check_launch(yg::launch_group_blind_rotate(a, stream), "group blind rotate launch");
+            return YG_OK;
+        });
+    }
     if (key->lazy()) {
         return guarded([&] {
             DeviceGuard g(ctx->device);
@@ -1011,6 +1144,18 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
     if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
     if (count == 0) return YG_OK;
     if (!d_in || !d_lut || !d_big) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (key->grouped()) {
+        return guarded([&] {
+            DeviceGuard g(ctx->device);
+            yg::GroupBrArgs a = group_args(ctx, key);
+            a.lwe_in = d_in;
+            a.lut = d_lut;
+            a.big_out = d_big;
+            a.count = count;
+            yg::check_launch(yg::launch_group_blind_rotate(a, stream), "group blind rotate launch");
+            return YG_OK;
+        });
+    }
     if (key->lazy()) {
         return guarded([&] {
             DeviceGuard g(ctx->device);

@@ -102,11 +102,17 @@ struct yg_key {
     uint64_t* d_lazy_tab = nullptr;
     int lazy_ls = 0;
     bool lazy() const { return d_lazy_cprime != nullptr; }
+    // A group-g key of the TrgswDft family: the used levels' words [keys][L][2][2][N], and one
+    // block of [wi | wip | wf | wfp] (N each) + psi^j 2^64 mod q [2N] + slot exponents [N].
+    uint64_t* d_group = nullptr;
+    uint64_t* d_group_tab = nullptr;
+    int group = 0, group_levels = 0;
+    bool grouped() const { return d_group != nullptr; }
 };
 
 namespace yg {
 
-// need_bsk: the key must hold GINX rows, or (lazy_ok) GINX rows or a lazy key.
+// need_bsk: the key must hold GINX rows, or (lazy_ok) GINX rows, a lazy key or a group key.
 int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bool lazy_ok = false);
 
 // Blind-rotation launch arguments of a context and key (buffers and count left empty).

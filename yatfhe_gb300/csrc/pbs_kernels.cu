@@ -636,6 +636,192 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
     }
 }
 
+// blindRotateNtt (yatfhe/src/blind_rotate.cpp:549-560) on the group-g key family, after
+// genNoiselessTrlweSample (or from a given accumulator), and the extraction; one ciphertext
+// per CTA of N/2 threads, thread t owning coefficients and slots t and t + N/2, the reference's
+// arithmetic mod q as in lazy_blind_rotate_kernel.  Per step the accumulator's digit
+// polynomials of the L used levels (digits of its l_full-level decomposition,
+// gadgetDecomposeTrlwe) go through one batch of 2L forward transforms, then per slot
+//   acc^[o] = sum_(lvl, col) D[lvl][col] . K'[lvl][col][o],
+// K' = K_0 + sum_(k2 > 0) NTT(X^(r_k2)) . K_k2 over the group's 2^g keys (rotateTrgswNtt and the
+// sums of blindRotateGroup2Ntt / Group3Ntt; r_k2 the sum of the a's whose bit is set in k2),
+// NTT(X^r) in slot s being psi^(r e_s) (a table lookup), then one inverse batch of 2.
+// Group 1 is the CMux of blindRotateNormalNtt: acc += EP(K_i, X^(a_i) acc - acc) for a_i != 0.
+template <int T>
+__global__ void __launch_bounds__(1024, 1) group_blind_rotate_kernel(const GroupBrArgs a) {
+    using TT = typename TorusOf<T>::type;
+    using U = typename TorusOf<T>::utype;
+    extern __shared__ __align__(16) unsigned char gr_smem[];
+    const int N = a.N, H = N >> 1, t = threadIdx.x, n = a.n, L = a.L, rb = a.radix_bits;
+    const int logN = 31 - __clz(N);
+    const int ct = blockIdx.x;
+    const int g = a.group, G = 1 << g;
+    const uint64_t q = a.q, qinv = a.qinv, q2 = 2 * q;
+    uint64_t* sw = reinterpret_cast<uint64_t*>(gr_smem);                  // [2L][N]
+    TT* acc = reinterpret_cast<TT*>(sw + (size_t)2 * L * N);              // [2][N]
+    int16_t* sa = reinterpret_cast<int16_t*>(acc + 2 * N);                // [n + 1]
+    const int jj[2] = {t, t + H};
+    const size_t keyw = (size_t)L * 4 * N;  // words of one key's used levels
+
+    auto lift = [q](int64_t x) -> uint64_t { return x < 0 ? (uint64_t)(x + (int64_t)q) : (uint64_t)x; };
+    auto addq = [q](uint64_t x, uint64_t y) -> uint64_t {
+        const uint64_t s = x + y;
+        return s >= q ? s - q : s;
+    };
+    auto red4 = [q, q2](uint64_t x) -> uint64_t {
+        x = x >= q2 ? x - q2 : x;
+        return x >= q ? x - q : x;
+    };
+    auto to_torus = [&](uint64_t v) -> TT {
+        v = mulshoup64(v, a.post, a.postp, q);
+        const int64_t c = v >= (q + 1) / 2 ? (int64_t)(v - q) : (int64_t)v;
+        if constexpr (T == 32) return (int32_t)(uint32_t)(uint64_t)c;
+        else return sext<56>(c);
+    };
+    auto norm = [N](int r) {
+        r %= 2 * N;
+        return r < 0 ? r + 2 * N : r;
+    };
+    // (X^r p)[j] for r in [0, 2N) (rotateTorusPolynomial, yatfhe/src/polynomial.cpp:184-193)
+    auto rot_at = [N](const TT* p, int r, int j) -> TT {
+        int x = j - r;
+        bool neg = false;
+        if (x < 0) {
+            x += N;
+            neg = true;
+        }
+        if (x < 0) {
+            x += N;
+            neg = false;
+        }
+        const TT v = p[x];
+        return neg ? tneg<T>(v) : v;
+    };
+
+    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81)
+    const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+    for (int i = t; i <= n; i += H) sa[i] = (int16_t)modswitch_down(in[i], 31 - logN, logN + 1);
+    __syncthreads();
+    if (a.acc_in) {
+        const int64_t* src = a.acc_in + (size_t)ct * 2 * N;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            acc[jj[e]] = (TT)src[jj[e]];
+            acc[N + jj[e]] = (TT)src[N + jj[e]];
+        }
+    } else {
+        // genNoiselessTrlweSample (yatfhe/src/trlwe.cpp:175-182): (0, X^(-b) v)
+        const int rb0 = norm(-(int)sa[n]);
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = jj[e];
+            int x = j - rb0;
+            bool neg = false;
+            if (x < 0) {
+                x += N;
+                neg = true;
+            }
+            if (x < 0) {
+                x += N;
+                neg = false;
+            }
+            const TT v = (TT)a.lut[x];
+            acc[j] = 0;
+            acc[N + j] = neg ? tneg<T>(v) : v;
+        }
+    }
+    __syncthreads();
+
+    const int steps = g == 1 ? n : n / g;
+    for (int s = 0; s < steps; ++s) {
+        int r1 = 0;
+        int rots[8];
+        if (g == 1) {
+            const int ai = sa[s];
+            if (ai == 0) continue;  // the same for every thread of the CTA
+            r1 = norm(ai);
+        } else {
+            for (int k2 = 1; k2 < G; ++k2) {
+                int r = 0;
+                for (int i2 = 0; i2 < g; ++i2)
+                    if ((k2 >> (g - 1 - i2)) & 1) r += sa[s * g + i2];
+                rots[k2] = norm(r);
+            }
+        }
+        // the input's digit polynomials of the used levels (group 1: of X^a acc - acc)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = jj[e];
+#pragma unroll
+            for (int poly = 0; poly < 2; ++poly) {
+                const TT* p = acc + poly * N;
+                const TT x = g == 1 ? tsub<T>(rot_at(p, r1, j), p[j]) : p[j];
+                zero_mean_digits<U, T>((U)x, a.l_full, rb, [&](int level, int d) {
+                    if (level < L) sw[(size_t)(level * 2 + poly) * N + j] = lift(d);
+                });
+            }
+        }
+        __syncthreads();
+        q_forward_batch(sw, 2 * L, N, logN, a.wf, a.wfp, q);
+        uint64_t h[2][2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = jj[e];
+            uint64_t R[8];
+            if (g > 1) {
+                const int ej = (int)a.slot_exp[j];
+                for (int k2 = 1; k2 < G; ++k2) R[k2] = a.psi_m[(rots[k2] * ej) & (2 * N - 1)];
+            }
+            const uint64_t* kb = a.key + (size_t)s * (g == 1 ? 1 : G) * keyw + j;
+            uint64_t h0 = 0, h1 = 0;
+            for (int lvl = 0; lvl < L; ++lvl)
+#pragma unroll
+                for (int col = 0; col < 2; ++col) {
+                    const uint64_t X = red4(sw[(size_t)(lvl * 2 + col) * N + j]);
+                    const size_t off = (size_t)((lvl * 2 + col) * 2) * N;
+                    uint64_t k0 = kb[off], k1 = kb[off + N];
+                    for (int k2 = 1; k2 < (g == 1 ? 1 : G); ++k2) {
+                        k0 = addq(k0, montmul64(R[k2], kb[(size_t)k2 * keyw + off], q, qinv));
+                        k1 = addq(k1, montmul64(R[k2], kb[(size_t)k2 * keyw + off + N], q, qinv));
+                    }
+                    h0 = addq(h0, montmul64(X, k0, q, qinv));
+                    h1 = addq(h1, montmul64(X, k1, q, qinv));
+                }
+            h[0][e] = h0;
+            h[1][e] = h1;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) sw[poly * N + jj[e]] = h[poly][e];
+        __syncthreads();
+        q_inverse_batch(sw, 2, N, logN, a.wi, a.wip, q);
+#pragma unroll
+        for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const TT r = to_torus(sw[poly * N + jj[e]]);
+                TT& dst = acc[poly * N + jj[e]];
+                dst = g == 1 ? tadd<T>(dst, r) : r;  // accumulateTrlwe for the CMux
+            }
+        __syncthreads();
+    }
+
+    if (a.acc_out) {
+        int64_t* dst = a.acc_out + (size_t)ct * 2 * N;
+        for (int idx = t; idx < 2 * N; idx += H) dst[idx] = (int64_t)acc[idx];
+    }
+    if (a.big_out) {
+        int32_t* dst = a.big_out + (size_t)ct * (N + 1);
+        for (int j = t; j <= N; j += H) {
+            const TT x = j == N ? acc[N] : (j == 0 ? acc[0] : tneg<T>(acc[N - j]));
+            if constexpr (T == 32) dst[j] = (int32_t)x;
+            else dst[j] = (int32_t)modswitch_down((int64_t)x, T - 32, 32);
+        }
+    }
+}
+
 // Teams of one ciphertext slice: one per RNS channel (kLayoutChannel), or one per channel
 // and accumulator row (kLayoutChannelRow).
 template <int SPLIT>
@@ -1475,6 +1661,22 @@ int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream) {
     };
     if (a.torus_bits == 32) return go(lazy_blind_rotate_kernel<32>);
     if (a.torus_bits == 56) return go(lazy_blind_rotate_kernel<56>);
+    return -1;
+}
+
+int launch_group_blind_rotate(const GroupBrArgs& a, void* stream) {
+    if (a.count <= 0) return 0;
+    if ((a.N != 1024 && a.N != 2048) || a.group < 1 || a.group > 3 || a.n % a.group || a.L < 1 ||
+        a.L > a.l_full || a.l_full > kGroupMaxLevels || (!a.lut && !a.acc_in))
+        return -1;
+    const size_t smem = group_br_smem_bytes(a.N, a.torus_bits, a.n, a.L);
+    auto go = [&](auto kern) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+        kern<<<a.count, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    };
+    if (a.torus_bits == 32) return go(group_blind_rotate_kernel<32>);
+    if (a.torus_bits == 56) return go(group_blind_rotate_kernel<56>);
     return -1;
 }
 

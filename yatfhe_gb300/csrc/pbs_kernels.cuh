@@ -158,6 +158,34 @@ __host__ __device__ inline size_t lazy_br_smem_bytes(int N, int torus_bits, int 
     return (b + 15) & ~(size_t)15;
 }
 
+// The blind rotation of the group-g key family (blindRotateNtt: group 1 = blindRotateNormalNtt,
+// groups 2 and 3 = blindRotateGroup2Ntt / blindRotateGroup3Ntt) with its extraction, one
+// ciphertext per CTA of N/2 threads, k = 1.  The key is the reference's NTT-domain TrgswDft
+// words of the levels the external product uses.
+constexpr int kGroupMaxLevels = 8;  // levels of the key's decomposition (the reference's l)
+struct GroupBrArgs {
+    const int32_t* lwe_in;   // [count][n+1]
+    const int64_t* lut;      // [N] test polynomial v, or null when acc_in is given
+    const int64_t* acc_in;   // [count][2 N] starting accumulator, or null
+    const uint64_t* key;     // [keys][L][2][2][N] NTT-domain words mod q ([lvl][col][col2])
+    const uint64_t* psi_m;   // [2 N] psi^j 2^64 mod q: slot s of NTT(X^r) is psi^(r e_s)
+    const uint64_t* slot_exp;// [N] e_s (odd, < 2N)
+    const uint64_t* wf;      // [N] psi^brv(k) mod q, and Shoup companions
+    const uint64_t* wfp;
+    const uint64_t* wi;      // [N] psi^-brv(k) mod q, and Shoup companions
+    const uint64_t* wip;
+    uint64_t q, qinv, post, postp;  // as in LazyBrArgs
+    int32_t* big_out;        // [count][N + 1] extracted LWE, or null
+    int64_t* acc_out;        // [count][2 N] accumulator, or null
+    int count, n, N, L, l_full, group, radix_bits, torus_bits;
+};
+__host__ __device__ inline size_t group_br_smem_bytes(int N, int torus_bits, int n, int L) {
+    size_t b = (size_t)2 * L * N * 8;
+    b += 2 * (size_t)N * (torus_bits == 32 ? 4 : 8);
+    b += ((size_t)n + 1) * 2;
+    return (b + 15) & ~(size_t)15;
+}
+
 // u32 words of one (step, level, row, channel) block of the device key: 2 output polys.
 __host__ __device__ inline size_t key_block_words(int N) { return 2 * (size_t)N; }
 __host__ __device__ inline size_t key_words(int n, int L, int N) {
@@ -220,5 +248,6 @@ constexpr int kNoVariant = -2;
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
 int launch_keyswitch(const KsArgs& a, void* stream);
 int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream);
+int launch_group_blind_rotate(const GroupBrArgs& a, void* stream);
 
 }  // namespace yg
