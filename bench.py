@@ -503,6 +503,70 @@ def leg_lazy(dev, steps=3, warmup=1, count=1216, cpu_sample=16):
             "sample_bit_exact": bit_exact}
 
 
+def leg_group(dev, group=2, steps=3, warmup=1, count=9728, cpu_sample=32):
+    """The group-g key family of blindRotateNtt (BootstrappingKey, param.group = g) on the
+    TORUS=32 set (n=630, N=1024, B=2^7, l=lApprox=3): seeded synthetic TrgswDft words (uniform
+    mod q), uploaded through yg_key_upload_group, then `count` bootstraps per step
+    (functionalBootstrappingNtt: group_blind_rotate_kernel, then the key switch).  Reports the
+    throughput, the device key bytes and the CPU restatement on a `cpu_sample`-ciphertext
+    sample with all host threads (also the bit-exact check of that sample)."""
+    import torch
+
+    from yatfhe_gb300 import _lib, api
+    from yatfhe_gb300.params import T32_N1024 as p
+
+    rng = np.random.default_rng(0x5EED000C + group)
+    keys = p.n if group == 1 else (p.n // group) << group
+    words = rng.integers(0, p.q_ntt, size=keys * p.l * (p.k + 1) ** 2 * p.N, dtype=np.uint64)
+    ksk = rng.integers(-(1 << 31), 1 << 31, size=p.ksk_words, dtype=np.int64).astype(np.int32)
+    ctx = api.Context(p, dev)
+    key = api.BootstrapKey.from_group_words(ctx, words, group).set_ksk(ksk)
+    lwe = synthetic_lwe(p, count, 0x5EED0010 + group)
+    lut = workload_lut(p)
+    d_in = torch.from_numpy(lwe).to(f"cuda:{dev}")
+    d_lut = torch.from_numpy(lut).to(f"cuda:{dev}")
+    d_big = torch.empty((count, p.k * p.N + 1), dtype=torch.int32, device=f"cuda:{dev}")
+    d_out = torch.empty_like(d_in)
+    L = _lib.lib()
+    stream = torch.cuda.Stream(device=dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        _lib.check(L.yg_blind_rotate_extract(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
+                                             ctypes.c_void_p(d_lut.data_ptr()), ctypes.c_void_p(d_big.data_ptr()),
+                                             count, sh))
+        _lib.check(L.yg_keyswitch(ctx.handle, key.handle, ctypes.c_void_p(d_big.data_ptr()),
+                                  ctypes.c_void_p(d_out.data_ptr()), count, sh))
+
+    for _ in range(warmup):
+        step()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        step()
+    b.record(stream)
+    stream.synchronize()
+    ms = a.elapsed_time(b)
+    from oracle.oracle import Restatement
+
+    threads = os.cpu_count() or 1
+    ora = Restatement(p)
+    ora.set_group(words.reshape(keys, p.l, p.k + 1, p.k + 1, p.N), group)
+    ora.set_ksk(ksk)
+    t0 = time.perf_counter()
+    cpu_out = ora.pbs_group(lwe[:cpu_sample], lut, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    bit_exact = bool(np.array_equal(cpu_out, d_out[:cpu_sample].cpu().numpy()))
+    return {"workload": f"group{group}_t32_n1024_batch{count}", "params": dict(params_config(p), group=group),
+            "ciphertexts_per_step": count, "value": count * steps / (ms / 1e3), "unit": "bootstraps/s",
+            "steps": steps, "ms_per_step": ms / steps, "key_device_bytes": key.device_bytes,
+            "cpu_baseline": {"value": cpu_sample / cpu_s, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+                             "sample": f"{cpu_sample} of the step's ciphertexts, restatement of "
+                                       "functionalBootstrappingNtt (blindRotateNtt on the group key)"},
+            "sample_bit_exact": bit_exact}
+
+
 def leg_keygen(dev, reps=3):
     """Key generation on the GPU for the TORUS=32 set (n=630, N=1024): seeded synthetic
     samples with the distributions of real ones (binary secrets, TUniform(2^8) / (2^18)
@@ -884,6 +948,8 @@ def main():
             "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
             "keygen_t32_n1024": _safe(leg_keygen, dev),
             "lazy_t32_n2048_batch1216": _safe(leg_lazy, dev),
+            "group2_t32_n1024_batch9728": _safe(leg_group, dev, 2),
+            "group3_t32_n1024_batch9728": _safe(leg_group, dev, 3),
             "mixed_t32x24_t56x8_zipf32768": _safe(leg_multi_tenant, dev),
             "serving_t32_128tenants_4GB": _safe(
                 leg_serving, dev, requests=args.serving_requests,
