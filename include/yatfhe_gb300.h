@@ -134,7 +134,7 @@ int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s
  * (yatfhe/src/blind_rotate.cpp:549-560: blindRotateNormalNtt, blindRotateGroup2Ntt or
  * blindRotateGroup3Ntt) in yg_pbs (then functionalBootstrappingNtt,
  * yatfhe/src/bootstrapping.cpp:60-68), yg_pbs_host, yg_blind_rotate (steps = n) and
- * yg_blind_rotate_extract; the other entry points refuse it like a lazy key.  Requires group
+ * yg_blind_rotate_extract and yg_blind_rotate_acc; the other entry points refuse it like a lazy key.  Requires group
  * 1, 2 or 3 dividing n, l_approx <= key_levels <= 8, key_levels * radix_bits <= torus_bits;
  * an unreduced word is rejected with YG_ERR_INVALID.  Synchronizes the device. */
 int yg_key_upload_group(yg_ctx* ctx, const uint64_t* h_words, int group, int key_levels, yg_key** out);
@@ -181,7 +181,9 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
 
 /* blindRotateMP21Ntt with the reference's own signature semantics
  * (yatfhe/include/yatfhe/blind_rotate.h:69): d_scaled is ScaledTlwe::a ([count][n], values
- * mod 2N in [-N, N)), d_acc ([count][(k+1) N] int64, a then b) is rotated in place. */
+ * mod 2N in [-N, N)), d_acc ([count][(k+1) N] int64, a then b) is rotated in place.  With a
+ * group key: blindRotateNtt (blind_rotate.h:13) in place, the same way; lazy keys are
+ * refused (their rotation builds the accumulator from the test polynomial). */
 int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled, int64_t* d_acc, int count,
                         void* stream);
 

@@ -16,6 +16,8 @@
 //   blindRotateJP22Ntt             yatfhe/include/yatfhe/blind_rotate.h:65 (binary keys)
 //   blindRotateWWL24Ntt            yatfhe/include/yatfhe/blind_rotate.h:61
 //   blindRotateLazyPipeAltNtt      yatfhe/include/yatfhe/blind_rotate.h:44-45
+//   blindRotateNtt                 yatfhe/include/yatfhe/blind_rotate.h:13 (groups 1-3)
+//   functionalBootstrappingNtt     yatfhe/include/yatfhe/bootstrapping.h:366-367
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
 // plus a batched form of the first, which the reference does not have.
 #ifndef YATFHE_GB300_REFERENCE_HPP
@@ -171,6 +173,42 @@ inline yg_key* device_key_lazy(yg_ctx* c, const BootstrappingKeyMPLazyPipeAlt& b
     return key;
 }
 
+// BootstrappingKey (yatfhe/include/yatfhe/bootstrapping.h:16-45) -> device key: the TrgswDft
+// words of every key, [keys][l][k+1][k+1][N], with the key's group; the key-switching key
+// attached when given.
+inline yg_key* device_key_group(yg_ctx* c, const std::vector<TrgswDft>& bskDft, int group,
+                                const TlweKeySwitchingKey* ksk, int k, int N) {
+    auto& r = reg();
+    auto it = r.keys.find(&bskDft);
+    yg_key* key = nullptr;
+    if (it == r.keys.end()) {
+        std::vector<uint64_t> words;
+        for (const auto& g : bskDft)
+            for (const auto& lv : g.trlweDftSamples)
+                for (const auto& t : lv)
+                    for (int poly = 0; poly <= k; poly++) {
+                        const auto& P = poly < k ? t.a[poly] : t.b;
+                        words.insert(words.end(), P.coeffs.begin(), P.coeffs.begin() + N);
+                    }
+        const int levels = bskDft.empty() ? 0 : bskDft[0].l;
+        check(yg_key_upload_group(c, words.data(), group, levels, &key));
+        r.keys[&bskDft] = key;
+    } else {
+        key = it->second;
+    }
+    if (ksk && r.ksk_of[&bskDft] != ksk) {
+        std::vector<int32_t> flat;
+        for (const auto& row : ksk->decomposedKsk)
+            for (const auto& t : row) {
+                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
+                flat.push_back(static_cast<int32_t>(t.b));
+            }
+        check(yg_key_set_ksk(key, flat.data()));
+        r.ksk_of[&bskDft] = ksk;
+    }
+    return key;
+}
+
 template <typename T>
 struct DeviceBuf {
     T* p = nullptr;
@@ -296,6 +334,39 @@ inline void blindRotateLazyPipeAltNtt(Trlwe& accum, const BootstrappingKeyMPLazy
     for (int p = 0; p < k; p++)
         for (int j = 0; j < N; j++) accum.a[p].coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(p) * N + j]);
     for (int j = 0; j < N; j++) accum.b.coeffs[j] = static_cast<Torus>(acc[static_cast<size_t>(k) * N + j]);
+}
+
+// blindRotateNtt: the group-g blind rotation (param.group selects blindRotateNormalNtt,
+// blindRotateGroup2Ntt or blindRotateGroup3Ntt, as in the reference) of accum, already
+// genNoiselessTrlweSample'd, in place.
+inline void blindRotateNtt(Trlwe& accum, const std::vector<TrgswDft>& bskDft, const ScaledTlwe& input,
+                           const YatfheParameters& param) {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    yg_ctx* c = detail::context(detail::params_of(param, param.lApprox));
+    yg_key* key = detail::device_key_group(c, bskDft, param.group, nullptr, param.k, param.N);
+    detail::rotate_accumulator(c, key, accum, input, param);
+}
+
+// functionalBootstrappingNtt: the bootstrap on a group key (rescale, noiseless sample,
+// blindRotateNtt, extraction, key switching), one ciphertext.
+inline void functionalBootstrappingNtt(Tlwe& out, const Tlwe& input, const BootstrappingKey& bsk,
+                                       const TlweKeySwitchingKey& ksk, const TorusPolynomial& v,
+                                       const YatfheParameters& param) {
+    auto& r = detail::reg();
+    std::lock_guard<std::mutex> g(r.mu);
+    const int n = param.n, N = param.N;
+    yg_ctx* c = detail::context(detail::params_of(param, param.lApprox));
+    yg_key* key = detail::device_key_group(c, bsk.bskDft, bsk.group, &ksk, param.k, N);
+    std::vector<int32_t> in(static_cast<size_t>(n) + 1), res(static_cast<size_t>(n) + 1);
+    for (int i = 0; i < n; i++) in[i] = static_cast<int32_t>(input.a[i]);
+    in[n] = static_cast<int32_t>(input.b);
+    std::vector<int64_t> lut(N);
+    for (int j = 0; j < N; j++) lut[j] = static_cast<int64_t>(v.coeffs[j]);
+    detail::check(yg_pbs_host(c, key, in.data(), res.data(), 1, lut.data(), nullptr));
+    if (out.a.size() != static_cast<size_t>(n)) out = Tlwe{n};
+    for (int i = 0; i < n; i++) out.a[i] = static_cast<LweTorus>(res[i]);
+    out.b = static_cast<LweTorus>(res[n]);
 }
 
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,

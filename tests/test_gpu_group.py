@@ -97,3 +97,32 @@ def test_gpu_group_refusals(built_lib):
     h = ctypes.c_void_p()
     with pytest.raises(ValueError, match="group 1, 2 or 3"):
         _lib.check(_lib.lib().yg_key_upload_group(ctx.handle, ctypes.c_void_p(ok.ctypes.data), 4, p.l, ctypes.byref(h)))
+
+
+def test_gpu_group_rotates_a_given_accumulator(built_lib):
+    """yg_blind_rotate_acc with a group key (the adapter's blindRotateNtt): the mask already
+    switched to mod 2N and the accumulator after genNoiselessTrlweSample, rotated in place,
+    equal to the restatement's blind rotation."""
+    import ctypes
+
+    from yatfhe_gb300 import _lib, api
+
+    p = small(T32_N1024, 12)
+    ora = Restatement(p)
+    ora.keygen_group(17, 2)
+    ctx = api.Context(p, 0)
+    key = api.BootstrapKey.from_group_words(ctx, ora.group_words(), 2)
+    rng = np.random.default_rng(11)
+    lwe = rng.integers(-(1 << 31), 1 << 31, size=(6, p.n + 1), dtype=np.int64).astype(np.int32)
+    lut = rng.integers(-(1 << 31), 1 << 31, size=p.N, dtype=np.int64)
+    scaled = np.stack([ora.modswitch(x) for x in lwe])
+    acc = np.zeros((len(lwe), 2 * p.N), np.int64)
+    for c in range(len(lwe)):
+        acc[c, p.N:] = ora.rotate(lut, -int(scaled[c, p.n]), False)  # genNoiselessTrlweSample
+    d_scaled = torch.from_numpy(np.ascontiguousarray(scaled[:, : p.n])).cuda()
+    d_acc = torch.from_numpy(acc).cuda()
+    _lib.check(_lib.lib().yg_blind_rotate_acc(ctx.handle, key.handle, ctypes.c_void_p(d_scaled.data_ptr()),
+                                              ctypes.c_void_p(d_acc.data_ptr()), len(lwe), None))
+    got = d_acc.cpu().numpy()
+    for c in range(len(lwe)):
+        np.testing.assert_array_equal(got[c], ora.blind_rotate_group(lwe[c], lut), err_msg=f"ciphertext {c}")

@@ -1182,10 +1182,22 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
 
 int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled, int64_t* d_acc, int count,
                         void* stream) {
-    if (int rc = check_key(ctx, key, true, false)) return rc;
+    if (int rc = check_key(ctx, key, true, false, key && key->grouped())) return rc;
     if (count < 0) return set_err(YG_ERR_INVALID, "bad count");
     if (count == 0) return YG_OK;
     if (!d_scaled || !d_acc) return set_err(YG_ERR_INVALID, "bad buffers");
+    if (key->grouped()) {
+        return guarded([&] {
+            DeviceGuard g(ctx->device);
+            yg::GroupBrArgs a = group_args(ctx, key);
+            a.scaled_in = d_scaled;
+            a.acc_in = d_acc;
+            a.acc_out = d_acc;
+            a.count = count;
+            yg::check_launch(yg::launch_group_blind_rotate(a, stream), "group blind rotate launch");
+            return YG_OK;
+        });
+    }
     return guarded([&] {
         DeviceGuard g(ctx->device);
         yg::BrArgs a = br_args(ctx, key);

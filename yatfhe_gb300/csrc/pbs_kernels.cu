@@ -698,9 +698,14 @@ __global__ void __launch_bounds__(1024, 1) group_blind_rotate_kernel(const Group
         return neg ? tneg<T>(v) : v;
     };
 
-    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81)
-    const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
-    for (int i = t; i <= n; i += H) sa[i] = (int16_t)modswitch_down(in[i], 31 - logN, logN + 1);
+    // rescaleTlweToNewMod into mod 2N (yatfhe/src/tlwe.cpp:75-81), unless given already scaled
+    if (a.scaled_in) {
+        const int32_t* in = a.scaled_in + (size_t)ct * n;
+        for (int i = t; i < n; i += H) sa[i] = (int16_t)in[i];
+    } else {
+        const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+        for (int i = t; i <= n; i += H) sa[i] = (int16_t)modswitch_down(in[i], 31 - logN, logN + 1);
+    }
     __syncthreads();
     if (a.acc_in) {
         const int64_t* src = a.acc_in + (size_t)ct * 2 * N;
@@ -1667,7 +1672,8 @@ int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream) {
 int launch_group_blind_rotate(const GroupBrArgs& a, void* stream) {
     if (a.count <= 0) return 0;
     if ((a.N != 1024 && a.N != 2048) || a.group < 1 || a.group > 3 || a.n % a.group || a.L < 1 ||
-        a.L > a.l_full || a.l_full > kGroupMaxLevels || (!a.lut && !a.acc_in))
+        a.L > a.l_full || a.l_full > kGroupMaxLevels || (!a.lut && !a.acc_in) || (!a.lwe_in && !a.scaled_in) ||
+        (a.scaled_in && !a.acc_in))
         return -1;
     const size_t smem = group_br_smem_bytes(a.N, a.torus_bits, a.n, a.L);
     auto go = [&](auto kern) {

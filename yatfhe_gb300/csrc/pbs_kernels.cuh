@@ -164,7 +164,8 @@ __host__ __device__ inline size_t lazy_br_smem_bytes(int N, int torus_bits, int 
 // words of the levels the external product uses.
 constexpr int kGroupMaxLevels = 8;  // levels of the key's decomposition (the reference's l)
 struct GroupBrArgs {
-    const int32_t* lwe_in;   // [count][n+1]
+    const int32_t* lwe_in;   // [count][n+1], or null when scaled_in is given
+    const int32_t* scaled_in;// [count][n] mask already switched to mod 2N (with acc_in), or null
     const int64_t* lut;      // [N] test polynomial v, or null when acc_in is given
     const int64_t* acc_in;   // [count][2 N] starting accumulator, or null
     const uint64_t* key;     // [keys][L][2][2][N] NTT-domain words mod q ([lvl][col][col2])
