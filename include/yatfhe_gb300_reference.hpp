@@ -16,6 +16,8 @@
 //   blindRotateJP22Ntt             yatfhe/include/yatfhe/blind_rotate.h:65 (binary keys)
 //   blindRotateWWL24Ntt            yatfhe/include/yatfhe/blind_rotate.h:61
 //   blindRotateLazyPipeAltNtt      yatfhe/include/yatfhe/blind_rotate.h:44-45
+//   blindRotateLazyPipeAltNttSweep yatfhe/include/yatfhe/blind_rotate.h:48-50
+//   blindRotateLazyPipeAltInitNtt  yatfhe/include/yatfhe/blind_rotate.h:56-57
 //   blindRotateNtt                 yatfhe/include/yatfhe/blind_rotate.h:13 (groups 1-3)
 //   functionalBootstrappingNtt     yatfhe/include/yatfhe/bootstrapping.h:366-367
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
@@ -35,6 +37,7 @@
 #include <vector>
 
 #include "yatfhe_gb300.h"
+#include "yautil/ya_serializer.h"  // deserializeBskLazyPipeAlt, for blindRotateLazyPipeAltInitNtt
 
 namespace yatfhe_gb300 {
 
@@ -367,6 +370,35 @@ inline void functionalBootstrappingNtt(Tlwe& out, const Tlwe& input, const Boots
     if (out.a.size() != static_cast<size_t>(n)) out = Tlwe{n};
     for (int i = 0; i < n; i++) out.a[i] = static_cast<LweTorus>(res[i]);
     out.b = static_cast<LweTorus>(res[n]);
+}
+
+// blindRotateLazyPipeAltNttSweep: the same rotation with another split of the reference's
+// CPU pipeline (moveNtt, unitsA), which does not change its result.
+inline void blindRotateLazyPipeAltNttSweep(Trlwe& accum, const BootstrappingKeyMPLazyPipeAlt& bsk,
+                                           const ScaledTlwe& input, const TorusPolynomial& v,
+                                           const std::vector<NttPolynomial>& gdVntt, int moveNtt, int unitsA,
+                                           const YatfheParameters& param) {
+    (void)moveNtt;
+    (void)unitsA;
+    yatfhe_gb300::blindRotateLazyPipeAltNtt(accum, bsk, input, v, gdVntt, param);
+}
+
+// blindRotateLazyPipeAltInitNtt: the key read from fileName into bsk (the reference reads it
+// while it rotates), then the same rotation on the GPU.
+inline void blindRotateLazyPipeAltInitNtt(Trlwe& accum, BootstrappingKeyMPLazyPipeAlt& bsk, const ScaledTlwe& input,
+                                          const TorusPolynomial& v, const std::string& fileName,
+                                          const std::vector<NttPolynomial>& gdVntt, const YatfheParameters& param) {
+    deserializeBskLazyPipeAlt(bsk, fileName, param.n);
+    {
+        auto& r = detail::reg();
+        std::lock_guard<std::mutex> g(r.mu);
+        auto it = r.keys.find(&bsk);
+        if (it != r.keys.end()) {  // a key cached for this object before it was read again
+            yg_key_destroy(it->second);
+            r.keys.erase(it);
+        }
+    }
+    yatfhe_gb300::blindRotateLazyPipeAltNtt(accum, bsk, input, v, gdVntt, param);
 }
 
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,

@@ -437,6 +437,14 @@ class Reference(_Common):
         self._call("pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
         return (out, acc) if with_acc else out
 
+    def pbs_lazy_sweep(self, lwe, v, move_ntt: int, units_a: int) -> np.ndarray:
+        """ref_pbs_lazy with blindRotateLazyPipeAltNttSweep's pipeline split."""
+        lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
+        v = np.ascontiguousarray(v, np.int64)
+        out = np.zeros_like(lwe)
+        self._call("pbs_lazy_sweep", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), move_ntt, units_a)
+        return out
+
     def set_keys(self, lwe_s, rlwe_s) -> None:
         a = np.ascontiguousarray(lwe_s, np.int32)
         b = np.ascontiguousarray(rlwe_s, np.int32)

@@ -676,6 +676,10 @@ int ref_load_lazy(const char* path) {
 // rotation: prepareGdV once (yatfhe/src/trgsw.cpp:911-927), then per ciphertext the lazy blind
 // rotation (which builds the accumulator from v itself), extraction and key switching.  acc0
 // (may be null) receives ciphertext 0's accumulator after the blind rotation.
+namespace {
+int sweep_move = -1, sweep_units = 2;  // ref_pbs_lazy_sweep's split; -1: blindRotateLazyPipeAltNtt
+}
+
 int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
     auto& s = st();
     if (!s.lazy || !s.ksk) return fail("ref_pbs_lazy: keys not loaded");
@@ -693,7 +697,10 @@ int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, i
             Trlwe acc{k, N};
             Tlwe big{s.ksk->nCurrKey};
             rescaleTlweToNewMod(sc, x);
-            blindRotateLazyPipeAltNtt(acc, *s.lazy, sc, vp, gdV, p);
+            if (sweep_move < 0)
+                blindRotateLazyPipeAltNtt(acc, *s.lazy, sc, vp, gdV, p);
+            else
+                blindRotateLazyPipeAltNttSweep(acc, *s.lazy, sc, vp, gdV, sweep_move, sweep_units, p);
             if (c == 0 && acc0) {
                 for (int r = 0; r < k; r++) fromPoly(acc0 + static_cast<size_t>(r) * N, acc.a[r], N);
                 fromPoly(acc0 + static_cast<size_t>(k) * N, acc.b, N);
@@ -781,6 +788,16 @@ int ref_pbs_group(const int32_t* in, int count, const int64_t* v, int32_t* out, 
             fromTlwe(out + static_cast<size_t>(c) * (n + 1), y, n);
         }
     });
+}
+
+// ref_pbs_lazy with blindRotateLazyPipeAltNttSweep (yatfhe/src/blind_rotate.cpp:1001-1135) and
+// the given split of its pipeline (moveNtt digit levels transformed in stageA, unitsA workers).
+int ref_pbs_lazy_sweep(const int32_t* in, int count, const int64_t* v, int32_t* out, int move_ntt, int units_a) {
+    sweep_move = move_ntt;
+    sweep_units = units_a;
+    const int rc = ref_pbs_lazy(in, count, v, out, nullptr);
+    sweep_move = -1;
+    return rc;
 }
 
 int ref_pool_size(void) { return static_cast<int>(ThreadPool::usableConcurrency()); }

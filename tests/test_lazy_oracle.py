@@ -113,3 +113,20 @@ def test_lazy_matches_reference(base, tmp_path):
     out, acc0 = ref.pbs_lazy(lwe, v, with_acc=True)
     np.testing.assert_array_equal(ora.blind_rotate_lazy(lwe[0], v), acc0)
     np.testing.assert_array_equal(ora.pbs_lazy(lwe, v, threads=3), out)
+
+
+@needs_reference
+def test_lazy_sweep_split_gives_the_same_outputs():
+    """blindRotateLazyPipeAltNttSweep only splits the pipeline's work differently (how many
+    digit levels stageA transforms, how many workers run it): every split gives the outputs
+    of blindRotateLazyPipeAltNtt, which is what the adapter maps it to."""
+    p = small(WWL24_T32_N2048, 6)
+    ref = o.Reference(p)
+    ref.keygen_lazy(12)
+    rng = np.random.default_rng(3)
+    mu = np.where(rng.integers(0, 2, 2) == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    lwe = ref.encrypt(mu)
+    v = lutmod.sign_lut(p.N, p.torus_bits)
+    want = ref.pbs_lazy(lwe, v)
+    for move, units in [(0, 1), (1, 2), (2, 2), (4, 3), (8, 4)]:
+        np.testing.assert_array_equal(ref.pbs_lazy_sweep(lwe, v, move, units), want, err_msg=f"{move}, {units}")

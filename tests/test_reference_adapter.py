@@ -22,13 +22,15 @@ void use(Tlwe& out, const Tlwe& in, const BootstrappingKeyMP& bsk, const TlweKey
          const TorusPolynomial& v, const YatfheParameters& p, Trlwe& acc, const ScaledTlwe& s,
          std::vector<Tlwe>& outs, const std::vector<Tlwe>& ins, const BootstrappingKeyWWL24& wwl,
          const BootstrappingKeyMPLazyPipeAlt& lazy, const std::vector<NttPolynomial>& gdV,
-         const BootstrappingKey& gbsk) {
+         const BootstrappingKey& gbsk, BootstrappingKeyMPLazyPipeAlt& lazy2) {
     yatfhe_gb300::functionalBootstrappingMPNtt(out, in, bsk, ksk, v, p);
     yatfhe_gb300::functionalBootstrappingMPNttBatch(outs, ins, bsk, ksk, v, p);
     yatfhe_gb300::blindRotateMP21Ntt(acc, bsk.bskDft, s, p);
     yatfhe_gb300::blindRotateJP22Ntt(acc, bsk, s, p);
     yatfhe_gb300::blindRotateWWL24Ntt(acc, wwl, s, p);
     yatfhe_gb300::blindRotateLazyPipeAltNtt(acc, lazy, s, v, gdV, p);
+    yatfhe_gb300::blindRotateLazyPipeAltNttSweep(acc, lazy, s, v, gdV, 2, 2, p);
+    yatfhe_gb300::blindRotateLazyPipeAltInitNtt(acc, lazy2, s, v, "BSK_OURS.bin", gdV, p);
     yatfhe_gb300::blindRotateNtt(acc, gbsk.bskDft, s, p);
     yatfhe_gb300::functionalBootstrappingNtt(out, in, gbsk, ksk, v, p);
     yatfhe_gb300::switchKeyForTlwe(out, ksk, in, p);
