@@ -19,7 +19,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF_TREE = Path(os.environ.get("YATFHE_REFERENCE", "/root/reference"))
+# The reference tree: $YATFHE_REFERENCE, else a checkout named "reference" beside this
+# repository.  Absent on machines that only run the restatement.
+REF_TREE = Path(os.environ.get("YATFHE_REFERENCE", HERE.parent.parent / "reference"))
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)

@@ -14,12 +14,16 @@
 // N = 2048); larger counts are rejected with YG_ERR_INVALID.
 //
 // The array's name is only a host-side stand-in in host code, so its device address is
-// looked up with cudaGetSymbolAddress, once per device with that device current, by the
-// first call on that device; make that first call before any stream capture.  All calls
-// share the one array and it keeps the previous call's contents: the blind-rotation
-// kernel overwrites every word the key switch then reads, so nothing has to start at zero,
-// but calls that overlap on the GPU (on different streams, or from several threads without
-// ordering) race on it and must be serialised by the caller.
+// looked up with cudaGetSymbolAddress, once per device with that device current.  The
+// driver loads a module's device variables lazily, so that lookup is also the moment the
+// array's 16 MiB are committed on the device.  A call with count 0 does this set-up alone,
+// and also loads the two kernels a call launches (kernels too are loaded on first use):
+// make it at start-up, before any stream capture and before the point from which the
+// caller allows no more allocation.  Without it, the first call with count > 0 on a device
+// does the set-up itself.  All calls share the one array and it keeps the previous call's
+// contents: the blind-rotation kernel overwrites every word the key switch then reads, so
+// nothing has to start at zero, but calls that overlap on the GPU (on different streams, or
+// from several threads without ordering) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -48,6 +52,16 @@ int32_t* scratch_on(int device) {
     return g_scratch_ptr[device];
 }
 
+// The set-up a call with count 0 does on the context's device (current): the scratch
+// address looked up, and the kernels of a call loaded in the context's launch shape.
+void setup(const yg_ctx* ctx) {
+    scratch_on(ctx->device);
+    const int rc = yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, ctx->per_cta,
+                                      ctx->layout);
+    if (rc == -1) yg::ck(cudaGetLastError(), "loading the blind-rotation kernel");
+    if (yg::preload_keyswitch() != 0) yg::ck(cudaGetLastError(), "loading the key-switching kernel");
+}
+
 }  // namespace
 
 extern "C" size_t yg_pbs_noalloc_max_count(const yg_ctx* ctx) {
@@ -59,7 +73,12 @@ extern "C" int yg_pbs_noalloc(yg_ctx* ctx, const yg_key* key, const int32_t* d_i
                               const int64_t* d_lut, void* stream) {
     if (int rc = yg::check_key(ctx, key, true, true)) return rc;
     if (count < 0 || (count > 0 && (!d_in || !d_out || !d_lut))) return yg::set_err(YG_ERR_INVALID, "bad buffers");
-    if (count == 0) return YG_OK;
+    if (count == 0)
+        return yg::guarded([&] {
+            yg::DeviceGuard g(ctx->device);
+            setup(ctx);
+            return YG_OK;
+        });
     const size_t max_count = yg_pbs_noalloc_max_count(ctx);
     if ((size_t)count > max_count)
         return yg::set_err(YG_ERR_INVALID, "yg_pbs_noalloc: " + std::to_string(count) +

@@ -1686,6 +1686,11 @@ int launch_group_blind_rotate(const GroupBrArgs& a, void* stream) {
     return -1;
 }
 
+int preload_keyswitch() {
+    cudaFuncAttributes attr;
+    return cudaFuncGetAttributes(&attr, keyswitch_kernel) == cudaSuccess ? 0 : -1;
+}
+
 int launch_keyswitch(const KsArgs& a, void* stream) {
     if (a.count <= 0) return 0;
     if (a.t > kKsMaxT) return -1;

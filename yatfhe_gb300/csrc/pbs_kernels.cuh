@@ -248,6 +248,9 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 constexpr int kNoVariant = -2;
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
 int launch_keyswitch(const KsArgs& a, void* stream);
+// Loads the key-switching kernel on the current device (the driver loads kernels lazily, on
+// first use); 0 on success.
+int preload_keyswitch();
 int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream);
 int launch_group_blind_rotate(const GroupBrArgs& a, void* stream);
 
