@@ -142,7 +142,7 @@ void validate(const yg_params& p) {
     if (p.l_approx < 1 || p.radix_bits < 1 || p.l_approx * p.radix_bits > p.torus_bits)
         throw std::invalid_argument("decomposeRow: l * radixBits exceeds the torus width");
     if (p.radix_bits > 15) throw std::invalid_argument("radix_bits must be <= 15 (int16 digits)");
-    // the channel-row layout at T = 32 sums 2 l products of transform outputs (< 22p) and
+    // the channel-row layout at T = 32 sums 2 l products of transform outputs (< 46p) and
     // key words (< p) exactly in 64 bits: below 2^64 for l <= 15
     if (p.l_approx > 15) throw std::invalid_argument("l must be <= 15");
     if (p.ks_level < 1 || p.ks_level > 16 || p.ks_radix_bits < 1 || p.ks_level * p.ks_radix_bits > 32 ||
@@ -156,21 +156,51 @@ void validate(const yg_params& p) {
     if (bound >= M / 4) throw std::invalid_argument("parameters exceed the exact range of the RNS");
 }
 
+// Twiddle tables of the team NTT (ntt.cuh), per channel [forward N | inverse 2N]:
+//   forward: psi^brv(k), thread-minor (thread_minor_layout); its first 32 entries also go to
+//            the constant bank;
+//   inverse, Cooley-Tukey form (prime set 1, N = 1024): entries 32 (2^sp - 1) + m 32 + tt =
+//            psi^-((N / 2^(5+sp)) (m 32 + tt)) for the stages on index bits 5 + sp, then
+//            992 + j = psi^-j (the twist); the constant bank gets psi^-((N / 2^sp) m) at
+//            2^sp + m for the stages on slot bits sp = 1..4 (entry 1: the twiddle 1 of bit 0);
+//   inverse, Gentleman-Sande form (the other shapes): psi^-brv(k), thread-minor, first 32
+//            entries to the constant bank.
 void ctx_init_tables(yg_ctx* c) {
     const int N = c->p.N;
-    std::vector<uint2> tw((size_t)yg::kChannels * 2 * N);
+    const size_t per = (size_t)3 * N;  // words of one channel's tables
+    const bool ct_inverse = c->ps == 1 && N == 1024;
+    std::vector<uint2> tw((size_t)yg::kChannels * per);
+    std::vector<uint2> heads((size_t)yg::kChannels * 2 * 32);
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimeSet[c->ps][ci];
         const u64 psi = minimal_root(N, p);
         const u64 psi_inv = invmod(psi, p);
+        uint2* fwd = &tw[ci * per];
+        uint2* inv = fwd + N;
+        auto pair = [p](u64 w) { return make_uint2((uint32_t)w, shoup32((uint32_t)w, p)); };
         for (int k = 0; k < N; k++) {
             const uint32_t e = brv(k, c->logN);
-            const uint32_t wf = (uint32_t)powmod(psi, e, p), wi = (uint32_t)powmod(psi_inv, e, p);
-            tw[((size_t)ci * 2 + 0) * N + k] = make_uint2(wf, shoup32(wf, p));
-            tw[((size_t)ci * 2 + 1) * N + k] = make_uint2(wi, shoup32(wi, p));
+            fwd[k] = pair(powmod(psi, e, p));
+            if (!ct_inverse) inv[k] = pair(powmod(psi_inv, e, p));
         }
-        thread_minor_layout(&tw[((size_t)ci * 2 + 0) * N], N);
-        thread_minor_layout(&tw[((size_t)ci * 2 + 1) * N], N);
+        thread_minor_layout(fwd, N);
+        for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + 0) * 32 + k] = fwd[k];
+        if (ct_inverse) {
+            for (int sp = 0; sp <= 4; sp++) {
+                const int h = 1 << sp;
+                for (int m = 0; m < h; m++)
+                    for (int tt = 0; tt < 32; tt++)
+                        inv[32 * (h - 1) + m * 32 + tt] = pair(powmod(psi_inv, (u64)(N / (32 * h)) * (m * 32 + tt), p));
+            }
+            for (int j = 0; j < N; j++) inv[992 + j] = pair(powmod(psi_inv, j, p));
+            uint2* hd = &heads[((size_t)ci * 2 + 1) * 32];
+            hd[0] = hd[1] = pair(1);
+            for (int sp = 1; sp <= 4; sp++)
+                for (int m = 0; m < (1 << sp); m++) hd[(1 << sp) + m] = pair(powmod(psi_inv, (u64)(N >> sp) * m, p));
+        } else {
+            thread_minor_layout(inv, N);
+            for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + 1) * 32 + k] = inv[k];
+        }
         // Montgomery form with N^-1 folded in: N^-1 2^32 mod p
         const uint32_t sc = (uint32_t)mulmod(invmod(N, p), ((u64)1 << 32) % p, p);
         c->conv_scale[ci] = sc;
@@ -178,17 +208,12 @@ void ctx_init_tables(yg_ctx* c) {
     }
     ck(cudaMalloc(&c->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
     ck(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
-    std::vector<uint2> heads((size_t)yg::kChannels * 2 * 32);
-    for (int ci = 0; ci < yg::kChannels; ci++)
-        for (int dir = 0; dir < 2; dir++)
-            for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + dir) * 32 + k] = tw[((size_t)ci * 2 + dir) * N + k];
     if (yg::set_twiddle_heads(c->logN, c->ps, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimeSet[c->ps][ci];
         uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
         for (int it = 0; it < 5; it++) pinv *= 2 - p * pinv;
-        c->ch[ci] = yg::Chan{p, 2 * p, (uint32_t)(0u - pinv), 0, c->d_tw + (size_t)ci * 2 * N,
-                             c->d_tw + ((size_t)ci * 2 + 1) * N};
+        c->ch[ci] = yg::Chan{p, 2 * p, (uint32_t)(0u - pinv), 0, c->d_tw + ci * per, c->d_tw + ci * per + N};
     }
     const u64 p0 = yg::kPrimeSet[c->ps][0], p1 = yg::kPrimeSet[c->ps][1], p2 = yg::kPrimeSet[c->ps][2];
     yg::Crt& k = c->crt;
@@ -205,8 +230,8 @@ void ctx_init_tables(yg_ctx* c) {
     k.p01 = p0 * p1;
     k.q = c->q;
     k.half_q = (c->q - 1) / 2;
-    k.a2 = (float)((double)k.p01 / (double)c->q);
-    k.a1 = (float)((double)p0 / (double)c->q);
+    k.a2 = (int64_t)((((u128)k.p01 << 32) + c->q / 2) / c->q);
+    k.a1 = (uint32_t)((((u128)p0 << 32) + c->q / 2) / c->q);
 }
 
 // NTT-domain key words -> device key.  Layout in: [n][L][k+1][k+1][N] u64.

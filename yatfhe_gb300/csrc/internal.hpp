@@ -78,7 +78,7 @@ struct yg_ctx {
     int ps = 0;             // RNS prime set (rns.cuh), fixed by the torus width
     int device = 0;
     uint64_t q = 0;
-    uint2* d_tw = nullptr;  // [3][2][N]: forward then inverse twiddles per channel
+    uint2* d_tw = nullptr;  // [3][3N]: forward twiddles (N), then the inverse table (2N) per channel
     yg::Chan ch[yg::kChannels]{};
     yg::Crt crt{};
     uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};

@@ -20,6 +20,17 @@
 // Forward: natural -> 5 register stages -> transpose through shared memory -> slot -> 5
 // register stages (+ the shuffle stage at N = 2048).  Inverse mirrors it.  Pointwise
 // products happen in the slot layout, so the key is stored in that layout.
+//
+// Prime set 1 (the 32-bit torus, p < 2^26.48) runs every stage on biased values (rns.cuh,
+// ct_bfly_b): the forward input carries an offset of at least 2p per stage (fwd_bias_*), so
+// no butterfly wraps and none reduces; outputs stay below 46p.  Its inverse at N = 1024 is
+// a Cooley-Tukey (decimation-in-time) transform too: on bit-reversed slots with
+// omega = psi^2, the stages on slot bits 0..4 take twiddles psi^-((N / 2^sp) m) that depend
+// only on the register index (constant bank; bit 0 needs none), the stages on bits 5..9
+// per-thread twiddles psi^-((N / 2^(5+sp)) (m 32 + tt)) (entries 32 (2^sp - 1) + m 32 + tt of
+// the inverse table), and a final twist by psi^-j (entries 992 + j) turns the cyclic
+// inverse into the negacyclic one.  Other shapes keep the Gentleman-Sande inverse with
+// psi^-brv(k) twiddles.
 #pragma once
 #include "rns.cuh"
 
@@ -63,6 +74,15 @@ __device__ __forceinline__ void team_sync(int bar) {
     }
 }
 
+// Offset of the forward transform's input.  Prime set 1: 2p per stage on top of the value
+// (signed digits |d| < p: one more p), so the biased butterflies never wrap; prime set 0:
+// p, which makes signed digits non-negative.
+template <int LOGN, int PS>
+__device__ __forceinline__ uint32_t fwd_bias_digits(uint32_t p) { return PS == 1 ? (2 * LOGN + 1) * p : p; }
+// The same for residues already in [0, p).
+template <int LOGN, int PS>
+__device__ __forceinline__ uint32_t fwd_bias_residues(uint32_t p) { return PS == 1 ? 2 * LOGN * p : 0; }
+
 template <int LOGN>
 __device__ __forceinline__ int slot_pos(int tt, int r) {
     if constexpr (LOGN == 10) return tt * 32 + r;
@@ -80,28 +100,34 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
                                             const uint32_t* tab = nullptr) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
+    const uint32_t neg_p = 0u - p;
     if constexpr (TAB) {
+        // prime set 1: offset 2p for each of the LOGN - 1 stages left, and p for t < p
+        const uint32_t bx = PS == 1 ? 2 * LOGN * p : p, by = PS == 1 ? 2 * LOGN * p : 3 * p;
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
             const int dx = (int)a[r], dy = (int)a[r + 16];
             const uint32_t t = tab[dy];
-            a[r] = (uint32_t)(dx + (int)p) + t;
-            a[r + 16] = (uint32_t)(dx + 3 * (int)p) - t;
+            a[r] = (uint32_t)dx + bx + t;
+            a[r + 16] = (uint32_t)dx + by - t;
         }
     }
     // Input residues < 2p; every butterfly adds at most 2p to the bound of its x input.
     // Prime set 0 (p < 2^29, 8p < 2^32): natural-layout stages 4p, 6p, 8p, reduce -> 6p, 8p;
     // slot-layout stages reduce -> 6p, 8p, reduce -> 6p, 8p, reduce -> 6p (then the N = 2048
-    // shuffle stage, reduce -> 6p).  Output < 8p.  Prime set 1 (p < 2^27, 32p < 2^32): no
-    // reduction; output < 22p (N = 1024) or 24p (N = 2048).
+    // shuffle stage, reduce -> 6p).  Output < 8p.  Prime set 1 (p < 2^26.48): biased
+    // butterflies, no reduction; the input offset (fwd_bias_*, or the table stage's 2 LOGN p)
+    // falls by less than 2p per stage and the value grows by less than 2p, so the output
+    // stays below (4 LOGN + 1) p + 2^14 < 46p < 2^32.
 #pragma unroll
     for (int sp = TAB ? 3 : 4; sp >= 0; --sp) {
         const int h = 1 << sp;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], c_tw_head[PS][LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))], p, two_p,
-                    PS == 0 && sp == 1);
+            const uint2 w = c_tw_head[PS][LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))];
+            if constexpr (PS == 1) ct_bfly_b(a[r], a[r + h], w, neg_p);
+            else ct_bfly(a[r], a[r + h], w, p, two_p, sp == 1);
         }
     }
     team_sync<LOGN>(bar);
@@ -118,7 +144,9 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
 #pragma unroll
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
-            ct_bfly(a[r], a[r + h], __ldg(&tw[(r >> (sp + 1)) * 32]), p, two_p, PS == 0 && (sp & 1) == 0);
+            const uint2 w = __ldg(&tw[(r >> (sp + 1)) * 32]);
+            if constexpr (PS == 1) ct_bfly_b(a[r], a[r + h], w, neg_p);
+            else ct_bfly(a[r], a[r + h], w, p, two_p, (sp & 1) == 0);
         }
     }
     if constexpr (LOGN == 11) {
@@ -130,15 +158,62 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
             const uint32_t xr = PS == 0 ? reduce_once(a[r], 2 * two_p) : a[r];  // U, held by the even lane
             const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
             const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
-            a[r] = odd ? other - t + two_p : xr + other;
+            a[r] = odd ? other - t + (PS == 1 ? 0u : two_p) : xr + other;
         }
     }
 }
 
+// Input residues in [0, 2p) in the slot layout; output N times the coefficients in [0, 2p),
+// natural layout.
 template <int LOGN, int PS>
 __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
+    if constexpr (PS == 1 && LOGN == 10) {
+        const uint32_t neg_p = 0u - p;
+        // slot bit 0: twiddle 1, no multiply; offsets 18p / 20p keep the nine biased stages
+        // that follow from wrapping: [0, 2p) -> [18p, 22p), at most 40p at the end
+        const uint32_t b18 = 18 * p, b20 = 20 * p;
+#pragma unroll
+        for (int r = 0; r < 32; r += 2) {
+            const uint32_t x = a[r], y = a[r + 1];
+            a[r] = x + y + b18;
+            a[r + 1] = x - y + b20;
+        }
+#pragma unroll
+        for (int sp = 1; sp <= 4; ++sp) {
+            const int h = 1 << sp;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                if (r & h) continue;
+                ct_bfly_b(a[r], a[r + h], c_tw_head[PS][0][team][1][h + (r & (h - 1))], neg_p);
+            }
+        }
+        team_sync<LOGN>(bar);
+#pragma unroll
+        for (int r = 0; r < 32; ++r) tb[tpad(slot_pos<LOGN>(tt, r))] = a[r];
+        team_sync<LOGN>(bar);
+#pragma unroll
+        for (int r = 0; r < 32; ++r) a[r] = tb[tpad(r * S + tt)];
+#pragma unroll
+        for (int sp = 0; sp <= 4; ++sp) {
+            const int h = 1 << sp;
+            const uint2* tw = pinned(ch.twi) + 32 * (h - 1) + tt;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                if (r & h) continue;
+                ct_bfly_b(a[r], a[r + h], __ldg(&tw[(r & (h - 1)) * 32]), neg_p);
+            }
+        }
+        // twist by psi^-j, j = r S + tt: the negacyclic transform from the cyclic one
+        const uint2* tw = pinned(ch.twi) + 992 + tt;
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            const uint2 w = __ldg(&tw[r * 32]);
+            a[r] = mulshoup(a[r], w.x, w.y, p);
+        }
+        return;
+    }
     const int gid = LOGN == 10 ? tt : (tt >> 1);
     if constexpr (LOGN == 11) {
         const bool odd = tt & 1;

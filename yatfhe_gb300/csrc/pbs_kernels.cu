@@ -118,8 +118,9 @@ __global__ void __launch_bounds__(3 * TeamShape<LOGN>::S) keyconv_kernel(const K
     const uint32_t scs = team == 0 ? a.scale_s[0] : (team == 1 ? a.scale_s[1] : a.scale_s[2]);
     const uint32_t* src = a.residues + ((size_t)poly * kChannels + team) * N;
     uint32_t x[32];
+    const uint32_t bias = fwd_bias_residues<LOGN, PS>(ch.p);
 #pragma unroll
-    for (int r = 0; r < 32; ++r) x[r] = src[r * S + tt];
+    for (int r = 0; r < 32; ++r) x[r] = src[r * S + tt] + bias;
     ntt_forward<LOGN, PS>(x, tb + team * Sh::TBUF, tt, team, team, ch);
     const int blk = poly >> 1, o = poly & 1;
     uint32_t* dst = a.key + ((size_t)blk * kChannels + team) * key_block_words(N);
@@ -928,8 +929,9 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 return;
             }
         }
+        const uint32_t bias = fwd_bias_digits<LOGN, PS>(ch.p);
 #pragma unroll
-        for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + tt] + (int32_t)ch.p);
+        for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + tt] + bias;
         ntt_forward<LOGN, PS>(x, mine, tt, team, bar, ch);
     };
 
@@ -1061,8 +1063,9 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 // this team's row: l forward NTTs.  After each one the two teams of the
                 // channel swap their transforms through their own regions, and each
                 // accumulates only the output it finishes (row 0 -> a, row 1 -> b) from both
-                // rows' digits, as exact 64-bit sums: 2 l products below 22p * p each stay
-                // under 2^64 with the 27-bit primes; one Montgomery reduction at the end.
+                // rows' digits, as exact 64-bit sums: 2 l products below 46p * p each stay
+                // under 2^64 with the 26.5-bit primes (l <= 15); one Montgomery reduction at
+                // the end.
                 const int row = hrow;
                 const uint32_t* other = xb + (team * 2 + (1 - hrow)) * Sh::TBUF;
                 uint64_t acc64[32];
@@ -1095,7 +1098,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                     }
                     pair_sync<LOGN>(pair_bar);  // the partner has read this region
                 }
-                // S 2^-32 mod p: m = lo(S) p^-1, (S - m p) / 2^32 = hi(S) - hi(m p) in (-p, 2^29.2),
+                // S 2^-32 mod p: m = lo(S) p^-1, (S - m p) / 2^32 = hi(S) - hi(m p) in (-p, 2^31.4),
                 // + p, then one Shoup reduction by 1 to [0, 2p) for the inverse transform
                 const uint32_t one_s = 0xFFFFFFFFu / ch.p;
 #pragma unroll
@@ -1332,8 +1335,9 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane];
             ntt_forward<10, PS, true>(x, mine, lane, c, 0, ch, tab0 + c * 132 + 64);
         } else {
+            const uint32_t bias = fwd_bias_digits<10, PS>(ch.p);
 #pragma unroll
-            for (int r = 0; r < 32; ++r) x[r] = (uint32_t)((int32_t)d[r * S + lane] + (int32_t)ch.p);
+            for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane] + bias;
             ntt_forward<10, PS>(x, mine, lane, c, 0, ch);
         }
         {
@@ -1345,7 +1349,7 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         const uint32_t* theirs = my_exch + (size_t)ph * team_words;
         ph ^= 1;
         // (3) output h: own row with K(lvl, h, h), the partner's row with K(lvl, 1-h, h);
-        // x < 22p and key words < p: the sum of two products fits 64 bits
+        // x < 46p and key words < p: the sum of two products fits 64 bits
         {
             const size_t blk = (size_t)i * L + lvl;
             const uint4* kown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
