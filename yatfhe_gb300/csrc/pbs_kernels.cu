@@ -1063,14 +1063,14 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
                 // this team's row: l forward NTTs.  After each one the two teams of the
                 // channel swap their transforms through their own regions, and each
                 // accumulates only the output it finishes (row 0 -> a, row 1 -> b) from both
-                // rows' digits, as exact 64-bit sums: 2 l products below 46p * p each stay
-                // under 2^64 with the 26.5-bit primes (l <= 15); one Montgomery reduction at
-                // the end.
+                // rows' digits: per level the two products (< 46p * p each) are summed exactly in
+                // 64 bits and reduced once (Montgomery, a term in (-p, 2.1p)); the 32-bit sum
+                // starts at l p, so it stays in (0, 3.1 l p), below 2^32 for l <= 15.
                 const int row = hrow;
                 const uint32_t* other = xb + (team * 2 + (1 - hrow)) * Sh::TBUF;
-                uint64_t acc64[32];
+                uint32_t acc32[32];
 #pragma unroll
-                for (int r = 0; r < 32; ++r) acc64[r] = 0;
+                for (int r = 0; r < 32; ++r) acc32[r] = L * ch.p;
                 for (int lvl = 0; lvl < L; ++lvl) {
                     uint32_t x[32];
                     load_and_forward(x, dig + ((size_t)row * L + lvl) * N);
@@ -1092,19 +1092,17 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             const int r = rr * 4 + e;
-                            acc64[r] += (uint64_t)x[r] * kav[e];
-                            acc64[r] += (uint64_t)other[r * S + tt] * kbv[e];
+                            const uint64_t sp = (uint64_t)x[r] * kav[e] + (uint64_t)other[r * S + tt] * kbv[e];
+                            acc32[r] += (uint32_t)(sp >> 32) - __umulhi((uint32_t)sp * pinv, ch.p);
                         }
                     }
                     pair_sync<LOGN>(pair_bar);  // the partner has read this region
                 }
-                // S 2^-32 mod p: m = lo(S) p^-1, (S - m p) / 2^32 = hi(S) - hi(m p) in (-p, 2^31.4),
-                // + p, then one Shoup reduction by 1 to [0, 2p) for the inverse transform
+                // one Shoup reduction by 1 to [0, 2p) for the inverse transform
                 const uint32_t one_s = 0xFFFFFFFFu / ch.p;
 #pragma unroll
                 for (int r = 0; r < 32; ++r) {
-                    const uint32_t lo = (uint32_t)acc64[r], hi = (uint32_t)(acc64[r] >> 32);
-                    const uint32_t t = hi - __umulhi(lo * pinv, ch.p) + ch.p;
+                    const uint32_t t = acc32[r];
                     oa[r] = t - __umulhi(t, one_s) * ch.p;
                 }
                 ntt_inverse<LOGN, PS>(oa, mine, tt, team, bar, ch);
@@ -1309,6 +1307,18 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         const int t2 = ai < 0 ? ai + 2 * N : ai;
         const bool wrap = t2 >= N;
         const int at = wrap ? t2 - N : t2;
+        // this step's key lines of the team (step 3 reads them), requested now so that they
+        // arrive in L1 while the digits and the forward transform are computed
+        {
+            const size_t blk = (size_t)i * L + lvl;
+            const uint4* po = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S + lane;
+            const uint4* pp = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S + lane;
+#pragma unroll
+            for (int rr = 0; rr < 8; ++rr) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(po + rr * S));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(pp + rr * S));
+            }
+        }
         // (1) X^{a_i} row - row, zero-mean digits (rotateTrlweMinusOne, gadgetDecomposeTrlwe)
         auto decompose = [&](auto lc, auto rc) {
             constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
@@ -1345,29 +1355,33 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
 #pragma unroll
             for (int r = 0; r < 32; ++r) dst[r * S + lane] = x[r];
         }
+        // (3) output h: own row with K(lvl, h, h), the partner's row with K(lvl, 1-h, h);
+        // x < 46p and key words < p: the sum of two products fits 64 bits.  The own row's
+        // products are formed while the partner may still be transforming.
+        const size_t blk = (size_t)i * L + lvl;
+        const uint4* kown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+        const uint4* kpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+        uint64_t own[32];
+#pragma unroll
+        for (int rr = 0; rr < 8; ++rr) {
+            const uint4 ka = ldg_keep(kown + rr * S + lane, keep);
+            const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) own[rr * 4 + e] = (uint64_t)x[rr * 4 + e] * kav[e];
+        }
         cluster.sync();  // both CTAs' transforms are in the partner's exchange regions
         const uint32_t* theirs = my_exch + (size_t)ph * team_words;
         ph ^= 1;
-        // (3) output h: own row with K(lvl, h, h), the partner's row with K(lvl, 1-h, h);
-        // x < 46p and key words < p: the sum of two products fits 64 bits
-        {
-            const size_t blk = (size_t)i * L + lvl;
-            const uint4* kown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
-            const uint4* kpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
 #pragma unroll
-            for (int rr = 0; rr < 8; ++rr) {
-                const uint4 ka = ldg_keep(kown + rr * S + lane, keep);
-                const uint4 kb = ldg_keep(kpar + rr * S + lane, keep);
-                const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
-                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+        for (int rr = 0; rr < 8; ++rr) {
+            const uint4 kb = ldg_keep(kpar + rr * S + lane, keep);
+            const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int r = rr * 4 + e;
-                    const uint64_t s = (uint64_t)x[r] * kav[e] + (uint64_t)theirs[r * S + lane] * kbv[e];
-                    // s 2^-32 mod p in [0, 2p): Montgomery, then a Shoup reduction by 1
-                    const uint32_t tt = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
-                    part[r * S + lane] = tt - __umulhi(tt, one_s) * ch.p;
-                }
+            for (int e = 0; e < 4; ++e) {
+                const int r = rr * 4 + e;
+                const uint64_t s = own[r] + (uint64_t)theirs[r * S + lane] * kbv[e];
+                // s 2^-32 mod p (Montgomery) + p: in (0, 3.1p), reduced after the level sum
+                part[r * S + lane] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
             }
         }
         __syncthreads();  // every partial is written
@@ -1377,8 +1391,11 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
 #pragma unroll
             for (int r = 0; r < 32; ++r) {
                 uint32_t v = 0;
-                for (int q = 0; q < L; ++q) v += partials[(size_t)(c * L + q) * Sh::TBUF + r * S + lane];
-                oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 2p each: < 8p; reduced to [0, 2p)
+                // unrolled to the largest level count, so the loads issue together
+#pragma unroll
+                for (int q = 0; q < kClusterMaxLevels; ++q)
+                    if (q < L) v += partials[(size_t)(c * L + q) * Sh::TBUF + r * S + lane];
+                oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
             }
             ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
             __syncwarp();
