@@ -720,14 +720,22 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
     points = []
     mismatches = peak["mismatched_requests"]
     for i, f in enumerate(fractions):
+        # SLO target 10 ms (this workload's p99 goal); the reference's 100 / 300 / 500 ms beside it
         r = srv.run_trace(pool, expect, requests=requests, warmup=100, rate=f * peak_rps, seed=100 + i,
-                          max_count=max_count)
+                          max_count=max_count, slo_ms=10.0)
         mismatches += r["mismatched_requests"]
         points.append({"fraction_of_peak": f, "offered_rps": r["offered_rate"], "served": r["served"],
                        "requests_per_s": r["requests_per_s"], "bootstraps_per_s": r["ciphertexts_per_s"],
                        "p50_ms": r["sojourn"]["p50_ms"], "p99_ms": r["sojourn"]["p99_ms"],
                        "queue_p99_ms": r["queue"]["p99_ms"], "service_p50_ms": r["service"]["p50_ms"],
-                       "hit_rate": r["hit_rate"], "key_misses": r["key_misses"], "batches": r["batches"]})
+                       "hit_rate": r["hit_rate"], "key_misses": r["key_misses"], "batches": r["batches"],
+                       "slo_ms": r["slo_ms"], "slo_violation_rate": r["slo_violation_rate"],
+                       "slo_violation_rate_100": r["slo_violation_rate_100"],
+                       "slo_violation_rate_300": r["slo_violation_rate_300"],
+                       "slo_violation_rate_500": r["slo_violation_rate_500"],
+                       "tenant_fairness_jain": r["tenant_fairness_jain"], "peak_queue_depth": r["peak_queue_depth"],
+                       "load_concurrency_peak": r["load_concurrency_peak"],
+                       "load_concurrency_mean": r["load_concurrency_mean"]})
     srv.close()
     at80 = min(points, key=lambda q: abs(q["fraction_of_peak"] - 0.8)) if points else None
     return {"workload": "serving_t32_128tenants_4GB", "tenants": tenants, "key_budget_bytes": int(budget),

@@ -300,6 +300,7 @@ typedef struct yg_trace_config {
     int queue_max; /* arrivals that find more requests than this unfinished are shed (0 = no bound) */
     const int32_t* h_pool;
     const int32_t* h_expect;
+    double slo_ms; /* sojourn target of slo_violation_rate (0 = 100 ms, the reference's default) */
 } yg_trace_config;
 typedef struct yg_latency {
     double mean_ms, p50_ms, p90_ms, p99_ms, p999_ms, max_ms;
@@ -310,8 +311,24 @@ typedef struct yg_trace_result {
     yg_latency sojourn, queue, service;
     uint64_t key_hits, key_misses, refill_bytes, batches;
     double hit_rate;
+    /* The reference harness's figures (ya_benchmark/blindrotate_serving.cpp:256-284, 324-336),
+     * over the measured requests: the share whose sojourn exceeds slo_ms and 100 / 300 / 500 ms;
+     * Jain's index of the tenants' mean sojourn times, (sum m)^2 / (tenants * sum m^2), 1 =
+     * every tenant waits the same; the most requests submitted and not yet started at once;
+     * key refills belonging to batches not yet finished, the most at once and the mean over
+     * batch launches. */
+    double slo_ms, slo_violation_rate, slo_violation_rate_100, slo_violation_rate_300, slo_violation_rate_500;
+    double tenant_fairness_jain;
+    int peak_queue_depth, load_concurrency_peak;
+    double load_concurrency_mean;
 } yg_trace_result;
 int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_trace_result* out);
+
+/* Health counter, no reference counterpart: how many bounded waits inside this library's
+ * kernels on ctx's device gave up since the library was loaded (the row-cluster layout's
+ * wait for its TMA key copies; the kernel then reads the key from global memory, so results
+ * stay correct).  0 in normal operation. */
+int yg_wait_timeouts(yg_ctx* ctx, uint64_t* out);
 
 /* Calibration, no reference counterpart: measured 32-bit multiply-add throughput of
  * `device` (operations per second), the denominator of the bootstrap's roofline. */

@@ -109,6 +109,35 @@ def test_blind_rotate_acc_reference_semantics(t32_small, layout):
     api.set_launch(ctx, 1, 0, 0)
 
 
+@pytest.mark.parametrize("levels", [3, 4])
+def test_row_cluster_key_stage_with_skipped_steps(levels, built_lib):
+    """The row-cluster layout copies each active step's key rows into shared memory by TMA
+    (l <= 3; at l = 4 it reads them from global memory): with CMux steps skipped (a_i = 0) at
+    the start, in the middle and at the end, 40 ciphertexts give the oracle's bootstrap, no
+    bounded wait gave up, and the result equals the channel layout's."""
+    import ctypes
+    import dataclasses
+
+    from yatfhe_gb300 import _lib, api
+
+    p = dataclasses.replace(small(T32_N1024, 24), l=levels, l_approx=levels, radix_bits=7 if levels == 3 else 5)
+    ora, ctx, key = _setup(p, 0x5EED0011 + levels, built_lib)
+    mu, lwe = _sign_inputs(ora, 40, 30 + levels)
+    for c in range(0, 40, 2):  # even ciphertexts: a few mask words 0, so those steps are skipped
+        lwe[c, [0, 1, 7, p.n - 1]] = 0
+    lut = lutmod.sign_lut(p.N, 32)
+    api.set_launch(ctx, 1, 0, 0)
+    want = _pbs_gpu(ctx, key, lwe, lut)
+    api.set_launch(ctx, 1, 0, 2)
+    got = _pbs_gpu(ctx, key, lwe, lut)
+    api.set_launch(ctx, 1, 0, 0)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got[:6], ora.pbs(lwe[:6], lut, threads=8))
+    n = ctypes.c_uint64(99)
+    _lib.check(_lib.lib().yg_wait_timeouts(ctx.handle, ctypes.byref(n)))
+    assert n.value == 0
+
+
 def test_keyswitch_alone_t32(t32_small):
     from yatfhe_gb300 import api
 

@@ -68,6 +68,19 @@ def test_trace_with_evictions_is_bit_exact(served):
     assert res["sojourn"]["p50_ms"] > 0 and res["sojourn"]["p99_ms"] >= res["sojourn"]["p50_ms"]
     c = srv.counters()
     assert c["key_slots"] == 2
+    # the reference harness's figures: SLO violation shares, Jain's index over the tenants'
+    # mean sojourn (1 / tenants <= J <= 1), peak queue depth, refills in flight
+    assert res["slo_ms"] == 100.0
+    for k in ("slo_violation_rate", "slo_violation_rate_100", "slo_violation_rate_300", "slo_violation_rate_500"):
+        assert 0.0 <= res[k] <= 1.0
+    assert res["slo_violation_rate"] == res["slo_violation_rate_100"]
+    assert res["slo_violation_rate_100"] >= res["slo_violation_rate_300"] >= res["slo_violation_rate_500"]
+    assert 1.0 / 6 - 1e-9 <= res["tenant_fairness_jain"] <= 1.0 + 1e-9
+    assert res["peak_queue_depth"] >= 1
+    assert 1 <= res["load_concurrency_peak"] and 0.0 < res["load_concurrency_mean"] <= res["load_concurrency_peak"]
+    tight = srv.run_trace(pool, expect, requests=60, warmup=0, rate=2000.0, zipf_s=1.1, max_count=16, seed=8,
+                          slo_ms=1e-6)
+    assert tight["slo_violation_rate"] == 1.0  # every sojourn exceeds a near-zero target
 
 
 def test_trace_sheds_beyond_queue_bound(served):

@@ -48,7 +48,7 @@ class TraceConfig(ctypes.Structure):
     _fields_ = [("requests", ctypes.c_int), ("warmup", ctypes.c_int), ("rate", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("zipf_s", ctypes.c_double), ("zipf_seed", ctypes.c_uint64),
                 ("tenants", ctypes.c_int), ("max_count", ctypes.c_int), ("queue_max", ctypes.c_int),
-                ("h_pool", ctypes.c_void_p), ("h_expect", ctypes.c_void_p)]
+                ("h_pool", ctypes.c_void_p), ("h_expect", ctypes.c_void_p), ("slo_ms", ctypes.c_double)]
 
 
 class Latency(ctypes.Structure):
@@ -61,7 +61,12 @@ class TraceResult(ctypes.Structure):
                 ("ciphertexts_per_s", ctypes.c_double), ("offered_rate", ctypes.c_double),
                 ("sojourn", Latency), ("queue", Latency), ("service", Latency),
                 ("key_hits", ctypes.c_uint64), ("key_misses", ctypes.c_uint64), ("refill_bytes", ctypes.c_uint64),
-                ("batches", ctypes.c_uint64), ("hit_rate", ctypes.c_double)]
+                ("batches", ctypes.c_uint64), ("hit_rate", ctypes.c_double),
+                ("slo_ms", ctypes.c_double), ("slo_violation_rate", ctypes.c_double),
+                ("slo_violation_rate_100", ctypes.c_double), ("slo_violation_rate_300", ctypes.c_double),
+                ("slo_violation_rate_500", ctypes.c_double), ("tenant_fairness_jain", ctypes.c_double),
+                ("peak_queue_depth", ctypes.c_int), ("load_concurrency_peak", ctypes.c_int),
+                ("load_concurrency_mean", ctypes.c_double)]
 
 
 _vp = ctypes.c_void_p
@@ -105,6 +110,7 @@ _SIGNATURES = {
     "yg_server_destroy": (None, [_vp]),
     "yg_server_run_trace": (ctypes.c_int, [_vp, ctypes.POINTER(TraceConfig), ctypes.POINTER(TraceResult)]),
     "yg_probe_int32_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "yg_wait_timeouts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64)]),
 }
 
 _lib = None

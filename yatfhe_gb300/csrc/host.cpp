@@ -1424,6 +1424,17 @@ int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out) {
     });
 }
 
+int yg_wait_timeouts(yg_ctx* ctx, uint64_t* out) {
+    if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        unsigned long long v = 0;
+        if (yg::read_wait_timeouts(&v) != 0) ck(cudaGetLastError(), "reading the wait-timeout counter");
+        *out = v;
+        return YG_OK;
+    });
+}
+
 int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm) {
     if (!ctx || per_cta < 1 || ctas_per_sm < 0) return set_err(YG_ERR_INVALID, "yg_ctx_set_launch: bad arguments");
     int fit = 0;

@@ -22,6 +22,9 @@
 
 namespace yg {
 
+// Bounded device-side waits that gave up (the kernel then took its fallback path).
+__device__ unsigned long long g_wait_timeouts;
+
 namespace {
 
 __device__ __forceinline__ Chan pick_chan(const Chan (&c)[kChannels], int team) {
@@ -43,6 +46,38 @@ __device__ __forceinline__ uint4 ldg_keep(const uint4* p, uint64_t pol) {
         : "l"(p), "l"(pol));
     return v;
 }
+
+// Bulk copies into shared memory (TMA, cp.async.bulk) tracked by an mbarrier: one thread
+// arms the barrier with the byte count and issues the copies; consumers wait for the phase.
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// global -> this CTA's shared memory, `bytes` (a multiple of 16) from 16-byte aligned addresses
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+// Waits for the barrier phase of this parity to complete, for at most `cycles` clocks
+// (false: it gave up).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long cycles) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > cycles) return false;
+    }
+}
+// about one second at the GB300's clock: far beyond any copy's latency
+constexpr long long kWaitCycles = 2000000000LL;
 
 // zeroMeanDigits (yatfhe/include/yatfhe/gadget_decomposition.h:76-95): signed balanced
 // digits of the top L*radix bits of a W-bit value, rounded half away from zero, carry
@@ -1226,7 +1261,12 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
 // each channel adds the l partials and runs the inverse transform; (5) all threads
 // recombine the channels (CRT) and add into row h.  The levels' transforms run side by
 // side, so a step takes about one forward and one inverse transform instead of l forward
-// ones: the latency shape for lone ciphertexts.
+// ones: the latency shape for lone ciphertexts.  With l <= kClusterStageLevels the key rows
+// a step multiplies with (output h of both rows, every level and channel: 18 x 4 KB at
+// l = 3) are copied into shared memory by TMA (cp.async.bulk, one thread, an mbarrier)
+// while the previous step's inverse transform, CRT and the step's digits and forward
+// transforms run; the wait for them is bounded in time, and a copy that does not arrive
+// counts in g_wait_timeouts and the CTA reads the key from global memory from then on.
 template <int T>
 __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster_kernel(const BrArgs a) {
     static_assert(T == 32, "the row-cluster layout is built for the 32-bit torus");
@@ -1249,21 +1289,51 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
 
     const size_t team_words = (size_t)kChannels * L * Sh::TBUF;
-    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);  // [3][L][TBUF] transposes, inverse outputs
-    uint32_t* partials = regions + team_words;              // [3][L][TBUF]
-    uint32_t* exch = partials + team_words;                 // [2][3][L][TBUF] written by the partner
+    // [3][L][TBUF]: transposes, then the partial sums (step 3), then the inverse outputs
+    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* exch = regions + team_words;                  // [2][3][L][TBUF] written by the partner
     int32_t* acc = reinterpret_cast<int32_t*>(exch + 2 * team_words);  // [N] row h
     int16_t* dig = reinterpret_cast<int16_t*>(acc + N);               // [L][N]
     int16_t* sa = dig + (size_t)L * N;                                // [n+1]
     uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
     uint32_t* mine = regions + (size_t)(c * L + lvl) * Sh::TBUF;
-    uint32_t* part = partials + (size_t)(c * L + lvl) * Sh::TBUF;
+    uint32_t* part = mine;  // the team's transpose region holds its partial sum after step 3
+    uint32_t* stage = reinterpret_cast<uint32_t*>(smem + brc_stage_offset(n, L));  // [L][2][3][1024]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + brc_smem_bytes(n, L) - 16);
+    volatile int* stage_ok = reinterpret_cast<volatile int*>(mbar + 1);
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
     uint32_t* my_exch = exch + (size_t)(c * L + lvl) * Sh::TBUF;     // + ph * team_words
     uint32_t* their_exch = cluster.map_shared_rank(my_exch, 1 - h);  // the partner CTA's same team
     int ph = 0;                                                      // exchange region of this step
 
     const uint4* key = !valid ? nullptr : (a.key_of ? a.key_table[a.key_of[ct]] : a.key);
     const int64_t* lut = !valid ? nullptr : (a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut);
+    // TMA stage of the key rows (uniform in the cluster; nothing runs for an invalid one)
+    bool tma = valid && L <= kClusterStageLevels;
+    if (tma && tid == 0) {
+        mbar_init(mbar_a, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // thread 0: arms the barrier and copies key rows of `step` (output h) into the stage
+    auto issue = [&](int step) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(mbar_a, (uint32_t)L * 2 * kChannels * 4096);
+        for (int lv = 0; lv < L; ++lv)
+            for (int row = 0; row < 2; ++row)
+                for (int cc = 0; cc < kChannels; ++cc) {
+                    const size_t blk = (size_t)step * L + lv;
+                    const uint4* src =
+                        key + ((blk * 2 + row) * kChannels + cc) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+                    bulk_copy_g2s((uint32_t)__cvta_generic_to_shared(stage + ((lv * 2 + row) * kChannels + cc) * 1024),
+                                  src, 4096, mbar_a);
+                }
+    };
+    auto next_active = [&](int from) {
+        while (from < a.steps && sa[from] == 0) ++from;
+        return from;
+    };
+    uint32_t phase = 0;          // parity of the stage's next barrier phase
+    bool outstanding = false;    // thread 0: a copy issued and not yet waited for
     const bool use_tab0 = a.radix_bits <= 7;
     if (use_tab0) {
         for (int idx = tid; idx < kChannels * 129; idx += NT) {
@@ -1284,6 +1354,13 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         for (int i = tid; i <= n; i += NT) sa[i] = 0;
     }
     __syncthreads();
+    if (tma && tid == 0) {
+        const int f = next_active(0);
+        if (f < a.steps) {
+            issue(f);
+            outstanding = true;
+        }
+    }
     if (valid && a.acc_in) {
         for (int j = tid; j < N; j += NT) acc[j] = (int32_t)a.acc_in[(size_t)ct * 2 * N + h * N + j];
     } else if (valid) {
@@ -1307,9 +1384,9 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         const int t2 = ai < 0 ? ai + 2 * N : ai;
         const bool wrap = t2 >= N;
         const int at = wrap ? t2 - N : t2;
-        // this step's key lines of the team (step 3 reads them), requested now so that they
-        // arrive in L1 while the digits and the forward transform are computed
-        {
+        // without the stage: this step's key lines of the team (step 3 reads them), requested
+        // now so that they arrive in L1 while the digits and the forward transform are computed
+        if (!tma) {
             const size_t blk = (size_t)i * L + lvl;
             const uint4* po = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S + lane;
             const uint4* pp = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S + lane;
@@ -1359,12 +1436,25 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         // x < 46p and key words < p: the sum of two products fits 64 bits.  The own row's
         // products are formed while the partner may still be transforming.
         const size_t blk = (size_t)i * L + lvl;
-        const uint4* kown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
-        const uint4* kpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+        const uint4* gown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+        const uint4* gpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
         uint64_t own[32];
+        // with the stage every thread waits for the step's copies (bounded); a thread that
+        // gives up reads the same key words from global memory
+        bool from_stage = false;
+        if (tma) {
+            from_stage = mbar_wait_bounded(mbar_a, phase, kWaitCycles);
+            if (!from_stage) atomicAdd(&g_wait_timeouts, 1ull);
+            if (tid == 0) {
+                if (from_stage) outstanding = false;
+                *stage_ok = from_stage;
+            }
+        }
+        const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + ((lvl * 2 + h) * kChannels + c) * 1024) : nullptr;
+        const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + ((lvl * 2 + (1 - h)) * kChannels + c) * 1024) : nullptr;
 #pragma unroll
         for (int rr = 0; rr < 8; ++rr) {
-            const uint4 ka = ldg_keep(kown + rr * S + lane, keep);
+            const uint4 ka = from_stage ? kown[rr * S + lane] : ldg_keep(gown + rr * S + lane, keep);
             const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) own[rr * 4 + e] = (uint64_t)x[rr * 4 + e] * kav[e];
@@ -1374,7 +1464,7 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         ph ^= 1;
 #pragma unroll
         for (int rr = 0; rr < 8; ++rr) {
-            const uint4 kb = ldg_keep(kpar + rr * S + lane, keep);
+            const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
             const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -1384,7 +1474,19 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 part[r * S + lane] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
             }
         }
-        __syncthreads();  // every partial is written
+        __syncthreads();  // every partial is written, and the stage has been read
+        if (tma) {
+            // the copy for the next active step runs while this step finishes
+            tma = *stage_ok;  // after thread 0 gave up the CTA reads the key from global memory
+            phase ^= 1;
+            if (tma && tid == 0) {
+                const int f = next_active(i + 1);
+                if (f < a.steps) {
+                    issue(f);
+                    outstanding = true;
+                }
+            }
+        }
         // (4) the level-0 team of each channel: sum of the l partials, inverse transform
         if (lvl == 0) {
             uint32_t oa[32];
@@ -1394,7 +1496,7 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 // unrolled to the largest level count, so the loads issue together
 #pragma unroll
                 for (int q = 0; q < kClusterMaxLevels; ++q)
-                    if (q < L) v += partials[(size_t)(c * L + q) * Sh::TBUF + r * S + lane];
+                    if (q < L) v += regions[(size_t)(c * L + q) * Sh::TBUF + r * S + lane];
                 oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
             }
             ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
@@ -1426,6 +1528,8 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             dst[N] = acc[0];
         }
     }
+    // a copy that timed out may still land: wait for it (bounded) before the CTA exits
+    if (outstanding && tid == 0 && !mbar_wait_bounded(mbar_a, phase ^ 1, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
     cluster.sync();  // neither CTA leaves while the other may still write into its regions
 }
 
@@ -1705,6 +1809,10 @@ int launch_group_blind_rotate(const GroupBrArgs& a, void* stream) {
     if (a.torus_bits == 32) return go(group_blind_rotate_kernel<32>);
     if (a.torus_bits == 56) return go(group_blind_rotate_kernel<56>);
     return -1;
+}
+
+int read_wait_timeouts(unsigned long long* out) {
+    return cudaMemcpyFromSymbol(out, g_wait_timeouts, sizeof(*out)) == cudaSuccess ? 0 : -1;
 }
 
 int preload_keyswitch() {

@@ -213,15 +213,22 @@ constexpr int kClusterMaxLevels = 4;
 constexpr int kTab0Half = 64;
 constexpr int kTab0Words = 2 * kTab0Half + 4;  // 129 used
 // Shared memory of one CTA of the row-cluster layout (N = 1024, T = 32): per team (channel,
-// level) a padded transpose region, a partial-sum region and two exchange regions the
-// partner CTA writes into, the accumulator row, its digits, the mod-2N input and the
-// first-stage digit tables.
-__host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
+// level) a padded transpose region (also its partial sum after the products) and two
+// exchange regions the partner CTA writes into, the accumulator row, its digits, the mod-2N
+// input, the first-stage digit tables and, for l <= kClusterStageLevels, the stage the next
+// step's key rows are copied into by TMA ([l][2 rows][3 channels][1024] words) with its
+// mbarrier and status word.
+constexpr int kClusterStageLevels = 3;
+__host__ __device__ inline size_t brc_stage_offset(int n, int L) {
     const size_t N = 1024, tbuf = N + N / 32;
-    size_t b = (size_t)kChannels * L * 4 * tbuf * 4;  // transposes, partials, 2 exchange buffers
+    size_t b = (size_t)kChannels * L * 3 * tbuf * 4;  // transposes / partials, 2 exchange buffers
     b += N * 4 + (size_t)L * N * 2 + ((size_t)n + 1) * 2;
     b = ((b + 3) & ~(size_t)3) + (size_t)kChannels * 132 * 4;
-    return (b + 15) & ~(size_t)15;
+    return (b + 127) & ~(size_t)127;
+}
+__host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
+    const size_t stage = L <= kClusterStageLevels ? (size_t)L * 2 * kChannels * 1024 * 4 : 0;
+    return brc_stage_offset(n, L) + stage + 16;
 }
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
@@ -248,6 +255,9 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 constexpr int kNoVariant = -2;
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
 int launch_keyswitch(const KsArgs& a, void* stream);
+// Bounded device-side waits on the current device that gave up since the library was loaded
+// (the kernels then read from global memory instead); 0 on success.
+int read_wait_timeouts(unsigned long long* out);
 // Loads the key-switching kernel on the current device (the driver loads kernels lazily, on
 // first use); 0 on success.
 int preload_keyswitch();

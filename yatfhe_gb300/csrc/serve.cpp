@@ -96,6 +96,7 @@ struct Batch {
     std::vector<Part> parts;
     std::vector<Tenant*> tenants;
     double t_finish = 0;  // stamped by the completion callback
+    int refills = 0;      // key refills this batch issued (in flight until it retires)
     std::atomic<bool> finished{false};
     bool busy = false;
     struct yg_server* server = nullptr;
@@ -131,6 +132,11 @@ struct yg_server {
 
     // statistics
     uint64_t hits = 0, misses = 0, refill_bytes = 0, batches_run = 0, ciphertexts_done = 0, requests_done = 0;
+    // requests submitted and not yet started (the reference's queue depth, peak since the
+    // last reset); key refills of batches not yet retired, sampled at every launch
+    int waiting = 0, waiting_peak = 0;
+    int refills_inflight = 0, refills_peak = 0;
+    uint64_t refill_samples = 0, refill_sample_sum = 0;
     double busy_since = 0;
 };
 
@@ -175,6 +181,8 @@ void retire(yg_server* s) {
             }
         }
         for (Tenant* t : b->tenants) t->pins--;
+        s->refills_inflight -= b->refills;
+        b->refills = 0;
         b->parts.clear();
         b->tenants.clear();
         b->busy = false;
@@ -207,6 +215,7 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     int total = 0;
     std::vector<Part> take;
     std::vector<Tenant*> used;
+    int refills = 0;
     while (!pending.empty()) {
         Request* r = pending.front();
         const int rest = r->count - r->admitted, room = s->cfg.max_batch - total;
@@ -226,6 +235,7 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
             ck(cudaEventRecord(t->ready, s->copy), "refill event");
             s->misses++;
             s->refill_bytes += s->bsk_bytes + s->ksk_bytes;
+            refills++;
         } else if (!in_batch) {
             s->hits++;
         }
@@ -249,7 +259,10 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     for (const Part& part : take) {
         Request* r = part.r;
         Tenant* t = s->tenants[r->tenant].get();
-        if (part.offset == 0) r->t_start = t0;
+        if (part.offset == 0) {
+            r->t_start = t0;
+            s->waiting--;
+        }
         ck(cudaMemcpyAsync(b->d_in + (size_t)off * n1, r->h_in + (size_t)part.offset * n1, (size_t)part.count * n1 * 4,
                            cudaMemcpyHostToDevice, b->stream),
            "copy in");
@@ -291,6 +304,11 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     }
     b->parts = std::move(take);
     b->tenants = std::move(used);
+    b->refills = refills;
+    s->refills_inflight += refills;
+    s->refills_peak = std::max(s->refills_peak, s->refills_inflight);
+    s->refill_sample_sum += s->refills_inflight;
+    s->refill_samples++;
     b->busy = true;
     b->finished.store(false);
     ck(cudaLaunchHostFunc(b->stream, batch_done_cb, b), "completion callback");
@@ -463,6 +481,7 @@ int64_t yg_server_submit(yg_server* s, int tenant, const int32_t* h_in, int32_t*
     Request* raw = r.get();
     s->requests[raw->id] = std::move(r);
     s->incoming.push_back(raw);
+    s->waiting_peak = std::max(s->waiting_peak, ++s->waiting);
     s->cv.notify_all();
     return raw->id;
 }
@@ -615,6 +634,7 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
         yg_server_counters before{};
         yg_server_counters after{};
         std::vector<double> soj, que, svc;
+        std::map<int, std::pair<double, long>> per_tenant;  // sum of sojourn (ms), requests
         int mismatched = 0, served = 0;
         double t_first = 0, t_last = 0;
         int64_t measured_cts = 0;
@@ -646,7 +666,13 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
                     free_slots.pop_front();
                 }
                 const int32_t* in = cfg->h_pool + (size_t)tenant * req_words;
-                if (i == cfg->warmup) yg_server_stats(s, &before);  // counters of the measured window
+                if (i == cfg->warmup) {  // counters of the measured window
+                    yg_server_stats(s, &before);
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    s->waiting_peak = s->waiting;
+                    s->refills_peak = s->refills_inflight;
+                    s->refill_samples = s->refill_sample_sum = 0;
+                }
                 const int64_t id = yg_server_submit(s, tenant, in, h_out + (size_t)slot * req_words, count);
                 if (id <= 0) break;
                 in_system++;
@@ -718,6 +744,9 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
                     measured_cts += it.count;
                     t_last = std::max(t_last, tm.t_done);
                     soj.push_back(1e3 * (tm.t_done - tm.t_submit));
+                    auto& pt = per_tenant[it.tenant];
+                    pt.first += soj.back();
+                    pt.second++;
                     que.push_back(1e3 * (tm.t_start - tm.t_submit));
                     svc.push_back(1e3 * (tm.t_done - tm.t_start));
                 }
@@ -754,6 +783,34 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
         out->batches = after.batches - before.batches;
         const double lookups = (double)(out->key_hits + out->key_misses);
         out->hit_rate = lookups > 0 ? out->key_hits / lookups : 0;
+        // the reference's SLO and fairness figures (blindrotate_serving.cpp:256-284, 324-336)
+        out->slo_ms = cfg->slo_ms > 0 ? cfg->slo_ms : 100.0;
+        auto violation = [&](double budget) {
+            size_t v = 0;
+            for (double x : soj) v += x > budget;
+            return soj.empty() ? 0.0 : (double)v / soj.size();
+        };
+        out->slo_violation_rate = violation(out->slo_ms);
+        out->slo_violation_rate_100 = violation(100.0);
+        out->slo_violation_rate_300 = violation(300.0);
+        out->slo_violation_rate_500 = violation(500.0);
+        out->tenant_fairness_jain = 1.0;
+        if (per_tenant.size() > 1) {
+            double sum = 0, sum_sq = 0;
+            for (const auto& e : per_tenant) {
+                const double m = e.second.first / e.second.second;
+                sum += m;
+                sum_sq += m * m;
+            }
+            out->tenant_fairness_jain = sum * sum / (per_tenant.size() * sum_sq);
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            out->peak_queue_depth = s->waiting_peak;
+            out->load_concurrency_peak = s->refills_peak;
+            out->load_concurrency_mean =
+                s->refill_samples ? (double)s->refill_sample_sum / s->refill_samples : 0.0;
+        }
         return YG_OK;
     });
 }

@@ -55,12 +55,13 @@ class Server:
         return {k: getattr(c, k) for k, _ in _lib.ServerCounters._fields_}
 
     def run_trace(self, pool, expect=None, *, requests: int, rate: float, warmup: int = 0, seed: int = 1,
-                  zipf_s: float = 1.1, zipf_seed: int = 20260816, max_count: int = 256, queue_max: int = 0) -> dict:
+                  zipf_s: float = 1.1, zipf_seed: int = 20260816, max_count: int = 256, queue_max: int = 0,
+                  slo_ms: float = 100.0) -> dict:
         """pool / expect: pinned int32 arrays [tenants, max_count, n+1] (expect may be None)."""
         tenants = pool.shape[0]
         cfg = _lib.TraceConfig(requests, warmup, float(rate), seed, float(zipf_s), zipf_seed, tenants, max_count,
                                queue_max, ctypes.c_void_p(_addr(pool)),
-                               None if expect is None else ctypes.c_void_p(_addr(expect)))
+                               None if expect is None else ctypes.c_void_p(_addr(expect)), float(slo_ms))
         r = _lib.TraceResult()
         _lib.check(_lib.lib().yg_server_run_trace(self._h, ctypes.byref(cfg), ctypes.byref(r)))
         out = {k: getattr(r, k) for k, _ in _lib.TraceResult._fields_ if k not in ("sojourn", "queue", "service")}
