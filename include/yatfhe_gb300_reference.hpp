@@ -5,8 +5,11 @@
 // header after them and call yatfhe_gb300::functionalBootstrappingMPNtt & co. with the
 // reference's own types; a `using namespace yatfhe_gb300;` or a qualified call swaps the
 // CPU implementation for the GPU one without touching the surrounding code.  Keys are
-// converted and uploaded on first use and cached per key object (address); call
-// yatfhe_gb300::forgetKeys() after mutating or destroying a key.  Failures throw the
+// converted and uploaded on first use and cached per key object (address) together with a
+// fingerprint (sizes and a few dozen words sampled across the key): a different key built
+// later at the same address is recognised and uploaded again.  A key changed in place is
+// only recognised if a sampled word changed: call yatfhe_gb300::forgetKeys() after
+// mutating a key, and to release the device copies.  Failures throw the
 // exception types the reference throws (std::invalid_argument for bad shapes, and
 // std::runtime_error otherwise).
 //
@@ -54,14 +57,20 @@ inline void cuda(cudaError_t e) {
     if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
 }
 
+struct CachedKey {
+    yg_key* key = nullptr;
+    uint64_t fp = 0;             // fingerprint of the key object it was made from
+    const void* ksk = nullptr;   // key-switching key attached to it, and its fingerprint
+    uint64_t ksk_fp = 0;
+};
+
 struct Registry {
     std::mutex mu;
     std::map<std::tuple<int, int, int, int, int, int, int, int>, yg_ctx*> ctxs;
-    std::map<const void*, yg_key*> keys;  // BootstrappingKeyMP / bskDft address -> device key
-    std::map<const void*, const void*> ksk_of;
+    std::map<const void*, CachedKey> keys;  // key object address -> device key
 
     ~Registry() {
-        for (auto& k : keys) yg_key_destroy(k.second);
+        for (auto& k : keys) yg_key_destroy(k.second.key);
         for (auto& c : ctxs) yg_ctx_destroy(c.second);
     }
 };
@@ -69,6 +78,80 @@ struct Registry {
 inline Registry& reg() {
     static Registry r;
     return r;
+}
+
+inline uint64_t mix(uint64_t h, uint64_t v) { return (h ^ (v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2))) * 0x100000001b3ULL; }
+
+template <typename P>
+inline uint64_t mix_poly(uint64_t h, const P& poly) {
+    const size_t m = poly.coeffs.size();
+    h = mix(h, m);
+    if (m)
+        for (size_t j : {size_t(0), m / 3, m / 2, m - 1}) h = mix(h, static_cast<uint64_t>(poly.coeffs[j]));
+    return h;
+}
+
+// the first, middle and last entries of a non-empty vector
+template <typename V>
+inline std::vector<size_t> probes(const V& v) {
+    return v.empty() ? std::vector<size_t>{} : std::vector<size_t>{0, v.size() / 2, v.size() - 1};
+}
+
+template <typename T>
+inline uint64_t mix_trlwe(uint64_t h, const T& t) {
+    for (const auto& a : t.a) h = mix_poly(h, a);
+    return mix_poly(h, t.b);
+}
+
+inline uint64_t fingerprint(const std::vector<std::vector<TrgswMPDft>>& bskDft) {
+    uint64_t h = mix(0, bskDft.size());
+    for (size_t i : probes(bskDft)) {
+        const TrgswMPDft& t = bskDft[i][0];
+        h = mix(h, static_cast<uint64_t>(t.l));
+        for (size_t lvl : probes(t.cPrime)) {
+            h = mix_trlwe(h, t.cPrime[lvl]);
+            if (lvl < t.c.size())
+                for (const auto& r : t.c[lvl]) h = mix_trlwe(h, r);
+        }
+    }
+    return h;
+}
+
+inline uint64_t fingerprint(const TlweKeySwitchingKey& ksk) {
+    uint64_t h = mix(1, ksk.decomposedKsk.size());
+    for (size_t i : probes(ksk.decomposedKsk))
+        for (size_t j : probes(ksk.decomposedKsk[i])) {
+            const Tlwe& t = ksk.decomposedKsk[i][j];
+            for (size_t e : probes(t.a)) h = mix(h, static_cast<uint64_t>(t.a[e]));
+            h = mix(h, static_cast<uint64_t>(t.b));
+        }
+    return h;
+}
+
+// The cached device key of the object at `addr` if its fingerprint still matches; a stale
+// entry (another key now at that address) is released.
+inline CachedKey* cached(const void* addr, uint64_t fp) {
+    auto& r = reg();
+    auto it = r.keys.find(addr);
+    if (it == r.keys.end()) return nullptr;
+    if (it->second.fp == fp) return &it->second;
+    yg_key_destroy(it->second.key);
+    r.keys.erase(it);
+    return nullptr;
+}
+
+inline void attach_ksk(CachedKey& e, const TlweKeySwitchingKey& ksk) {
+    const uint64_t fp = fingerprint(ksk);
+    if (e.ksk == &ksk && e.ksk_fp == fp) return;
+    std::vector<int32_t> flat;
+    for (const auto& row : ksk.decomposedKsk)
+        for (const auto& t : row) {
+            for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
+            flat.push_back(static_cast<int32_t>(t.b));
+        }
+    check(yg_key_set_ksk(e.key, flat.data()));
+    e.ksk = &ksk;
+    e.ksk_fp = fp;
 }
 
 inline yg_params params_of(const YatfheParameters& p, int levels) {
@@ -105,35 +188,26 @@ inline std::vector<uint64_t> flatten(const std::vector<std::vector<TrgswMPDft>>&
 
 inline yg_key* device_key(yg_ctx* c, const std::vector<std::vector<TrgswMPDft>>& bskDft, const TlweKeySwitchingKey* ksk,
                           int k, int N) {
-    auto& r = reg();
-    auto it = r.keys.find(&bskDft);
-    yg_key* key = nullptr;
-    if (it == r.keys.end()) {
+    const uint64_t fp = fingerprint(bskDft);
+    CachedKey* e = cached(&bskDft, fp);
+    if (!e) {
         const auto w = flatten(bskDft, k, N);
+        yg_key* key = nullptr;
         check(yg_key_upload_bsk_ntt(c, w.data(), &key));
-        r.keys[&bskDft] = key;
-    } else {
-        key = it->second;
+        e = &(reg().keys[&bskDft] = CachedKey{key, fp, nullptr, 0});
     }
-    if (ksk && r.ksk_of[&bskDft] != ksk) {
-        std::vector<int32_t> flat;
-        for (const auto& row : ksk->decomposedKsk)
-            for (const auto& t : row) {
-                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
-                flat.push_back(static_cast<int32_t>(t.b));
-            }
-        check(yg_key_set_ksk(key, flat.data()));
-        r.ksk_of[&bskDft] = ksk;
-    }
-    return key;
+    if (ksk) attach_ksk(*e, *ksk);
+    return e->key;
 }
 
 // BootstrappingKeyWWL24 (yatfhe/include/yatfhe/bootstrapping.h:116-135) -> device key: the
 // cPrime rows [n][l][k+1][N] and the s2 key [levels][k+1][N]; the GPU derives the GINX rows.
 inline yg_key* device_key_wwl24(yg_ctx* c, const BootstrappingKeyWWL24& bsk, int k, int N) {
-    auto& r = reg();
-    auto it = r.keys.find(&bsk);
-    if (it != r.keys.end()) return it->second;
+    uint64_t fp = mix(2, bsk.bskDft.size());
+    for (size_t i : probes(bsk.bskDft))
+        for (size_t lvl : probes(bsk.bskDft[i].cPrime)) fp = mix_trlwe(fp, bsk.bskDft[i].cPrime[lvl]);
+    for (size_t lvl : probes(bsk.s2Dft.trlweDfts)) fp = mix_trlwe(fp, bsk.s2Dft.trlweDfts[lvl]);
+    if (CachedKey* e = cached(&bsk, fp)) return e->key;
     std::vector<uint64_t> cprime, s2;
     auto put = [&](std::vector<uint64_t>& w, const TrlweDft& t) {
         for (int poly = 0; poly <= k; poly++) {
@@ -146,7 +220,7 @@ inline yg_key* device_key_wwl24(yg_ctx* c, const BootstrappingKeyWWL24& bsk, int
     for (const auto& t : bsk.s2Dft.trlweDfts) put(s2, t);
     yg_key* key = nullptr;
     check(yg_key_upload_wwl24_ntt(c, cprime.data(), s2.data(), static_cast<int>(bsk.s2Dft.trlweDfts.size()), &key));
-    r.keys[&bsk] = key;
+    reg().keys[&bsk] = CachedKey{key, fp, nullptr, 0};
     return key;
 }
 
@@ -154,9 +228,11 @@ inline yg_key* device_key_wwl24(yg_ctx* c, const BootstrappingKeyWWL24& bsk, int
 // the half rows bskPrime[i].cPrime [n][l][k+1][N] as torus values and the s2 key
 // [levels][k+1][N]; the device keeps both as they are.
 inline yg_key* device_key_lazy(yg_ctx* c, const BootstrappingKeyMPLazyPipeAlt& bsk, int k, int N) {
-    auto& r = reg();
-    auto it = r.keys.find(&bsk);
-    if (it != r.keys.end()) return it->second;
+    uint64_t fp = mix(3, bsk.bskPrime.size());
+    for (size_t i : probes(bsk.bskPrime))
+        for (size_t lvl : probes(bsk.bskPrime[i].cPrime)) fp = mix_trlwe(fp, bsk.bskPrime[i].cPrime[lvl]);
+    for (size_t lvl : probes(bsk.s2Dft.trlweDfts)) fp = mix_trlwe(fp, bsk.s2Dft.trlweDfts[lvl]);
+    if (CachedKey* e = cached(&bsk, fp)) return e->key;
     std::vector<int64_t> cprime;
     std::vector<uint64_t> s2;
     for (const auto& g : bsk.bskPrime)
@@ -172,7 +248,7 @@ inline yg_key* device_key_lazy(yg_ctx* c, const BootstrappingKeyMPLazyPipeAlt& b
         }
     yg_key* key = nullptr;
     check(yg_key_upload_lazy(c, cprime.data(), s2.data(), static_cast<int>(bsk.s2Dft.trlweDfts.size()), &key));
-    r.keys[&bsk] = key;
+    reg().keys[&bsk] = CachedKey{key, fp, nullptr, 0};
     return key;
 }
 
@@ -181,10 +257,13 @@ inline yg_key* device_key_lazy(yg_ctx* c, const BootstrappingKeyMPLazyPipeAlt& b
 // attached when given.
 inline yg_key* device_key_group(yg_ctx* c, const std::vector<TrgswDft>& bskDft, int group,
                                 const TlweKeySwitchingKey* ksk, int k, int N) {
-    auto& r = reg();
-    auto it = r.keys.find(&bskDft);
-    yg_key* key = nullptr;
-    if (it == r.keys.end()) {
+    uint64_t fp = mix(mix(4, static_cast<uint64_t>(group)), bskDft.size());
+    for (size_t i : probes(bskDft))
+        for (size_t lvl : probes(bskDft[i].trlweDftSamples))
+            for (const auto& t : bskDft[i].trlweDftSamples[lvl]) fp = mix_trlwe(fp, t);
+    CachedKey* e = cached(&bskDft, fp);
+    if (!e) {
+        yg_key* key = nullptr;
         std::vector<uint64_t> words;
         for (const auto& g : bskDft)
             for (const auto& lv : g.trlweDftSamples)
@@ -195,21 +274,10 @@ inline yg_key* device_key_group(yg_ctx* c, const std::vector<TrgswDft>& bskDft, 
                     }
         const int levels = bskDft.empty() ? 0 : bskDft[0].l;
         check(yg_key_upload_group(c, words.data(), group, levels, &key));
-        r.keys[&bskDft] = key;
-    } else {
-        key = it->second;
+        e = &(reg().keys[&bskDft] = CachedKey{key, fp, nullptr, 0});
     }
-    if (ksk && r.ksk_of[&bskDft] != ksk) {
-        std::vector<int32_t> flat;
-        for (const auto& row : ksk->decomposedKsk)
-            for (const auto& t : row) {
-                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
-                flat.push_back(static_cast<int32_t>(t.b));
-            }
-        check(yg_key_set_ksk(key, flat.data()));
-        r.ksk_of[&bskDft] = ksk;
-    }
-    return key;
+    if (ksk) attach_ksk(*e, *ksk);
+    return e->key;
 }
 
 template <typename T>
@@ -224,9 +292,8 @@ struct DeviceBuf {
 inline void forgetKeys() {
     auto& r = detail::reg();
     std::lock_guard<std::mutex> g(r.mu);
-    for (auto& k : r.keys) yg_key_destroy(k.second);
+    for (auto& k : r.keys) yg_key_destroy(k.second.key);
     r.keys.clear();
-    r.ksk_of.clear();
 }
 
 // Batched functionalBootstrappingMPNtt: out[i] = PBS(in[i]) under one key, one launch.
@@ -394,7 +461,7 @@ inline void blindRotateLazyPipeAltInitNtt(Trlwe& accum, BootstrappingKeyMPLazyPi
         std::lock_guard<std::mutex> g(r.mu);
         auto it = r.keys.find(&bsk);
         if (it != r.keys.end()) {  // a key cached for this object before it was read again
-            yg_key_destroy(it->second);
+            yg_key_destroy(it->second.key);
             r.keys.erase(it);
         }
     }
@@ -413,23 +480,13 @@ inline void switchKeyForTlwe(Tlwe& output, const TlweKeySwitchingKey& ksk, const
     std::lock_guard<std::mutex> g(r.mu);
     yg_ctx* c = detail::context(detail::params_of(param, param.lApprox));
     auto it = r.keys.find(&ksk);
-    yg_key* key = nullptr;
     if (it == r.keys.end()) {
+        yg_key* key = nullptr;
         detail::check(yg_key_create_ksk_only(c, &key));
-        r.keys[&ksk] = key;
-    } else {
-        key = it->second;
+        it = r.keys.emplace(&ksk, detail::CachedKey{key, 0, nullptr, 0}).first;
     }
-    if (r.ksk_of[&ksk] != &ksk) {
-        std::vector<int32_t> flat;
-        for (const auto& row : ksk.decomposedKsk)
-            for (const auto& t : row) {
-                for (auto a : t.a) flat.push_back(static_cast<int32_t>(a));
-                flat.push_back(static_cast<int32_t>(t.b));
-            }
-        detail::check(yg_key_set_ksk(key, flat.data()));
-        r.ksk_of[&ksk] = &ksk;
-    }
+    detail::attach_ksk(it->second, ksk);
+    yg_key* key = it->second.key;
     const int kN = param.k * param.N, n = param.n;
     std::vector<int32_t> big(kN + 1), res(n + 1);
     for (int j = 0; j < kN; j++) big[j] = static_cast<int32_t>(input.a[j]);

@@ -1,0 +1,144 @@
+// adapter_run.cpp -- TEST INFRASTRUCTURE ONLY.  Runs the C++ adapter
+// (include/yatfhe_gb300_reference.hpp) the way a reference user would, in the shape of the
+// reference's own BOOTSTRAPPING.MP21 test (google_tests/bootstrappping_test.cpp:83-131), and
+// compares every result with the reference function it replaces, called directly on the same
+// objects.  Linked with the reference library built from its sources (oracle/_ref) and the
+// CPU stand-in of the C ABI (yg_on_reference.cpp).  Exit status 0 when everything matches.
+#include <cstdio>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include "yatfhe/blind_rotate.h"
+#include "yatfhe/bootstrapping.h"
+#include "yatfhe/keyswitching.h"
+#include "yatfhe/numeric.h"
+#include "yatfhe/polynomial.h"
+#include "yatfhe/tlwe.h"
+#include "yatfhe/trlwe.h"
+#include "yautil/initializer.h"
+#include "yatfhe_gb300_reference.hpp"
+
+extern "C" void yg_test_use_params(const YatfheParameters* p);
+extern "C" int yg_test_uploads(void);
+
+namespace {
+
+int failures = 0;
+
+bool same(const Tlwe& x, const Tlwe& y) { return x.a == y.a && x.b == y.b; }
+bool same(const Trlwe& x, const Trlwe& y) {
+    for (size_t r = 0; r < x.a.size(); r++)
+        if (x.a[r].coeffs != y.a[r].coeffs) return false;
+    return x.b.coeffs == y.b.coeffs;
+}
+
+void expect(bool ok, const char* what) {
+    std::printf("%s %s\n", ok ? "ok  " : "FAIL", what);
+    failures += !ok;
+}
+
+}  // namespace
+
+int main() {
+    YatfheParameters param{};
+    param.n = 48;
+    param.torusBase = 8;
+    param.setRadixBits(7);
+    param.l = 3;
+    param.lApprox = 3;
+    initYatfhe(param);
+    yg_test_use_params(&param);
+
+    TlweKey tlweKey{param.n};
+    TrgswKey trgswKey{param};
+    TrlweKey& trlweKey = trgswKey.trlweKey;
+    TlweKeySwitchingKey ksKey{param};
+    genTlweKey(tlweKey);
+    genTrlweKey(trlweKey);
+    // the bootstrapping key lives in storage the test can reuse for a second key
+    alignas(BootstrappingKeyMP) unsigned char storage[sizeof(BootstrappingKeyMP)];
+    auto* bsk = new (storage) BootstrappingKeyMP{param, param.lApprox};
+    genBootstrappingKeyMP(*bsk, trgswKey, tlweKey, param);
+    TlweKey tlweKsKey = tlweKey;
+    genTlweKeySwitchingKey(ksKey, trlweKey, tlweKsKey, param);
+
+    TorusPolynomial v{param.N};
+    generateTestPolynomial(v, param.torusBase, 2 * param.N);
+    std::vector<Tlwe> inputs;
+    // messages in [0, torusBase / 2): the half the negacyclic test polynomial maps to itself
+    // (the reference's test bootstraps 3 with torusBase 8)
+    for (Integer m : {0, 1, 2, 3, 1, 3}) {
+        Tlwe in{param.n};
+        symEncTlwe(in, modSwitchToTorusGeneral(m, param.torusBase, LWE_Q), tlweKey);
+        inputs.push_back(in);
+    }
+
+    // functionalBootstrappingMPNtt, one ciphertext at a time and batched
+    bool pbs_ok = true, dec_ok = true;
+    std::vector<Tlwe> want;
+    for (const Tlwe& in : inputs) {
+        Tlwe ref{param.n}, got{param.n};
+        functionalBootstrappingMPNtt(ref, in, *bsk, ksKey, v, param);
+        yatfhe_gb300::functionalBootstrappingMPNtt(got, in, *bsk, ksKey, v, param);
+        pbs_ok &= same(ref, got);
+        Tlwe in_copy = in;
+        dec_ok &= symDecTlweToInt(got, tlweKey, param.torusBase) == symDecTlweToInt(in_copy, tlweKey, param.torusBase);
+        want.push_back(ref);
+    }
+    expect(pbs_ok, "functionalBootstrappingMPNtt == the reference's");
+    expect(dec_ok, "outputs decrypt to the inputs' messages");
+    std::vector<Tlwe> outs;
+    yatfhe_gb300::functionalBootstrappingMPNttBatch(outs, inputs, *bsk, ksKey, v, param);
+    bool batch_ok = outs.size() == inputs.size();
+    for (size_t i = 0; batch_ok && i < outs.size(); i++) batch_ok = same(outs[i], want[i]);
+    expect(batch_ok, "functionalBootstrappingMPNttBatch == the reference's, per ciphertext");
+    expect(yg_test_uploads() == 1, "the key was converted once and then taken from the cache");
+
+    // blindRotateMP21Ntt / blindRotateJP22Ntt on a caller-built accumulator, then extraction
+    // and switchKeyForTlwe
+    ScaledTlwe scaled{param.N * 2, param.n};
+    rescaleTlweToNewMod(scaled, inputs[3]);
+    Trlwe acc_ref{param.k, param.N}, acc_got{param.k, param.N}, acc_jp{param.k, param.N};
+    genNoiselessTrlweSample(acc_ref, v, scaled);
+    acc_got = acc_ref;
+    acc_jp = acc_ref;
+    blindRotateMP21Ntt(acc_ref, bsk->bskDft, scaled, param);
+    yatfhe_gb300::blindRotateMP21Ntt(acc_got, bsk->bskDft, scaled, param);
+    yatfhe_gb300::blindRotateJP22Ntt(acc_jp, *bsk, scaled, param);
+    expect(same(acc_ref, acc_got), "blindRotateMP21Ntt == the reference's");
+    expect(same(acc_ref, acc_jp), "blindRotateJP22Ntt == blindRotateMP21Ntt of the reference");
+    Tlwe big{ksKey.nCurrKey}, ks_ref{param.n}, ks_got{param.n};
+    extractTlweFromTrlwe(big, acc_ref, param.driftPhase);
+    switchKeyForTlwe(ks_ref, ksKey, big, param);
+    yatfhe_gb300::switchKeyForTlwe(ks_got, ksKey, big, param);
+    expect(same(ks_ref, ks_got), "switchKeyForTlwe == the reference's");
+    expect(same(ks_ref, want[3]), "rotate + extract + switch == functionalBootstrappingMPNtt");
+
+    // a new key built at the address of the old one: the cache must not serve the old one
+    const int uploads = yg_test_uploads();
+    bsk->~BootstrappingKeyMP();
+    bsk = new (storage) BootstrappingKeyMP{param, param.lApprox};
+    genBootstrappingKeyMP(*bsk, trgswKey, tlweKey, param);
+    bool new_ok = true;
+    for (const Tlwe& in : inputs) {
+        Tlwe ref{param.n}, got{param.n};
+        functionalBootstrappingMPNtt(ref, in, *bsk, ksKey, v, param);
+        yatfhe_gb300::functionalBootstrappingMPNtt(got, in, *bsk, ksKey, v, param);
+        new_ok &= same(ref, got);
+    }
+    expect(new_ok, "a new key at the same address gives the reference's results with the new key");
+    expect(yg_test_uploads() == uploads + 1, "the new key was uploaded once");
+
+    // forgetKeys() drops the cache: the next call converts the key again
+    yatfhe_gb300::forgetKeys();
+    Tlwe got{param.n}, ref{param.n};
+    yatfhe_gb300::functionalBootstrappingMPNtt(got, inputs[0], *bsk, ksKey, v, param);
+    functionalBootstrappingMPNtt(ref, inputs[0], *bsk, ksKey, v, param);
+    expect(same(ref, got) && yg_test_uploads() == uploads + 2, "after forgetKeys() the key is converted again");
+
+    yatfhe_gb300::forgetKeys();
+    bsk->~BootstrappingKeyMP();
+    std::printf("%d failure(s)\n", failures);
+    return failures ? 1 : 0;
+}

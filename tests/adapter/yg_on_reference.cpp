@@ -1,0 +1,181 @@
+// yg_on_reference.cpp -- TEST INFRASTRUCTURE ONLY.  A CPU stand-in for the part of the GB300
+// C ABI (include/yatfhe_gb300.h) that the C++ adapter (include/yatfhe_gb300_reference.hpp)
+// calls for GINX keys, built on the reference's own functions, plus host-memory versions of
+// the three CUDA memory calls the adapter makes.  Each entry point rebuilds the reference's
+// objects from the flat buffers the adapter produced and calls the reference function the
+// real entry point replaces; so a program that runs the adapter against this file gets the
+// reference's own result exactly when the adapter's conversions (word order, levels, rows,
+// signs, widths, the key cache) are right.  The CUDA side of the same ABI is checked by the
+// GPU tests.  Linked only into tests/adapter/adapter_run.cpp.
+#include <cuda_runtime_api.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "yatfhe/blind_rotate.h"
+#include "yatfhe/bootstrapping.h"
+#include "yatfhe/keyswitching.h"
+#include "yatfhe/tlwe.h"
+#include "yatfhe/trlwe.h"
+#include "yatfhe_gb300.h"
+
+struct yg_ctx {
+    yg_params p;
+};
+
+struct yg_key {
+    std::unique_ptr<BootstrappingKeyMP> bsk;
+    std::unique_ptr<TlweKeySwitchingKey> ksk;
+};
+
+namespace {
+
+const YatfheParameters* g_param = nullptr;
+thread_local std::string g_err;
+int g_uploads = 0;  // GINX key uploads (the driver checks the adapter's key cache with it)
+
+int fail(int rc, const std::string& what) {
+    g_err = what;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+// the process-wide parameters the reference functions run with (the driver's initYatfhe)
+void yg_test_use_params(const YatfheParameters* p) { g_param = p; }
+int yg_test_uploads(void) { return g_uploads; }
+
+const char* yg_last_error(void) { return g_err.c_str(); }
+
+int yg_ctx_create(const yg_params* q, int device, yg_ctx** out) {
+    const YatfheParameters& p = *g_param;
+    if (device != 0) return fail(YG_ERR_INVALID, "device");
+    if (q->n != p.n || q->N != p.N || q->k != p.k || q->radix_bits != p.radixBits || q->l_approx != p.lApprox ||
+        q->ks_radix_bits != p.ksRadixBits || q->ks_level != p.ksLevel || q->torus_bits != p.torusBits)
+        return fail(YG_ERR_INVALID, "parameters differ from the reference's");
+    *out = new yg_ctx{*q};
+    return YG_OK;
+}
+
+void yg_ctx_destroy(yg_ctx* c) { delete c; }
+
+// [n][l][k+1][k+1][N] words -> BootstrappingKeyMP::bskDft
+int yg_key_upload_bsk_ntt(yg_ctx* c, const uint64_t* w, yg_key** out) {
+    const YatfheParameters& p = *g_param;
+    auto key = std::make_unique<yg_key>();
+    key->bsk = std::make_unique<BootstrappingKeyMP>(p, c->p.l_approx);
+    size_t o = 0;
+    for (auto& g : key->bsk->bskDft) {
+        TrgswMPDft& t = g[0];
+        for (int lvl = 0; lvl < t.l; lvl++)
+            for (int row = 0; row <= p.k; row++) {
+                TrlweDft& r = row < p.k ? t.c[lvl][row] : t.cPrime[lvl];
+                for (int poly = 0; poly <= p.k; poly++) {
+                    NttPolynomial& P = poly < p.k ? r.a[poly] : r.b;
+                    std::memcpy(P.coeffs.data(), w + o, sizeof(uint64_t) * p.N);
+                    o += p.N;
+                }
+            }
+    }
+    g_uploads++;
+    *out = key.release();
+    return YG_OK;
+}
+
+int yg_key_create_ksk_only(yg_ctx*, yg_key** out) {
+    *out = new yg_key{};
+    return YG_OK;
+}
+
+// [k N][t][n + 1] int32 words -> TlweKeySwitchingKey::decomposedKsk
+int yg_key_set_ksk(yg_key* key, const int32_t* w) {
+    const YatfheParameters& p = *g_param;
+    key->ksk = std::make_unique<TlweKeySwitchingKey>(p);
+    size_t o = 0;
+    for (auto& row : key->ksk->decomposedKsk)
+        for (auto& t : row) {
+            for (int i = 0; i < p.n; i++) t.a[i] = static_cast<LweTorus>(w[o + i]);
+            t.b = static_cast<LweTorus>(w[o + p.n]);
+            o += p.n + 1;
+        }
+    return YG_OK;
+}
+
+void yg_key_destroy(yg_key* key) { delete key; }
+
+// functionalBootstrappingMPNtt per ciphertext (yatfhe/src/bootstrapping.cpp:71-80)
+int yg_pbs_host(yg_ctx*, const yg_key* key, const int32_t* in, int32_t* out, int count, const int64_t* lut, void*) {
+    const YatfheParameters& p = *g_param;
+    if (!key->bsk || !key->ksk) return fail(YG_ERR_STATE, "no key");
+    TorusPolynomial v{p.N};
+    for (int j = 0; j < p.N; j++) v.coeffs[j] = static_cast<Torus>(lut[j]);
+    for (int c = 0; c < count; c++) {
+        Tlwe x{p.n}, y{p.n};
+        const int32_t* w = in + static_cast<size_t>(c) * (p.n + 1);
+        for (int i = 0; i < p.n; i++) x.a[i] = static_cast<LweTorus>(w[i]);
+        x.b = static_cast<LweTorus>(w[p.n]);
+        functionalBootstrappingMPNtt(y, x, *key->bsk, *key->ksk, v, p);
+        int32_t* o = out + static_cast<size_t>(c) * (p.n + 1);
+        for (int i = 0; i < p.n; i++) o[i] = static_cast<int32_t>(y.a[i]);
+        o[p.n] = static_cast<int32_t>(y.b);
+    }
+    return YG_OK;
+}
+
+// blindRotateMP21Ntt in place (yatfhe/src/blind_rotate.cpp:1538-1565)
+int yg_blind_rotate_acc(yg_ctx*, const yg_key* key, const int32_t* scaled, int64_t* acc, int count, void*) {
+    const YatfheParameters& p = *g_param;
+    for (int c = 0; c < count; c++) {
+        ScaledTlwe s{2 * p.N, p.n};
+        for (int i = 0; i < p.n; i++) s.a[i] = scaled[static_cast<size_t>(c) * p.n + i];
+        Trlwe t{p.k, p.N};
+        int64_t* a = acc + static_cast<size_t>(c) * (p.k + 1) * p.N;
+        for (int r = 0; r < p.k; r++)
+            for (int j = 0; j < p.N; j++) t.a[r].coeffs[j] = static_cast<Torus>(a[static_cast<size_t>(r) * p.N + j]);
+        for (int j = 0; j < p.N; j++) t.b.coeffs[j] = static_cast<Torus>(a[static_cast<size_t>(p.k) * p.N + j]);
+        blindRotateMP21Ntt(t, key->bsk->bskDft, s, p);
+        for (int r = 0; r < p.k; r++)
+            for (int j = 0; j < p.N; j++) a[static_cast<size_t>(r) * p.N + j] = static_cast<int64_t>(t.a[r].coeffs[j]);
+        for (int j = 0; j < p.N; j++) a[static_cast<size_t>(p.k) * p.N + j] = static_cast<int64_t>(t.b.coeffs[j]);
+    }
+    return YG_OK;
+}
+
+// switchKeyForTlwe (yatfhe/src/keyswitching.cpp:48-72)
+int yg_keyswitch(yg_ctx*, const yg_key* key, const int32_t* big, int32_t* out, int count, void*) {
+    const YatfheParameters& p = *g_param;
+    const int kN = p.k * p.N;
+    for (int c = 0; c < count; c++) {
+        Tlwe x{kN}, y{p.n};
+        const int32_t* w = big + static_cast<size_t>(c) * (kN + 1);
+        for (int i = 0; i < kN; i++) x.a[i] = static_cast<LweTorus>(w[i]);
+        x.b = static_cast<LweTorus>(w[kN]);
+        switchKeyForTlwe(y, *key->ksk, x, p);
+        int32_t* o = out + static_cast<size_t>(c) * (p.n + 1);
+        for (int i = 0; i < p.n; i++) o[i] = static_cast<int32_t>(y.a[i]);
+        o[p.n] = static_cast<int32_t>(y.b);
+    }
+    return YG_OK;
+}
+
+// "device" memory of this stand-in: host memory
+cudaError_t cudaMalloc(void** p, size_t n) {
+    *p = std::malloc(n ? n : 1);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+cudaError_t cudaFree(void* p) {
+    std::free(p);
+    return cudaSuccess;
+}
+cudaError_t cudaMemcpy(void* dst, const void* src, size_t n, enum cudaMemcpyKind) {
+    std::memcpy(dst, src, n);
+    return cudaSuccess;
+}
+const char* cudaGetErrorString(cudaError_t) { return "stand-in CUDA error"; }
+
+}  // extern "C"

@@ -51,3 +51,33 @@ def test_adapter_compiles_against_reference_headers(tmp_path, torus):
            f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include", str(f)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(not REF_INC.exists(), reason="reference headers not present")
+def test_adapter_runs_against_the_reference(tmp_path):
+    """The adapter run end to end in the shape of the reference's BOOTSTRAPPING.MP21 test
+    (google_tests/bootstrappping_test.cpp:83-131): tests/adapter/adapter_run.cpp calls
+    yatfhe_gb300::functionalBootstrappingMPNtt (single and batched), blindRotateMP21Ntt,
+    blindRotateJP22Ntt and switchKeyForTlwe with the reference's own types and compares each
+    result with the reference function itself on the same objects.  Below the adapter, the
+    C ABI is a CPU stand-in built on the reference's functions (tests/adapter/yg_on_reference.cpp),
+    so any error in the adapter's conversions changes a result; the GPU side of that ABI is
+    covered by the -m gpu tests.  Also checked: the key cache converts a key once, a new key
+    built at a freed key's address is recognised and uploaded again, and forgetKeys()."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    o.build_reference()
+    lib_dir = ROOT / "oracle" / "_ref"
+    exe = tmp_path / "adapter_run"
+    src = ROOT / "tests" / "adapter"
+    cmd = [cxx, "-std=c++17", "-O2", "-DNDEBUG", "-pthread", "-DUSING_NTT=HEXL", "-DTORUS32", f"-I{REF_INC}",
+           f"-I{ROOT / 'oracle' / 'shim'}", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include",
+           str(src / "adapter_run.cpp"), str(src / "yg_on_reference.cpp"), f"-L{lib_dir}", "-lyatfhe_ref_t32",
+           f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600,
+                         env={**__import__("os").environ, "YATFHE_THREADS": "4"})
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "0 failure(s)" in run.stdout
