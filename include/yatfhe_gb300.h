@@ -119,9 +119,9 @@ int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);
  * torus word size (4 bytes at T = 32, a quarter of the GINX rows' bytes), and every
  * bootstrap rebuilds each CMux step's TRGSW from them as blindRotateLazyPipeAltNtt
  * (yatfhe/src/blind_rotate.cpp:995-1135) does.  Such a key runs yg_pbs, yg_pbs_host,
- * yg_blind_rotate (steps = n) and yg_blind_rotate_extract with the lazy blind rotation; the
- * batch plans, the serving loop, yg_pbs_noalloc and yg_blind_rotate_acc reject it with
- * YG_ERR_INVALID.  Requires n >= 2, l_approx <= 8, radix_bits <= 15, s2_levels <= 8 and
+ * yg_blind_rotate (steps = n), yg_blind_rotate_extract, the batch plans (with other lazy keys
+ * of the same s2 levels) and the serving loop (a lazy-key server) with the lazy blind
+ * rotation; yg_pbs_noalloc and yg_blind_rotate_acc reject it with YG_ERR_INVALID.  Requires n >= 2, l_approx <= 8, radix_bits <= 15, s2_levels <= 8 and
  * s2_levels * radix_bits <= torus_bits; an unreduced s2 word or a row value that is not a
  * sign-extended torus value is rejected with YG_ERR_INVALID.  Synchronizes the device. */
 int yg_key_upload_lazy(yg_ctx* ctx, const int64_t* h_cprime, const uint64_t* h_s2, int s2_levels, yg_key** out);
@@ -212,7 +212,9 @@ int yg_keyswitch(yg_ctx* ctx, const yg_key* key, const int32_t* d_big, int32_t* 
  * in a CUDA graph and replayed.  h_key_ids / h_lut_ids are host arrays of `count` indices
  * into keys[] / d_luts[] (NULL: every ciphertext uses entry 0).  Ciphertexts that share a
  * key should be contiguous: the key switch streams one KSK per run of them.  All keys must
- * belong to `ctx` and carry a KSK. */
+ * belong to `ctx`, carry a KSK and be of one family: GINX rows (WWL+24 keys included) or
+ * lazy keys with the same s2 levels (then the lazy blind rotation runs, the launch shape
+ * below does not apply); group keys are refused. */
 typedef struct yg_plan yg_plan;
 int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const int32_t* h_key_ids,
                    const int64_t* const* d_luts, int num_luts, const int32_t* h_lut_ids, int count, yg_plan** out);
@@ -270,9 +272,13 @@ typedef struct yg_request_times {
 } yg_request_times;
 int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out);
 /* Snapshots `key` (BSK + KSK, device layout) into pinned host memory; the key object may be
- * destroyed afterwards.  Any key handle works, whatever format it was made from (GINX or
- * WWL+24), so tenants of both families share one cache.  h_lut: the tenant's test
- * polynomial ([N] int64). */
+ * destroyed afterwards.  The first tenant fixes the server's key family: GINX rows (keys
+ * made from GINX or WWL+24 words share one cache) or lazy keys, whose HBM slots hold only the
+ * half rows and the s2 key (about a third of the GINX rows' bytes at the reference's default
+ * 32-bit set, so the same key_budget_bytes holds that many more tenants) and whose batches
+ * run the lazy blind rotation; a tenant of the other family is refused with YG_ERR_INVALID,
+ * as are group keys.  A budget smaller than one tenant's keys is refused here.  h_lut: the
+ * tenant's test polynomial ([N] int64). */
 int yg_server_add_tenant(yg_server* s, int tenant, const yg_key* key, const int64_t* h_lut);
 int yg_server_start(yg_server* s);
 /* Returns a request id (> 0) or a negative status. */

@@ -94,9 +94,12 @@ def test_gpu_lazy_file_host_buffers_and_refusals(tmp_path, built_lib):
     b = api.functional_bootstrapping_mp_ntt_host(ctx, kw, lwe, lut)
     np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(a, ora.pbs_lazy(lwe, lut, threads=8))
-    # entry points that take GINX rows only
-    with pytest.raises(ValueError, match="keys run through"):
-        api.BatchPlan(ctx, [kw], [d_lut], 4)
+    # a plan takes keys of one family
+    og = Restatement(p)
+    og.keygen(8)
+    kg = api.BootstrapKey.from_ntt_words(ctx, og.bsk_ntt()).set_ksk(og.ksk())
+    with pytest.raises(ValueError, match="one family"):
+        api.BatchPlan(ctx, [kw, kg], [d_lut], 4, key_ids=[0, 0, 1, 1])
     with pytest.raises(ValueError, match="steps = n"):
         api.blind_rotate_mp21_ntt(ctx, kw, d_in, d_lut, steps=3)
     # a row word that is not a sign-extended torus value
@@ -110,3 +113,78 @@ def test_gpu_lazy_file_host_buffers_and_refusals(tmp_path, built_lib):
     ow.save_wwl24_file(tmp_path / "w.bin")
     with pytest.raises(OSError, match="expected"):
         api.BootstrapKey.from_lazy_file(ctx, tmp_path / "w.bin")
+
+
+def _lazy_tenants(p, seeds):
+    from yatfhe_gb300 import api
+
+    ctx = api.Context(p, 0)
+    oras, keys = [], []
+    for sd in seeds:
+        o = Restatement(p)
+        o.keygen_lazy(sd)
+        cprime, s2 = o.lazy_words()
+        oras.append(o)
+        keys.append(api.BootstrapKey.from_lazy_words(ctx, cprime, s2).set_ksk(o.ksk()))
+    return ctx, oras, keys
+
+
+def test_lazy_keys_in_a_multi_key_plan(built_lib):
+    """Several lazy keys and test polynomials in one launch pair (yg_plan_*, the lazy blind
+    rotation reading a per-ciphertext key table): every output equals the same ciphertext
+    bootstrapped alone under its own key, which equals the restatement."""
+    from yatfhe_gb300 import api
+
+    p = small(WWL24_T32_N2048, 9)
+    ctx, oras, keys = _lazy_tenants(p, [41, 42, 43])
+    rng = np.random.default_rng(4)
+    counts = [5, 1, 12]
+    key_ids = np.concatenate([np.full(c, t, np.int32) for t, c in enumerate(counts)])
+    lwe = np.concatenate([_random_case(p, max(c, 4), 50 + t)[0][:c] for t, c in enumerate(counts)])
+    luts_np = [_random_case(p, 4, 60)[1], _random_case(p, 4, 61)[1]]
+    lut_ids = rng.integers(0, 2, len(lwe)).astype(np.int32)
+    luts = [torch.from_numpy(v).cuda() for v in luts_np]
+    d_in = torch.from_numpy(lwe).cuda()
+    plan = api.BatchPlan(ctx, keys, luts, len(lwe), key_ids=key_ids, lut_ids=lut_ids)
+    got = plan.run(d_in, torch.empty_like(d_in)).cpu().numpy()
+    torch.cuda.synchronize()
+    for c in range(len(lwe)):
+        alone = api.functional_bootstrapping_mp_ntt(ctx, keys[key_ids[c]], d_in[c:c + 1], luts[lut_ids[c]])
+        np.testing.assert_array_equal(got[c], alone.cpu().numpy()[0], err_msg=f"ciphertext {c}")
+    for c in (0, 5, 6):
+        np.testing.assert_array_equal(got[c:c + 1], oras[key_ids[c]].pbs_lazy(lwe[c:c + 1], luts_np[lut_ids[c]], threads=8))
+
+
+def test_serving_lazy_tenants(built_lib):
+    """The serving loop with lazy keys: a lazy server's HBM slots hold the half rows and the s2
+    key (a third of the GINX rows' bytes at this set), so the same budget holds more tenants;
+    a trace with evictions returns every output equal to the same ciphertexts bootstrapped
+    alone."""
+    from yatfhe_gb300 import api, serving
+
+    p = small(WWL24_T32_N2048, 9)
+    tenants, max_count = 6, 8
+    ctx, oras, keys = _lazy_tenants(p, [70 + t for t in range(tenants)])
+    og = Restatement(p)
+    og.keygen(70)
+    ginx = api.BootstrapKey.from_ntt_words(ctx, og.bsk_ntt()).set_ksk(og.ksk())
+    budget = 2.5 * keys[0].device_bytes
+    srv = serving.Server(ctx, key_budget_bytes=budget, max_batch=32, max_inflight=2)
+    pool = torch.empty((tenants, max_count, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    for t in range(tenants):
+        lwe, lut = _random_case(p, max_count, 80 + t)
+        srv.add_tenant(t, keys[t], lut)
+        pool[t] = torch.from_numpy(lwe)
+        expect[t] = api.functional_bootstrapping_mp_ntt(ctx, keys[t], torch.from_numpy(lwe).cuda(),
+                                                        torch.from_numpy(lut).cuda()).cpu()
+    with pytest.raises(ValueError, match="one family"):
+        srv.add_tenant(tenants, ginx, lut)
+    srv.start()
+    res = srv.run_trace(pool, expect, requests=120, warmup=0, rate=2000.0, zipf_s=1.1, max_count=max_count, seed=5)
+    c = srv.counters()
+    srv.close()
+    assert res["served"] == 120 and res["mismatched_requests"] == 0
+    assert c["key_slots"] == 2 and res["key_misses"] > 0
+    # the same budget holds fewer GINX tenants (their rows take three times the bytes)
+    assert int(budget // ginx.device_bytes) < c["key_slots"]

@@ -853,6 +853,23 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
 
 }  // namespace
 
+namespace yg {
+
+LazyBrArgs lazy_launch_args(const yg_ctx* c, const yg_key* key) { return lazy_args(c, key); }
+
+size_t lazy_cprime_bytes(const yg_params& p) {
+    return (size_t)p.n * p.l_approx * (p.k + 1) * p.N * (p.torus_bits == 32 ? 4 : 8);
+}
+
+size_t lazy_tab_words(const yg_params& p, int Ls) { return 4 * (size_t)p.N + 2 * (size_t)Ls * (p.k + 1) * p.N; }
+
+LazyKeyRef lazy_key_ref(const yg_params& p, const void* cprime, const uint64_t* tab, int Ls) {
+    const uint64_t* s2 = tab + 4 * (size_t)p.N;
+    return LazyKeyRef{cprime, s2, s2 + (size_t)Ls * (p.k + 1) * p.N};
+}
+
+}  // namespace yg
+
 extern "C" {
 
 const char* yg_last_error(void) { return yg::last_error_slot().c_str(); }
@@ -1276,6 +1293,10 @@ struct yg_plan {
     yg::KsTile* d_tiles = nullptr;
     int num_tiles = 0;
     int32_t* d_big = nullptr;
+    // lazy ("OURS") keys: the lazy blind rotation, keys by table
+    bool lazy = false;
+    yg::LazyKeyRef* d_lazy_keys = nullptr;
+    yg::LazyBrArgs lazy_tmpl{};
 };
 
 namespace {
@@ -1287,6 +1308,7 @@ void plan_free(yg_plan* p) {
     cudaFree(p->d_lut_of);
     cudaFree(p->d_tiles);
     cudaFree(p->d_big);
+    cudaFree(p->d_lazy_keys);
 }
 
 template <typename T>
@@ -1306,8 +1328,14 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
     if (!ctx || !keys || num_keys < 1 || !d_luts || num_luts < 1 || count < 0 || !out)
         return set_err(YG_ERR_INVALID, "yg_plan_create: bad arguments");
     *out = nullptr;
-    for (int i = 0; i < num_keys; i++)
-        if (int rc = check_key(ctx, keys[i], true, true)) return rc;
+    // one key family per plan: GINX rows (and keys derived into them), or lazy keys with the
+    // same number of s2 levels
+    for (int i = 0; i < num_keys; i++) {
+        if (int rc = check_key(ctx, keys[i], true, true, true)) return rc;
+        if (keys[i]->grouped()) return set_err(YG_ERR_INVALID, "yg_plan_create: group keys run through yg_pbs");
+        if (keys[i]->lazy() != keys[0]->lazy() || keys[i]->lazy_ls != keys[0]->lazy_ls)
+            return set_err(YG_ERR_INVALID, "yg_plan_create: a plan takes keys of one family (GINX or lazy)");
+    }
     for (int i = 0; i < num_luts; i++)
         if (!d_luts[i]) return set_err(YG_ERR_INVALID, "yg_plan_create: null LUT");
     for (int c = 0; c < count; c++) {
@@ -1325,6 +1353,14 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
         p->lut0 = d_luts[0];
         try {
             const bool multi_key = h_key_ids && num_keys > 1;
+            p->lazy = keys[0]->lazy();
+            if (p->lazy) p->lazy_tmpl = yg::lazy_launch_args(ctx, keys[0]);
+            if (multi_key && p->lazy) {
+                std::vector<yg::LazyKeyRef> table(num_keys);
+                for (int i = 0; i < num_keys; i++)
+                    table[i] = yg::lazy_key_ref(ctx->p, keys[i]->d_lazy_cprime, keys[i]->d_lazy_tab, keys[i]->lazy_ls);
+                p->d_lazy_keys = upload_vec(table, "plan lazy key table");
+            }
             if (multi_key) {
                 std::vector<const uint4*> table(num_keys);
                 for (int i = 0; i < num_keys; i++) table[i] = reinterpret_cast<const uint4*>(keys[i]->d_bsk);
@@ -1377,6 +1413,23 @@ int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream
     yg_ctx* ctx = plan->ctx;
     return guarded([&] {
         DeviceGuard g(ctx->device);
+        const int kN = ctx->p.k * ctx->p.N;
+        if (plan->lazy) {
+            yg::LazyBrArgs a = plan->lazy_tmpl;
+            a.lwe_in = d_in;
+            a.lut = plan->lut0;
+            a.keys = plan->d_lazy_keys;
+            a.key_of = plan->d_lazy_keys ? plan->d_key_of : nullptr;
+            a.lut_table = plan->d_lut_table;
+            a.lut_of = plan->d_lut_of;
+            a.big_out = plan->d_big;
+            a.count = plan->count;
+            yg::check_launch(yg::launch_lazy_blind_rotate(a, stream), "lazy blind rotate launch");
+            yg::KsArgs k{plan->d_big, plan->key0->d_ksk, d_out, plan->count, kN, ctx->p.n, ctx->p.ks_level,
+                         ctx->p.ks_radix_bits, plan->d_tiles, plan->num_tiles};
+            yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");
+            return YG_OK;
+        }
         yg::BrArgs a = br_args(ctx, plan->key0);
         a.lwe_in = d_in;
         a.lut = plan->lut0;
@@ -1392,7 +1445,6 @@ int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream
             a.grid = plan->grid;
         }
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
-        const int kN = ctx->p.k * ctx->p.N;
         yg::KsArgs k{plan->d_big, plan->key0->d_ksk, d_out, plan->count, kN, ctx->p.n, ctx->p.ks_level,
                      ctx->p.ks_radix_bits, plan->d_tiles, plan->num_tiles};
         yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");

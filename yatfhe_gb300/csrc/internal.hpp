@@ -117,5 +117,12 @@ int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bo
 
 // Blind-rotation launch arguments of a context and key (buffers and count left empty).
 BrArgs br_args(const yg_ctx* c, const yg_key* key);
+// The same for a lazy key (the lazy blind rotation).
+LazyBrArgs lazy_launch_args(const yg_ctx* c, const yg_key* key);
+// A lazy key's device parts: the half rows (bytes), the table block of [wi | wip | wf | wfp]
+// (N words each) then [s2 | s2p] ([Ls][k+1][N] each), and the kernel's view of one key.
+size_t lazy_cprime_bytes(const yg_params& p);
+size_t lazy_tab_words(const yg_params& p, int Ls);
+LazyKeyRef lazy_key_ref(const yg_params& p, const void* cprime, const uint64_t* tab, int Ls);
 
 }  // namespace yg

@@ -478,7 +478,12 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
     uint64_t* sw = reinterpret_cast<uint64_t*>(lz_smem);                  // [Ls + 3][N]
     TT* acc = reinterpret_cast<TT*>(sw + (size_t)M * N);                  // [2][N]
     int16_t* sa = reinterpret_cast<int16_t*>(acc + 2 * N);                // [n + 1]
-    const TT* cpr = static_cast<const TT*>(a.cprime);
+    // this ciphertext's key and test polynomial (one of many when the launch has tables)
+    const LazyKeyRef kr = a.key_of ? a.keys[a.key_of[ct]] : LazyKeyRef{a.cprime, a.s2, a.s2p};
+    const TT* cpr = static_cast<const TT*>(kr.cprime);
+    const uint64_t* s2 = kr.s2;
+    const uint64_t* s2p = kr.s2p;
+    const int64_t* lut = a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut;
     const int jj[2] = {t, t + H};
 
     auto lift = [q](int64_t x) -> uint64_t { return x < 0 ? (uint64_t)(x + (int64_t)q) : (uint64_t)x; };
@@ -555,7 +560,7 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int j = jj[e];
-                sw[j] = lift(digit_at((TT)a.lut[j], L, lvl));
+                sw[j] = lift(digit_at((TT)lut[j], L, lvl));
                 sw[N + j] = lift((int64_t)src[j]);
                 sw[2 * N + j] = lift((int64_t)src[N + j]);
             }
@@ -579,7 +584,7 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
             for (int e = 0; e < 2; ++e) {
                 const int j = jj[e];
                 TT x = tsub<T>(rot_at(acc + poly * N, r0, j), acc[poly * N + j]);
-                if (poly == 1) x = tadd<T>(x, (TT)a.lut[j]);
+                if (poly == 1) x = tadd<T>(x, (TT)lut[j]);
                 tv[poly][e] = x;
             }
         __syncthreads();
@@ -640,8 +645,8 @@ __global__ void __launch_bounds__(1024, 1) lazy_blind_rotate_kernel(const LazyBr
                 for (int gl = 0; gl < Ls; ++gl) {
                     const uint64_t D = sw[(size_t)gl * N + j];
                     const size_t o = (size_t)gl * 2 * N + j;
-                    ca = add2(ca, mulshoup64_lazy(D, a.s2[o], a.s2p[o], q));
-                    cb = add2(cb, mulshoup64_lazy(D, a.s2[o + N], a.s2p[o + N], q));
+                    ca = add2(ca, mulshoup64_lazy(D, s2[o], s2p[o], q));
+                    cb = add2(cb, mulshoup64_lazy(D, s2[o + N], s2p[o + N], q));
                     cpa = add2(cpa, mulshoup64_lazy(D, a.recomp[gl], a.recompp[gl], q));
                 }
                 const uint64_t bh = red4(sw[(size_t)Ls * N + j]);

@@ -129,12 +129,25 @@ struct KeygenKskArgs {
 // half TRGSW rows in the coefficient domain (torus words) and the NTT-domain s2 key; every
 // CMux step rebuilds the rows of its TRGSW for the ciphertext from them.
 constexpr int kLazyMaxLevels = 8;  // levels of the half rows (l_approx) and of the s2 key
+// One lazy key as the kernel reads it (see LazyBrArgs).
+struct LazyKeyRef {
+    const void* cprime;
+    const uint64_t* s2;
+    const uint64_t* s2p;
+};
+
 struct LazyBrArgs {
     const int32_t* lwe_in;   // [count][n+1]
     const int64_t* lut;      // [N] test polynomial v (torus, sign-extended)
     const void* cprime;      // [n][L][2][N] half rows (a, b): int32 words at T = 32, int64 at T = 56
     const uint64_t* s2;      // [Ls][2][N] NTT-domain s2 key mod q
     const uint64_t* s2p;     // [Ls][2][N] floor(s2 2^64 / q)
+    // many keys in one launch: ciphertext c uses keys[key_of[c]] (cprime, s2, s2p above
+    // unused) and lut_table[lut_of[c]]; null = the single key / LUT above
+    const LazyKeyRef* keys;
+    const int32_t* key_of;
+    const int64_t* const* lut_table;
+    const int32_t* lut_of;
     const uint64_t* wf;      // [N] psi^brv(k) mod q, and Shoup companions
     const uint64_t* wfp;
     const uint64_t* wi;      // [N] psi^-brv(k) mod q, and Shoup companions

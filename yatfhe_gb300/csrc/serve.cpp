@@ -108,6 +108,15 @@ struct yg_server {
     yg_ctx* ctx = nullptr;
     yg_server_config cfg{};
     size_t bsk_bytes = 0, ksk_bytes = 0;
+    // The key family of the tenants, fixed by the first one: GINX rows (and keys derived into
+    // them), or lazy keys, whose slot holds [half rows | table block] and whose batches run
+    // the lazy blind rotation with a per-slot key table and server-owned transform tables.
+    bool family_set = false, lazy = false;
+    int lazy_ls = 0;
+    size_t lazy_cprime_bytes = 0;
+    yg::LazyBrArgs lazy_tmpl{};
+    yg::LazyKeyRef* d_lazy_slot_table = nullptr;
+    uint64_t* d_lazy_tables = nullptr;
     int nslots = 0;
     std::vector<uint32_t*> slot_bsk;
     std::vector<int32_t*> slot_ksk;
@@ -283,6 +292,17 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     ck(cudaMemcpyAsync(b->d_tiles, b->h_tiles, (size_t)ntiles * sizeof(yg::KsTile), cudaMemcpyHostToDevice, b->stream),
        "tables");
     for (Tenant* t : used) ck(cudaStreamWaitEvent(b->stream, t->ready, 0), "wait refill");
+    if (s->lazy) {
+        yg::LazyBrArgs la = s->lazy_tmpl;
+        la.keys = s->d_lazy_slot_table;
+        la.key_of = b->d_key_of;
+        la.lut_table = s->d_lut_table;
+        la.lut_of = b->d_lut_of;
+        la.lwe_in = b->d_in;
+        la.big_out = b->d_big;
+        la.count = total;
+        yg::check_launch(yg::launch_lazy_blind_rotate(la, b->stream), "lazy blind rotate launch");
+    } else {
     yg::BrArgs a = yg::br_args(s->ctx, nullptr);
     a.key = nullptr;
     a.key_table = s->d_slot_table;
@@ -293,6 +313,7 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     a.big_out = b->d_big;
     a.count = total;
     yg::check_launch(yg::launch_blind_rotate(s->ctx->logN, p.torus_bits, a, b->stream), "blind rotate launch");
+    }
     yg::KsArgs k{b->d_big, nullptr, b->d_out, total, kN, p.n, p.ks_level, p.ks_radix_bits, b->d_tiles, ntiles};
     yg::check_launch(yg::launch_keyswitch(k, b->stream), "keyswitch launch");
     off = 0;
@@ -352,6 +373,52 @@ void worker_loop(yg_server* s) {
     }
 }
 
+// The first tenant's key is lazy: the slots are re-made for lazy keys ([half rows | table
+// block] + KSK, so the budget holds more of them), with the kernel's per-slot key table and
+// the transform tables in server memory (the key object may be destroyed after it is added).
+void use_lazy_slots(yg_server* s, const yg_key* key) {
+    const yg_params& p = s->ctx->p;
+    const size_t cp = yg::lazy_cprime_bytes(p), tab_words = yg::lazy_tab_words(p, key->lazy_ls);
+    const size_t bsk = cp + tab_words * 8;
+    const int nslots = (int)(s->cfg.key_budget_bytes / (bsk + s->ksk_bytes));
+    if (nslots < 1) throw std::invalid_argument("key budget smaller than one tenant's keys");
+    for (auto* b : s->slot_bsk) cudaFree(b);
+    for (auto* k : s->slot_ksk) cudaFree(k);
+    s->slot_bsk.clear();
+    s->slot_ksk.clear();
+    s->slot_owner.clear();
+    s->lazy = true;
+    s->lazy_ls = key->lazy_ls;
+    s->lazy_cprime_bytes = cp;
+    s->bsk_bytes = bsk;
+    s->nslots = nslots;
+    std::vector<yg::LazyKeyRef> refs;
+    for (int i = 0; i < nslots; i++) {
+        uint32_t* b = nullptr;
+        int32_t* k = nullptr;
+        ck(cudaMalloc(&b, bsk), "key slot");
+        s->slot_bsk.push_back(b);
+        ck(cudaMalloc(&k, s->ksk_bytes), "key slot");
+        s->slot_ksk.push_back(k);
+        s->slot_owner.push_back(-1);
+        const unsigned char* base = reinterpret_cast<const unsigned char*>(b);
+        refs.push_back(yg::lazy_key_ref(p, base, reinterpret_cast<const uint64_t*>(base + cp), key->lazy_ls));
+    }
+    ck(cudaMalloc(&s->d_lazy_slot_table, refs.size() * sizeof(yg::LazyKeyRef)), "lazy slot table");
+    ck(cudaMemcpy(s->d_lazy_slot_table, refs.data(), refs.size() * sizeof(yg::LazyKeyRef), cudaMemcpyHostToDevice),
+       "lazy slot table");
+    // the transforms' tables ([wi | wip | wf | wfp], N words each) are the same for every key
+    ck(cudaMalloc(&s->d_lazy_tables, 4 * (size_t)p.N * 8), "lazy tables");
+    ck(cudaMemcpy(s->d_lazy_tables, key->d_lazy_tab, 4 * (size_t)p.N * 8, cudaMemcpyDeviceToDevice), "lazy tables");
+    s->lazy_tmpl = yg::lazy_launch_args(s->ctx, key);
+    s->lazy_tmpl.cprime = nullptr;
+    s->lazy_tmpl.s2 = s->lazy_tmpl.s2p = nullptr;
+    s->lazy_tmpl.wi = s->d_lazy_tables;
+    s->lazy_tmpl.wip = s->d_lazy_tables + p.N;
+    s->lazy_tmpl.wf = s->d_lazy_tables + 2 * (size_t)p.N;
+    s->lazy_tmpl.wfp = s->d_lazy_tables + 3 * (size_t)p.N;
+}
+
 }  // namespace
 
 extern "C" {
@@ -368,8 +435,10 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
         const yg_params& p = ctx->p;
         s->bsk_bytes = yg::key_words(p.n, p.l_approx, p.N) * 4;
         s->ksk_bytes = (size_t)p.k * p.N * p.ks_level * (p.n + 1) * 4;
+        // GINX slots; a budget too small for them may still hold lazy keys (the first
+        // tenant's family decides, use_lazy_slots)
         s->nslots = (int)(cfg->key_budget_bytes / (s->bsk_bytes + s->ksk_bytes));
-        if (s->nslots < 1) throw std::invalid_argument("key budget smaller than one tenant's keys");
+        if (s->nslots < 1) s->nslots = 0;
         if (cfg->max_tenants < 1) throw std::invalid_argument("max_tenants must be positive");
         auto fail_clean = [&]() {
             for (auto* b : s->slot_bsk) cudaFree(b);
@@ -391,7 +460,7 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
             }
             std::vector<const uint4*> table;
             for (uint32_t* b : s->slot_bsk) table.push_back(reinterpret_cast<const uint4*>(b));
-            ck(cudaMalloc(&s->d_slot_table, table.size() * sizeof(void*)), "slot table");
+            ck(cudaMalloc(&s->d_slot_table, std::max<size_t>(1, table.size()) * sizeof(void*)), "slot table");
             ck(cudaMemcpy(s->d_slot_table, table.data(), table.size() * sizeof(void*), cudaMemcpyHostToDevice),
                "slot table");
             ck(cudaMalloc(&s->d_lut_table, (size_t)cfg->max_tenants * sizeof(void*)), "LUT table");
@@ -423,20 +492,34 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
 
 int yg_server_add_tenant(yg_server* s, int tenant, const yg_key* key, const int64_t* h_lut) {
     if (!s || !key || !h_lut || tenant < 0) return set_err(YG_ERR_INVALID, "yg_server_add_tenant: bad arguments");
-    if (int rc = yg::check_key(s->ctx, key, true, true)) return rc;
+    if (int rc = yg::check_key(s->ctx, key, true, true, true)) return rc;
+    if (key->grouped()) return set_err(YG_ERR_INVALID, "yg_server_add_tenant: group keys run through yg_pbs");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->running) return set_err(YG_ERR_STATE, "tenants must be added before yg_server_start");
     if (s->tenants.count(tenant)) return set_err(YG_ERR_INVALID, "tenant already registered");
     if ((int)s->by_index.size() >= s->cfg.max_tenants) return set_err(YG_ERR_INVALID, "too many tenants");
+    if (s->family_set && (key->lazy() != s->lazy || key->lazy_ls != s->lazy_ls))
+        return set_err(YG_ERR_INVALID, "yg_server_add_tenant: a server serves keys of one family (GINX or lazy)");
     return guarded([&] {
         yg::DeviceGuard g(s->ctx->device);
+        if (!s->family_set && key->lazy()) use_lazy_slots(s, key);
+        if (s->nslots < 1) throw std::invalid_argument("key budget smaller than one tenant's keys");
+        s->family_set = true;
         auto t = std::make_unique<Tenant>();
         t->id = tenant;
         t->index = (int)s->by_index.size();
         try {
             ck(cudaMallocHost(&t->h_bsk, s->bsk_bytes), "pinned key image");
             ck(cudaMallocHost(&t->h_ksk, s->ksk_bytes), "pinned key image");
-            ck(cudaMemcpy(t->h_bsk, key->d_bsk, s->bsk_bytes, cudaMemcpyDeviceToHost), "key image");
+            if (s->lazy) {  // [half rows | table block], the slot's layout
+                unsigned char* img = reinterpret_cast<unsigned char*>(t->h_bsk);
+                ck(cudaMemcpy(img, key->d_lazy_cprime, s->lazy_cprime_bytes, cudaMemcpyDeviceToHost), "key image");
+                ck(cudaMemcpy(img + s->lazy_cprime_bytes, key->d_lazy_tab, s->bsk_bytes - s->lazy_cprime_bytes,
+                              cudaMemcpyDeviceToHost),
+                   "key image");
+            } else {
+                ck(cudaMemcpy(t->h_bsk, key->d_bsk, s->bsk_bytes, cudaMemcpyDeviceToHost), "key image");
+            }
             ck(cudaMemcpy(t->h_ksk, key->d_ksk, s->ksk_bytes, cudaMemcpyDeviceToHost), "key image");
             ck(cudaMalloc(&t->d_lut, (size_t)s->ctx->p.N * 8), "LUT");
             ck(cudaMemcpy(t->d_lut, h_lut, (size_t)s->ctx->p.N * 8, cudaMemcpyHostToDevice), "LUT");
@@ -540,6 +623,8 @@ void yg_server_destroy(yg_server* s) {
     for (auto* k : s->slot_ksk) cudaFree(k);
     cudaFree(s->d_slot_table);
     cudaFree(s->d_lut_table);
+    cudaFree(s->d_lazy_slot_table);
+    cudaFree(s->d_lazy_tables);
     cudaStreamDestroy(s->copy);
     delete s;
 }
