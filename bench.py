@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--params", default="t32_n1024")
     ap.add_argument("--count", type=int, default=0, help="ciphertexts per step (default 65536 / 16384)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving", "serving_lazy"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-call / sweep legs and other workloads")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
@@ -749,6 +749,67 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
             "bit_exact_vs_alone": mismatches == 0, "setup_s": setup_s}
 
 
+def leg_serving_lazy(dev, requests=300, fractions=(0.5, 0.8), tenants=48, budget=4e9, max_count=64, max_batch=152,
+                     max_inflight=2):
+    """The serving loop with lazy ("OURS") keys on the reference's default TORUS=32 set (n=680,
+    N=2048, lApprox=4, s2 key with 8 levels): 48 tenants with seeded synthetic half rows, s2
+    keys and KSKs, a 4 GB HBM key budget, requests of 1..64 ciphertexts (log-uniform), Zipf(1.1)
+    tenants, Poisson arrivals at fractions of the measured peak.  Reports how many tenants the
+    budget holds against GINX keys of the same set, p50/p99, hit rate, and that every output
+    equals the same ciphertexts bootstrapped alone."""
+    import torch
+
+    from yatfhe_gb300 import api, serving
+    from yatfhe_gb300.params import WWL24_T32_N2048 as p
+
+    ctx = api.Context(p, dev)
+    lut_np = workload_lut(p)
+    d_lut = torch.from_numpy(lut_np).to(f"cuda:{dev}")
+    pool = torch.empty((tenants, max_count, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    srv = serving.Server(ctx, key_budget_bytes=budget, max_batch=max_batch, max_inflight=max_inflight,
+                         max_tenants=tenants)
+    row = (p.k + 1) * p.N
+    t_setup = time.perf_counter()
+    key_bytes = 0
+    for t in range(tenants):
+        rng = np.random.default_rng(0x5EED4000 + t)
+        cprime = rng.integers(-(1 << 31), 1 << 31, size=p.n * p.l_approx * row, dtype=np.int64)
+        s2 = rng.integers(0, p.q_ntt, size=p.l * row, dtype=np.uint64)
+        ksk = rng.integers(-(1 << 31), 1 << 31, size=p.ksk_words, dtype=np.int64).astype(np.int32)
+        key = api.BootstrapKey.from_lazy_words(ctx, cprime, s2).set_ksk(ksk)
+        key_bytes = key.device_bytes
+        lwe = synthetic_lwe(p, max_count, 0x5EED5000 + t)
+        pool[t] = torch.from_numpy(lwe)
+        expect[t] = api.functional_bootstrapping_mp_ntt(ctx, key, pool[t].to(f"cuda:{dev}"), d_lut).cpu()
+        srv.add_tenant(t, key, lut_np)
+        key.close()
+    setup_s = time.perf_counter() - t_setup
+    srv.start()
+    slots = srv.counters()["key_slots"]
+    ginx_bytes = p.n * p.l_approx * 2 * 3 * 2 * p.N * 4 + p.ksk_words * 4  # device rows + KSK of a GINX key
+    peak = srv.run_trace(pool, expect, requests=requests, warmup=20, rate=1e6, seed=21, max_count=max_count)
+    points, mismatches = [], peak["mismatched_requests"]
+    for i, f in enumerate(fractions):
+        r = srv.run_trace(pool, expect, requests=requests, warmup=20, rate=f * peak["requests_per_s"], seed=200 + i,
+                          max_count=max_count, slo_ms=100.0)
+        mismatches += r["mismatched_requests"]
+        points.append({"fraction_of_peak": f, "offered_rps": r["offered_rate"], "served": r["served"],
+                       "bootstraps_per_s": r["ciphertexts_per_s"], "p50_ms": r["sojourn"]["p50_ms"],
+                       "p99_ms": r["sojourn"]["p99_ms"], "hit_rate": r["hit_rate"], "key_misses": r["key_misses"],
+                       "slo_violation_rate_100": r["slo_violation_rate_100"],
+                       "tenant_fairness_jain": r["tenant_fairness_jain"]})
+    srv.close()
+    return {"workload": f"serving_lazy_t32_n2048_{tenants}tenants_4GB", "tenants": tenants,
+            "key_budget_bytes": int(budget), "key_slots": slots, "lazy_key_device_bytes": key_bytes,
+            "ginx_key_device_bytes_same_set": ginx_bytes, "ginx_slots_same_budget": int(budget // ginx_bytes),
+            "request_sizes": f"floor(exp(U(0, ln {max_count + 1}))), 1..{max_count}",
+            "peak": {"requests_per_s": peak["requests_per_s"], "bootstraps_per_s": peak["ciphertexts_per_s"],
+                     "hit_rate": peak["hit_rate"]},
+            "points": points, "mismatched_requests": mismatches, "bit_exact_vs_alone": mismatches == 0,
+            "setup_s": setup_s}
+
+
 # ------------------------------------------------------------------------------ reference arm
 
 def reference_arm(args, p, config, threads):
@@ -826,6 +887,14 @@ def main():
 
     if args.workload != "batch":
         if rank != 0:
+            return
+        if args.workload == "serving_lazy":
+            r = leg_serving_lazy(dev)
+            line = {"metric": "serving with lazy keys: tenants resident in 4 GB", "value": r["key_slots"],
+                    "unit": "tenants", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "int32 torus / u64 mod q", "data": "synthetic",
+                    "config": {"workload": r["workload"]}, "result": r}
+            print(json.dumps(line))
             return
         if args.workload == "multi_tenant":
             r = leg_multi_tenant(dev, steps=args.steps, warmup=args.warmup)
@@ -963,6 +1032,7 @@ def main():
                 leg_serving, dev, requests=args.serving_requests,
                 fractions=tuple(float(x) for x in args.serving_fractions.split(",")),
                 max_batch=args.serving_max_batch, max_inflight=args.serving_inflight),
+            "serving_lazy_t32_n2048_48tenants_4GB": _safe(leg_serving_lazy, dev),
         }
 
     line = {
