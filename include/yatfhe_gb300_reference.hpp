@@ -21,6 +21,7 @@
 //   blindRotateLazyPipeAltNtt      yatfhe/include/yatfhe/blind_rotate.h:44-45
 //   blindRotateLazyPipeAltNttSweep yatfhe/include/yatfhe/blind_rotate.h:48-50
 //   blindRotateLazyPipeAltInitNtt  yatfhe/include/yatfhe/blind_rotate.h:56-57
+//   blindRotateLazyPipeAltNoFirstNtt yatfhe/include/yatfhe/blind_rotate.h:53
 //   blindRotateNtt                 yatfhe/include/yatfhe/blind_rotate.h:13 (groups 1-3)
 //   functionalBootstrappingNtt     yatfhe/include/yatfhe/bootstrapping.h:366-367
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
@@ -466,6 +467,17 @@ inline void blindRotateLazyPipeAltInitNtt(Trlwe& accum, BootstrappingKeyMPLazyPi
         }
     }
     yatfhe_gb300::blindRotateLazyPipeAltNtt(accum, bsk, input, v, gdVntt, param);
+}
+
+// blindRotateLazyPipeAltNoFirstNtt: the first key index through the ordinary chain instead of
+// the first-component shortcut.  Both give the same accumulator bit for bit (the shortcut is
+// that chain's first external product, the same polynomial mod q before the one rounding;
+// tests/test_lazy_oracle.py checks it on the reference itself), so the GPU lazy rotation
+// serves it.
+inline void blindRotateLazyPipeAltNoFirstNtt(Trlwe& accum, const BootstrappingKeyMPLazyPipeAlt& bsk,
+                                             const ScaledTlwe& input, const TorusPolynomial& v,
+                                             const YatfheParameters& param) {
+    yatfhe_gb300::blindRotateLazyPipeAltNtt(accum, bsk, input, v, {}, param);
 }
 
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,

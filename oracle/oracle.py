@@ -340,20 +340,23 @@ class Restatement(_Common):
     def load_lazy_file(self, path) -> None:
         self._call("load_lazy_file", str(path).encode())
 
-    def blind_rotate_lazy(self, lwe, v) -> np.ndarray:
-        """The accumulator [(k+1) N] after the lazy blind rotation of one ciphertext."""
+    def blind_rotate_lazy(self, lwe, v, no_first: bool = False) -> np.ndarray:
+        """The accumulator [(k+1) N] after the lazy blind rotation of one ciphertext
+        (blindRotateLazyPipeAltNtt, or with no_first blindRotateLazyPipeAltNoFirstNtt)."""
         lwe = np.ascontiguousarray(lwe, np.int32).reshape(self.p.n + 1)
         v = np.ascontiguousarray(v, np.int64)
         acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
-        self._call("blind_rotate_lazy", _ptr(lwe, _i32p), _ptr(v, _i64p), _ptr(acc, _i64p))
+        self._call("blind_rotate_lazy_no_first" if no_first else "blind_rotate_lazy", _ptr(lwe, _i32p),
+                   _ptr(v, _i64p), _ptr(acc, _i64p))
         return acc
 
-    def pbs_lazy(self, lwe, v, threads: int = 1) -> np.ndarray:
-        """The bootstrap with blindRotateLazyPipeAltNtt on the lazy key."""
+    def pbs_lazy(self, lwe, v, threads: int = 1, no_first: bool = False) -> np.ndarray:
+        """The bootstrap with blindRotateLazyPipeAltNtt (or NoFirstNtt) on the lazy key."""
         lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
         v = np.ascontiguousarray(v, np.int64)
         out = np.zeros_like(lwe)
-        self._call("pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), threads)
+        self._call("pbs_lazy_no_first" if no_first else "pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p),
+                   _ptr(out, _i32p), threads)
         return out
 
     @property
@@ -429,14 +432,16 @@ class Reference(_Common):
     def load_lazy_file(self, path) -> None:
         self._call("load_lazy", str(path).encode())
 
-    def pbs_lazy(self, lwe, v, with_acc: bool = False):
-        """functionalBootstrappingMPNtt's composition around blindRotateLazyPipeAltNtt; with_acc
-        also returns ciphertext 0's accumulator after the blind rotation."""
+    def pbs_lazy(self, lwe, v, with_acc: bool = False, no_first: bool = False):
+        """functionalBootstrappingMPNtt's composition around blindRotateLazyPipeAltNtt (or, with
+        no_first, blindRotateLazyPipeAltNoFirstNtt); with_acc also returns ciphertext 0's
+        accumulator after the blind rotation."""
         lwe = np.ascontiguousarray(lwe, np.int32).reshape(-1, self.p.n + 1)
         v = np.ascontiguousarray(v, np.int64)
         out = np.zeros_like(lwe)
         acc = np.zeros((self.p.k + 1) * self.p.N, np.int64)
-        self._call("pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p), _ptr(out, _i32p), _ptr(acc, _i64p))
+        self._call("pbs_lazy_no_first" if no_first else "pbs_lazy", _ptr(lwe, _i32p), len(lwe), _ptr(v, _i64p),
+                   _ptr(out, _i32p), _ptr(acc, _i64p))
         return (out, acc) if with_acc else out
 
     def pbs_lazy_sweep(self, lwe, v, move_ntt: int, units_a: int) -> np.ndarray:

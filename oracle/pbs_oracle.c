@@ -811,11 +811,13 @@ typedef struct {
     const int64_t* v;
     int32_t* out;
     int begin, end;
-    int lazy;  /* 1: blindRotateLazyPipeAltNtt on the lazy key, 2: blindRotateNtt on the group key */
+    int lazy;  /* 1: blindRotateLazyPipeAltNtt on the lazy key, 2: blindRotateNtt on the group key,
+                  3: blindRotateLazyPipeAltNoFirstNtt on the lazy key */
     int rc;
 } pbs_job;
 
-static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc);
+static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc,
+                             int no_first);
 static int blind_rotate_group(const po_ctx* c, const int32_t* scaled, const int64_t* v, int64_t* acc);
 
 /* functionalBootstrappingMPNtt (yatfhe/src/bootstrapping.cpp:71-80). */
@@ -837,7 +839,7 @@ static void* pbs_worker(void* arg) {
             if (j->lazy == 2) {
                 if (blind_rotate_group(c, scaled, j->v, acc)) { j->rc = -1; break; }
             } else if (j->lazy) {
-                if (blind_rotate_lazy(c, &s, scaled, j->v, acc)) { j->rc = -1; break; }
+                if (blind_rotate_lazy(c, &s, scaled, j->v, acc, j->lazy == 3)) { j->rc = -1; break; }
             } else {
                 blind_rotate(c, &s, scaled, j->v, acc, NULL, 0, NULL);
             }
@@ -1312,13 +1314,18 @@ int po_load_lazy_file(po_ctx* c, const char* path) {
  *   c[lvl][k1].a[k2]  = sum_l' D_l' . s2[l'].a[k2] + NTT(cP.b)
  *   c[lvl][k1].b      = sum_l' D_l' . s2[l'].b                       (all mod q).
  */
-static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc) {
+/* blindRotateLazyPipeAltNtt (yatfhe/src/blind_rotate.cpp:995-1135), or with no_first
+ * blindRotateLazyPipeAltNoFirstNtt (:1137-1267): the accumulator starts as X^-b (0, v) and
+ * every key index, the first one included, takes the ordinary chain (rotate, decompose,
+ * scheme switch, in-place external product). */
+static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scaled, const int64_t* v, int64_t* acc,
+                             int no_first) {
     const int n = c->p.n, N = c->p.N, k = c->p.k, k1 = k + 1, L = c->L, Ls = c->p.l, T = c->T;
     const int rb = c->p.radix_bits;
     const uint64_t q = c->q;
     const nq_barrett* br = &c->plan.br;
     const size_t row = (size_t)k1 * N, lvlWords = (size_t)k1 * row;
-    if (!c->lazy_cprime || !c->wwl_s2 || n < 2 || L > 64 || Ls > 64) return -1;
+    if (!c->lazy_cprime || !c->wwl_s2 || n < (no_first ? 1 : 2) || L > 64 || Ls > 64) return -1;
     uint64_t* rows = (uint64_t*)malloc(sizeof(uint64_t) * L * lvlWords);  /* [lvl][r][o][N] */
     uint64_t* recomp = (uint64_t*)malloc(sizeof(uint64_t) * Ls * N);      /* NTT(2^(T-(l'+1) radix)) */
     uint64_t* gdv = (uint64_t*)malloc(sizeof(uint64_t) * L * N);
@@ -1343,6 +1350,13 @@ static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scal
     }
     for (int l = 0; l < L; l++) ntt_from_torus(c, gdv + (size_t)l * N, dig + (size_t)l * N);
 
+    if (no_first) {
+        /* the accumulator init of blindRotateLazyPipeAltNoFirstNtt (:1205-1210): X^-b (0, v) */
+        memset(tmp, 0, sizeof(int64_t) * row);
+        for (int j = 0; j < N; j++) tmp[(size_t)k * N + j] = v[j];
+        for (int o = 0; o < k1; o++) rotate_poly(c, acc + (size_t)o * N, tmp + (size_t)o * N, -scaled[n], 0);
+        goto chain;
+    }
     /* first component */
     memset(hat, 0, sizeof(uint64_t) * row);
     for (int lvl = 0; lvl < L; lvl++) {
@@ -1358,7 +1372,8 @@ static int blind_rotate_lazy(const po_ctx* c, ep_scratch* s, const int32_t* scal
     for (int j = 0; j < N; j++) tmp[(size_t)k * N + j] = sext(tmp[(size_t)k * N + j] + v[j], T);
     for (int o = 0; o < k1; o++) rotate_poly(c, acc + (size_t)o * N, tmp + (size_t)o * N, -scaled[n], 0);
 
-    for (int i = 1; i < n; i++) {
+chain:
+    for (int i = no_first ? 0 : 1; i < n; i++) {
         const int a = scaled[i];
         if (a == 0) continue;
         for (int lvl = 0; lvl < L; lvl++) {
@@ -1408,7 +1423,7 @@ int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t
         return fail(c, "po_blind_rotate_lazy: out of memory");
     }
     po_modswitch(c, in, scaled);
-    const int rc = blind_rotate_lazy(c, &s, scaled, v, acc_out);
+    const int rc = blind_rotate_lazy(c, &s, scaled, v, acc_out, 0);
     ep_free(&s);
     free(scaled);
     return rc ? fail(c, "po_blind_rotate_lazy: no lazy key, or n < 2") : 0;
@@ -1419,6 +1434,27 @@ int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t
 int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
     if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_pbs_lazy: no lazy key");
     return pbs_run(c, in, count, v, out, threads, 1);
+}
+
+/* The same two with blindRotateLazyPipeAltNoFirstNtt (yatfhe/src/blind_rotate.cpp:1137-1267). */
+int po_blind_rotate_lazy_no_first(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out) {
+    ep_scratch s;
+    int32_t* scaled = (int32_t*)malloc(sizeof(int32_t) * (c->p.n + 1));
+    if (ep_alloc(c, &s) || !scaled) {
+        ep_free(&s);
+        free(scaled);
+        return fail(c, "po_blind_rotate_lazy_no_first: out of memory");
+    }
+    po_modswitch(c, in, scaled);
+    const int rc = blind_rotate_lazy(c, &s, scaled, v, acc_out, 1);
+    ep_free(&s);
+    free(scaled);
+    return rc ? fail(c, "po_blind_rotate_lazy_no_first: no lazy key") : 0;
+}
+
+int po_pbs_lazy_no_first(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads) {
+    if (!c->lazy_cprime || !c->wwl_s2) return fail(c, "po_pbs_lazy_no_first: no lazy key");
+    return pbs_run(c, in, count, v, out, threads, 3);
 }
 
 /* ------------------------------------------------------------------ group keys */

@@ -76,6 +76,8 @@ int po_save_lazy_file(po_ctx* c, const char* path);
 int po_load_lazy_file(po_ctx* c, const char* path);
 int po_blind_rotate_lazy(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out);
 int po_pbs_lazy(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
+int po_blind_rotate_lazy_no_first(po_ctx* c, const int32_t* in, const int64_t* v, int64_t* acc_out);
+int po_pbs_lazy_no_first(po_ctx* c, const int32_t* in, int count, const int64_t* v, int32_t* out, int threads);
 
 /* Group-g keys of blindRotateNtt (BootstrappingKey, TrgswDft rows [keys][l][k+1][k+1][N] in the
  * NTT domain; keys = n for g = 1, n / g * 2^g otherwise; g divides n). */

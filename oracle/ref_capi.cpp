@@ -678,6 +678,7 @@ int ref_load_lazy(const char* path) {
 // (may be null) receives ciphertext 0's accumulator after the blind rotation.
 namespace {
 int sweep_move = -1, sweep_units = 2;  // ref_pbs_lazy_sweep's split; -1: blindRotateLazyPipeAltNtt
+bool lazy_no_first = false;            // ref_pbs_lazy_no_first: blindRotateLazyPipeAltNoFirstNtt
 }
 
 int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
@@ -697,7 +698,9 @@ int ref_pbs_lazy(const int32_t* in, int count, const int64_t* v, int32_t* out, i
             Trlwe acc{k, N};
             Tlwe big{s.ksk->nCurrKey};
             rescaleTlweToNewMod(sc, x);
-            if (sweep_move < 0)
+            if (lazy_no_first)
+                blindRotateLazyPipeAltNoFirstNtt(acc, *s.lazy, sc, vp, p);
+            else if (sweep_move < 0)
                 blindRotateLazyPipeAltNtt(acc, *s.lazy, sc, vp, gdV, p);
             else
                 blindRotateLazyPipeAltNttSweep(acc, *s.lazy, sc, vp, gdV, sweep_move, sweep_units, p);
@@ -797,6 +800,15 @@ int ref_pbs_lazy_sweep(const int32_t* in, int count, const int64_t* v, int32_t* 
     sweep_units = units_a;
     const int rc = ref_pbs_lazy(in, count, v, out, nullptr);
     sweep_move = -1;
+    return rc;
+}
+
+// ref_pbs_lazy with blindRotateLazyPipeAltNoFirstNtt (yatfhe/src/blind_rotate.cpp:1137-1267)
+// in place of blindRotateLazyPipeAltNtt.
+int ref_pbs_lazy_no_first(const int32_t* in, int count, const int64_t* v, int32_t* out, int64_t* acc0) {
+    lazy_no_first = true;
+    const int rc = ref_pbs_lazy(in, count, v, out, acc0);
+    lazy_no_first = false;
     return rc;
 }
 

@@ -130,3 +130,34 @@ def test_lazy_sweep_split_gives_the_same_outputs():
     want = ref.pbs_lazy(lwe, v)
     for move, units in [(0, 1), (1, 2), (2, 2), (4, 3), (8, 4)]:
         np.testing.assert_array_equal(ref.pbs_lazy_sweep(lwe, v, move, units), want, err_msg=f"{move}, {units}")
+
+
+@needs_reference
+@pytest.mark.parametrize("base", [WWL24_T32_N2048, WWL24_T56_N2048])
+def test_lazy_no_first_matches_reference(base):
+    """blindRotateLazyPipeAltNoFirstNtt (yatfhe/src/blind_rotate.cpp:1137-1267): the accumulator
+    X^-b (0, v) and the ordinary chain for every key index, the first one included.  The
+    restatement's accumulators and outputs equal the reference's, with skipped steps (a_0 = 0,
+    a run of zeros) among the inputs.  They also equal blindRotateLazyPipeAltNtt's bit for
+    bit: the first-component shortcut X^-b ((X^a_0 - 1) derived + (0, v)) is the in-place
+    external product of X^-b (0, v) with the first key index's TRGSW, the same exact
+    polynomial mod q before the one rounding, so the GPU lazy rotation serves both."""
+    p = small(base, 6)
+    ref, ora = o.Reference(p), Restatement(p)
+    ref.keygen_lazy(23)
+    ora.keygen_lazy(23)
+    rng = np.random.default_rng(7)
+    mu = np.where(rng.integers(0, 2, 4) == 1, 1 << 29, -(1 << 29)).astype(np.int64)
+    lwe = ref.encrypt(mu)
+    lwe[1, 0] = 0                # a_0 = 0: the first step is skipped
+    lwe[2, 1:4] = 0              # a run of skipped steps
+    v = lutmod.sign_lut(p.N, p.torus_bits)
+    out, acc0 = ref.pbs_lazy(lwe, v, with_acc=True, no_first=True)
+    np.testing.assert_array_equal(ora.blind_rotate_lazy(lwe[0], v, no_first=True), acc0)
+    np.testing.assert_array_equal(ora.pbs_lazy(lwe, v, threads=3, no_first=True), out)
+    np.testing.assert_array_equal(ref.decrypt(out[[0, 3]], 8), np.where(mu[[0, 3]] > 0, 1, -1))
+    for c in range(len(lwe)):
+        out1, acc1 = ref.pbs_lazy(lwe[c:c + 1], v, with_acc=True)
+        out2, acc2 = ref.pbs_lazy(lwe[c:c + 1], v, with_acc=True, no_first=True)
+        np.testing.assert_array_equal(acc1, acc2, err_msg=f"accumulator of ciphertext {c}")
+        np.testing.assert_array_equal(out1, out2)

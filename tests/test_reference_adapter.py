@@ -31,6 +31,7 @@ void use(Tlwe& out, const Tlwe& in, const BootstrappingKeyMP& bsk, const TlweKey
     yatfhe_gb300::blindRotateLazyPipeAltNtt(acc, lazy, s, v, gdV, p);
     yatfhe_gb300::blindRotateLazyPipeAltNttSweep(acc, lazy, s, v, gdV, 2, 2, p);
     yatfhe_gb300::blindRotateLazyPipeAltInitNtt(acc, lazy2, s, v, "BSK_OURS.bin", gdV, p);
+    yatfhe_gb300::blindRotateLazyPipeAltNoFirstNtt(acc, lazy, s, v, p);
     yatfhe_gb300::blindRotateNtt(acc, gbsk.bskDft, s, p);
     yatfhe_gb300::functionalBootstrappingNtt(out, in, gbsk, ksk, v, p);
     yatfhe_gb300::switchKeyForTlwe(out, ksk, in, p);
