@@ -107,6 +107,40 @@ int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h
                            const uint64_t* h_bsk_mask, const int32_t* h_ksk_mask, const int32_t* h_ksk_noise,
                            uint64_t* h_bsk_words, int32_t* h_ksk, yg_key** out);
 
+/* Key generation with the randomness drawn on the GPU: the secrets (genTlweKey /
+ * genTrlweKey, yatfhe/src/tlwe.cpp:10-18, yatfhe/src/trlwe.cpp:70-81: uniform bits), the BSK
+ * samples' TUniform(rlwe_noise_b) noise and uniform masks mod q (encryptTrgswMPNtt,
+ * yatfhe/src/trgsw.cpp:36-51; genTUniformNoise, yatfhe/src/numeric.cpp:47-55) and the KSK
+ * samples' uniform 32-bit masks and TUniform(lwe_noise_b) noise (genTlweKeySwitchingKey,
+ * yatfhe/src/keyswitching.cpp:19-29), then the arithmetic of yg_keygen_from_samples on them.
+ * The generator is ChaCha20 (RFC 8439) in counter mode keyed by `seed` (one key per array),
+ * so the same seed gives the same key on any GPU; the values have the reference's
+ * distributions, not its words (its RNG is one sequential stream).  h_lwe_s [n] and
+ * h_rlwe_s [k N] receive the secrets when not null.  0 <= lwe_noise_b, rlwe_noise_b <= 30
+ * (the noise is kept as int32).  Synchronizes. */
+int yg_keygen(yg_ctx* ctx, uint64_t seed, int lwe_noise_b, int rlwe_noise_b, int32_t* h_lwe_s, int32_t* h_rlwe_s,
+              yg_key** out);
+
+/* The samples yg_keygen draws for `seed`, in the layouts of yg_keygen_from_samples: fed back
+ * to it they give yg_keygen's key bit for bit.  Synchronizes. */
+int yg_draw_keygen_samples(yg_ctx* ctx, uint64_t seed, int lwe_noise_b, int rlwe_noise_b, int32_t* h_lwe_s,
+                           int32_t* h_rlwe_s, int32_t* h_bsk_noise, uint64_t* h_bsk_mask, int32_t* h_ksk_mask,
+                           int32_t* h_ksk_noise);
+
+/* symEncTlwe (yatfhe/src/tlwe.cpp:21-31) of `count` messages on the GPU, one warp per
+ * ciphertext: d_out[i] = (a, sum_j a_j s_j + mu_i + e_i mod 2^32) with d_s [n] the binary LWE
+ * secret, d_mu [count] the torus messages (taken mod 2^32), uniform 32-bit masks a and
+ * TUniform(lwe_noise_b) noise e drawn by ChaCha20 from (seed, call): one (seed, call) pair
+ * gives one set of ciphertexts, so a caller encrypting in several calls gives each its own
+ * `call`.  d_out is [count][n + 1] int32.  Device pointers; asynchronous on `stream`. */
+int yg_encrypt_lwe(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, int count, uint64_t seed, uint32_t call,
+                   int lwe_noise_b, int32_t* d_out, void* stream);
+
+/* As yg_encrypt_lwe with the samples given: d_mask [count][n] and d_noise [count] (the
+ * reference's draws give the reference's ciphertexts bit for bit). */
+int yg_encrypt_lwe_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const int32_t* d_mask,
+                                const int32_t* d_noise, int count, int32_t* d_out, void* stream);
+
 /* Replaces deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): reads a file written
  * by serializeBskWWL24 (:220-229) and uploads it as above. */
 int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);

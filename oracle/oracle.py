@@ -276,6 +276,16 @@ class Restatement(_Common):
     def load_bsk_file(self, path) -> None:
         self._call("load_bsk_file", str(path).encode())
 
+    def encrypt_samples(self, mu):
+        """encrypt(mu) that also returns each ciphertext's mask [count][n] and noise [count]."""
+        mu = np.ascontiguousarray(mu, np.int64)
+        out = self._alloc_lwe(len(mu))
+        mask = np.zeros((len(mu), self.p.n), np.int32)
+        noise = np.zeros(len(mu), np.int32)
+        self._call("encrypt_samples", _ptr(mu, _i64p), len(mu), _ptr(out, _i32p), _ptr(mask, _i32p),
+                   _ptr(noise, _i32p))
+        return out, mask, noise
+
     def keygen_samples(self, seed: int) -> dict:
         """keygen(seed) that also returns its random samples: the secrets, the BSK samples'
         noise [n][l][k+1][N] and masks [n][l][k+1][k][N], the KSK samples' masks [kN][t][n]

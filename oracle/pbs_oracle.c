@@ -431,6 +431,19 @@ int po_encrypt(po_ctx* c, const int64_t* mu, int count, int32_t* out) {
     return 0;
 }
 
+/* po_encrypt with each ciphertext's random samples written out: mask [count][n] (the
+ * uniform a_i) and noise [count] (the TUniform(lwe_noise_b) error of b). */
+int po_encrypt_samples(po_ctx* c, const int64_t* mu, int count, int32_t* out, int32_t* mask, int32_t* noise) {
+    if (!c->have_rng) return fail(c, "po_encrypt_samples: no RNG stream (run po_keygen first)");
+    const int n = c->p.n;
+    for (int i = 0; i < count; i++) {
+        int32_t* row = out + (size_t)i * (n + 1);
+        enc_tlwe(c, row, mu[i], c->lwe_s, n, noise + i);
+        memcpy(mask + (size_t)i * n, row, sizeof(int32_t) * n);
+    }
+    return 0;
+}
+
 /* symDecTlweToInt (yatfhe/src/tlwe.cpp:44-53) with roundTorusGeneralError (numeric.cpp:95-98)
  * and modSwitchToTorusGeneral (numeric.cpp:182-187), all mod LWE_Q = 2^32. */
 static int64_t int_mod_p(int64_t a, int64_t p) {

@@ -82,6 +82,12 @@ _SIGNATURES = {
     "yg_key_load_lazy_file": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "yg_key_upload_group": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
     "yg_keygen_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "yg_keygen": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.POINTER(_vp)]),
+    "yg_draw_keygen_samples": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
+                                              _vp, _vp]),
+    "yg_encrypt_lwe": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int,
+                                      _vp, _vp]),
+    "yg_encrypt_lwe_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
     "yg_key_set_ksk": (ctypes.c_int, [_vp, _vp]),
     "yg_key_destroy": (None, [_vp]),
     "yg_key_device_bytes": (ctypes.c_size_t, [_vp]),

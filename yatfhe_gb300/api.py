@@ -319,6 +319,62 @@ def keygen_from_samples(ctx: Context, samples: dict, return_keys: bool = False):
     return (key, words, ksk) if return_keys else key
 
 
+def keygen(ctx: Context, seed: int, lwe_noise_b: int, rlwe_noise_b: int, return_secrets: bool = False):
+    """Key generation with every random value drawn on the GPU (yg_keygen): ChaCha20 counter
+    mode keyed by `seed`, the reference's distributions (binary secrets, TUniform noise,
+    uniform masks).  Returns the device key (with BSK and KSK), and with return_secrets also
+    the secrets (lwe_s [n], rlwe_s [kN] int32)."""
+    p = ctx.params
+    lwe_s = np.zeros(p.n, np.int32)
+    rlwe_s = np.zeros(p.k * p.N, np.int32)
+    h = ctypes.c_void_p()
+    _lib.check(_lib.lib().yg_keygen(ctx.handle, seed, lwe_noise_b, rlwe_noise_b, ctypes.c_void_p(lwe_s.ctypes.data),
+                                    ctypes.c_void_p(rlwe_s.ctypes.data), ctypes.byref(h)))
+    key = BootstrapKey(ctx, h)
+    return (key, lwe_s, rlwe_s) if return_secrets else key
+
+
+def draw_keygen_samples(ctx: Context, seed: int, lwe_noise_b: int, rlwe_noise_b: int) -> dict:
+    """The random samples keygen(seed) draws, in the layouts keygen_from_samples takes."""
+    p = ctx.params
+    k1, kN = p.k + 1, p.k * p.N
+    d = {"lwe_s": np.zeros(p.n, np.int32), "rlwe_s": np.zeros(kN, np.int32),
+         "bsk_noise": np.zeros((p.n, p.l_approx, k1, p.N), np.int32),
+         "bsk_mask": np.zeros((p.n, p.l_approx, k1, p.k, p.N), np.uint64),
+         "ksk_mask": np.zeros((kN, p.ks_level, p.n), np.int32),
+         "ksk_noise": np.zeros((kN, p.ks_level), np.int32)}
+    ptrs = [ctypes.c_void_p(d[f].ctypes.data) for f in ("lwe_s", "rlwe_s", "bsk_noise", "bsk_mask", "ksk_mask",
+                                                         "ksk_noise")]
+    _lib.check(_lib.lib().yg_draw_keygen_samples(ctx.handle, seed, lwe_noise_b, rlwe_noise_b, *ptrs))
+    return d
+
+
+def sym_enc_tlwe(ctx: Context, lwe_s, mu, seed: int, call: int, lwe_noise_b: int, out=None, stream=None):
+    """symEncTlwe (yatfhe/src/tlwe.cpp:21-31) of the messages `mu` (int64 [count], torus mod
+    2^32) under the binary secret `lwe_s` (int32 [n]), all on the GPU with masks and noise
+    drawn from (seed, call): ciphertexts [count, n + 1] int32."""
+    torch = _torch()
+    n1 = ctx.params.n + 1
+    if out is None:
+        out = torch.empty((mu.shape[0], n1), dtype=torch.int32, device=mu.device)
+    _lib.check(_lib.lib().yg_encrypt_lwe(ctx.handle, _dptr(lwe_s, "int32", "lwe_s"), _dptr(mu, "int64", "mu"),
+                                         mu.shape[0], seed, call, lwe_noise_b, _dptr(out, "int32", "out"),
+                                         _stream_handle(stream)))
+    return out
+
+
+def sym_enc_tlwe_from_samples(ctx: Context, lwe_s, mu, mask, noise, out=None, stream=None):
+    """sym_enc_tlwe with the masks (int32 [count, n]) and noise (int32 [count]) given."""
+    torch = _torch()
+    n1 = ctx.params.n + 1
+    if out is None:
+        out = torch.empty((mu.shape[0], n1), dtype=torch.int32, device=mu.device)
+    _lib.check(_lib.lib().yg_encrypt_lwe_from_samples(
+        ctx.handle, _dptr(lwe_s, "int32", "lwe_s"), _dptr(mu, "int64", "mu"), _dptr(mask, "int32", "mask"),
+        _dptr(noise, "int32", "noise"), mu.shape[0], _dptr(out, "int32", "out"), _stream_handle(stream)))
+    return out
+
+
 def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
     """blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412): the blind rotation on a
     WWL+24 key, whose GINX rows were derived on the GPU at upload."""

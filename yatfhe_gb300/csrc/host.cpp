@@ -479,14 +479,64 @@ void upload_group(yg_ctx* c, yg_key* key, const u64* words, int group, int key_l
 // Key generation arithmetic on the GPU from caller-drawn samples (see yg_keygen_from_samples):
 // the NTT of the RLWE secret mod q (host, exact), the BSK samples (keygen_bsk_kernel), the
 // usual conversion of the NTT-domain words, and the KSK samples (keygen_ksk_kernel).
-void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int32_t* rlwe_s, const int32_t* bsk_noise,
-                         const u64* bsk_mask, const int32_t* ksk_mask, const int32_t* ksk_noise, u64* h_words,
-                         int32_t* h_ksk) {
+// Device buffers of one key generation's samples (the layouts of yg_keygen_from_samples).
+struct KeygenSamples {
+    int32_t *lwe_s, *rlwe_s, *noise, *kmask, *knoise;
+    u64* mask;
+    size_t samples, ksk_samples;
+};
+
+KeygenSamples alloc_samples(const yg_ctx* c, DeviceScratch& scratch) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->p.l_approx, kN = k * N;
+    KeygenSamples d{};
+    d.samples = (size_t)n * L * (k + 1);
+    d.ksk_samples = (size_t)kN * c->p.ks_level;
+    d.lwe_s = scratch.alloc<int32_t>(n, "cudaMalloc keygen");
+    d.rlwe_s = scratch.alloc<int32_t>(kN, "cudaMalloc keygen");
+    d.noise = scratch.alloc<int32_t>(d.samples * N, "cudaMalloc keygen noise");
+    d.mask = scratch.alloc<u64>(d.samples * k * N, "cudaMalloc keygen masks");
+    d.kmask = scratch.alloc<int32_t>(d.ksk_samples * n, "cudaMalloc keygen KSK masks");
+    d.knoise = scratch.alloc<int32_t>(d.ksk_samples, "cudaMalloc keygen KSK noise");
+    return d;
+}
+
+// Domains of the GPU draws (sampling.cu): one ChaCha20 key per array of a draw.
+enum : uint32_t { kDomLweS = 1, kDomRlweS, kDomBskNoise, kDomBskMask, kDomKskMask, kDomKskNoise, kDomEncrypt = 16 };
+
+void draw(int32_t* out_i32, u64* out_u64, size_t count, uint64_t seed, uint32_t domain, int kind, int b, u64 q) {
+    yg::DrawArgs a{};
+    a.out_i32 = out_i32;
+    a.out_u64 = out_u64;
+    a.count = count;
+    a.seed = seed;
+    a.q = q;
+    a.domain = domain;
+    a.kind = kind;
+    a.b = b;
+    a.per_block = kind == yg::kDrawTUniform ? 8 : (kind == yg::kDrawModQ ? 4 : 16);
+    yg::check_launch(yg::launch_draw(a, nullptr), "draw launch");
+}
+
+// Every sample of a key generation drawn on the GPU from `seed`, with the distributions of
+// genTlweKey, genTrlweKey, encryptTrgswMPNtt (TUniform(rlwe_noise_b) noise, uniform masks mod
+// q) and genTlweKeySwitchingKey (uniform 32-bit masks, TUniform(lwe_noise_b) noise).
+void draw_keygen_samples(const yg_ctx* c, uint64_t seed, int lwe_noise_b, int rlwe_noise_b, const KeygenSamples& d) {
+    if (lwe_noise_b < 0 || lwe_noise_b > 30 || rlwe_noise_b < 0 || rlwe_noise_b > 30)
+        throw std::invalid_argument("noise widths: 0 <= lwe_noise_b, rlwe_noise_b <= 30");
+    const int n = c->p.n, N = c->p.N, k = c->p.k;
+    draw(d.lwe_s, nullptr, (size_t)n, seed, kDomLweS, yg::kDrawBit, 0, 0);
+    draw(d.rlwe_s, nullptr, (size_t)k * N, seed, kDomRlweS, yg::kDrawBit, 0, 0);
+    draw(d.noise, nullptr, d.samples * N, seed, kDomBskNoise, yg::kDrawTUniform, rlwe_noise_b, 0);
+    draw(nullptr, d.mask, d.samples * k * N, seed, kDomBskMask, yg::kDrawModQ, 0, c->q);
+    draw(d.kmask, nullptr, d.ksk_samples * n, seed, kDomKskMask, yg::kDrawU32, 0, 0);
+    draw(d.knoise, nullptr, d.ksk_samples, seed, kDomKskNoise, yg::kDrawTUniform, lwe_noise_b, 0);
+}
+
+// The key from samples already on the device (the secret's transform is computed on the
+// host from rlwe_s).
+void keygen_on_device(yg_ctx* c, yg_key* key, const int32_t* rlwe_s, const KeygenSamples& d, u64* h_words,
+                      int32_t* h_ksk, DeviceScratch& scratch) {
     const int n = c->p.n, N = c->p.N, k = c->p.k, L = c->p.l_approx, t = c->p.ks_level, kN = k * N;
-    for (int i = 0; i < n; i++)
-        if (lwe_s[i] != 0 && lwe_s[i] != 1) throw std::invalid_argument("LWE secret must be binary");
-    for (int i = 0; i < kN; i++)
-        if (rlwe_s[i] != 0 && rlwe_s[i] != 1) throw std::invalid_argument("RLWE secret must be binary");
     const QTables& qt = *c->qtab;
     const u64 q = c->q;
     // NTT(s) mod q, the forward transform the kernels use (Cooley-Tukey, psi^brv twiddles)
@@ -503,32 +553,18 @@ void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int
                 }
         for (int j = 0; j < N; j++) s_ntt_p[(size_t)r * N + j] = (u64)(((u128)a[j] << 64) / q);
     }
-    const size_t samples = (size_t)n * L * (k + 1), words = samples * (k + 1) * N;
-    const size_t ksk_samples = (size_t)kN * t;
-    DeviceScratch scratch;
+    const size_t words = d.samples * (k + 1) * N;
     DeviceQTables tw(scratch, qt);
-    int32_t* d_lwe_s = scratch.alloc<int32_t>(n, "cudaMalloc keygen");
-    int32_t* d_rlwe_s = scratch.alloc<int32_t>(kN, "cudaMalloc keygen");
-    int32_t* d_noise = scratch.alloc<int32_t>(samples * N, "cudaMalloc keygen noise");
-    u64* d_mask = scratch.alloc<u64>(samples * k * N, "cudaMalloc keygen masks");
     u64* d_s = scratch.alloc<u64>(2 * (size_t)kN, "cudaMalloc keygen secret");
     u64* d_words = scratch.alloc<u64>(words, "cudaMalloc keygen words");
-    int32_t* d_kmask = scratch.alloc<int32_t>(ksk_samples * n, "cudaMalloc keygen KSK masks");
-    int32_t* d_knoise = scratch.alloc<int32_t>(ksk_samples, "cudaMalloc keygen KSK noise");
     int* d_bad = scratch.alloc<int>(1, "cudaMalloc flag");
-    ck(cudaMemcpy(d_lwe_s, lwe_s, n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
-    ck(cudaMemcpy(d_rlwe_s, rlwe_s, kN * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
-    ck(cudaMemcpy(d_noise, bsk_noise, samples * N * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen noise");
-    ck(cudaMemcpy(d_mask, bsk_mask, samples * k * N * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen masks");
     ck(cudaMemcpy(d_s, s_ntt.data(), kN * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen secret");
     ck(cudaMemcpy(d_s + kN, s_ntt_p.data(), kN * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen secret");
-    ck(cudaMemcpy(d_kmask, ksk_mask, ksk_samples * n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK masks");
-    ck(cudaMemcpy(d_knoise, ksk_noise, ksk_samples * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK noise");
     ck(cudaMemset(d_bad, 0, sizeof(int)), "clear flag");
     yg::KeygenBskArgs a{};
-    a.lwe_s = d_lwe_s;
-    a.noise = d_noise;
-    a.mask = d_mask;
+    a.lwe_s = d.lwe_s;
+    a.noise = d.noise;
+    a.mask = d.mask;
     a.s_ntt = d_s;
     a.s_ntt_p = d_s + kN;
     a.wf = tw.wf;
@@ -548,12 +584,31 @@ void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int
     if (bad) throw std::invalid_argument("BSK mask word not reduced mod q");
     if (h_words) ck(cudaMemcpy(h_words, d_words, words * sizeof(u64), cudaMemcpyDeviceToHost), "download BSK words");
     convert_bsk_words(c, key, d_words, scratch, tw);
-    key->ksk_bytes = ksk_samples * (n + 1) * sizeof(int32_t);
+    key->ksk_bytes = d.ksk_samples * (n + 1) * sizeof(int32_t);
     ck(cudaMalloc(&key->d_ksk, key->ksk_bytes), "cudaMalloc ksk");
-    yg::KeygenKskArgs kk{d_lwe_s, d_rlwe_s, d_kmask, d_knoise, key->d_ksk, n, kN, t, c->p.ks_radix_bits};
+    yg::KeygenKskArgs kk{d.lwe_s, d.rlwe_s, d.kmask, d.knoise, key->d_ksk, n, kN, t, c->p.ks_radix_bits};
     yg::check_launch(yg::launch_keygen_ksk(kk, nullptr), "keygen KSK launch");
     if (h_ksk) ck(cudaMemcpy(h_ksk, key->d_ksk, key->ksk_bytes, cudaMemcpyDeviceToHost), "download KSK");
     ck(cudaDeviceSynchronize(), "keygen");
+}
+
+void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int32_t* rlwe_s, const int32_t* bsk_noise,
+                         const u64* bsk_mask, const int32_t* ksk_mask, const int32_t* ksk_noise, u64* h_words,
+                         int32_t* h_ksk) {
+    const int n = c->p.n, N = c->p.N, k = c->p.k, kN = k * N;
+    for (int i = 0; i < n; i++)
+        if (lwe_s[i] != 0 && lwe_s[i] != 1) throw std::invalid_argument("LWE secret must be binary");
+    for (int i = 0; i < kN; i++)
+        if (rlwe_s[i] != 0 && rlwe_s[i] != 1) throw std::invalid_argument("RLWE secret must be binary");
+    DeviceScratch scratch;
+    const KeygenSamples d = alloc_samples(c, scratch);
+    ck(cudaMemcpy(d.lwe_s, lwe_s, n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
+    ck(cudaMemcpy(d.rlwe_s, rlwe_s, kN * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen");
+    ck(cudaMemcpy(d.noise, bsk_noise, d.samples * N * sizeof(int32_t), cudaMemcpyHostToDevice), "upload keygen noise");
+    ck(cudaMemcpy(d.mask, bsk_mask, d.samples * k * N * sizeof(u64), cudaMemcpyHostToDevice), "upload keygen masks");
+    ck(cudaMemcpy(d.kmask, ksk_mask, d.ksk_samples * n * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK masks");
+    ck(cudaMemcpy(d.knoise, ksk_noise, d.ksk_samples * sizeof(int32_t), cudaMemcpyHostToDevice), "upload KSK noise");
+    keygen_on_device(c, key, rlwe_s, d, h_words, h_ksk, scratch);
 }
 
 // deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)
@@ -1032,6 +1087,84 @@ int yg_keygen_from_samples(yg_ctx* ctx, const int32_t* h_lwe_s, const int32_t* h
             throw;
         }
         *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_draw_keygen_samples(yg_ctx* ctx, uint64_t seed, int lwe_noise_b, int rlwe_noise_b, int32_t* h_lwe_s,
+                           int32_t* h_rlwe_s, int32_t* h_bsk_noise, uint64_t* h_bsk_mask, int32_t* h_ksk_mask,
+                           int32_t* h_ksk_noise) {
+    if (!ctx || !h_lwe_s || !h_rlwe_s || !h_bsk_noise || !h_bsk_mask || !h_ksk_mask || !h_ksk_noise)
+        return set_err(YG_ERR_INVALID, "null argument");
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        DeviceScratch scratch;
+        const KeygenSamples d = alloc_samples(ctx, scratch);
+        draw_keygen_samples(ctx, seed, lwe_noise_b, rlwe_noise_b, d);
+        const int n = ctx->p.n, N = ctx->p.N, k = ctx->p.k;
+        ck(cudaMemcpy(h_lwe_s, d.lwe_s, n * sizeof(int32_t), cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(h_rlwe_s, d.rlwe_s, (size_t)k * N * sizeof(int32_t), cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(h_bsk_noise, d.noise, d.samples * N * sizeof(int32_t), cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(h_bsk_mask, d.mask, d.samples * k * N * sizeof(u64), cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(h_ksk_mask, d.kmask, d.ksk_samples * n * sizeof(int32_t), cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(h_ksk_noise, d.knoise, d.ksk_samples * sizeof(int32_t), cudaMemcpyDeviceToHost), "download");
+        return YG_OK;
+    });
+}
+
+int yg_keygen(yg_ctx* ctx, uint64_t seed, int lwe_noise_b, int rlwe_noise_b, int32_t* h_lwe_s, int32_t* h_rlwe_s,
+              yg_key** out) {
+    if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        auto k = std::make_unique<yg_key>();
+        k->ctx = ctx;
+        try {
+            DeviceScratch scratch;
+            const KeygenSamples d = alloc_samples(ctx, scratch);
+            draw_keygen_samples(ctx, seed, lwe_noise_b, rlwe_noise_b, d);
+            const int n = ctx->p.n, kN = ctx->p.k * ctx->p.N;
+            std::vector<int32_t> lwe_s(n), rlwe_s(kN);
+            ck(cudaMemcpy(lwe_s.data(), d.lwe_s, n * sizeof(int32_t), cudaMemcpyDeviceToHost), "download secret");
+            ck(cudaMemcpy(rlwe_s.data(), d.rlwe_s, kN * sizeof(int32_t), cudaMemcpyDeviceToHost), "download secret");
+            keygen_on_device(ctx, k.get(), rlwe_s.data(), d, nullptr, nullptr, scratch);
+            if (h_lwe_s) std::copy(lwe_s.begin(), lwe_s.end(), h_lwe_s);
+            if (h_rlwe_s) std::copy(rlwe_s.begin(), rlwe_s.end(), h_rlwe_s);
+        } catch (...) {
+            if (k->d_bsk) cudaFree(k->d_bsk);
+            if (k->d_ksk) cudaFree(k->d_ksk);
+            k->d_bsk = nullptr;
+            k->d_ksk = nullptr;
+            throw;
+        }
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_encrypt_lwe(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, int count, uint64_t seed, uint32_t call,
+                   int lwe_noise_b, int32_t* d_out, void* stream) {
+    if (!ctx || count < 0 || (count > 0 && (!d_s || !d_mu || !d_out)) || lwe_noise_b < 0 || lwe_noise_b > 30)
+        return set_err(YG_ERR_INVALID, "yg_encrypt_lwe: bad arguments");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::EncryptArgs a{d_s, d_mu, nullptr, nullptr, d_out, seed, kDomEncrypt, call, count, ctx->p.n, lwe_noise_b};
+        yg::check_launch(yg::launch_encrypt_lwe(a, stream), "encrypt launch");
+        return YG_OK;
+    });
+}
+
+int yg_encrypt_lwe_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const int32_t* d_mask,
+                                const int32_t* d_noise, int count, int32_t* d_out, void* stream) {
+    if (!ctx || count < 0 || (count > 0 && (!d_s || !d_mu || !d_mask || !d_noise || !d_out)))
+        return set_err(YG_ERR_INVALID, "yg_encrypt_lwe_from_samples: bad arguments");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::EncryptArgs a{d_s, d_mu, d_mask, d_noise, d_out, 0, 0, 0, count, ctx->p.n, 0};
+        yg::check_launch(yg::launch_encrypt_lwe(a, stream), "encrypt launch");
         return YG_OK;
     });
 }

@@ -115,6 +115,36 @@ struct KeygenBskArgs {
     int n, N, k, L, radix_bits, torus_bits;
     int* bad;                 // set to 1 when a mask word is not reduced mod q
 };
+// Randomness drawn on the GPU (sampling.cu): `count` values of one kind from the ChaCha20
+// stream of (seed, domain, stream).
+constexpr int kDrawBit = 0;       // 0/1, one per word
+constexpr int kDrawU32 = 1;       // uniform 32-bit words
+constexpr int kDrawTUniform = 2;  // TUniform(b), 64 bits each
+constexpr int kDrawModQ = 3;      // uniform mod q, 128 bits each
+struct DrawArgs {
+    int32_t* out_i32;   // kDrawBit, kDrawU32, kDrawTUniform
+    uint64_t* out_u64;  // kDrawModQ
+    uint64_t count;
+    uint64_t seed;
+    uint64_t q;
+    uint32_t domain, stream;
+    int kind, b;
+    int per_block;      // values per 64-byte block: 16, 16, 8, 4
+};
+// symEncTlwe on `count` ciphertexts: masks and noise drawn (seed, domain, call) or given.
+struct EncryptArgs {
+    const int32_t* s;      // [n] binary LWE secret
+    const int64_t* mu;     // [count] messages (torus, mod 2^32)
+    const int32_t* mask;   // [count][n] or null (drawn)
+    const int32_t* noise;  // [count] or null (drawn, TUniform(noise_b))
+    int32_t* out;          // [count][n + 1]
+    uint64_t seed;
+    uint32_t domain, call;
+    int count, n, noise_b;
+};
+int launch_draw(const DrawArgs& a, void* stream);
+int launch_encrypt_lwe(const EncryptArgs& a, void* stream);
+
 struct KeygenKskArgs {
     const int32_t* lwe_s;     // [n] 0/1
     const int32_t* rlwe_s;    // [kN] 0/1
