@@ -16,7 +16,7 @@ carries the plain per-call form, a batch-size sweep and the other workloads unde
 in one CUDA graph, and the 128-tenant serving trace (p50/p99 at 50-100 % of peak).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--params t32_n1024|t56_n2048]
-                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving]
+                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving|serving_lazy|encrypt]
 Multi-GPU: one process per GPU (torchrun); every rank bootstraps its own batch (weak
 scaling, no data-path collective).
 """
@@ -53,7 +53,8 @@ def parse_args():
     ap.add_argument("--params", default="t32_n1024")
     ap.add_argument("--count", type=int, default=0, help="ciphertexts per step (default 65536 / 16384)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving", "serving_lazy"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving", "serving_lazy",
+                                                                  "encrypt"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-call / sweep legs and other workloads")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
@@ -598,6 +599,88 @@ def leg_keygen(dev, reps=3):
             "sample_host_bytes": int(sum(v.nbytes for v in smp.values()))}
 
 
+def leg_encrypt(dev, count=1 << 20, steps=5, warmup=3, cpu_sample=20000):
+    """symEncTlwe on the GPU for the TORUS=32 set (n=630): `count` messages per step encrypted
+    by yg_encrypt_lwe (masks and TUniform(2^18) noise drawn by ChaCha20 in the kernel) and by
+    yg_encrypt_lwe_from_samples (masks and noise read from HBM), timed with CUDA events on the
+    launching stream (outputs of 2.6 GB, larger than L2); ciphertexts/s and the HBM view of
+    the algorithmic bytes (drawn: 8 B message + 4 (n + 1) B ciphertext; from samples: + 4 n B
+    mask + 4 B noise), and the CPU restatement (one thread, its sequential RNG) on a sample.
+    Also yg_keygen's wall time (secrets, BSK and KSK from one seed, everything on the GPU)."""
+    import torch
+
+    from yatfhe_gb300 import api
+    from yatfhe_gb300.params import T32_N1024 as p
+
+    ctx = api.Context(p, dev)
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        key = api.keygen(ctx, 0x5EED0011, p.lwe_noise_b, p.rlwe_noise_b)
+        times.append(time.perf_counter() - t0)
+        key.close()
+    rng = np.random.default_rng(0x5EED0012)
+    n = p.n
+    cuda = f"cuda:{dev}"
+    d_s = torch.from_numpy(rng.integers(0, 2, n).astype(np.int32)).to(cuda)
+    d_mu = torch.from_numpy((rng.integers(0, 4, count) << 29).astype(np.int64)).to(cuda)
+    d_mask = torch.from_numpy(rng.integers(-(1 << 31), 1 << 31, (count, n), dtype=np.int32)).to(cuda)
+    d_noise = torch.from_numpy(rng.integers(-(1 << 18), (1 << 18) + 1, count).astype(np.int32)).to(cuda)
+    d_out = torch.empty((count, n + 1), dtype=torch.int32, device=cuda)
+    stream = torch.cuda.Stream(device=dev)
+    hbm = measured_peaks().get("hbm_gbs", FALLBACK_HBM_GBS)
+
+    def timed(fn, alg_bytes):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fn()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            stream.synchronize()
+            ev[0].record(stream)
+            for i in range(steps):
+                fn(i)
+            ev[1].record(stream)
+            stream.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / steps
+        gbs = alg_bytes / (ms / 1e3) / 1e9
+        return {"ciphertexts_per_s": count / (ms / 1e3), "launch_ms": ms, "algorithmic_bytes": alg_bytes,
+                "achieved_gbs": gbs, "hbm_frac": gbs / hbm}
+
+    drawn = timed(lambda i=0: api.sym_enc_tlwe(ctx, d_s, d_mu, 7, i, p.lwe_noise_b, out=d_out, stream=stream),
+                  count * (8 + 4 * (n + 1)))
+    given = timed(lambda i=0: api.sym_enc_tlwe_from_samples(ctx, d_s, d_mu, d_mask, d_noise, out=d_out,
+                                                            stream=stream),
+                  count * (8 + 4 * (n + 1) + 4 * n + 4))
+    del d_mask, d_noise
+    rcount = 16384
+    d_rs = torch.from_numpy(rng.integers(0, 2, p.k * p.N).astype(np.int32)).to(cuda)
+    d_rmu = torch.from_numpy(rng.integers(-(1 << 31), 1 << 31, (rcount, p.N), dtype=np.int64)).to(cuda)
+    d_rout = torch.empty((rcount, p.k + 1, p.N), dtype=torch.int64, device=cuda)
+    rlwe = timed(lambda i=0: api.sym_enc_trlwe_ntt(ctx, d_rs, d_rmu, 9, i, p.rlwe_noise_b, out=d_rout, stream=stream),
+                 rcount * p.N * (8 + 8 * (p.k + 1)))
+    rlwe["samples_per_s"] = rlwe.pop("ciphertexts_per_s") * rcount / count
+    rlwe["count"] = rcount
+    from oracle.oracle import Restatement
+
+    ora = Restatement(p)
+    ora.keygen(0x5EED0013)
+    mu = (rng.integers(0, 4, cpu_sample) << 29).astype(np.int64)
+    t0 = time.perf_counter()
+    ora.encrypt(mu)
+    cpu_s = time.perf_counter() - t0
+    rmu = rng.integers(-(1 << 31), 1 << 31, (200, p.N), dtype=np.int64)
+    t0 = time.perf_counter()
+    ora.encrypt_rlwe_ntt_samples(rmu)
+    cpu_rlwe_s = time.perf_counter() - t0
+    return {"params": params_config(p), "count": count, "keygen_seeded_s": min(times), "keygen_seeded_s_all": times,
+            "encrypt_drawn": drawn, "encrypt_from_samples": given, "rlwe_encrypt_ntt_drawn": rlwe,
+            "cpu_rlwe_encrypt_ntt": {"value": 200 / cpu_rlwe_s, "unit": "samples/s", "cores": 1, "kind": "port"},
+            "hbm_peak_gbs": hbm,
+            "cpu_baseline": {"value": cpu_sample / cpu_s, "unit": "ciphertexts/s", "cores": 1, "kind": "port",
+                             "sample": f"{cpu_sample} encryptions by the restatement of symEncTlwe"}}
+
+
 def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
     """32 tenants with their own keys: 24 on the TORUS=32 set, 8 on the TORUS=56 set;
     per-tenant ciphertext counts from Zipf(1.1) over the 32 tenants (32,768 draws).  Each
@@ -896,6 +979,14 @@ def main():
                     "config": {"workload": r["workload"]}, "result": r}
             print(json.dumps(line))
             return
+        if args.workload == "encrypt":
+            r = leg_encrypt(dev)
+            line = {"metric": "LWE encryptions per second", "value": r["encrypt_drawn"]["ciphertexts_per_s"],
+                    "unit": "ciphertexts/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                    "config": {"workload": "encrypt_t32_n630_batch1048576"}, "result": r}
+            print(json.dumps(line))
+            return
         if args.workload == "multi_tenant":
             r = leg_multi_tenant(dev, steps=args.steps, warmup=args.warmup)
             line = {"metric": METRIC, "value": r["value"], "unit": "bootstraps/s", "n_gpus": 1,
@@ -1024,6 +1115,7 @@ def main():
             "t56_n2048_batch16384": _safe(leg_t56, dev),
             "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
             "keygen_t32_n1024": _safe(leg_keygen, dev),
+            "encrypt_t32_n630_batch1048576": _safe(leg_encrypt, dev),
             "lazy_t32_n2048_batch1216": _safe(leg_lazy, dev),
             "group2_t32_n1024_batch9728": _safe(leg_group, dev, 2),
             "group3_t32_n1024_batch9728": _safe(leg_group, dev, 3),

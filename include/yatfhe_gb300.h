@@ -141,6 +141,21 @@ int yg_encrypt_lwe(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, int cou
 int yg_encrypt_lwe_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const int32_t* d_mask,
                                 const int32_t* d_noise, int count, int32_t* d_out, void* stream);
 
+/* symEncTrlweMultiSampleSimple (yatfhe/src/trlwe.cpp:40-47,62-64; yatfhe/include/yatfhe/trlwe.h:518)
+ * of `count` torus polynomials on the GPU: d_out[i] = (a, NTT(sext(mu_i + e_i)) + a . NTT(s)
+ * mod q), NTT-domain words [count][k+1][N] (a_0 .. a_{k-1}, b) with masks a uniform mod q and
+ * TUniform(rlwe_noise_b) noise e drawn by ChaCha20 from (seed, call).  d_s [k N] is the binary
+ * RLWE secret, d_mu [count][N] the plaintext torus coefficients (int64, reduced to the torus
+ * width).  Device pointers; asynchronous on `stream` (its scratch comes from the stream's
+ * memory pool).  Requires k = 1. */
+int yg_encrypt_rlwe_ntt(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, int count, uint64_t seed, uint32_t call,
+                        int rlwe_noise_b, uint64_t* d_out, void* stream);
+
+/* As yg_encrypt_rlwe_ntt with the samples given: d_mask [count][k][N] (words < q) and d_noise
+ * [count][N].  Synchronizes `stream`; a mask word >= q gives YG_ERR_INVALID. */
+int yg_encrypt_rlwe_ntt_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const uint64_t* d_mask,
+                                     const int32_t* d_noise, int count, uint64_t* d_out, void* stream);
+
 /* Replaces deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): reads a file written
  * by serializeBskWWL24 (:220-229) and uploads it as above. */
 int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);

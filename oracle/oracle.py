@@ -286,6 +286,18 @@ class Restatement(_Common):
                    _ptr(noise, _i32p))
         return out, mask, noise
 
+    def encrypt_rlwe_ntt_samples(self, mu):
+        """NTT-domain RLWE encryptions of the torus polynomials mu [count][N]: the samples
+        [count][k+1][N] (uint64 mod q) with their masks [count][k][N] and noise [count][N]."""
+        p = self.p
+        mu = np.ascontiguousarray(mu, np.int64).reshape(-1, p.N)
+        out = np.zeros((len(mu), p.k + 1, p.N), np.uint64)
+        mask = np.zeros((len(mu), p.k, p.N), np.uint64)
+        noise = np.zeros((len(mu), p.N), np.int32)
+        self._call("encrypt_rlwe_ntt_samples", _ptr(mu, _i64p), len(mu), _ptr(out, _u64p), _ptr(mask, _u64p),
+                   _ptr(noise, _i32p))
+        return out, mask, noise
+
     def keygen_samples(self, seed: int) -> dict:
         """keygen(seed) that also returns its random samples: the secrets, the BSK samples'
         noise [n][l][k+1][N] and masks [n][l][k+1][k][N], the KSK samples' masks [kN][t][n]

@@ -444,6 +444,23 @@ int po_encrypt_samples(po_ctx* c, const int64_t* mu, int count, int32_t* out, in
     return 0;
 }
 
+/* symEncTrlweMultiSampleSimple (yatfhe/src/trlwe.cpp:40-47,62-64: initTrlweMultiSampleSimple
+ * then symEncTrlweNttSimple) of `count` torus polynomials mu [count][N] into NTT-domain
+ * samples out [count][k+1][N] (a_0 .. a_{k-1}, b), each sample's TUniform(rlwe_noise_b)
+ * noise [count][N] and uniform masks [count][k][N] written out. */
+int po_encrypt_rlwe_ntt_samples(po_ctx* c, const int64_t* mu, int count, uint64_t* out, uint64_t* mask,
+                                int32_t* noise) {
+    if (!c->have_rng) return fail(c, "po_encrypt_rlwe_ntt_samples: no RNG stream (run po_keygen first)");
+    const int N = c->p.N, k = c->p.k;
+    int64_t* tmpT = (int64_t*)malloc(sizeof(int64_t) * N);
+    if (!tmpT) return fail(c, "po_encrypt_rlwe_ntt_samples: out of memory");
+    for (int i = 0; i < count; i++)
+        enc_trlwe_ntt(c, out + (size_t)i * (k + 1) * N, mu + (size_t)i * N, tmpT, noise + (size_t)i * N,
+                      mask + (size_t)i * k * N);
+    free(tmpT);
+    return 0;
+}
+
 /* symDecTlweToInt (yatfhe/src/tlwe.cpp:44-53) with roundTorusGeneralError (numeric.cpp:95-98)
  * and modSwitchToTorusGeneral (numeric.cpp:182-187), all mod LWE_Q = 2^32. */
 static int64_t int_mod_p(int64_t a, int64_t p) {

@@ -33,6 +33,8 @@ uint64_t po_qntt(po_ctx* c);
 int po_keygen(po_ctx* c, uint64_t seed);
 int po_encrypt(po_ctx* c, const int64_t* mu, int count, int32_t* out);
 int po_encrypt_samples(po_ctx* c, const int64_t* mu, int count, int32_t* out, int32_t* mask, int32_t* noise);
+int po_encrypt_rlwe_ntt_samples(po_ctx* c, const int64_t* mu, int count, uint64_t* out, uint64_t* mask,
+                                int32_t* noise);
 int po_decrypt(po_ctx* c, const int32_t* in, int count, int base, int32_t* out);
 
 int po_get_keys(po_ctx* c, int32_t* lwe_s, int32_t* rlwe_s);

@@ -141,3 +141,64 @@ def test_encrypt_draws_depend_on_seed_and_call(built_lib):
     assert np.abs(e).max() <= 16 and abs(e.mean()) < 1.0  # standard error of the mean ~0.15
     # every ciphertext's mask differs from every other's
     assert len({r.tobytes() for r in x[:, :p.n]}) == len(x)
+
+
+@pytest.mark.parametrize("base", [T32_N1024, T56_N2048])
+def test_rlwe_encrypt_from_samples_matches_restatement(base, built_lib):
+    """symEncTrlweMultiSampleSimple fed the restatement's draws: bit-exact NTT-domain samples;
+    an unreduced mask word is refused."""
+    from yatfhe_gb300 import api
+
+    p = small(base, 8)
+    ora = Restatement(p)
+    ora.keygen(9)
+    _, rlwe_s = ora.keys()
+    rng = np.random.default_rng(6)
+    half = 1 << (p.torus_bits - 1)
+    mu = rng.integers(-half, half, (5, p.N), dtype=np.int64)
+    want, mask, noise = ora.encrypt_rlwe_ntt_samples(mu)
+    ctx = api.Context(p, 0)
+    d_s = torch.from_numpy(rlwe_s).cuda()
+    d_mu = torch.from_numpy(mu).cuda()
+    got = api.sym_enc_trlwe_ntt_from_samples(ctx, d_s, d_mu, torch.from_numpy(mask.view(np.int64)).cuda(),
+                                             torch.from_numpy(noise).cuda())
+    np.testing.assert_array_equal(got.cpu().numpy().view(np.uint64), want)
+    bad = mask.copy()
+    bad[3, 0, 17] = np.uint64(ora.q)
+    with pytest.raises(Exception, match="not reduced"):
+        api.sym_enc_trlwe_ntt_from_samples(ctx, d_s, d_mu, torch.from_numpy(bad.view(np.int64)).cuda(),
+                                           torch.from_numpy(noise).cuda())
+
+
+@pytest.mark.parametrize("base", [T32_N1024, T56_N2048])
+def test_rlwe_encrypt_drawn_decrypts(base, built_lib):
+    """GPU-drawn RLWE encryptions: INTT(b - a . NTT(s)) is mu plus TUniform(rlwe_noise_b) noise,
+    the masks are reduced, and (seed, call) fixes the samples."""
+    from yatfhe_gb300 import api
+
+    p = small(base, 8)
+    ora = Restatement(p)
+    q = ora.q
+    rng = np.random.default_rng(8)
+    rlwe_s = rng.integers(0, 2, p.k * p.N).astype(np.int32)
+    half = 1 << (p.torus_bits - 1)
+    mu = rng.integers(-half, half, (3, p.N), dtype=np.int64)
+    ctx = api.Context(p, 0)
+    d_s = torch.from_numpy(rlwe_s).cuda()
+    d_mu = torch.from_numpy(mu).cuda()
+    out = api.sym_enc_trlwe_ntt(ctx, d_s, d_mu, 21, 4, p.rlwe_noise_b).cpu().numpy().view(np.uint64)
+    again = api.sym_enc_trlwe_ntt(ctx, d_s, d_mu, 21, 4, p.rlwe_noise_b).cpu().numpy().view(np.uint64)
+    other = api.sym_enc_trlwe_ntt(ctx, d_s, d_mu, 21, 5, p.rlwe_noise_b).cpu().numpy().view(np.uint64)
+    np.testing.assert_array_equal(out, again)
+    assert (out[:, 0] != other[:, 0]).mean() > 0.99
+    assert int(out.max()) < q
+    s_ntt = [int(x) for x in ora.ntt_forward(rlwe_s.astype(np.int64))]
+    bound = 1 << p.rlwe_noise_b
+    for i in range(len(mu)):
+        a = [int(x) for x in out[i, 0]]
+        b = [int(x) for x in out[i, 1]]
+        diff = np.array([(bj - aj * sj) % q for aj, bj, sj in zip(a, b, s_ntt)], np.uint64)
+        phase = ora.ntt_inverse(diff)
+        e = (phase - mu[i]) & ((1 << p.torus_bits) - 1)
+        e = np.where(e >= half, e - (1 << p.torus_bits), e)
+        assert np.abs(e).max() <= bound and np.abs(e).max() > bound // 4, (i, np.abs(e).max())

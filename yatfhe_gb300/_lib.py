@@ -88,6 +88,9 @@ _SIGNATURES = {
     "yg_encrypt_lwe": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int,
                                       _vp, _vp]),
     "yg_encrypt_lwe_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+    "yg_encrypt_rlwe_ntt": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.c_int, _vp, _vp]),
+    "yg_encrypt_rlwe_ntt_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
     "yg_key_set_ksk": (ctypes.c_int, [_vp, _vp]),
     "yg_key_destroy": (None, [_vp]),
     "yg_key_device_bytes": (ctypes.c_size_t, [_vp]),

@@ -375,6 +375,41 @@ def sym_enc_tlwe_from_samples(ctx: Context, lwe_s, mu, mask, noise, out=None, st
     return out
 
 
+def _dptr_words(t, what: str):
+    """A contiguous CUDA tensor of 64-bit words (uint64, or int64 holding the same bits)."""
+    torch = _torch()
+    if not t.is_cuda or t.dtype not in (torch.int64, getattr(torch, "uint64", torch.int64)) or not t.is_contiguous():
+        raise ValueError(f"{what} must be a contiguous CUDA tensor of uint64 or int64")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def sym_enc_trlwe_ntt(ctx: Context, rlwe_s, mu, seed: int, call: int, rlwe_noise_b: int, out=None, stream=None):
+    """symEncTrlweMultiSampleSimple (yatfhe/src/trlwe.cpp:40-47,62-64) of the torus polynomials
+    `mu` (int64 [count, N]) under the binary secret `rlwe_s` (int32 [kN]), on the GPU with masks
+    and noise drawn from (seed, call): NTT-domain samples [count, k+1, N] of words mod q
+    (int64 tensor holding the uint64 words)."""
+    torch = _torch()
+    p = ctx.params
+    if out is None:
+        out = torch.empty((mu.shape[0], p.k + 1, p.N), dtype=torch.int64, device=mu.device)
+    _lib.check(_lib.lib().yg_encrypt_rlwe_ntt(ctx.handle, _dptr(rlwe_s, "int32", "rlwe_s"), _dptr(mu, "int64", "mu"),
+                                              mu.shape[0], seed, call, rlwe_noise_b, _dptr_words(out, "out"),
+                                              _stream_handle(stream)))
+    return out
+
+
+def sym_enc_trlwe_ntt_from_samples(ctx: Context, rlwe_s, mu, mask, noise, out=None, stream=None):
+    """sym_enc_trlwe_ntt with the masks (words [count, k, N]) and noise (int32 [count, N]) given."""
+    torch = _torch()
+    p = ctx.params
+    if out is None:
+        out = torch.empty((mu.shape[0], p.k + 1, p.N), dtype=torch.int64, device=mu.device)
+    _lib.check(_lib.lib().yg_encrypt_rlwe_ntt_from_samples(
+        ctx.handle, _dptr(rlwe_s, "int32", "rlwe_s"), _dptr(mu, "int64", "mu"), _dptr_words(mask, "mask"),
+        _dptr(noise, "int32", "noise"), mu.shape[0], _dptr_words(out, "out"), _stream_handle(stream)))
+    return out
+
+
 def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
     """blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412): the blind rotation on a
     WWL+24 key, whose GINX rows were derived on the GPU at upload."""

@@ -611,6 +611,45 @@ void keygen_from_samples(yg_ctx* c, yg_key* key, const int32_t* lwe_s, const int
     keygen_on_device(c, key, rlwe_s, d, h_words, h_ksk, scratch);
 }
 
+// The context's mod-q forward twiddles on the device, uploaded by the first caller.
+const u64* ctx_qfwd(yg_ctx* c) {
+    std::lock_guard<std::mutex> lk(c->qfwd_mu);
+    if (!c->d_qfwd) {
+        const size_t N = (size_t)c->p.N;
+        u64* d = nullptr;
+        ck(cudaMalloc(&d, 2 * N * sizeof(u64)), "cudaMalloc mod-q twiddles");
+        if (cudaMemcpy(d, c->qtab->wf.data(), N * sizeof(u64), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d + N, c->qtab->wfp.data(), N * sizeof(u64), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(d);
+            throw CudaError("upload mod-q twiddles");
+        }
+        c->d_qfwd = d;
+    }
+    return c->d_qfwd;
+}
+
+// Launch arguments of the NTT-domain RLWE encryption (buffers left to the caller):
+// q^-1 mod 2^64 by Newton's iteration (each step doubles the correct low bits of an odd
+// q's inverse, from 3 bits for inv = q) and 2^128 mod q.
+yg::EncryptRlweArgs rlwe_encrypt_args(yg_ctx* c) {
+    yg::EncryptRlweArgs a{};
+    const u64 q = c->q;
+    u64 inv = q;
+    for (int i = 0; i < 6; i++) inv *= 2 - q * inv;
+    const u64 r1 = (u64)(((u128)1 << 64) % q);
+    const u64* tw = ctx_qfwd(c);
+    a.wf = tw;
+    a.wfp = tw + c->p.N;
+    a.q = q;
+    a.qinv = inv;
+    a.r2 = mulmod(r1, r1, q);
+    a.N = c->p.N;
+    a.k = c->p.k;
+    a.torus_bits = c->p.torus_bits;
+    a.ctas = 2 * c->sm_count;
+    return a;
+}
+
 // deserializeBskMP / deserialize(TrgswMPDft|TrlweDft|NttPolynomial)
 // (yatfhe/src/ya_serializer.cpp:21-30,87-98,193-218,287-303): native-endian PODs.
 struct Reader {
@@ -953,6 +992,7 @@ void yg_ctx_destroy(yg_ctx* ctx) {
     if (!ctx) return;
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->d_qfwd) cudaFree(ctx->d_qfwd);
     delete ctx;
 }
 
@@ -1165,6 +1205,87 @@ int yg_encrypt_lwe_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* 
         DeviceGuard g(ctx->device);
         yg::EncryptArgs a{d_s, d_mu, d_mask, d_noise, d_out, 0, 0, 0, count, ctx->p.n, 0};
         yg::check_launch(yg::launch_encrypt_lwe(a, stream), "encrypt launch");
+        return YG_OK;
+    });
+}
+
+int yg_encrypt_rlwe_ntt(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, int count, uint64_t seed, uint32_t call,
+                        int rlwe_noise_b, uint64_t* d_out, void* stream) {
+    if (!ctx || count < 0 || (count > 0 && (!d_s || !d_mu || !d_out)) || rlwe_noise_b < 0 || rlwe_noise_b > 30)
+        return set_err(YG_ERR_INVALID, "yg_encrypt_rlwe_ntt: bad arguments");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::EncryptRlweArgs a = rlwe_encrypt_args(ctx);
+        const cudaStream_t st = (cudaStream_t)stream;
+        const size_t N = (size_t)ctx->p.N, k = (size_t)ctx->p.k;
+        int32_t* noise = nullptr;
+        u64* mask = nullptr;
+        ck(cudaMallocAsync((void**)&noise, count * N * sizeof(int32_t), st), "cudaMallocAsync noise");
+        if (cudaMallocAsync((void**)&mask, count * k * N * sizeof(u64), st) != cudaSuccess) {
+            cudaFreeAsync(noise, st);
+            throw CudaError("cudaMallocAsync masks");
+        }
+        yg::DrawArgs dn{};
+        dn.out_i32 = noise;
+        dn.count = count * N;
+        dn.seed = seed;
+        dn.domain = kDomEncrypt + 1;
+        dn.stream = call;
+        dn.kind = yg::kDrawTUniform;
+        dn.b = rlwe_noise_b;
+        dn.per_block = 8;
+        yg::DrawArgs dm{};
+        dm.out_u64 = mask;
+        dm.count = count * k * N;
+        dm.seed = seed;
+        dm.q = ctx->q;
+        dm.domain = kDomEncrypt + 2;
+        dm.stream = call;
+        dm.kind = yg::kDrawModQ;
+        dm.per_block = 4;
+        a.s = d_s;
+        a.mu = d_mu;
+        a.noise = noise;
+        a.mask = mask;
+        a.out = d_out;
+        a.count = count;
+        const int rc = (yg::launch_draw(dn, stream) || yg::launch_draw(dm, stream) ||
+                        yg::launch_encrypt_rlwe_ntt(a, stream)) ? -1 : 0;
+        cudaFreeAsync(mask, st);
+        cudaFreeAsync(noise, st);
+        yg::check_launch(rc, "RLWE encryption launch");
+        return YG_OK;
+    });
+}
+
+int yg_encrypt_rlwe_ntt_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const uint64_t* d_mask,
+                                     const int32_t* d_noise, int count, uint64_t* d_out, void* stream) {
+    if (!ctx || count < 0 || (count > 0 && (!d_s || !d_mu || !d_mask || !d_noise || !d_out)))
+        return set_err(YG_ERR_INVALID, "yg_encrypt_rlwe_ntt_from_samples: bad arguments");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(ctx->device);
+        yg::EncryptRlweArgs a = rlwe_encrypt_args(ctx);
+        const cudaStream_t st = (cudaStream_t)stream;
+        int* bad = nullptr;
+        ck(cudaMallocAsync((void**)&bad, sizeof(int), st), "cudaMallocAsync flag");
+        a.s = d_s;
+        a.mu = d_mu;
+        a.noise = d_noise;
+        a.mask = d_mask;
+        a.out = d_out;
+        a.count = count;
+        a.bad = bad;
+        int h_bad = 0;
+        cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+        const int rc = e == cudaSuccess ? yg::launch_encrypt_rlwe_ntt(a, stream) : -1;
+        if (rc == 0) e = cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(bad, st);
+        yg::check_launch(rc, "RLWE encryption launch");
+        ck(e, "RLWE encryption flag");
+        ck(cudaStreamSynchronize(st), "RLWE encryption");
+        if (h_bad) return set_err(YG_ERR_INVALID, "RLWE mask word not reduced mod q");
         return YG_OK;
     });
 }

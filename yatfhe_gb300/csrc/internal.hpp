@@ -89,6 +89,8 @@ struct yg_ctx {
     int ctas_per_sm = 0;   // persistent CTAs per SM, 0 = one CTA per ciphertext group
     cudaStream_t side = nullptr;  // second stream of the pipelined host-buffer bootstrap
     std::mutex side_mu;           // creates `side` once
+    uint64_t* d_qfwd = nullptr;   // [wf | wfp] (N each): mod-q forward twiddles, made by the first RLWE encryption
+    std::mutex qfwd_mu;           // creates `d_qfwd` once
 };
 
 struct yg_key {

@@ -399,6 +399,54 @@ __device__ __forceinline__ uint64_t mulshoup64_lazy(uint64_t x, uint64_t w, uint
     return x * w - __umul64hi(x, wp) * q;
 }
 
+// symEncTrlweMultiSampleSimple (yatfhe/src/trlwe.cpp:40-47 initTrlweMultiSampleSimple then
+// :62-64 symEncTrlweNttSimple): b = NTT(sext(mu + e)) + sum_r a_r . NTT(s_r) mod q with the
+// masks a_r uniform in the NTT domain; N/2 threads, one sample per pass of a CTA.  Each CTA
+// first transforms the secret into shared memory in Montgomery form (NTT(s) 2^64 mod q, from
+// one Montgomery product with 2^128 mod q), so one Montgomery product with a mask gives
+// a_r . NTT(s_r) mod q exactly.
+template <int T>
+__global__ void __launch_bounds__(1024) encrypt_rlwe_ntt_kernel(const EncryptRlweArgs a) {
+    extern __shared__ uint64_t sw[];  // [N] transform, then [k][N] NTT(s) 2^64 mod q
+    const int N = a.N, k = a.k;
+    uint64_t* sm = sw + N;
+    const uint64_t q = a.q;
+    for (int r = 0; r < k; ++r) {
+        for (int j = threadIdx.x; j < N; j += blockDim.x) sw[j] = a.s[(size_t)r * N + j] != 0 ? 1 : 0;
+        __syncthreads();
+        q_forward_in_smem(sw, N, a.wf, a.wfp, q);
+        for (int j = threadIdx.x; j < N; j += blockDim.x) sm[(size_t)r * N + j] = montmul64(sw[j], a.r2, q, a.qinv);
+        __syncthreads();
+    }
+    for (int c = blockIdx.x; c < a.count; c += gridDim.x) {
+        const int64_t* mu = a.mu + (size_t)c * N;
+        const int32_t* e = a.noise + (size_t)c * N;
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            const int64_t v = sext<T>(mu[j] + (int64_t)e[j]);
+            sw[j] = v < 0 ? (uint64_t)(v + (int64_t)q) : (uint64_t)v;
+        }
+        __syncthreads();
+        q_forward_in_smem(sw, N, a.wf, a.wfp, q);
+        const uint64_t* msk = a.mask + (size_t)c * k * N;
+        uint64_t* out = a.out + (size_t)c * (k + 1) * N;
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            uint64_t b = sw[j];
+            for (int r = 0; r < k; ++r) {
+                uint64_t m = msk[(size_t)r * N + j];
+                if (m >= q) {
+                    if (a.bad) atomicExch(a.bad, 1);
+                    m = 0;
+                }
+                const uint64_t prod = montmul64(m, sm[(size_t)r * N + j], q, a.qinv);
+                b = b + prod >= q ? b + prod - q : b + prod;
+                out[(size_t)r * N + j] = m;
+            }
+            out[(size_t)k * N + j] = b;
+        }
+        __syncthreads();  // sw is rewritten by the next sample
+    }
+}
+
 // M forward transforms mod q of the polynomials sw[k N .. k N + N), k < M, in the convention
 // of q_forward_in_smem, sharing each stage's twiddle loads and barrier.  Harvey's lazy
 // butterflies: words in [0, 4q) in and out (4q < 2^64 for both moduli), so the results are
@@ -1770,6 +1818,20 @@ int launch_keygen_bsk(const KeygenBskArgs& a, void* stream) {
         keygen_bsk_kernel<32><<<blocks, a.N / 2, smem, (cudaStream_t)stream>>>(a);
     else if (a.torus_bits == 56)
         keygen_bsk_kernel<56><<<blocks, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_encrypt_rlwe_ntt(const EncryptRlweArgs& a, void* stream) {
+    if (a.count <= 0) return 0;
+    if ((a.N != 1024 && a.N != 2048) || a.k != 1 || a.ctas < 1) return -1;
+    const size_t smem = (size_t)(a.k + 1) * a.N * sizeof(uint64_t);
+    const int grid = a.count < a.ctas ? a.count : a.ctas;
+    if (a.torus_bits == 32)
+        encrypt_rlwe_ntt_kernel<32><<<grid, a.N / 2, smem, (cudaStream_t)stream>>>(a);
+    else if (a.torus_bits == 56)
+        encrypt_rlwe_ntt_kernel<56><<<grid, a.N / 2, smem, (cudaStream_t)stream>>>(a);
     else
         return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;

@@ -142,6 +142,20 @@ struct EncryptArgs {
     uint32_t domain, call;
     int count, n, noise_b;
 };
+// symEncTrlweMultiSampleSimple on `count` torus polynomials: NTT-domain samples [a_r | b].
+struct EncryptRlweArgs {
+    const int32_t* s;       // [k][N] binary RLWE secret
+    const int64_t* mu;      // [count][N] torus plaintext coefficients
+    const int32_t* noise;   // [count][N] TUniform noise
+    const uint64_t* mask;   // [count][k][N] uniform NTT-domain masks (< q)
+    uint64_t* out;          // [count][k+1][N]
+    const uint64_t* wf;     // [N] psi^brv(k) mod q, and Shoup companions
+    const uint64_t* wfp;
+    uint64_t q, qinv, r2;   // q^-1 mod 2^64, 2^128 mod q
+    int count, N, k, torus_bits, ctas;
+    int* bad;               // set to 1 when a mask word is not reduced mod q (may be null)
+};
+int launch_encrypt_rlwe_ntt(const EncryptRlweArgs& a, void* stream);
 int launch_draw(const DrawArgs& a, void* stream);
 int launch_encrypt_lwe(const EncryptArgs& a, void* stream);
 

@@ -106,41 +106,64 @@ __global__ void draw_kernel(const DrawArgs a) {
     }
 }
 
+constexpr int kEncWarps = 8;           // warps (ciphertexts) per CTA
+constexpr int kEncChunk = 32 * 16;      // mask words one warp draws per pass: a block per lane
+
 // symEncTlwe (yatfhe/src/tlwe.cpp:21-31), one warp per ciphertext: b = sum a_i s_i + mu + e
-// mod LWE_Q = 2^32.  With a seed the masks and the TUniform(noise_b) noise are drawn here (the
+// mod LWE_Q = 2^32.  DRAWN: the masks and the TUniform(noise_b) noise are drawn here (the
 // masks of ciphertext c are words of stream 2 c + 0, its noise stream 2 c + 1 of the call's
-// domain), else they are read from mask / noise.
-__global__ void encrypt_lwe_kernel(const EncryptArgs a) {
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (warp >= a.count) return;
+// domain); a pass gives each lane one 16-word block, and the words go through shared memory
+// (index rotated by lane / 2 so that neither the block writes nor the row reads conflict on a
+// bank) so that the ciphertext row is written, and the secret read, with consecutive lanes on
+// consecutive words.  Otherwise the masks and noise are read from mask / noise (streamed:
+// read once), several loads in flight per lane.
+template <bool DRAWN>
+__global__ void __launch_bounds__(kEncWarps * 32) encrypt_lwe_kernel(const EncryptArgs a) {
+    __shared__ uint32_t stage[DRAWN ? kEncWarps : 1][DRAWN ? kEncChunk : 1];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * kEncWarps + wib;
+    if (warp >= a.count) return;  // whole warps leave; only __syncwarp below
     const int n = a.n;
-    int32_t* out = a.out + (size_t)warp * (n + 1);
+    int32_t* __restrict__ out = a.out + (size_t)warp * (n + 1);
+    const int32_t* __restrict__ s = a.s;
     uint32_t sum = 0;
     const uint32_t key[8] = {(uint32_t)a.seed, (uint32_t)(a.seed >> 32), a.domain, 0, 0, 0, 0, 0};
-    for (int base = 0; base < n; base += 32 * 16) {
-        // lane `lane` owns the block (base / 16 + lane) of this ciphertext's mask words
-        uint32_t w[16];
-        const int blk = base / 16 + lane;
-        if (!a.mask) chacha_block(key, (uint32_t)blk, 2u * (uint32_t)warp, (uint32_t)a.call, 0, w);
+    if constexpr (DRAWN) {
+        uint32_t* st = stage[wib];
+        for (int base = 0; base < n; base += kEncChunk) {
+            uint32_t w[16];
+            chacha_block(key, (uint32_t)(base / 16 + lane), 2u * (uint32_t)warp, (uint32_t)a.call, 0, w);
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            const int i = base + lane * 16 + e;
-            if (i >= n) break;
-            const int32_t ai = a.mask ? a.mask[(size_t)warp * n + i] : (int32_t)w[e];
-            out[i] = ai;
-            if (a.s[i]) sum += (uint32_t)ai;
+            for (int e = 0; e < 16; ++e) st[lane * 16 + ((e + (lane >> 1)) & 15)] = w[e];
+            __syncwarp();
+            const int lim = min(kEncChunk, n - base);
+            for (int j = lane; j < lim; j += 32) {
+                const int blk = j >> 4;
+                const uint32_t ai = st[blk * 16 + (((j & 15) + (blk >> 1)) & 15)];
+                __stcs(out + base + j, (int32_t)ai);
+                sum += s[base + j] ? ai : 0u;
+            }
+            __syncwarp();
+        }
+    } else {
+        const int32_t* __restrict__ mrow = a.mask + (size_t)warp * n;
+#pragma unroll 8
+        for (int j = lane; j < n; j += 32) {
+            const uint32_t ai = (uint32_t)__ldcs(mrow + j);
+            __stcs(out + j, (int32_t)ai);
+            sum += s[j] ? ai : 0u;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if (lane == 0) {
         int64_t e;
-        if (a.noise) {
-            e = a.noise[warp];
-        } else {
+        if constexpr (DRAWN) {
             uint32_t w[16];
             chacha_block(key, 0, 2u * (uint32_t)warp + 1, (uint32_t)a.call, 0, w);
             e = tuniform(((uint64_t)w[1] << 32) | w[0], a.noise_b);
+        } else {
+            e = a.noise[warp];
         }
         out[n] = (int32_t)((uint32_t)a.mu[warp] + (uint32_t)e + sum);
     }
@@ -160,8 +183,12 @@ int launch_draw(const DrawArgs& a, void* stream) {
 
 int launch_encrypt_lwe(const EncryptArgs& a, void* stream) {
     if (a.count <= 0) return 0;
-    const int threads = 256, per = threads / 32;
-    encrypt_lwe_kernel<<<(a.count + per - 1) / per, threads, 0, (cudaStream_t)stream>>>(a);
+    const unsigned grid = (unsigned)((a.count + kEncWarps - 1) / kEncWarps);
+    if ((a.mask == nullptr) != (a.noise == nullptr)) return -1;  // both drawn or both given
+    if (a.mask)
+        encrypt_lwe_kernel<false><<<grid, kEncWarps * 32, 0, (cudaStream_t)stream>>>(a);
+    else
+        encrypt_lwe_kernel<true><<<grid, kEncWarps * 32, 0, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
