@@ -606,7 +606,8 @@ def leg_encrypt(dev, count=1 << 20, steps=5, warmup=3, cpu_sample=20000):
     launching stream (outputs of 2.6 GB, larger than L2); ciphertexts/s and the HBM view of
     the algorithmic bytes (drawn: 8 B message + 4 (n + 1) B ciphertext; from samples: + 4 n B
     mask + 4 B noise), and the CPU restatement (one thread, its sequential RNG) on a sample.
-    Also yg_keygen's wall time (secrets, BSK and KSK from one seed, everything on the GPU)."""
+    Also yg_keygen's wall time (secrets, BSK and KSK from one seed, everything on the GPU) and
+    yg_encrypt_rlwe_ntt on 16384 polynomials (N = 1024, masks and noise drawn on the GPU)."""
     import torch
 
     from yatfhe_gb300 import api
