@@ -89,6 +89,16 @@ __device__ __forceinline__ int slot_pos(int tt, int r) {
     else return (tt >> 1) * 64 + 2 * r + (tt & 1);
 }
 
+// The slot of register r of thread tt in the forward transform's output (the layout of the
+// pointwise products and of the stored key): slot_pos at N = 1024; at N = 2048 each lane of
+// a pair holds whole index-bit-0 pairs, the even lane pairs 0..15 and the odd lane pairs
+// 16..31, the pair's U slot in register k and its V slot in register 16 + k.
+template <int LOGN>
+__host__ __device__ __forceinline__ int slot_pos_out(int tt, int r) {
+    if constexpr (LOGN == 10) return tt * 32 + r;
+    else return (tt >> 1) * 64 + 2 * ((r & 15) + ((tt & 1) << 4)) + (r >> 4);
+}
+
 // PS is the prime set (rns.cuh) of `ch`: it picks the constant-bank twiddles and the
 // reduction schedule of the forward transform.
 // TAB: the input holds signed digits d (|d| <= 64, as int32) instead of residues, and the
@@ -150,15 +160,23 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
         }
     }
     if constexpr (LOGN == 11) {
+        // index bit 0: the pair of register r is (U, V) = (even lane's a[r], odd lane's a[r]).
+        // The even lane takes pairs 0..15 and the odd lane pairs 16..31: one exchange of 16
+        // values each way, and each lane runs 16 whole butterflies.  Output (the split slot
+        // layout, slot_pos_out): a[k] = U' and a[16 + k] = V' of pair k (even lane) or pair
+        // 16 + k (odd lane).
         const bool odd = tt & 1;
-        const uint2* tw = pinned(ch.twf) + 1024 + gid;
+        const uint2* tw = pinned(ch.twf) + 1024 + gid + (odd ? 16 * 32 : 0);
 #pragma unroll
-        for (int r = 0; r < 32; ++r) {
-            const uint2 w = __ldg(&tw[r * 32]);
-            const uint32_t xr = PS == 0 ? reduce_once(a[r], 2 * two_p) : a[r];  // U, held by the even lane
-            const uint32_t t = mulshoup(a[r], w.x, w.y, p);    // W V, held by the odd lane
-            const uint32_t other = __shfl_xor_sync(0xffffffffu, odd ? t : xr, 1);
-            a[r] = odd ? other - t + (PS == 1 ? 0u : two_p) : xr + other;
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t recv = __shfl_xor_sync(0xffffffffu, odd ? a[k] : a[16 + k], 1);
+            uint32_t u = odd ? recv : a[k];
+            uint32_t v = odd ? a[16 + k] : recv;
+            const uint2 w = __ldg(&tw[k * 32]);
+            if constexpr (PS == 1) ct_bfly_b(u, v, w, neg_p);
+            else ct_bfly(u, v, w, p, two_p, true);
+            a[k] = u;
+            a[16 + k] = v;
         }
     }
 }
@@ -216,16 +234,21 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
     }
     const int gid = LOGN == 10 ? tt : (tt >> 1);
     if constexpr (LOGN == 11) {
+        // index bit 0 on the split slot layout of the forward transform's output: each lane
+        // holds whole pairs (a[k], a[16 + k]), runs their 16 butterflies, and one exchange of
+        // 16 values each way returns the U outputs to the even lane and the V outputs to the
+        // odd lane (register r = pair r) for the stages that follow.
         const bool odd = tt & 1;
-        const uint2* tw = pinned(ch.twi) + 1024 + gid;
+        const uint2* tw = pinned(ch.twi) + 1024 + gid + (odd ? 16 * 32 : 0);
 #pragma unroll
-        for (int r = 0; r < 32; ++r) {
-            const uint2 w = __ldg(&tw[r * 32]);
-            const uint32_t mine = a[r];
-            const uint32_t other = __shfl_xor_sync(0xffffffffu, mine, 1);
-            const uint32_t s = mine + other;
-            const uint32_t d = other - mine + two_p;  // U - V for the odd lane
-            a[r] = odd ? mulshoup(d, w.x, w.y, p) : reduce_once(s, two_p);
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t u = a[k], v = a[16 + k];
+            const uint2 w = __ldg(&tw[k * 32]);
+            const uint32_t su = reduce_once(u + v, two_p);
+            const uint32_t dv = mulshoup(u - v + two_p, w.x, w.y, p);
+            const uint32_t recv = __shfl_xor_sync(0xffffffffu, odd ? su : dv, 1);
+            a[k] = odd ? recv : su;
+            a[16 + k] = odd ? dv : recv;
         }
     }
 #pragma unroll
