@@ -156,6 +156,27 @@ int yg_encrypt_rlwe_ntt(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, in
 int yg_encrypt_rlwe_ntt_from_samples(yg_ctx* ctx, const int32_t* d_s, const int64_t* d_mu, const uint64_t* d_mask,
                                      const int32_t* d_noise, int count, uint64_t* d_out, void* stream);
 
+/* The approximate-CRT blind rotation (blindRotateApproxCRTNtt, yatfhe/src/blind_rotate.cpp:
+ * 577-589) with the conversions the reference's BLIND_ROT_APPROX_CRT_NTT test puts around it
+ * (decompTrlweMcrt, trlweMcrtToCrt, recompTrlweCrt; yatfhe/include/yatfhe/trlwe.h:333-440), on
+ * the torus Q_CRT = 251 241 239 233 with k = 1.  Its key is separate from yg_ctx: the residue
+ * rows of BootstrappingKeyCRT::bsk8 (yatfhe/include/yatfhe/bootstrapping.h:351-361),
+ * h_bsk8 int8 [n][4 primes][2 levels][2 rows][2 polys (a, b)][N], each a residue centred mod
+ * its prime (|v| <= 125, else YG_ERR_INVALID); the device keeps their transforms mod
+ * 2^24 - 2^14 + 1 (NttNative24's field), 16 N bytes per key row.  N = 1024 or 2048.
+ * Synchronizes the device. */
+typedef struct yg_crt_key yg_crt_key;
+int yg_crt_key_upload(int device, int n, int N, const int8_t* h_bsk8, yg_crt_key** out);
+
+/* d_acc_in [count][2][N]: each ciphertext's starting TRLWE sample (a then b) as torus values
+ * mod Q_CRT (int32, centred); d_rot [count][n]: the rotation amounts a_i (any integers; taken
+ * mod 2N, a_i = 0 skipped as the reference skips it); d_acc_out [count][2][N] receives the
+ * rotated sample.  Device pointers; asynchronous on `stream`. */
+int yg_crt_blind_rotate(yg_crt_key* key, const int32_t* d_acc_in, const int32_t* d_rot, int count, int32_t* d_acc_out,
+                        void* stream);
+size_t yg_crt_key_device_bytes(const yg_crt_key* key);
+void yg_crt_key_destroy(yg_crt_key* key);
+
 /* Replaces deserializeBskWWL24 (yatfhe/src/ya_serializer.cpp:231-246): reads a file written
  * by serializeBskWWL24 (:220-229) and uploads it as above. */
 int yg_key_load_wwl24_file(yg_ctx* ctx, const char* path, yg_key** out);

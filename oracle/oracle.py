@@ -224,7 +224,8 @@ class Restatement(_Common):
     prefix = "po_"
     _lib = None
 
-    def __init__(self, p):
+    @staticmethod
+    def load():
         if Restatement._lib is None:
             so = HERE / "_build" / "liboracle.so"
             if not so.exists():
@@ -236,6 +237,10 @@ class Restatement(_Common):
             Restatement._lib.po_destroy.argtypes = [ctypes.c_void_p]
             Restatement._lib.po_qntt.restype = ctypes.c_uint64
             Restatement._lib.po_qntt.argtypes = [ctypes.c_void_p]
+        return Restatement._lib
+
+    def __init__(self, p):
+        Restatement.load()
         self.p = p
         cp = _cparams(p)
         self._h = Restatement._lib.po_create(ctypes.byref(cp))
@@ -505,3 +510,89 @@ def _restatement_rotate(self, poly, a: int, minus_one: bool) -> np.ndarray:
 
 
 Restatement.rotate = _restatement_rotate
+
+
+# ------------------------------------------------------------------ approximate CRT
+
+CRT_PRIMES = (251, 241, 239, 233)
+CRT_Q = 251 * 241 * 239 * 233
+
+
+def crt_blind_rotate(bsk8, acc_in, rot):
+    """The restatement of blindRotateApproxCRTNtt with its conversions (po_crt_blind_rotate):
+    bsk8 int8 [n][4][2][2][2][N], acc_in torus values mod Q_CRT [2][N], rot [n].  Returns the
+    rotated sample [2][N] (int64) and the residue samples after the rotation [4][2][N] (int8)."""
+    bsk8 = np.ascontiguousarray(bsk8, np.int8)
+    n, N = bsk8.shape[0], bsk8.shape[-1]
+    acc_in = np.ascontiguousarray(acc_in, np.int64).reshape(2, N)
+    rot = np.ascontiguousarray(rot, np.int32).reshape(n)
+    out = np.zeros((2, N), np.int64)
+    mcrt = np.zeros((4, 2, N), np.int8)
+    rc = Restatement.load().po_crt_blind_rotate(n, N, _ptr(bsk8, ctypes.c_void_p), _ptr(acc_in, _i64p),
+                                                _ptr(rot, _i32p), _ptr(out, _i64p), _ptr(mcrt, ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("po_crt_blind_rotate failed")
+    return out, mcrt
+
+
+class CrtReference:
+    """The reference's ApproxCRT path (ref_crt_*, T32 build): keys, encryption, decryption and
+    the blind rotation, process-global like Reference."""
+
+    def __init__(self, n: int, N: int, rlwe_noise_b: int = 3, torus_base: int = 4):
+        so = HERE / "_ref" / "libyatfhe_ref_t32.so"
+        if not so.exists():
+            build_reference()
+        if 32 not in Reference._libs:
+            lib = ctypes.CDLL(str(so))
+            lib.ref_last_error.restype = ctypes.c_char_p
+            lib.ref_ntt_root.restype = ctypes.c_uint64
+            Reference._libs[32] = lib
+        self.lib = Reference._libs[32]
+        self.n, self.N, self.base = n, N, torus_base
+        if self.lib.ref_crt_setup(n, N, rlwe_noise_b, torus_base) != 0:
+            raise RuntimeError(self.lib.ref_last_error().decode())
+
+    def _call(self, name, *args):
+        if getattr(self.lib, "ref_crt_" + name)(*args) != 0:
+            raise RuntimeError(f"ref_crt_{name}: {self.lib.ref_last_error().decode()}")
+
+    def keygen(self, seed: int):
+        self._call("keygen", ctypes.c_uint64(seed))
+
+    def bsk8(self) -> np.ndarray:
+        out = np.zeros((self.n, 4, 2, 2, 2, self.N), np.int8)
+        self._call("export_bsk8", _ptr(out, ctypes.c_void_p))
+        return out
+
+    def set_bsk8(self, bsk8) -> None:
+        a = np.ascontiguousarray(bsk8, np.int8)
+        self._call("import_bsk8", _ptr(a, ctypes.c_void_p))
+
+    def lwe_key(self) -> np.ndarray:
+        s = np.zeros(self.n, np.int32)
+        z = np.zeros(self.N, np.int32)
+        if self.lib.ref_export_keys(_ptr(s, _i32p), _ptr(z, _i32p)) != 0:
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        return s
+
+    def encrypt(self, plain) -> np.ndarray:
+        plain = np.ascontiguousarray(plain, np.int32)
+        out = np.zeros((2, self.N), np.int64)
+        self._call("encrypt", _ptr(plain, _i32p), _ptr(out, _i64p))
+        return out
+
+    def decrypt(self, acc) -> np.ndarray:
+        acc = np.ascontiguousarray(acc, np.int64)
+        out = np.zeros(self.N, np.int32)
+        self._call("decrypt", _ptr(acc, _i64p), _ptr(out, _i32p))
+        return out
+
+    def blind_rotate(self, acc_in, rot, ntt: bool = True):
+        acc_in = np.ascontiguousarray(acc_in, np.int64)
+        rot = np.ascontiguousarray(rot, np.int32)
+        out = np.zeros((2, self.N), np.int64)
+        mcrt = np.zeros((4, 2, self.N), np.int8)
+        self._call("blind_rotate", _ptr(acc_in, _i64p), _ptr(rot, _i32p), int(ntt), _ptr(out, _i64p),
+                   _ptr(mcrt, ctypes.c_void_p))
+        return out, mcrt

@@ -1687,3 +1687,219 @@ int po_pbs_group(po_ctx* c, const int32_t* in, int count, const int64_t* v, int3
     if (!c->grp_bsk) return fail(c, "po_pbs_group: no group key");
     return pbs_run(c, in, count, v, out, threads, 2);
 }
+
+/* ------------------------------------------------------------------ approximate CRT (ApproxCRT) */
+
+/*
+ * blindRotateApproxCRTNtt (yatfhe/src/blind_rotate.cpp:577-589) with the conversions the
+ * reference's BLIND_ROT_APPROX_CRT_NTT test puts around it (google_tests/blindrot_test.cpp:
+ * 633-636): decompTrlweMcrt, the rotation, trlweMcrtToCrt, recompTrlweCrt
+ * (yatfhe/include/yatfhe/trlwe.h:333-440).  The torus is Q_CRT = 251 241 239 233; the
+ * accumulator is kept as d = 4 residue samples (int8, centred mod q_d, the low primes
+ * scaled by taoU); per step (controlMuxApproxCRTNtt, yatfhe/src/cmux.cpp:45-57):
+ *   tmp_d = X^a acc_d - acc_d mod q_d (rotateInt8PolynomialMinusOne, polynomial.cpp:262-271);
+ *   decompTrlweApproxCrt (yatfhe/src/crt.cpp:102-140): low = 233 tmp_2 + 239 tmp_3 (the
+ *     qLow / ql weights), digit_l = intModP(tmp_l - low, q_l) for the two high primes;
+ *   broadcastTrlweApproxCrt (crt.cpp:142-164): digit_l reduced mod q_d where |digit_l| > q_d / 2;
+ *   externalProductTrgswApproxCrtNtt (yatfhe/src/trgsw.cpp:607-657): the negacyclic products
+ *     with the key rows summed mod MOD = 2^24 - 2^14 + 1 (NttNative24), centred mod MOD, then
+ *     centred mod q_d (applyIntt, yatfhe/src/ntt24.cpp:222-240);
+ *   accumulateTrlweModP: acc_d = longModP(res_d + acc_d, q_d).
+ * The products go through this file's own negacyclic NTT mod MOD: any exact negacyclic
+ * product mod MOD gives the same integers as the reference's NTT24.
+ * bsk8: int8 [n][d][dh][k+1 rows][k+1 polys][N] (k = 1); in, out: torus values [2][N] (a, b);
+ * rot: the rotation amounts [n]; mcrt (may be NULL): int8 [d][2][N] residues after the rotation.
+ */
+#define PO_CRT_D 4
+#define PO_CRT_DH 2
+#define PO_CRT_MOD 16760833u /* (1 << 24) - (1 << 14) + 1 */
+static const int po_crt_q[PO_CRT_D] = {251, 241, 239, 233};
+
+static int crt_mod_p(int64_t a, int64_t p) { return (int)int_mod_p(a, p); }
+
+static uint32_t crt_pow(uint64_t b, uint64_t e) {
+    uint64_t r = 1;
+    b %= PO_CRT_MOD;
+    while (e) {
+        if (e & 1) r = r * b % PO_CRT_MOD;
+        b = b * b % PO_CRT_MOD;
+        e >>= 1;
+    }
+    return (uint32_t)r;
+}
+
+typedef struct {
+    int N, logN;
+    uint32_t* w;     /* psi^brv(k), k < N */
+    uint32_t* wi;    /* psi^-brv(k) */
+    uint32_t ninv;
+} crt_ntt;
+
+static int crt_brv(int x, int bits) {
+    int r = 0;
+    for (int i = 0; i < bits; i++) r |= ((x >> i) & 1) << (bits - 1 - i);
+    return r;
+}
+
+static int crt_ntt_init(crt_ntt* t, int N) {
+    t->N = N;
+    t->logN = 0;
+    while ((1 << t->logN) < N) t->logN++;
+    t->w = (uint32_t*)malloc(sizeof(uint32_t) * N);
+    t->wi = (uint32_t*)malloc(sizeof(uint32_t) * N);
+    if (!t->w || !t->wi) return -1;
+    /* 7 generates the multiplicative group mod MOD (NttNative24::PRIM_ROOT) */
+    const uint32_t psi = crt_pow(7, (PO_CRT_MOD - 1) / (2 * (uint64_t)N));
+    const uint32_t psi_inv = crt_pow(psi, PO_CRT_MOD - 2);
+    for (int k = 0; k < N; k++) {
+        t->w[k] = crt_pow(psi, (uint64_t)crt_brv(k, t->logN));
+        t->wi[k] = crt_pow(psi_inv, (uint64_t)crt_brv(k, t->logN));
+    }
+    t->ninv = crt_pow((uint64_t)N, PO_CRT_MOD - 2);
+    return 0;
+}
+
+static void crt_ntt_free(crt_ntt* t) {
+    free(t->w);
+    free(t->wi);
+}
+
+/* negacyclic forward (Cooley-Tukey, bit-reversed out) and inverse (Gentleman-Sande) mod MOD */
+static void crt_fwd(const crt_ntt* t, uint32_t* a) {
+    const int N = t->N;
+    for (int m = 1, span = N / 2; m < N; m <<= 1, span >>= 1)
+        for (int g = 0; g < m; g++)
+            for (int j = 2 * g * span; j < 2 * g * span + span; j++) {
+                const uint32_t u = a[j], v = (uint32_t)((uint64_t)a[j + span] * t->w[m + g] % PO_CRT_MOD);
+                a[j] = u + v >= PO_CRT_MOD ? u + v - PO_CRT_MOD : u + v;
+                a[j + span] = u >= v ? u - v : u + PO_CRT_MOD - v;
+            }
+}
+
+static void crt_inv(const crt_ntt* t, uint32_t* a) {
+    const int N = t->N;
+    for (int m = N / 2, span = 1; m >= 1; m >>= 1, span <<= 1)
+        for (int g = 0; g < m; g++)
+            for (int j = 2 * g * span; j < 2 * g * span + span; j++) {
+                const uint32_t u = a[j], v = a[j + span];
+                a[j] = u + v >= PO_CRT_MOD ? u + v - PO_CRT_MOD : u + v;
+                a[j + span] = (uint32_t)((uint64_t)(u >= v ? u - v : u + PO_CRT_MOD - v) * t->wi[m + g] % PO_CRT_MOD);
+            }
+    for (int j = 0; j < N; j++) a[j] = (uint32_t)((uint64_t)a[j] * t->ninv % PO_CRT_MOD);
+}
+
+static uint32_t crt_lift(int v) { return (uint32_t)((v % (int)PO_CRT_MOD + (int)PO_CRT_MOD) % (int)PO_CRT_MOD); }
+
+/* The constants of initYatfhe (yatfhe/src/initializer.cpp:31-83): taoU / taoUInv of the low
+ * primes and the CRT weights z_d = (Q/q_d) ((Q/q_d)^-1 mod q_d). */
+static int64_t crt_inv_small(int64_t a, int64_t m) {
+    a %= m;
+    if (a < 0) a += m;
+    for (int64_t x = 1; x < m; x++)
+        if (a * x % m == 1) return x;
+    return 0;
+}
+
+int po_crt_blind_rotate(int n, int N, const int8_t* bsk8, const int64_t* in, const int32_t* rot, int64_t* out,
+                        int8_t* mcrt) {
+    if (n < 1 || (N & (N - 1)) || N < 2 || N > 4096 || !bsk8 || !in || !rot || !out) return -1;
+    const int64_t qLow = (int64_t)po_crt_q[2] * po_crt_q[3];
+    const int64_t qCRT = (int64_t)po_crt_q[0] * po_crt_q[1] * qLow;
+    int64_t taoU[PO_CRT_D] = {1, 1, 1, 1}, taoUInv[PO_CRT_D] = {1, 1, 1, 1}, z[PO_CRT_D];
+    for (int u = 0; u < 2; u++) {
+        const int64_t ql = po_crt_q[PO_CRT_DH + u];
+        taoU[PO_CRT_DH + u] = crt_inv_small(qLow / ql, ql);
+        taoUInv[PO_CRT_DH + u] = int_mod_p(qLow / ql, ql);
+    }
+    for (int d = 0; d < PO_CRT_D; d++) {
+        const int64_t qt = qCRT / po_crt_q[d];
+        z[d] = qt * crt_inv_small(qt, po_crt_q[d]);
+    }
+    const int64_t lowW[2] = {qLow / po_crt_q[2], qLow / po_crt_q[3]};
+    crt_ntt t;
+    if (crt_ntt_init(&t, N)) return -1;
+    const size_t polys = (size_t)n * PO_CRT_D * PO_CRT_DH * 2 * 2;
+    uint32_t* key = (uint32_t*)malloc(sizeof(uint32_t) * polys * N);
+    int* acc = (int*)malloc(sizeof(int) * PO_CRT_D * 2 * N);
+    int* nxt = (int*)malloc(sizeof(int) * PO_CRT_D * 2 * N);
+    int* dig = (int*)malloc(sizeof(int) * PO_CRT_DH * 2 * N);
+    uint32_t* x = (uint32_t*)malloc(sizeof(uint32_t) * N);
+    uint32_t* sum = (uint32_t*)malloc(sizeof(uint32_t) * 2 * N);
+    if (!key || !acc || !nxt || !dig || !x || !sum) {
+        free(key); free(acc); free(nxt); free(dig); free(x); free(sum);
+        crt_ntt_free(&t);
+        return -1;
+    }
+    for (size_t pi = 0; pi < polys; pi++) {
+        uint32_t* kp = key + pi * N;
+        for (int j = 0; j < N; j++) kp[j] = crt_lift(bsk8[pi * N + j]);
+        crt_fwd(&t, kp);
+    }
+    /* decompTrlweMcrt */
+    for (int d = 0; d < PO_CRT_D; d++)
+        for (int r = 0; r < 2; r++)
+            for (int j = 0; j < N; j++) acc[(d * 2 + r) * N + j] = crt_mod_p(taoU[d] * in[r * N + j], po_crt_q[d]);
+    for (int i = 0; i < n; i++) {
+        if (rot[i] == 0) continue;
+        int a = rot[i] % (2 * N);
+        if (a < 0) a += 2 * N;
+        const int wrapSign = a < N ? 1 : -1;
+        if (a >= N) a -= N;
+        /* rotate minus one, decompose, per coefficient */
+        for (int r = 0; r < 2; r++)
+            for (int j = 0; j < N; j++) {
+                int tmp[PO_CRT_D];
+                for (int d = 0; d < PO_CRT_D; d++) {
+                    const int* A = acc + (d * 2 + r) * N;
+                    const int v = (j < a ? -A[j - a + N] : A[j - a]) * wrapSign;
+                    tmp[d] = crt_mod_p(v - A[j], po_crt_q[d]);
+                }
+                const int64_t low = lowW[0] * tmp[2] + lowW[1] * tmp[3];
+                for (int l = 0; l < PO_CRT_DH; l++) dig[(l * 2 + r) * N + j] = crt_mod_p(tmp[l] - low, po_crt_q[l]);
+            }
+        for (int d = 0; d < PO_CRT_D; d++) {
+            const int qd = po_crt_q[d], qdHalf = qd / 2;
+            memset(sum, 0, sizeof(uint32_t) * 2 * N);
+            for (int l = 0; l < PO_CRT_DH; l++)
+                for (int r = 0; r < 2; r++) {
+                    for (int j = 0; j < N; j++) {
+                        const int v = dig[(l * 2 + r) * N + j];
+                        x[j] = crt_lift(v > qdHalf || v < -qdHalf ? crt_mod_p(v, qd) : v);
+                    }
+                    crt_fwd(&t, x);
+                    const uint32_t* kr = key + ((((size_t)i * PO_CRT_D + d) * PO_CRT_DH + l) * 2 + r) * 2 * N;
+                    for (int c = 0; c < 2; c++)
+                        for (int j = 0; j < N; j++)
+                            sum[c * N + j] = (uint32_t)((sum[c * N + j] + (uint64_t)x[j] * kr[c * N + j]) % PO_CRT_MOD);
+                }
+            for (int c = 0; c < 2; c++) {
+                crt_inv(&t, sum + c * N);
+                for (int j = 0; j < N; j++) {
+                    uint32_t v = sum[c * N + j];
+                    const int centred = v >= (PO_CRT_MOD + 1) / 2 ? (int)v - (int)PO_CRT_MOD : (int)v;
+                    const int res = crt_mod_p(centred, qd);
+                    nxt[(d * 2 + c) * N + j] = crt_mod_p((int64_t)res + acc[(d * 2 + c) * N + j], qd);
+                }
+            }
+        }
+        int* sw = acc;
+        acc = nxt;
+        nxt = sw;
+    }
+    if (mcrt)
+        for (size_t e = 0; e < (size_t)PO_CRT_D * 2 * N; e++) mcrt[e] = (int8_t)acc[e];
+    /* trlweMcrtToCrt, recompTrlweCrt */
+    for (int r = 0; r < 2; r++)
+        for (int j = 0; j < N; j++) {
+            int64_t s = 0;
+            for (int d = 0; d < PO_CRT_D; d++) {
+                int v = acc[(d * 2 + r) * N + j];
+                if (d >= PO_CRT_DH) v = crt_mod_p(taoUInv[d] * v, po_crt_q[d]);
+                s += (int64_t)v * z[d];
+            }
+            out[r * N + j] = int_mod_p(s, qCRT);
+        }
+    free(key); free(acc); free(nxt); free(dig); free(x); free(sum);
+    crt_ntt_free(&t);
+    return 0;
+}

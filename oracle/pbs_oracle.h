@@ -94,6 +94,12 @@ int po_pbs_group(po_ctx* c, const int32_t* in, int count, const int64_t* v, int3
 int po_keygen_samples(po_ctx* c, uint64_t seed, int32_t* lwe_s, int32_t* rlwe_s, int32_t* bsk_noise,
                       uint64_t* bsk_mask, int32_t* ksk_mask, int32_t* ksk_noise);
 
+/* The approximate-CRT blind rotation blindRotateApproxCRTNtt with its input and output
+ * conversions (see pbs_oracle.c): bsk8 int8 [n][4][2][2][2][N], in/out torus values mod Q_CRT
+ * [2][N], rot [n]; mcrt (may be NULL) int8 [4][2][N].  Needs no context. */
+int po_crt_blind_rotate(int n, int N, const int8_t* bsk8, const int64_t* in, const int32_t* rot, int64_t* out,
+                        int8_t* mcrt);
+
 #ifdef __cplusplus
 }
 #endif

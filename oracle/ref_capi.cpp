@@ -18,6 +18,8 @@
 
 #include "yatfhe/blind_rotate.h"
 #include "yatfhe/bootstrapping.h"
+#include "yatfhe/crt.h"
+#include "yatfhe/ntt24.h"
 #include "yatfhe/gadget_decomposition.h"
 #include "yatfhe/keyswitching.h"
 #include "yatfhe/ntt_hexl.h"
@@ -813,5 +815,167 @@ int ref_pbs_lazy_no_first(const int32_t* in, int count, const int64_t* v, int32_
 }
 
 int ref_pool_size(void) { return static_cast<int>(ThreadPool::usableConcurrency()); }
+
+// ---------------------------------------------------------------- approximate CRT (ApproxCRT)
+// The setting of the reference's BLIND_ROT_APPROX_CRT(_NTT) tests (google_tests/blindrot_test.cpp:
+// 505-640): the torus is Q_CRT = 251 241 239 233 (param.q = Q_CRT), the accumulator is kept as
+// d = 4 Trlwe8 residue samples, the key is BootstrappingKeyCRT (yatfhe/include/yatfhe/
+// bootstrapping.h:351-361).  param.l is set to param.dh (2): encryptTrgswApproxCRT adds
+// param.w[lvl] for every level of a Trgsw{param} (yatfhe/src/trgsw.cpp:248-263) and w has dh
+// entries, while decompTrgswMcrt keeps the first dh levels (yatfhe/src/trgsw.cpp:334-360).
+
+static std::unique_ptr<BootstrappingKeyCRT> crt_key;
+
+int ref_crt_setup(int n, int N, int rlwe_noise_b, int torus_base) {
+    return guarded([&] {
+        auto& s = st();
+        s.param = YatfheParameters{};
+        auto& q = s.param;
+        q.q = Q_CRT;
+        q.n = n;
+        q.N = N;
+        q.l = q.dh;
+        q.rlweNoiseB = rlwe_noise_b;
+        q.torusBase = torus_base;
+        initYatfhe(q);
+        s.lweKey.reset();
+        s.trgswKey.reset();
+        s.bsk.reset();
+        s.wwl.reset();
+        s.lazy.reset();
+        s.gbsk.reset();
+        s.ksk.reset();
+        crt_key.reset();
+        s.ready = true;
+    });
+}
+
+// genTlweKey, genTrlweKey, then the per-i body of genBootstrappingKeyApproxCrt
+// (yatfhe/src/bootstrapping.cpp:425-440: encryptTrgswApproxCRT, decompTrgswMcrt, the NTT24 of
+// every residue Trgsw8) for i = 0..n-1 in order on one RNG stream.
+int ref_crt_keygen(uint64_t seed) {
+    if (!st().ready) return fail("ref_crt_keygen: ref_crt_setup not called");
+    return guarded([&] {
+        auto& s = st();
+        auto& p = s.param;
+        (void)rng();
+        yatfhe_oracle_set_seed(seed);
+        rng = ChaCha20Rng();
+        s.lweKey = std::make_unique<TlweKey>(p);
+        s.trgswKey = std::make_unique<TrgswKey>(p);
+        crt_key = std::make_unique<BootstrappingKeyCRT>(p);
+        genTlweKey(*s.lweKey);
+        genTrlweKey(s.trgswKey->trlweKey);
+        for (int i = 0; i < p.n; i++) {
+            Trgsw tmp{p};
+            encryptTrgswApproxCRT(tmp, p, *s.trgswKey, s.lweKey->s[i]);
+            decompTrgswMcrt(crt_key->bsk8[i], tmp, p);
+            for (int d = 0; d < p.d; d++) NttNative24::applyNttForRgsw(crt_key->bskCRT[i][d], crt_key->bsk8[i][d]);
+        }
+    });
+}
+
+// bsk8 as int8 [n][d][dh][k+1 rows][k+1 polys: a_0 .. a_{k-1}, b][N].
+int ref_crt_export_bsk8(int8_t* out) {
+    if (!crt_key) return fail("ref_crt_export_bsk8: no key");
+    const auto& p = st().param;
+    size_t o = 0;
+    for (int i = 0; i < p.n; i++)
+        for (int d = 0; d < p.d; d++)
+            for (int l = 0; l < p.dh; l++)
+                for (int r = 0; r <= p.k; r++) {
+                    const auto& t = crt_key->bsk8[i][d].trlweSamples[l][r];
+                    for (int c = 0; c <= p.k; c++) {
+                        const auto& poly = c < p.k ? t.a[c] : t.b;
+                        std::memcpy(out + o, poly.coeffs.data(), p.N);
+                        o += p.N;
+                    }
+                }
+    return 0;
+}
+
+// The other direction, for keys made elsewhere (the NTT24 forms are recomputed).
+int ref_crt_import_bsk8(const int8_t* in) {
+    if (!st().ready) return fail("ref_crt_import_bsk8: ref_crt_setup not called");
+    return guarded([&] {
+        const auto& p = st().param;
+        crt_key = std::make_unique<BootstrappingKeyCRT>(p);
+        size_t o = 0;
+        for (int i = 0; i < p.n; i++)
+            for (int d = 0; d < p.d; d++) {
+                for (int l = 0; l < p.dh; l++)
+                    for (int r = 0; r <= p.k; r++) {
+                        auto& t = crt_key->bsk8[i][d].trlweSamples[l][r];
+                        for (int c = 0; c <= p.k; c++) {
+                            auto& poly = c < p.k ? t.a[c] : t.b;
+                            std::memcpy(poly.coeffs.data(), in + o, p.N);
+                            o += p.N;
+                        }
+                    }
+                NttNative24::applyNttForRgsw(crt_key->bskCRT[i][d], crt_key->bsk8[i][d]);
+            }
+    });
+}
+
+// symEncTrlweMultiSample (yatfhe/src/trlwe.cpp:98-101) of plain [N] (messages mod torus_base,
+// modSwitchToTorus32 as the reference's test does): out [k+1][N] torus values (a, then b).
+int ref_crt_encrypt(const int32_t* plain, int64_t* out) {
+    if (!st().trgswKey) return fail("ref_crt_encrypt: no key");
+    return guarded([&] {
+        const auto& p = st().param;
+        std::vector<Torus> mu(p.N);
+        for (int j = 0; j < p.N; j++) mu[j] = modSwitchToTorus32(plain[j], p.torusBase);
+        Trlwe t{p.k, p.N};
+        symEncTrlweMultiSample(t, st().trgswKey->trlweKey, mu);
+        for (int c = 0; c < p.k; c++) fromPoly(out + (size_t)c * p.N, t.a[c], p.N);
+        fromPoly(out + (size_t)p.k * p.N, t.b, p.N);
+    });
+}
+
+// symDecTrlweToInt (yatfhe/src/trlwe.cpp:131-138).
+int ref_crt_decrypt(const int64_t* in, int32_t* out) {
+    if (!st().trgswKey) return fail("ref_crt_decrypt: no key");
+    return guarded([&] {
+        const auto& p = st().param;
+        Trlwe t{p.k, p.N};
+        for (int c = 0; c < p.k; c++) toPoly(t.a[c], in + (size_t)c * p.N, p.N);
+        toPoly(t.b, in + (size_t)p.k * p.N, p.N);
+        IntPolynomial dec{p.N};
+        symDecTrlweToInt(dec, t, st().trgswKey->trlweKey, p.torusBase);
+        for (int j = 0; j < p.N; j++) out[j] = static_cast<int32_t>(dec.coeffs[j]);
+    });
+}
+
+// The reference test's sequence around the blind rotation: decompTrlweMcrt, then
+// blindRotateApproxCRTNtt (ntt != 0) or blindRotateApproxCRT (yatfhe/src/blind_rotate.cpp:
+// 563-589), trlweMcrtToCrt and recompTrlweCrt (yatfhe/include/yatfhe/trlwe.h:333-440).
+// in/out: [k+1][N] torus values; rot [n]: the rotation amounts a_i; mcrt (if not null):
+// the d residue samples after the rotation, int8 [d][k+1][N].
+int ref_crt_blind_rotate(const int64_t* in, const int32_t* rot, int ntt, int64_t* out, int8_t* mcrt) {
+    if (!crt_key) return fail("ref_crt_blind_rotate: no key");
+    return guarded([&] {
+        const auto& p = st().param;
+        Trlwe t{p.k, p.N};
+        for (int c = 0; c < p.k; c++) toPoly(t.a[c], in + (size_t)c * p.N, p.N);
+        toPoly(t.b, in + (size_t)p.k * p.N, p.N);
+        ScaledTlwe s{p.N * 2, p.n};
+        for (int i = 0; i < p.n; i++) s.a[i] = rot[i];
+        std::vector<Trlwe8> acc(p.d, Trlwe8{p.k, p.N});
+        decompTrlweMcrt(acc, t, p);
+        if (ntt) blindRotateApproxCRTNtt(acc, crt_key->bskCRT, s, p);
+        else blindRotateApproxCRT(acc, crt_key->bsk8, s, p);
+        if (mcrt)
+            for (int d = 0; d < p.d; d++)
+                for (int c = 0; c <= p.k; c++) {
+                    const auto& poly = c < p.k ? acc[d].a[c] : acc[d].b;
+                    std::memcpy(mcrt + ((size_t)d * (p.k + 1) + c) * p.N, poly.coeffs.data(), p.N);
+                }
+        trlweMcrtToCrt(acc, p);
+        Trlwe r{p.k, p.N};
+        recompTrlweCrt(r, acc, p);
+        for (int c = 0; c < p.k; c++) fromPoly(out + (size_t)c * p.N, r.a[c], p.N);
+        fromPoly(out + (size_t)p.k * p.N, r.b, p.N);
+    });
+}
 
 }  // extern "C"

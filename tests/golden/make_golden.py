@@ -10,7 +10,11 @@ parameter set and key seed:
     the test polynomial, the reference's outputs of functionalBootstrappingMPNtt, its
     decryptions, and the blind-rotation accumulator of ciphertext 0 after a few CMux steps.
 
-    python tests/golden/make_golden.py [ginx] [wwl24] [lazy] [group]
+and, for the approximate-CRT blind rotation (blindRotateApproxCRTNtt on the torus Q_CRT), the
+reference's residue key rows (small n: they are stored whole), an encrypted plaintext, the
+rotation amounts, the rotated sample, its residue samples and its decryption.
+
+    python tests/golden/make_golden.py [ginx] [wwl24] [lazy] [group] [crt]
 """
 from __future__ import annotations
 
@@ -23,7 +27,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parents[1]))
 
-from oracle.oracle import Reference  # noqa: E402
+from oracle.oracle import CrtReference, Reference  # noqa: E402
 from yatfhe_gb300 import lut as lutmod  # noqa: E402
 from yatfhe_gb300.params import T32_N1024, T56_N2048, WWL24_T32_N2048, WWL24_T56_N2048, small  # noqa: E402
 
@@ -180,10 +184,31 @@ def make_group(name, p, group, seed, count, mseed):
     print(f"{name}: {count} ciphertexts, outputs decrypt to the messages")
 
 
+CRT_CASES = {
+    # name: (n, N, key seed, message seed)
+    "crt_n3_n2048_seed5eed0011": (3, 2048, 0x5EED0011, 21),
+}
+
+
+def make_crt(name, n, N, seed, mseed):
+    r = CrtReference(n, N)
+    r.keygen(seed)
+    rng = np.random.default_rng(mseed)
+    plain = rng.integers(-r.base // 2, r.base // 2, N).astype(np.int32)
+    ct = r.encrypt(plain)
+    rot = rng.integers(1, 2 * N, n).astype(np.int32)
+    out, mcrt = r.blind_rotate(ct, rot)
+    s = r.lwe_key()
+    np.savez_compressed(HERE / f"{name}.npz", bsk8=r.bsk8(), acc_in=ct.astype(np.int32), rot=rot,
+                        acc_out=out.astype(np.int32), mcrt=mcrt, plain=plain, lwe_s=s, dec=r.decrypt(out),
+                        shift=np.array([int((rot.astype(np.int64) * s).sum()) % (2 * N)]))
+    print(name)
+
+
 if __name__ == "__main__":
-    # optional arguments: the families to (re)generate, of "ginx", "wwl24", "lazy", "group"
+    # optional arguments: the families to (re)generate, of "ginx", "wwl24", "lazy", "group", "crt"
     # (default all)
-    families = set(sys.argv[1:]) or {"ginx", "wwl24", "lazy", "group"}
+    families = set(sys.argv[1:]) or {"ginx", "wwl24", "lazy", "group", "crt"}
     if "ginx" in families:
         for name, (p, seed, count, mseed) in CASES.items():
             make(name, p, seed, count, mseed)
@@ -196,3 +221,6 @@ if __name__ == "__main__":
     if "group" in families:
         for name, (p, group, seed, count, mseed) in GROUP_CASES.items():
             make_group(name, p, group, seed, count, mseed)
+    if "crt" in families:
+        for name, (n, N, seed, mseed) in CRT_CASES.items():
+            make_crt(name, n, N, seed, mseed)

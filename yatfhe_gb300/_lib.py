@@ -91,6 +91,10 @@ _SIGNATURES = {
     "yg_encrypt_rlwe_ntt": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,
                                            ctypes.c_int, _vp, _vp]),
     "yg_encrypt_rlwe_ntt_from_samples": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+    "yg_crt_key_upload": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
+    "yg_crt_blind_rotate": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp, _vp]),
+    "yg_crt_key_device_bytes": (ctypes.c_size_t, [_vp]),
+    "yg_crt_key_destroy": (None, [_vp]),
     "yg_key_set_ksk": (ctypes.c_int, [_vp, _vp]),
     "yg_key_destroy": (None, [_vp]),
     "yg_key_device_bytes": (ctypes.c_size_t, [_vp]),

@@ -410,6 +410,47 @@ def sym_enc_trlwe_ntt_from_samples(ctx: Context, rlwe_s, mu, mask, noise, out=No
     return out
 
 
+class CrtKey:
+    """A key of the approximate-CRT blind rotation (yg_crt_key_upload): the residue rows of the
+    reference's BootstrappingKeyCRT::bsk8, int8 [n][4][2][2][2][N], on the torus Q_CRT."""
+
+    def __init__(self, bsk8: np.ndarray, device: int = 0):
+        a = np.ascontiguousarray(bsk8, np.int8)
+        if a.ndim != 6 or a.shape[1:5] != (4, 2, 2, 2):
+            raise ValueError("bsk8 must have shape [n, 4, 2, 2, 2, N]")
+        self.n, self.N = a.shape[0], a.shape[-1]
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().yg_crt_key_upload(device, self.n, self.N, ctypes.c_void_p(a.ctypes.data),
+                                                ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.lib().yg_crt_key_device_bytes(self._h))
+
+    def blind_rotate(self, acc_in, rot, out=None, stream=None):
+        """blindRotateApproxCRTNtt with decompTrlweMcrt before and trlweMcrtToCrt +
+        recompTrlweCrt after, per ciphertext: acc_in int32 [count, 2, N] (torus values mod
+        Q_CRT), rot int32 [count, n]; returns the rotated samples int32 [count, 2, N]."""
+        torch = _torch()
+        if out is None:
+            out = torch.empty_like(acc_in)
+        _lib.check(_lib.lib().yg_crt_blind_rotate(self._h, _dptr(acc_in, "int32", "acc_in"), _dptr(rot, "int32", "rot"),
+                                                  acc_in.shape[0], _dptr(out, "int32", "out"), _stream_handle(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().yg_crt_key_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def blind_rotate_wwl24_ntt(ctx: Context, key: BootstrapKey, lwe_in, lut, steps: int | None = None, stream=None):
     """blindRotateWWL24Ntt (yatfhe/src/blind_rotate.cpp:1383-1412): the blind rotation on a
     WWL+24 key, whose GINX rows were derived on the GPU at upload."""

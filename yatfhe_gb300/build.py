@@ -19,7 +19,7 @@ INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", f"-I{INCLUDE}"]
-SOURCES = ["pbs_kernels.cu", "calibrate.cu", "noalloc.cu", "sampling.cu", "host.cpp", "serve.cpp"]
+SOURCES = ["pbs_kernels.cu", "calibrate.cu", "noalloc.cu", "sampling.cu", "crt_kernels.cu", "host.cpp", "serve.cpp"]
 
 
 def nvcc() -> str:

@@ -165,6 +165,47 @@ void validate(const yg_params& p) {
 //            2^sp + m for the stages on slot bits sp = 1..4 (entry 1: the twiddle 1 of bit 0);
 //   inverse, Gentleman-Sande form (the other shapes): psi^-brv(k), thread-minor, first 32
 //            entries to the constant bank.
+// One prime's tables: tw [N forward | 2N inverse], heads [forward 32 | inverse 32].
+void team_tables(uint32_t p, int N, int logN, bool ct_inverse, uint2* tw, uint2* heads) {
+    const u64 psi = minimal_root(N, p);
+    const u64 psi_inv = invmod(psi, p);
+    uint2* fwd = tw;
+    uint2* inv = fwd + N;
+    auto pair = [p](u64 w) { return make_uint2((uint32_t)w, shoup32((uint32_t)w, p)); };
+    for (int k = 0; k < N; k++) {
+        const uint32_t e = brv(k, logN);
+        fwd[k] = pair(powmod(psi, e, p));
+        if (!ct_inverse) inv[k] = pair(powmod(psi_inv, e, p));
+    }
+    thread_minor_layout(fwd, N);
+    for (int k = 0; k < 32; k++) heads[k] = fwd[k];
+    if (ct_inverse) {
+        for (int sp = 0; sp <= 4; sp++) {
+            const int h = 1 << sp;
+            for (int m = 0; m < h; m++)
+                for (int tt = 0; tt < 32; tt++)
+                    inv[32 * (h - 1) + m * 32 + tt] = pair(powmod(psi_inv, (u64)(N / (32 * h)) * (m * 32 + tt), p));
+        }
+        for (int j = 0; j < N; j++) inv[992 + j] = pair(powmod(psi_inv, j, p));
+        uint2* hd = heads + 32;
+        hd[0] = hd[1] = pair(1);
+        for (int sp = 1; sp <= 4; sp++)
+            for (int m = 0; m < (1 << sp); m++) hd[(1 << sp) + m] = pair(powmod(psi_inv, (u64)(N >> sp) * m, p));
+    } else {
+        thread_minor_layout(inv, N);
+        for (int k = 0; k < 32; k++) heads[32 + k] = inv[k];
+    }
+}
+
+// Montgomery form with N^-1 folded in: N^-1 2^32 mod p
+uint32_t conv_scale_for(uint32_t p, int N) { return (uint32_t)mulmod(invmod(N, p), ((u64)1 << 32) % p, p); }
+
+uint32_t neg_pinv32(uint32_t p) {
+    uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
+    for (int it = 0; it < 5; it++) pinv *= 2 - p * pinv;
+    return 0u - pinv;
+}
+
 void ctx_init_tables(yg_ctx* c) {
     const int N = c->p.N;
     const size_t per = (size_t)3 * N;  // words of one channel's tables
@@ -173,36 +214,8 @@ void ctx_init_tables(yg_ctx* c) {
     std::vector<uint2> heads((size_t)yg::kChannels * 2 * 32);
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimeSet[c->ps][ci];
-        const u64 psi = minimal_root(N, p);
-        const u64 psi_inv = invmod(psi, p);
-        uint2* fwd = &tw[ci * per];
-        uint2* inv = fwd + N;
-        auto pair = [p](u64 w) { return make_uint2((uint32_t)w, shoup32((uint32_t)w, p)); };
-        for (int k = 0; k < N; k++) {
-            const uint32_t e = brv(k, c->logN);
-            fwd[k] = pair(powmod(psi, e, p));
-            if (!ct_inverse) inv[k] = pair(powmod(psi_inv, e, p));
-        }
-        thread_minor_layout(fwd, N);
-        for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + 0) * 32 + k] = fwd[k];
-        if (ct_inverse) {
-            for (int sp = 0; sp <= 4; sp++) {
-                const int h = 1 << sp;
-                for (int m = 0; m < h; m++)
-                    for (int tt = 0; tt < 32; tt++)
-                        inv[32 * (h - 1) + m * 32 + tt] = pair(powmod(psi_inv, (u64)(N / (32 * h)) * (m * 32 + tt), p));
-            }
-            for (int j = 0; j < N; j++) inv[992 + j] = pair(powmod(psi_inv, j, p));
-            uint2* hd = &heads[((size_t)ci * 2 + 1) * 32];
-            hd[0] = hd[1] = pair(1);
-            for (int sp = 1; sp <= 4; sp++)
-                for (int m = 0; m < (1 << sp); m++) hd[(1 << sp) + m] = pair(powmod(psi_inv, (u64)(N >> sp) * m, p));
-        } else {
-            thread_minor_layout(inv, N);
-            for (int k = 0; k < 32; k++) heads[((size_t)ci * 2 + 1) * 32 + k] = inv[k];
-        }
-        // Montgomery form with N^-1 folded in: N^-1 2^32 mod p
-        const uint32_t sc = (uint32_t)mulmod(invmod(N, p), ((u64)1 << 32) % p, p);
+        team_tables(p, N, c->logN, ct_inverse, &tw[ci * per], &heads[(size_t)ci * 2 * 32]);
+        const uint32_t sc = conv_scale_for(p, N);
         c->conv_scale[ci] = sc;
         c->conv_scale_s[ci] = shoup32(sc, p);
     }
@@ -211,9 +224,7 @@ void ctx_init_tables(yg_ctx* c) {
     if (yg::set_twiddle_heads(c->logN, c->ps, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimeSet[c->ps][ci];
-        uint32_t pinv = 1;  // p^-1 mod 2^32 by Newton iteration
-        for (int it = 0; it < 5; it++) pinv *= 2 - p * pinv;
-        c->ch[ci] = yg::Chan{p, 2 * p, (uint32_t)(0u - pinv), 0, c->d_tw + ci * per, c->d_tw + ci * per + N};
+        c->ch[ci] = yg::Chan{p, 2 * p, neg_pinv32(p), 0, c->d_tw + ci * per, c->d_tw + ci * per + N};
     }
     const u64 p0 = yg::kPrimeSet[c->ps][0], p1 = yg::kPrimeSet[c->ps][1], p2 = yg::kPrimeSet[c->ps][2];
     yg::Crt& k = c->crt;
@@ -1288,6 +1299,128 @@ int yg_encrypt_rlwe_ntt_from_samples(yg_ctx* ctx, const int32_t* d_s, const int6
         if (h_bad) return set_err(YG_ERR_INVALID, "RLWE mask word not reduced mod q");
         return YG_OK;
     });
+}
+
+// ------------------------------------------------------------------ approximate CRT
+
+struct yg_crt_key {
+    int device = 0, n = 0, N = 0, logN = 0, sm_count = 0;
+    uint2* d_tw = nullptr;        // [N forward | 2N inverse] tables of 2^24 - 2^14 + 1
+    uint32_t* d_key = nullptr;    // [n][d][dh][2 rows] key blocks (key_block_words(N) each)
+    size_t key_bytes = 0;
+    yg::Chan ch{};
+    yg::CrtBrArgs args{};         // constants of the rotation (buffers and count left empty)
+};
+
+namespace {
+
+int64_t inv_small(int64_t a, int64_t m) {
+    a %= m;
+    if (a < 0) a += m;
+    for (int64_t x = 1; x < m; x++)
+        if (a * x % m == 1) return x;
+    throw std::invalid_argument("not invertible");
+}
+
+}  // namespace
+
+int yg_crt_key_upload(int device, int n, int N, const int8_t* h_bsk8, yg_crt_key** out) {
+    if (!h_bsk8 || !out) return set_err(YG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (n < 1 || n > 4096 || (N != 1024 && N != 2048)) return set_err(YG_ERR_INVALID, "ApproxCRT key: 1 <= n <= 4096, N = 1024 or 2048");
+    return guarded([&] {
+        DeviceGuard g(device);
+        auto k = std::make_unique<yg_crt_key>();
+        k->device = device;
+        k->n = n;
+        k->N = N;
+        k->logN = N == 1024 ? 10 : 11;
+        ck(cudaDeviceGetAttribute(&k->sm_count, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        const size_t rows = (size_t)n * yg::kCrtD * yg::kCrtDh * 2;
+        const size_t bytes8 = rows * 2 * N;
+        for (size_t e = 0; e < bytes8; e++) {
+            const int v = h_bsk8[e];
+            if (v < -125 || v > 125) throw std::invalid_argument("ApproxCRT key residue outside [-125, 125]");
+        }
+        // the transform tables of 2^24 - 2^14 + 1 (the Gentleman-Sande inverse at both N)
+        const uint32_t p = yg::kMod24;
+        std::vector<uint2> tw((size_t)3 * N), heads((size_t)yg::kChannels * 2 * 32);
+        team_tables(p, N, k->logN, false, tw.data(), heads.data());
+        for (int ci = 1; ci < yg::kChannels; ci++) std::copy(heads.begin(), heads.begin() + 64, heads.begin() + ci * 64);
+        try {
+            ck(cudaMalloc(&k->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
+            ck(cudaMemcpy(k->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
+            if (yg::set_crt_twiddle_heads(k->logN, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
+            k->ch = yg::Chan{p, 2 * p, neg_pinv32(p), 0, k->d_tw, k->d_tw + N};
+            k->key_bytes = rows * yg::key_block_words(N) * sizeof(uint32_t);
+            ck(cudaMalloc(&k->d_key, k->key_bytes), "cudaMalloc ApproxCRT key");
+            DeviceScratch scratch;
+            int8_t* d8 = scratch.alloc<int8_t>(bytes8, "cudaMalloc key upload");
+            ck(cudaMemcpy(d8, h_bsk8, bytes8, cudaMemcpyHostToDevice), "upload ApproxCRT key");
+            const uint32_t sc = conv_scale_for(p, N);
+            yg::CrtKeyConvArgs ka{d8, k->d_key, k->ch, sc, shoup32(sc, p), (int)rows};
+            yg::check_launch(yg::launch_crt_keyconv(k->logN, ka, nullptr), "ApproxCRT key conversion");
+            ck(cudaDeviceSynchronize(), "ApproxCRT key conversion");
+        } catch (...) {
+            if (k->d_tw) cudaFree(k->d_tw);
+            if (k->d_key) cudaFree(k->d_key);
+            throw;
+        }
+        // initYatfhe's constants of the CRT (yatfhe/src/initializer.cpp:31-83): taoU and
+        // taoUInv of the low primes, z_d = (Q / q_d) ((Q / q_d)^-1 mod q_d)
+        const int64_t q[yg::kCrtD] = {251, 241, 239, 233};
+        const int64_t qLow = q[2] * q[3], Q = q[0] * q[1] * qLow;
+        yg::CrtBrArgs& a = k->args;
+        for (int d = 0; d < yg::kCrtD; d++) {
+            a.tao_u[d] = a.tao_u_inv[d] = 1;
+            if (d >= yg::kCrtDh) {
+                a.tao_u[d] = inv_small(qLow / q[d], q[d]);
+                a.tao_u_inv[d] = (qLow / q[d]) % q[d];
+            }
+            a.z[d] = (Q / q[d]) * inv_small(Q / q[d], q[d]);
+        }
+        a.q_crt = Q;
+        a.key = k->d_key;
+        a.ch = k->ch;
+        a.n = n;
+        *out = k.release();
+        return YG_OK;
+    });
+}
+
+int yg_crt_blind_rotate(yg_crt_key* key, const int32_t* d_acc_in, const int32_t* d_rot, int count, int32_t* d_acc_out,
+                        void* stream) {
+    if (!key || count < 0 || (count > 0 && (!d_acc_in || !d_rot || !d_acc_out)))
+        return set_err(YG_ERR_INVALID, "yg_crt_blind_rotate: bad arguments");
+    if (count == 0) return YG_OK;
+    return guarded([&] {
+        DeviceGuard g(key->device);
+        yg::CrtBrArgs a = key->args;
+        a.acc_in = d_acc_in;
+        a.rot = d_rot;
+        a.acc_out = d_acc_out;
+        a.count = count;
+        int per_sm = 0;
+        ck(yg::crt_blind_rotate_ctas_per_sm(key->logN, key->n, &per_sm) == 0 ? cudaSuccess : cudaErrorInvalidValue,
+           "ApproxCRT occupancy");
+        if (per_sm < 1) throw std::invalid_argument("ApproxCRT blind rotation does not fit an SM");
+        const int grid = std::min(count, per_sm * key->sm_count);
+        yg::check_launch(yg::launch_crt_blind_rotate(key->logN, a, grid, stream), "ApproxCRT blind rotation");
+        return YG_OK;
+    });
+}
+
+size_t yg_crt_key_device_bytes(const yg_crt_key* key) { return key ? key->key_bytes : 0; }
+
+void yg_crt_key_destroy(yg_crt_key* key) {
+    if (!key) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(key->device);
+    if (key->d_tw) cudaFree(key->d_tw);
+    if (key->d_key) cudaFree(key->d_key);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete key;
 }
 
 int yg_key_set_ksk(yg_key* key, const int32_t* h_ksk) {

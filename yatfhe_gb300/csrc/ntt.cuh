@@ -21,7 +21,7 @@
 // register stages (+ the shuffle stage at N = 2048).  Inverse mirrors it.  Pointwise
 // products happen in the slot layout, so the key is stored in that layout.
 //
-// Prime set 1 (the 32-bit torus, p < 2^26.48) runs every stage on biased values (rns.cuh,
+// Prime sets 1 and 2 (p < 2^26.48) run every stage on biased values (rns.cuh,
 // ct_bfly_b): the forward input carries an offset of at least 2p per stage (fwd_bias_*), so
 // no butterfly wraps and none reduces; outputs stay below 46p.  Its inverse at N = 1024 is
 // a Cooley-Tukey (decimation-in-time) transform too: on bit-reversed slots with
@@ -78,10 +78,10 @@ __device__ __forceinline__ void team_sync(int bar) {
 // (signed digits |d| < p: one more p), so the biased butterflies never wrap; prime set 0:
 // p, which makes signed digits non-negative.
 template <int LOGN, int PS>
-__device__ __forceinline__ uint32_t fwd_bias_digits(uint32_t p) { return PS == 1 ? (2 * LOGN + 1) * p : p; }
+__device__ __forceinline__ uint32_t fwd_bias_digits(uint32_t p) { return PS != 0 ? (2 * LOGN + 1) * p : p; }
 // The same for residues already in [0, p).
 template <int LOGN, int PS>
-__device__ __forceinline__ uint32_t fwd_bias_residues(uint32_t p) { return PS == 1 ? 2 * LOGN * p : 0; }
+__device__ __forceinline__ uint32_t fwd_bias_residues(uint32_t p) { return PS != 0 ? 2 * LOGN * p : 0; }
 
 template <int LOGN>
 __device__ __forceinline__ int slot_pos(int tt, int r) {
@@ -113,7 +113,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
     const uint32_t neg_p = 0u - p;
     if constexpr (TAB) {
         // prime set 1: offset 2p for each of the LOGN - 1 stages left, and p for t < p
-        const uint32_t bx = PS == 1 ? 2 * LOGN * p : p, by = PS == 1 ? 2 * LOGN * p : 3 * p;
+        const uint32_t bx = PS != 0 ? 2 * LOGN * p : p, by = PS != 0 ? 2 * LOGN * p : 3 * p;
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
             const int dx = (int)a[r], dy = (int)a[r + 16];
@@ -136,7 +136,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
             const uint2 w = c_tw_head[PS][LOGN - 10][team][0][(1 << (4 - sp)) + (r >> (sp + 1))];
-            if constexpr (PS == 1) ct_bfly_b(a[r], a[r + h], w, neg_p);
+            if constexpr (PS != 0) ct_bfly_b(a[r], a[r + h], w, neg_p);
             else ct_bfly(a[r], a[r + h], w, p, two_p, sp == 1);
         }
     }
@@ -155,7 +155,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
         for (int r = 0; r < 32; ++r) {
             if (r & h) continue;
             const uint2 w = __ldg(&tw[(r >> (sp + 1)) * 32]);
-            if constexpr (PS == 1) ct_bfly_b(a[r], a[r + h], w, neg_p);
+            if constexpr (PS != 0) ct_bfly_b(a[r], a[r + h], w, neg_p);
             else ct_bfly(a[r], a[r + h], w, p, two_p, (sp & 1) == 0);
         }
     }
@@ -173,7 +173,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
             uint32_t u = odd ? recv : a[k];
             uint32_t v = odd ? a[16 + k] : recv;
             const uint2 w = __ldg(&tw[k * 32]);
-            if constexpr (PS == 1) ct_bfly_b(u, v, w, neg_p);
+            if constexpr (PS != 0) ct_bfly_b(u, v, w, neg_p);
             else ct_bfly(u, v, w, p, two_p, true);
             a[k] = u;
             a[16 + k] = v;

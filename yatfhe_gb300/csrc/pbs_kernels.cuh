@@ -156,6 +156,29 @@ struct EncryptRlweArgs {
     int* bad;               // set to 1 when a mask word is not reduced mod q (may be null)
 };
 int launch_encrypt_rlwe_ntt(const EncryptRlweArgs& a, void* stream);
+// Approximate-CRT blind rotation (crt_kernels.cu): four residue primes, two high digits.
+constexpr int kCrtD = 4, kCrtDh = 2;
+struct CrtKeyConvArgs {
+    const int8_t* bsk8;      // [n][d][dh][2 rows][2 polys][N] residues (int8, centred mod q_d)
+    uint32_t* key;           // [n][d][dh][2 rows] blocks of key_block_words(N)
+    Chan ch;                 // prime set 2
+    uint32_t scale, scale_s; // N^-1 2^32 mod p, Shoup companion
+    int rows;                // n d dh 2
+};
+struct CrtBrArgs {
+    const uint32_t* key;
+    Chan ch;
+    const int32_t* acc_in;   // [count][2][N] torus values mod Q_CRT
+    const int32_t* rot;      // [count][n] rotation amounts
+    int32_t* acc_out;        // [count][2][N]
+    int64_t tao_u[kCrtD], tao_u_inv[kCrtD], z[kCrtD], q_crt;
+    int count, n;
+};
+size_t crt_br_smem_bytes(int N, int n);
+int set_crt_twiddle_heads(int logN, const uint2* heads);
+int launch_crt_keyconv(int logN, const CrtKeyConvArgs& a, void* stream);
+int launch_crt_blind_rotate(int logN, const CrtBrArgs& a, int grid, void* stream);
+int crt_blind_rotate_ctas_per_sm(int logN, int n, int* out);
 int launch_draw(const DrawArgs& a, void* stream);
 int launch_encrypt_lwe(const EncryptArgs& a, void* stream);
 

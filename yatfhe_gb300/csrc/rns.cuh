@@ -23,9 +23,14 @@ constexpr int kChannels = 3;
 //          32 bits, so both transforms run on biased values without any reduction (ntt.cuh:
 //          an input offset by 2p per remaining stage keeps x - r >= 0, and 11 stages of
 //          growth by < 2p stay below 46p).
-constexpr int kPrimeSets = 2;
+//   set 2: the single 24-bit prime 2^24 - 2^14 + 1 (NttNative24's modulus) in every channel
+//          slot, for the approximate-CRT blind rotation, whose products are taken mod that
+//          prime itself; biased transforms as in set 1.
+constexpr int kPrimeSets = 3;
+constexpr uint32_t kMod24 = (1u << 24) - (1u << 14) + 1;
 constexpr uint32_t kPrimeSet[kPrimeSets][kChannels] = {{536813569u, 536690689u, 536641537u},
-                                                       {93356033u, 93290497u, 93192193u}};
+                                                       {93356033u, 93290497u, 93192193u},
+                                                       {kMod24, kMod24, kMod24}};
 __host__ __device__ constexpr int prime_set_for(int torus_bits) { return torus_bits == 32 ? 1 : 0; }
 
 // Per-channel constants the kernels read.
