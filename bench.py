@@ -16,7 +16,7 @@ carries the plain per-call form, a batch-size sweep and the other workloads unde
 in one CUDA graph, and the 128-tenant serving trace (p50/p99 at 50-100 % of peak).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--params t32_n1024|t56_n2048]
-                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving|serving_lazy|encrypt]
+                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving|serving_lazy|encrypt|crt]
 Multi-GPU: one process per GPU (torchrun); every rank bootstraps its own batch (weak
 scaling, no data-path collective).
 """
@@ -54,7 +54,7 @@ def parse_args():
     ap.add_argument("--count", type=int, default=0, help="ciphertexts per step (default 65536 / 16384)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving", "serving_lazy",
-                                                                  "encrypt"])
+                                                                  "encrypt", "crt"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-call / sweep legs and other workloads")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
@@ -599,6 +599,70 @@ def leg_keygen(dev, reps=3):
             "sample_host_bytes": int(sum(v.nbytes for v in smp.values()))}
 
 
+def crt_ops_per_rotation(n, N):
+    """Multiply-class 32-bit operations of one approximate-CRT blind rotation: per CMux step 16
+    forward and 8 inverse transforms of (N/2) log2 N butterflies and 32 N key products, 3
+    operations per modular product (one 24-bit channel, Shoup or Montgomery)."""
+    lg = int(np.log2(N))
+    return 3 * n * (24 * (N // 2) * lg + 32 * N)
+
+
+def leg_crt(dev, count=2432, steps=3, warmup=1, cpu_sample=2):
+    """The approximate-CRT blind rotation (blindRotateApproxCRTNtt with decompTrlweMcrt before
+    and trlweMcrtToCrt + recompTrlweCrt after) at the reference's default size, n = 680,
+    N = 2048 on the torus Q_CRT: seeded synthetic residue keys (uniform centred residues, the
+    value range of real ones) and samples, `count` rotations per step timed with CUDA events on
+    the launching stream; the CPU restatement on a `cpu_sample`-rotation sample (one thread)
+    checks the sample bit for bit."""
+    import torch
+
+    from oracle.oracle import CRT_Q, crt_blind_rotate
+    from yatfhe_gb300 import api
+
+    n, N = 680, 2048
+    rng = np.random.default_rng(0x5EED0015)
+    bsk8 = np.empty((n, 4, 2, 2, 2, N), np.int8)
+    for d, q in enumerate((251, 241, 239, 233)):
+        bsk8[:, d] = rng.integers(-(q // 2), q // 2 + 1, size=bsk8[:, d].shape)
+    t0 = time.perf_counter()
+    key = api.CrtKey(bsk8, dev)
+    upload_s = time.perf_counter() - t0
+    cuda = f"cuda:{dev}"
+    acc = rng.integers(-(CRT_Q // 2), CRT_Q // 2 + 1, size=(count, 2, N)).astype(np.int32)
+    rot = rng.integers(0, 2 * N, size=(count, n)).astype(np.int32)
+    d_acc, d_rot = torch.from_numpy(acc).to(cuda), torch.from_numpy(rot).to(cuda)
+    d_out = torch.empty_like(d_acc)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            key.blind_rotate(d_acc, d_rot, out=d_out, stream=stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        stream.synchronize()
+        ev[0].record(stream)
+        for _ in range(steps):
+            key.blind_rotate(d_acc, d_rot, out=d_out, stream=stream)
+        ev[1].record(stream)
+        stream.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    value = count / (ms / 1e3)
+    ops = crt_ops_per_rotation(n, N)
+    peak = int32_peak(dev)
+    out = d_out.cpu().numpy()
+    t0 = time.perf_counter()
+    same = all(np.array_equal(crt_blind_rotate(bsk8, acc[c], rot[c])[0], out[c]) for c in range(cpu_sample))
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"crt_n{n}_n{N}_batch{count}", "rotations_per_s": value, "ms_per_step": ms,
+            "key_upload_s": upload_s, "key_device_bytes": key.device_bytes,
+            "roofline": {"bound": "int32", "kernel": "crt_blind_rotate_kernel", "ops_per_rotation": ops,
+                         "achieved": ops * value / 1e12, "peak": peak, "unit": "TOP/s",
+                         "frac": ops * value / 1e12 / peak,
+                         "peak_source": "measured: yg_probe_int32_rate (32-bit IMAD chains, all SMs)"},
+            "cpu_baseline": {"value": cpu_sample / cpu_s, "unit": "rotations/s", "cores": 1, "kind": "port",
+                             "sample": f"{cpu_sample} of the step's rotations, restatement of "
+                                       "blindRotateApproxCRTNtt (one thread)"},
+            "sample_bit_exact": bool(same)}
+
+
 def leg_encrypt(dev, count=1 << 20, steps=5, warmup=3, cpu_sample=20000):
     """symEncTlwe on the GPU for the TORUS=32 set (n=630): `count` messages per step encrypted
     by yg_encrypt_lwe (masks and TUniform(2^18) noise drawn by ChaCha20 in the kernel) and by
@@ -980,6 +1044,14 @@ def main():
                     "config": {"workload": r["workload"]}, "result": r}
             print(json.dumps(line))
             return
+        if args.workload == "crt":
+            r = leg_crt(dev)
+            line = {"metric": "approximate-CRT blind rotations per second", "value": r["rotations_per_s"],
+                    "unit": "rotations/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "int8 residues / u32 mod 2^24-2^14+1", "data": "synthetic",
+                    "config": {"workload": r["workload"]}, "result": r}
+            print(json.dumps(line))
+            return
         if args.workload == "encrypt":
             r = leg_encrypt(dev)
             line = {"metric": "LWE encryptions per second", "value": r["encrypt_drawn"]["ciphertexts_per_s"],
@@ -1117,6 +1189,7 @@ def main():
             "wwl24_t32_n2048_batch16384": _safe(leg_wwl24, dev),
             "keygen_t32_n1024": _safe(leg_keygen, dev),
             "encrypt_t32_n630_batch1048576": _safe(leg_encrypt, dev),
+            "crt_n680_n2048_batch2432": _safe(leg_crt, dev),
             "lazy_t32_n2048_batch1216": _safe(leg_lazy, dev),
             "group2_t32_n1024_batch9728": _safe(leg_group, dev, 2),
             "group3_t32_n1024_batch9728": _safe(leg_group, dev, 3),

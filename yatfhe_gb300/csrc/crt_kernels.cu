@@ -85,8 +85,10 @@ __global__ void __launch_bounds__(2 * TeamShape<LOGN>::S) crt_keyconv_kernel(con
     }
 }
 
+// Two CTAs per SM (a register cap of 128 at N = 2048): measured 10.1 k against 7.4 k rotations/s
+// with one CTA of 211 registers (n = 680, N = 2048, 1,216 ciphertexts, outputs identical).
 template <int LOGN>
-__global__ void __launch_bounds__(kCrtD * TeamShape<LOGN>::S) crt_blind_rotate_kernel(const CrtBrArgs a) {
+__global__ void __launch_bounds__(kCrtD * TeamShape<LOGN>::S, 2) crt_blind_rotate_kernel(const CrtBrArgs a) {
     using Sh = TeamShape<LOGN>;
     constexpr int N = Sh::N, S = Sh::S, T = kCrtD * S;
     extern __shared__ __align__(16) unsigned char smem[];
