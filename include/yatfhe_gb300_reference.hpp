@@ -25,6 +25,7 @@
 //   blindRotateNtt                 yatfhe/include/yatfhe/blind_rotate.h:13 (groups 1-3)
 //   functionalBootstrappingNtt     yatfhe/include/yatfhe/bootstrapping.h:366-367
 //   switchKeyForTlwe               yatfhe/include/yatfhe/keyswitching.h:48
+//   blindRotateApproxCRTNtt        yatfhe/include/yatfhe/blind_rotate.h:18-19
 // plus a batched form of the first, which the reference does not have.
 #ifndef YATFHE_GB300_REFERENCE_HPP
 #define YATFHE_GB300_REFERENCE_HPP
@@ -42,6 +43,7 @@
 
 #include "yatfhe_gb300.h"
 #include "yautil/ya_serializer.h"  // deserializeBskLazyPipeAlt, for blindRotateLazyPipeAltInitNtt
+#include "yatfhe/ntt24.h"          // NttNative24::applyIntt, for blindRotateApproxCRTNtt's key
 
 namespace yatfhe_gb300 {
 
@@ -65,13 +67,20 @@ struct CachedKey {
     uint64_t ksk_fp = 0;
 };
 
+struct CachedCrtKey {
+    yg_crt_key* key = nullptr;
+    uint64_t fp = 0;
+};
+
 struct Registry {
     std::mutex mu;
     std::map<std::tuple<int, int, int, int, int, int, int, int>, yg_ctx*> ctxs;
     std::map<const void*, CachedKey> keys;  // key object address -> device key
+    std::map<const void*, CachedCrtKey> crt_keys;  // BootstrappingKeyCRT::bskCRT address -> device key
 
     ~Registry() {
         for (auto& k : keys) yg_key_destroy(k.second.key);
+        for (auto& k : crt_keys) yg_crt_key_destroy(k.second.key);
         for (auto& c : ctxs) yg_ctx_destroy(c.second);
     }
 };
@@ -295,6 +304,8 @@ inline void forgetKeys() {
     std::lock_guard<std::mutex> g(r.mu);
     for (auto& k : r.keys) yg_key_destroy(k.second.key);
     r.keys.clear();
+    for (auto& k : r.crt_keys) yg_crt_key_destroy(k.second.key);
+    r.crt_keys.clear();
 }
 
 // Batched functionalBootstrappingMPNtt: out[i] = PBS(in[i]) under one key, one launch.
@@ -483,6 +494,101 @@ inline void blindRotateLazyPipeAltNoFirstNtt(Trlwe& accum, const BootstrappingKe
 inline void blindRotateJP22Ntt(Trlwe& accum, const BootstrappingKeyMP& bsk, const ScaledTlwe& input,
                                const YatfheParameters& param) {
     yatfhe_gb300::blindRotateMP21Ntt(accum, bsk.bskDft, input, param);
+}
+
+namespace detail {
+
+// BootstrappingKeyCRT::bskCRT (yatfhe/include/yatfhe/bootstrapping.h:351-361) -> the residue rows
+// [n][d][dh][k+1][k+1][N] (int8) the device key is made from: the reference's inverse NTT24 with
+// the reduction mod q_d (NttNative24::applyIntt) returns the rows the NTT24 forms were made of.
+inline std::vector<int8_t> flatten_crt(const std::vector<std::vector<TrgswDft24>>& bskCRT, const YatfheParameters& p) {
+    const int N = p.N, k = p.k;
+    std::vector<int8_t> out;
+    out.reserve(bskCRT.size() * p.d * p.dh * (k + 1) * (k + 1) * (size_t)N);
+    Int8Polynomial poly{N};
+    for (const auto& perPrime : bskCRT) {
+        if ((int)perPrime.size() != p.d) throw std::invalid_argument("bskCRT: one TrgswDft24 per prime");
+        for (int d = 0; d < p.d; d++) {
+            const TrgswDft24& t = perPrime[d];
+            if (t.l < p.dh) throw std::invalid_argument("bskCRT: fewer levels than dh");
+            for (int l = 0; l < p.dh; l++)
+                for (int r = 0; r <= k; r++) {
+                    const auto& row = t.trlweDftSamples[l][r];
+                    for (int c = 0; c <= k; c++) {
+                        NttNative24::applyIntt(poly, c < k ? row.a[c] : row.b, p.qd[d]);
+                        out.insert(out.end(), poly.coeffs.begin(), poly.coeffs.end());
+                    }
+                }
+        }
+    }
+    return out;
+}
+
+inline uint64_t fingerprint(const std::vector<std::vector<TrgswDft24>>& bskCRT) {
+    uint64_t h = mix(0x43525400ULL, bskCRT.size());
+    for (size_t i : probes(bskCRT))
+        for (const auto& t : bskCRT[i]) {
+            h = mix(h, t.trlweDftSamples.size());
+            for (const auto& lvl : t.trlweDftSamples)
+                for (const auto& row : lvl) {
+                    h = mix_poly(h, row.b);
+                    for (const auto& a : row.a) h = mix_poly(h, a);
+                }
+        }
+    return h;
+}
+
+}  // namespace detail
+
+// blindRotateApproxCRTNtt: accum (d residue samples, as decompTrlweMcrt leaves them) rotated in
+// place.  The samples go to torus values mod Q_CRT (trlweMcrtToCrt + recompTrlweCrt on a copy)
+// and come back by decompTrlweMcrt; on centred residues the two conversions invert each other,
+// and the GPU entry point applies the same pair around the rotation.
+inline void blindRotateApproxCRTNtt(std::vector<Trlwe8>& accum, const std::vector<std::vector<TrgswDft24>>& bskCRT,
+                                    const ScaledTlwe& input, const YatfheParameters& param) {
+    if (param.k != 1) throw std::invalid_argument("blindRotateApproxCRTNtt: k = 1 only");
+    if ((int)accum.size() != param.d) throw std::invalid_argument("blindRotateApproxCRTNtt: one Trlwe8 per prime");
+    if ((int)bskCRT.size() < input.n || input.n != param.n)
+        throw std::invalid_argument("blindRotateApproxCRTNtt: key and input sizes differ");
+    const int N = param.N;
+    yg_crt_key* key = nullptr;
+    {
+        auto& r = detail::reg();
+        std::lock_guard<std::mutex> g(r.mu);
+        const uint64_t fp = detail::fingerprint(bskCRT);
+        auto it = r.crt_keys.find(&bskCRT);
+        if (it != r.crt_keys.end() && it->second.fp != fp) {
+            yg_crt_key_destroy(it->second.key);
+            r.crt_keys.erase(it);
+            it = r.crt_keys.end();
+        }
+        if (it == r.crt_keys.end()) {
+            const std::vector<int8_t> rows = detail::flatten_crt(bskCRT, param);
+            yg_crt_key* k = nullptr;
+            detail::check(yg_crt_key_upload(0, param.n, N, rows.data(), &k));
+            it = r.crt_keys.emplace(&bskCRT, detail::CachedCrtKey{k, fp}).first;
+        }
+        key = it->second.key;
+    }
+    std::vector<Trlwe8> tmp = accum;
+    trlweMcrtToCrt(tmp, param);
+    Trlwe t{param.k, N};
+    recompTrlweCrt(t, tmp, param);
+    std::vector<int32_t> acc(2 * (size_t)N), rot(input.a.begin(), input.a.begin() + param.n);
+    for (int j = 0; j < N; j++) {
+        acc[j] = static_cast<int32_t>(t.a[0].coeffs[j]);
+        acc[N + j] = static_cast<int32_t>(t.b.coeffs[j]);
+    }
+    detail::DeviceBuf<int32_t> d_acc(acc.size()), d_rot(rot.size()), d_out(acc.size());
+    detail::cuda(cudaMemcpy(d_acc.p, acc.data(), acc.size() * 4, cudaMemcpyHostToDevice));
+    detail::cuda(cudaMemcpy(d_rot.p, rot.data(), rot.size() * 4, cudaMemcpyHostToDevice));
+    detail::check(yg_crt_blind_rotate(key, d_acc.p, d_rot.p, 1, d_out.p, nullptr));
+    detail::cuda(cudaMemcpy(acc.data(), d_out.p, acc.size() * 4, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < N; j++) {
+        t.a[0].coeffs[j] = static_cast<Torus>(acc[j]);
+        t.b.coeffs[j] = static_cast<Torus>(acc[N + j]);
+    }
+    decompTrlweMcrt(accum, t, param);
 }
 
 inline void switchKeyForTlwe(Tlwe& output, const TlweKeySwitchingKey& ksk, const Tlwe& input,

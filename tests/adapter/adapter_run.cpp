@@ -16,11 +16,13 @@
 #include "yatfhe/polynomial.h"
 #include "yatfhe/tlwe.h"
 #include "yatfhe/trlwe.h"
+#include "yatfhe/trgsw.h"
 #include "yautil/initializer.h"
 #include "yatfhe_gb300_reference.hpp"
 
 extern "C" void yg_test_use_params(const YatfheParameters* p);
 extern "C" int yg_test_uploads(void);
+extern "C" int yg_test_crt_uploads(void);
 
 namespace {
 
@@ -139,6 +141,49 @@ int main() {
 
     yatfhe_gb300::forgetKeys();
     bsk->~BootstrappingKeyMP();
+
+    // blindRotateApproxCRTNtt in the setting of the reference's BLIND_ROT_APPROX_CRT_NTT test
+    // (google_tests/blindrot_test.cpp:574-640): the torus Q_CRT, its own key generation and
+    // encryption; param.l = dh keeps encryptTrgswApproxCRT inside its gadget vector
+    {
+        YatfheParameters cp{};
+        cp.q = Q_CRT;
+        cp.n = 12;
+        cp.l = cp.dh;
+        initYatfhe(cp);
+        yg_test_use_params(&cp);
+        TlweKey lk{cp.n};
+        TrgswKey tk{cp};
+        genTlweKey(lk);
+        genTrlweKey(tk.trlweKey);
+        BootstrappingKeyCRT crtKey{cp};
+        genBootstrappingKeyApproxCrt(crtKey, tk, lk, cp);
+        std::vector<Torus> mu(cp.N);
+        for (int j = 0; j < cp.N; j++) mu[j] = modSwitchToTorus32(j % cp.torusBase - cp.torusBase / 2, cp.torusBase);
+        Trlwe in{cp.k, cp.N};
+        symEncTrlweMultiSample(in, tk.trlweKey, mu);
+        ScaledTlwe s{2 * cp.N, cp.n};
+        for (int i = 0; i < cp.n; i++) s.a[i] = (i * 577 + 13) % (4 * cp.N) - 2 * cp.N;
+        s.a[3] = 0;
+        std::vector<Trlwe8> want(cp.d, Trlwe8{cp.k, cp.N});
+        decompTrlweMcrt(want, in, cp);
+        std::vector<Trlwe8> got = want;
+        ::blindRotateApproxCRTNtt(want, crtKey.bskCRT, s, cp);
+        const int before = yg_test_crt_uploads();
+        yatfhe_gb300::blindRotateApproxCRTNtt(got, crtKey.bskCRT, s, cp);
+        auto same8 = [&](const std::vector<Trlwe8>& x, const std::vector<Trlwe8>& y) {
+            for (int d = 0; d < cp.d; d++)
+                if (x[d].a[0].coeffs != y[d].a[0].coeffs || x[d].b.coeffs != y[d].b.coeffs) return false;
+            return true;
+        };
+        expect(same8(want, got), "blindRotateApproxCRTNtt equals the reference's");
+        std::vector<Trlwe8> again(cp.d, Trlwe8{cp.k, cp.N});
+        decompTrlweMcrt(again, in, cp);
+        yatfhe_gb300::blindRotateApproxCRTNtt(again, crtKey.bskCRT, s, cp);
+        expect(same8(want, again) && yg_test_crt_uploads() == before + 1,
+               "blindRotateApproxCRTNtt converts its key once");
+        yatfhe_gb300::forgetKeys();
+    }
     std::printf("%d failure(s)\n", failures);
     return failures ? 1 : 0;
 }

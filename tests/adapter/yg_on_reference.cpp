@@ -18,6 +18,7 @@
 #include "yatfhe/blind_rotate.h"
 #include "yatfhe/bootstrapping.h"
 #include "yatfhe/keyswitching.h"
+#include "yatfhe/ntt24.h"
 #include "yatfhe/tlwe.h"
 #include "yatfhe/trlwe.h"
 #include "yatfhe_gb300.h"
@@ -31,11 +32,16 @@ struct yg_key {
     std::unique_ptr<TlweKeySwitchingKey> ksk;
 };
 
+struct yg_crt_key {
+    std::unique_ptr<BootstrappingKeyCRT> bsk;
+};
+
 namespace {
 
 const YatfheParameters* g_param = nullptr;
 thread_local std::string g_err;
 int g_uploads = 0;  // GINX key uploads (the driver checks the adapter's key cache with it)
+int g_crt_uploads = 0;
 
 int fail(int rc, const std::string& what) {
     g_err = what;
@@ -49,6 +55,7 @@ extern "C" {
 // the process-wide parameters the reference functions run with (the driver's initYatfhe)
 void yg_test_use_params(const YatfheParameters* p) { g_param = p; }
 int yg_test_uploads(void) { return g_uploads; }
+int yg_test_crt_uploads(void) { return g_crt_uploads; }
 
 const char* yg_last_error(void) { return g_err.c_str(); }
 
@@ -162,6 +169,61 @@ int yg_keyswitch(yg_ctx*, const yg_key* key, const int32_t* big, int32_t* out, i
     }
     return YG_OK;
 }
+
+// residue rows [n][d][dh][k+1][k+1][N] -> BootstrappingKeyCRT (bsk8 and its NTT24 forms)
+int yg_crt_key_upload(int device, int n, int N, const int8_t* h, yg_crt_key** out) {
+    const YatfheParameters& p = *g_param;
+    if (device != 0 || n != p.n || N != p.N) return fail(YG_ERR_INVALID, "ApproxCRT key shape");
+    auto key = std::make_unique<yg_crt_key>();
+    key->bsk = std::make_unique<BootstrappingKeyCRT>(p);
+    size_t o = 0;
+    for (int i = 0; i < p.n; i++)
+        for (int d = 0; d < p.d; d++) {
+            for (int l = 0; l < p.dh; l++)
+                for (int r = 0; r <= p.k; r++) {
+                    Trlwe8& t = key->bsk->bsk8[i][d].trlweSamples[l][r];
+                    for (int c = 0; c <= p.k; c++) {
+                        Int8Polynomial& P = c < p.k ? t.a[c] : t.b;
+                        std::memcpy(P.coeffs.data(), h + o, p.N);
+                        o += p.N;
+                    }
+                }
+            NttNative24::applyNttForRgsw(key->bsk->bskCRT[i][d], key->bsk->bsk8[i][d]);
+        }
+    g_crt_uploads++;
+    *out = key.release();
+    return YG_OK;
+}
+
+// decompTrlweMcrt, blindRotateApproxCRTNtt, trlweMcrtToCrt, recompTrlweCrt per ciphertext
+int yg_crt_blind_rotate(yg_crt_key* key, const int32_t* in, const int32_t* rot, int count, int32_t* out, void*) {
+    const YatfheParameters& p = *g_param;
+    const int N = p.N;
+    for (int c = 0; c < count; c++) {
+        Trlwe t{p.k, N};
+        const int32_t* w = in + static_cast<size_t>(c) * 2 * N;
+        for (int j = 0; j < N; j++) {
+            t.a[0].coeffs[j] = static_cast<Torus>(w[j]);
+            t.b.coeffs[j] = static_cast<Torus>(w[N + j]);
+        }
+        ScaledTlwe s{2 * N, p.n};
+        for (int i = 0; i < p.n; i++) s.a[i] = rot[static_cast<size_t>(c) * p.n + i];
+        std::vector<Trlwe8> acc(p.d, Trlwe8{p.k, N});
+        decompTrlweMcrt(acc, t, p);
+        blindRotateApproxCRTNtt(acc, key->bsk->bskCRT, s, p);
+        trlweMcrtToCrt(acc, p);
+        Trlwe r{p.k, N};
+        recompTrlweCrt(r, acc, p);
+        int32_t* o = out + static_cast<size_t>(c) * 2 * N;
+        for (int j = 0; j < N; j++) {
+            o[j] = static_cast<int32_t>(r.a[0].coeffs[j]);
+            o[N + j] = static_cast<int32_t>(r.b.coeffs[j]);
+        }
+    }
+    return YG_OK;
+}
+
+void yg_crt_key_destroy(yg_crt_key* key) { delete key; }
 
 // "device" memory of this stand-in: host memory
 cudaError_t cudaMalloc(void** p, size_t n) {

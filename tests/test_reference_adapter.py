@@ -22,7 +22,8 @@ void use(Tlwe& out, const Tlwe& in, const BootstrappingKeyMP& bsk, const TlweKey
          const TorusPolynomial& v, const YatfheParameters& p, Trlwe& acc, const ScaledTlwe& s,
          std::vector<Tlwe>& outs, const std::vector<Tlwe>& ins, const BootstrappingKeyWWL24& wwl,
          const BootstrappingKeyMPLazyPipeAlt& lazy, const std::vector<NttPolynomial>& gdV,
-         const BootstrappingKey& gbsk, BootstrappingKeyMPLazyPipeAlt& lazy2) {
+         const BootstrappingKey& gbsk, BootstrappingKeyMPLazyPipeAlt& lazy2, std::vector<Trlwe8>& acc8,
+         const BootstrappingKeyCRT& crt) {
     yatfhe_gb300::functionalBootstrappingMPNtt(out, in, bsk, ksk, v, p);
     yatfhe_gb300::functionalBootstrappingMPNttBatch(outs, ins, bsk, ksk, v, p);
     yatfhe_gb300::blindRotateMP21Ntt(acc, bsk.bskDft, s, p);
@@ -35,6 +36,7 @@ void use(Tlwe& out, const Tlwe& in, const BootstrappingKeyMP& bsk, const TlweKey
     yatfhe_gb300::blindRotateNtt(acc, gbsk.bskDft, s, p);
     yatfhe_gb300::functionalBootstrappingNtt(out, in, gbsk, ksk, v, p);
     yatfhe_gb300::switchKeyForTlwe(out, ksk, in, p);
+    yatfhe_gb300::blindRotateApproxCRTNtt(acc8, crt.bskCRT, s, p);
     yatfhe_gb300::forgetKeys();
 }
 """
@@ -59,7 +61,7 @@ def test_adapter_runs_against_the_reference(tmp_path):
     """The adapter run end to end in the shape of the reference's BOOTSTRAPPING.MP21 test
     (google_tests/bootstrappping_test.cpp:83-131): tests/adapter/adapter_run.cpp calls
     yatfhe_gb300::functionalBootstrappingMPNtt (single and batched), blindRotateMP21Ntt,
-    blindRotateJP22Ntt and switchKeyForTlwe with the reference's own types and compares each
+    blindRotateJP22Ntt, switchKeyForTlwe and blindRotateApproxCRTNtt with the reference's own types and compares each
     result with the reference function itself on the same objects.  Below the adapter, the
     C ABI is a CPU stand-in built on the reference's functions (tests/adapter/yg_on_reference.cpp),
     so any error in the adapter's conversions changes a result; the GPU side of that ABI is
