@@ -457,13 +457,18 @@ inline void blindRotateLazyPipeAltNttSweep(Trlwe& accum, const BootstrappingKeyM
                                            const ScaledTlwe& input, const TorusPolynomial& v,
                                            const std::vector<NttPolynomial>& gdVntt, int moveNtt, int unitsA,
                                            const YatfheParameters& param) {
-    (void)moveNtt;
-    (void)unitsA;
+    // the splits only shape the reference's CPU pipeline (every split gives the same result);
+    // the reference sizes its buffers by them, so non-positive ones are refused here
+    if (moveNtt < 1 || unitsA < 1)
+        throw std::invalid_argument("blindRotateLazyPipeAltNttSweep: moveNtt and unitsA must be >= 1");
     yatfhe_gb300::blindRotateLazyPipeAltNtt(accum, bsk, input, v, gdVntt, param);
 }
 
 // blindRotateLazyPipeAltInitNtt: the key read from fileName into bsk (the reference reads it
-// while it rotates), then the same rotation on the GPU.
+// while it rotates), then the same rotation on the GPU.  Like the reference, every call reads
+// the file; every call also uploads and converts the key again (about 45 MB at the default
+// T32 set), so a caller rotating many inputs under one file should read it once and call
+// blindRotateLazyPipeAltNtt.
 inline void blindRotateLazyPipeAltInitNtt(Trlwe& accum, BootstrappingKeyMPLazyPipeAlt& bsk, const ScaledTlwe& input,
                                           const TorusPolynomial& v, const std::string& fileName,
                                           const std::vector<NttPolynomial>& gdVntt, const YatfheParameters& param) {

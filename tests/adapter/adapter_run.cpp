@@ -5,6 +5,7 @@
 // objects.  Linked with the reference library built from its sources (oracle/_ref) and the
 // CPU stand-in of the C ABI (yg_on_reference.cpp).  Exit status 0 when everything matches.
 #include <cstdio>
+#include <string>
 #include <memory>
 #include <new>
 #include <vector>
@@ -18,6 +19,7 @@
 #include "yatfhe/trlwe.h"
 #include "yatfhe/trgsw.h"
 #include "yautil/initializer.h"
+#include "yautil/ya_serializer.h"
 #include "yatfhe_gb300_reference.hpp"
 
 extern "C" void yg_test_use_params(const YatfheParameters* p);
@@ -141,6 +143,61 @@ int main() {
 
     yatfhe_gb300::forgetKeys();
     bsk->~BootstrappingKeyMP();
+
+    // the lazy ("OURS") rotations on the reference's default T32 set with a small n: the adapter's
+    // blindRotateLazyPipeAltNtt, its Sweep, NoFirst and Init (file) forms against the reference's
+    {
+        YatfheParameters lp{};
+        lp.n = 16;
+        initYatfhe(lp);
+        yg_test_use_params(&lp);
+        TlweKey lk{lp.n};
+        TrgswKey tk{lp};
+        genTlweKey(lk);
+        genTrlweKey(tk.trlweKey);
+        BootstrappingKeyMPLazyPipeAlt lazy{lp, lp.lApprox, true};
+        for (int i = 0; i < lazy.n; i++) encryptTrgswMP(lazy.bskPrime[i], lk.s[i], tk, 0, lp);
+        symEncTrlevWithKeyNtt(lazy.s2Dft, tk.trlweKey, tk.trlweKey.s, true, lp);
+        TorusPolynomial lv{lp.N};
+        for (int j = 0; j < lp.N; j++) lv.coeffs[j] = static_cast<Torus>((j % 4) - 2) << 29;
+        Tlwe x{lp.n};
+        symEncTlwe(x, static_cast<Torus>(1) << 30, lk);
+        ScaledTlwe sc{2 * lp.N, lp.n};
+        rescaleTlweToNewMod(sc, x);
+        sc.a[2] = 0;  // a skipped step
+        std::vector<NttPolynomial> gdV;
+        prepareGdV(gdV, lv, lp);
+        Trlwe want{lp.k, lp.N}, got{lp.k, lp.N};
+        ::blindRotateLazyPipeAltNtt(want, lazy, sc, lv, gdV, lp);
+        const int up0 = yg_test_uploads();
+        yatfhe_gb300::blindRotateLazyPipeAltNtt(got, lazy, sc, lv, gdV, lp);
+        expect(same(want, got), "blindRotateLazyPipeAltNtt equals the reference's");
+        Trlwe sweep{lp.k, lp.N};
+        yatfhe_gb300::blindRotateLazyPipeAltNttSweep(sweep, lazy, sc, lv, gdV, 3, 1, lp);
+        expect(same(want, sweep) && yg_test_uploads() == up0 + 1, "Sweep form: same result, key converted once");
+        Trlwe nf{lp.k, lp.N}, nfRef{lp.k, lp.N};
+        ::blindRotateLazyPipeAltNoFirstNtt(nfRef, lazy, sc, lv, lp);
+        yatfhe_gb300::blindRotateLazyPipeAltNoFirstNtt(nf, lazy, sc, lv, lp);
+        expect(same(nfRef, nf), "blindRotateLazyPipeAltNoFirstNtt equals the reference's");
+        const std::string file = "adapter_run_lazy_key.bin";
+        serializeBskLazyPipeAlt(lazy, file);
+        BootstrappingKeyMPLazyPipeAlt holder{lp, lp.lApprox, true};
+        Trlwe init1{lp.k, lp.N}, init2{lp.k, lp.N};
+        const int up1 = yg_test_uploads();
+        yatfhe_gb300::blindRotateLazyPipeAltInitNtt(init1, holder, sc, lv, file, gdV, lp);
+        yatfhe_gb300::blindRotateLazyPipeAltInitNtt(init2, holder, sc, lv, file, gdV, lp);
+        expect(same(want, init1) && same(want, init2) && yg_test_uploads() == up1 + 2,
+               "InitNtt form: the key read from the file, uploaded again on each call");
+        bool refused = false;
+        try {
+            yatfhe_gb300::blindRotateLazyPipeAltNttSweep(sweep, lazy, sc, lv, gdV, 0, 1, lp);
+        } catch (const std::invalid_argument&) {
+            refused = true;
+        }
+        expect(refused, "Sweep form: moveNtt < 1 refused");
+        std::remove(file.c_str());
+        yatfhe_gb300::forgetKeys();
+    }
 
     // blindRotateApproxCRTNtt in the setting of the reference's BLIND_ROT_APPROX_CRT_NTT test
     // (google_tests/blindrot_test.cpp:574-640): the torus Q_CRT, its own key generation and

@@ -19,6 +19,7 @@
 #include "yatfhe/bootstrapping.h"
 #include "yatfhe/keyswitching.h"
 #include "yatfhe/ntt24.h"
+#include "yatfhe/trgsw.h"
 #include "yatfhe/tlwe.h"
 #include "yatfhe/trlwe.h"
 #include "yatfhe_gb300.h"
@@ -30,6 +31,7 @@ struct yg_ctx {
 struct yg_key {
     std::unique_ptr<BootstrappingKeyMP> bsk;
     std::unique_ptr<TlweKeySwitchingKey> ksk;
+    std::unique_ptr<BootstrappingKeyMPLazyPipeAlt> lazy;
 };
 
 struct yg_crt_key {
@@ -166,6 +168,60 @@ int yg_keyswitch(yg_ctx*, const yg_key* key, const int32_t* big, int32_t* out, i
         int32_t* o = out + static_cast<size_t>(c) * (p.n + 1);
         for (int i = 0; i < p.n; i++) o[i] = static_cast<int32_t>(y.a[i]);
         o[p.n] = static_cast<int32_t>(y.b);
+    }
+    return YG_OK;
+}
+
+// half rows [n][L][k+1][N] (torus values) + s2 key [Ls][k+1][N] (NTT words) ->
+// BootstrappingKeyMPLazyPipeAlt
+int yg_key_upload_lazy(yg_ctx* c, const int64_t* cprime, const uint64_t* s2, int s2_levels, yg_key** out) {
+    const YatfheParameters& p = *g_param;
+    if (s2_levels != p.l) return fail(YG_ERR_INVALID, "s2 levels");
+    auto key = std::make_unique<yg_key>();
+    key->lazy = std::make_unique<BootstrappingKeyMPLazyPipeAlt>(p, c->p.l_approx, true);
+    size_t o = 0;
+    for (auto& t : key->lazy->bskPrime)
+        for (int lvl = 0; lvl < c->p.l_approx; lvl++)
+            for (int poly = 0; poly <= p.k; poly++) {
+                TorusPolynomial& P = poly < p.k ? t.cPrime[lvl].a[poly] : t.cPrime[lvl].b;
+                for (int j = 0; j < p.N; j++) P.coeffs[j] = static_cast<Torus>(cprime[o++]);
+            }
+    o = 0;
+    for (auto& t : key->lazy->s2Dft.trlweDfts)
+        for (int poly = 0; poly <= p.k; poly++) {
+            NttPolynomial& P = poly < p.k ? t.a[poly] : t.b;
+            std::memcpy(P.coeffs.data(), s2 + o, sizeof(uint64_t) * p.N);
+            o += p.N;
+        }
+    g_uploads++;
+    *out = key.release();
+    return YG_OK;
+}
+
+// the whole blind rotation from the test polynomial (lazy keys: blindRotateLazyPipeAltNtt,
+// which builds its accumulator from v and the input itself)
+int yg_blind_rotate(yg_ctx*, const yg_key* key, const int32_t* in, const int64_t* lut, int64_t* acc, int count,
+                    int steps, void*) {
+    const YatfheParameters& p = *g_param;
+    if (!key->lazy || steps != p.n) return fail(YG_ERR_INVALID, "stand-in: lazy keys, whole rotations only");
+    const int n = p.n, N = p.N, k = p.k;
+    TorusPolynomial v{N};
+    for (int j = 0; j < N; j++) v.coeffs[j] = static_cast<Torus>(lut[j]);
+    std::vector<NttPolynomial> gdV;
+    prepareGdV(gdV, v, p);
+    for (int c = 0; c < count; c++) {
+        Tlwe x{n};
+        const int32_t* w = in + static_cast<size_t>(c) * (n + 1);
+        for (int i = 0; i < n; i++) x.a[i] = static_cast<LweTorus>(w[i]);
+        x.b = static_cast<LweTorus>(w[n]);
+        ScaledTlwe sc{2 * N, n};
+        rescaleTlweToNewMod(sc, x);
+        Trlwe a{k, N};
+        blindRotateLazyPipeAltNtt(a, *key->lazy, sc, v, gdV, p);
+        int64_t* o = acc + static_cast<size_t>(c) * (k + 1) * N;
+        for (int r = 0; r < k; r++)
+            for (int j = 0; j < N; j++) o[static_cast<size_t>(r) * N + j] = static_cast<int64_t>(a.a[r].coeffs[j]);
+        for (int j = 0; j < N; j++) o[static_cast<size_t>(k) * N + j] = static_cast<int64_t>(a.b.coeffs[j]);
     }
     return YG_OK;
 }

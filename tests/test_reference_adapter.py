@@ -61,7 +61,9 @@ def test_adapter_runs_against_the_reference(tmp_path):
     """The adapter run end to end in the shape of the reference's BOOTSTRAPPING.MP21 test
     (google_tests/bootstrappping_test.cpp:83-131): tests/adapter/adapter_run.cpp calls
     yatfhe_gb300::functionalBootstrappingMPNtt (single and batched), blindRotateMP21Ntt,
-    blindRotateJP22Ntt, switchKeyForTlwe and blindRotateApproxCRTNtt with the reference's own types and compares each
+    blindRotateJP22Ntt, switchKeyForTlwe, the lazy rotations (blindRotateLazyPipeAltNtt and its
+    Sweep, NoFirst and Init forms, the last reading a key file twice) and blindRotateApproxCRTNtt
+    with the reference's own types and compares each
     result with the reference function itself on the same objects.  Below the adapter, the
     C ABI is a CPU stand-in built on the reference's functions (tests/adapter/yg_on_reference.cpp),
     so any error in the adapter's conversions changes a result; the GPU side of that ABI is
@@ -80,7 +82,7 @@ def test_adapter_runs_against_the_reference(tmp_path):
            f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600,
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600, cwd=tmp_path,
                          env={**__import__("os").environ, "YATFHE_THREADS": "4"})
     assert run.returncode == 0, run.stdout + run.stderr
     assert "0 failure(s)" in run.stdout
