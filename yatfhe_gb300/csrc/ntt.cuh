@@ -38,6 +38,9 @@ namespace yg {
 
 __device__ __forceinline__ int tpad(int j) { return j + (j >> 5); }
 
+// words per digit-product table (ntt_forward TAB = 2): digits -64..64 at offset 64
+constexpr int kTab0WordsNtt = 132;
+
 // The per-thread twiddle addresses depend only on the thread, so the compiler would hoist
 // those loads out of the CMux loop and keep them live in registers across the whole step;
 // reading the table pointer through a volatile move inside each transform keeps the loads
@@ -101,17 +104,42 @@ __host__ __device__ __forceinline__ int slot_pos_out(int tt, int r) {
 
 // PS is the prime set (rns.cuh) of `ch`: it picks the constant-bank twiddles and the
 // reduction schedule of the forward transform.
-// TAB: the input holds signed digits d (|d| <= 64, as int32) instead of residues, and the
+// TAB = 1: the input holds signed digits d (|d| <= 64, as int32) instead of residues, and the
 // first stage (pairs j, j + N/2, twiddle psi^(N/2)) reads psi^(N/2) d mod p from `tab`
 // (indexed by d) instead of multiplying: x' = d_x + p + t, y' = d_x + 3p - t, both < 4p as
 // in the residue path.
-template <int LOGN, int PS, bool TAB = false>
+// TAB = 2 (prime set 1): the first two stages at once from five tables T_w[d] = w d mod p,
+// tab[t kTab0Words + d] for w = w1, w2, w1 w2, w3, w1 w3 (w1 = psi^brv(1), the first stage's
+// twiddle; w2, w3 = psi^brv(2), psi^brv(3), the second's): for the digits d0..d3 of registers
+// r, r + 8, r + 16, r + 24 (r < 8) the two stages give
+//   d0 + T1[d2] + T2[d1] + T12[d3],  d0 + T1[d2] - T2[d1] - T12[d3],
+//   d0 - T1[d2] + T3[d1] - T13[d3],  d0 - T1[d2] - T3[d1] + T13[d3]
+// on a (2 LOGN - 1) p offset (2p for each stage left): five lookups and no multiply for
+// four outputs, where the two radix-2 stages take two lookups and two Shoup products.
+template <int LOGN, int PS, int TAB = 0>
 __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int tt, int team, int bar, const Chan& ch,
                                             const uint32_t* tab = nullptr) {
     constexpr int S = TeamShape<LOGN>::S;
     const uint32_t p = ch.p, two_p = ch.two_p;
     const uint32_t neg_p = 0u - p;
-    if constexpr (TAB) {
+    if constexpr (TAB == 2) {
+        static_assert(PS == 1, "the two-stage tables are built for prime set 1");
+        constexpr int W = kTab0WordsNtt;
+        // offset (2 LOGN - 1) p: every output at least (2 LOGN - 4) p - 64, two p per stage left
+        const uint32_t boff = (2 * LOGN - 1) * p;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int d0 = (int)a[r], d1 = (int)a[r + 8], d2 = (int)a[r + 16], d3 = (int)a[r + 24];
+            const uint32_t t1 = tab[d2], t2 = tab[W + d1], t12 = tab[2 * W + d3];
+            const uint32_t t3 = tab[3 * W + d1], t13 = tab[4 * W + d3];
+            const uint32_t base = (uint32_t)d0 + boff;
+            const uint32_t hi = base + t1, lo = base - t1;
+            a[r] = hi + t2 + t12;
+            a[r + 8] = hi - t2 - t12;
+            a[r + 16] = lo + t3 - t13;
+            a[r + 24] = lo - t3 + t13;
+        }
+    } else if constexpr (TAB == 1) {
         // prime set 1: offset 2p for each of the LOGN - 1 stages left, and p for t < p
         const uint32_t bx = PS != 0 ? 2 * LOGN * p : p, by = PS != 0 ? 2 * LOGN * p : 3 * p;
 #pragma unroll
@@ -130,7 +158,7 @@ __device__ __forceinline__ void ntt_forward(uint32_t (&a)[32], uint32_t* tb, int
     // falls by less than 2p per stage and the value grows by less than 2p, so the output
     // stays below (4 LOGN + 1) p + 2^14 < 46p < 2^32.
 #pragma unroll
-    for (int sp = TAB ? 3 : 4; sp >= 0; --sp) {
+    for (int sp = TAB == 2 ? 2 : (TAB ? 3 : 4); sp >= 0; --sp) {
         const int h = 1 << sp;
 #pragma unroll
         for (int r = 0; r < 32; ++r) {

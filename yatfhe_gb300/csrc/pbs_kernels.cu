@@ -992,15 +992,21 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
     constexpr int DROWS = SPLIT ? 2 : digit_rows(T);
     int16_t* dig = reinterpret_cast<int16_t*>(acc + 2 * N);                     // [DROWS][L][N]
     int16_t* sa = dig + DROWS * L * N;                                           // [n+1]
-    // T = 32: first-stage product tables of the forward transforms, [3][kTab0Words]
+    // T = 32: the digit-product tables of the forward transforms' first two stages,
+    // [3][kTab0Tables][kTab0Words]: w d mod p for w = w1, w2, w1 w2, w3, w1 w3 (ntt.cuh, TAB = 2)
     uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
     const bool use_tab0 = T == 32 && a.radix_bits <= 7;
+    static_assert(kTab0Words == kTab0WordsNtt, "one table stride");
     if (use_tab0) {
-        for (int idx = ltid; idx < kChannels * (2 * kTab0Half + 1); idx += ST) {
-            const int c = idx / (2 * kTab0Half + 1), d = idx - c * (2 * kTab0Half + 1) - kTab0Half;
-            const uint32_t pc = pick_chan(a.ch, c).p;
-            const int64_t v = (int64_t)c_tw_head[PS][LOGN - 10][c][0][1].x * d % pc;
-            tab0[c * kTab0Words + kTab0Half + d] = (uint32_t)(v < 0 ? v + pc : v);
+        constexpr int D = 2 * kTab0Half + 1;
+        for (int idx = ltid; idx < kChannels * kTab0Tables * D; idx += ST) {
+            const int c = idx / (kTab0Tables * D), t = (idx / D) % kTab0Tables, d = idx % D - kTab0Half;
+            const int64_t pc = pick_chan(a.ch, c).p;
+            const int64_t w1 = c_tw_head[PS][LOGN - 10][c][0][1].x, w2 = c_tw_head[PS][LOGN - 10][c][0][2].x;
+            const int64_t w3 = c_tw_head[PS][LOGN - 10][c][0][3].x;
+            const int64_t w = t == 0 ? w1 : t == 1 ? w2 : t == 2 ? w1 * w2 % pc : t == 3 ? w3 : w1 * w3 % pc;
+            const int64_t v = w * d % pc;
+            tab0[(c * kTab0Tables + t) * kTab0Words + kTab0Half + d] = (uint32_t)(v < 0 ? v + pc : v);
         }
     }
     // the team's transpose region: region 0 of its channel (channel layout, the inverse
@@ -1013,7 +1019,7 @@ __global__ void __maxnreg__(kBrMaxRegs) blind_rotate_kernel(const BrArgs a) {
             if (use_tab0) {
 #pragma unroll
                 for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + tt];
-                ntt_forward<LOGN, PS, true>(x, mine, tt, team, bar, ch, tab0 + team * kTab0Words + kTab0Half);
+                ntt_forward<LOGN, PS, 2>(x, mine, tt, team, bar, ch, tab0 + team * kTab0Tables * kTab0Words + kTab0Half);
                 return;
             }
         }
@@ -1475,7 +1481,7 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         if (use_tab0) {
 #pragma unroll
             for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane];
-            ntt_forward<10, PS, true>(x, mine, lane, c, 0, ch, tab0 + c * 132 + 64);
+            ntt_forward<10, PS, 1>(x, mine, lane, c, 0, ch, tab0 + c * 132 + 64);
         } else {
             const uint32_t bias = fwd_bias_digits<10, PS>(ch.p);
 #pragma unroll

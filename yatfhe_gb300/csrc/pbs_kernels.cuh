@@ -292,6 +292,7 @@ constexpr int kClusterMaxLevels = 4;
 // psi_c^(N/2) d mod p_c for the digits d in [-64, 64] (radices up to 7), per channel.
 constexpr int kTab0Half = 64;
 constexpr int kTab0Words = 2 * kTab0Half + 4;  // 129 used
+constexpr int kTab0Tables = 5;                 // T1, T2, T12, T3, T13 per channel (ntt.cuh, TAB = 2)
 // Shared memory of one CTA of the row-cluster layout (N = 1024, T = 32): per team (channel,
 // level) a padded transpose region (also its partial sum after the products) and two
 // exchange regions the partner CTA writes into, the accumulator row, its digits, the mod-2N
@@ -317,7 +318,7 @@ __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n,
     b += 2 * N * (torus_bits == 32 ? 4 : 8);
     b += (size_t)(layout == kLayoutChannelRow ? 2 : digit_rows(torus_bits)) * L * N * 2;
     b += ((size_t)n + 1) * 2;
-    if (torus_bits == 32) b = ((b + 3) & ~(size_t)3) + (size_t)kChannels * kTab0Words * 4;
+    if (torus_bits == 32) b = ((b + 3) & ~(size_t)3) + (size_t)kChannels * kTab0Tables * kTab0Words * 4;
     return (b + 15) & ~(size_t)15;
 }
 // Uploads the first 32 forward and inverse twiddles of each channel of prime set ps
