@@ -68,3 +68,18 @@ def test_default_size_and_edges(built_lib):
     bad[0, 0, 0, 0, 0, 5] = -128
     with pytest.raises(Exception, match="outside"):
         api.CrtKey(bad)
+
+
+def test_persistent_grid_covers_every_ciphertext(built_lib):
+    """More ciphertexts than resident CTAs (two per SM): the grid loops, and ciphertexts of
+    every round equal the restatement."""
+    from yatfhe_gb300 import api
+
+    n, N = 6, 1024
+    count = 2 * torch.cuda.get_device_properties(0).multi_processor_count * 2 + 37
+    bsk8, acc, rot = random_case(n, N, count, 99)
+    key = api.CrtKey(bsk8)
+    out = key.blind_rotate(torch.from_numpy(acc).cuda(), torch.from_numpy(rot).cuda()).cpu().numpy()
+    for c in sorted({0, 1, count // 2, count // 2 + 1, count - 2, count - 1}):
+        want, _ = crt_blind_rotate(bsk8, acc[c], rot[c])
+        np.testing.assert_array_equal(out[c], want)

@@ -202,3 +202,23 @@ def test_rlwe_encrypt_drawn_decrypts(base, built_lib):
         e = (phase - mu[i]) & ((1 << p.torus_bits) - 1)
         e = np.where(e >= half, e - (1 << p.torus_bits), e)
         assert np.abs(e).max() <= bound and np.abs(e).max() > bound // 4, (i, np.abs(e).max())
+
+
+def test_sampling_arguments(built_lib):
+    """Empty batches are no-ops; out-of-range noise widths and unreduced masks are refused."""
+    from yatfhe_gb300 import api
+
+    p = small(T32_N1024, 16)
+    ctx = api.Context(p, 0)
+    s = torch.zeros(p.n, dtype=torch.int32, device="cuda")
+    mu = torch.zeros(0, dtype=torch.int64, device="cuda")
+    assert api.sym_enc_tlwe(ctx, s, mu, 1, 0, 4).shape == (0, p.n + 1)
+    rs = torch.zeros(p.N, dtype=torch.int32, device="cuda")
+    rmu = torch.zeros((0, p.N), dtype=torch.int64, device="cuda")
+    assert api.sym_enc_trlwe_ntt(ctx, rs, rmu, 1, 0, 4).shape == (0, 2, p.N)
+    with pytest.raises(Exception):
+        api.sym_enc_tlwe(ctx, s, torch.zeros(4, dtype=torch.int64, device="cuda"), 1, 0, 31)
+    with pytest.raises(Exception):
+        api.keygen(ctx, 1, 18, 31)
+    with pytest.raises(Exception):
+        api.draw_keygen_samples(ctx, 1, -1, 8)

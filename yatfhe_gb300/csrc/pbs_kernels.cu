@@ -454,20 +454,50 @@ __global__ void __launch_bounds__(1024) encrypt_rlwe_ntt_kernel(const EncryptRlw
 __device__ void q_forward_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
                                 uint64_t q) {
     const uint64_t q2 = 2 * q;
-    for (int s = 0; s < logN; ++s) {
-        const int m = 1 << s, lt = logN - 1 - s, t = 1 << lt;
-        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-            const int i = b >> lt, j = b & (t - 1);
-            const int xi = (i << (lt + 1)) + j;
-            const uint64_t W = w[m + i], Wp = wp[m + i];
-            for (int k = 0; k < M; ++k) {
-                uint64_t* p = sw + (size_t)k * N;
-                uint64_t u = p[xi];
-                u = u >= q2 ? u - q2 : u;
-                const uint64_t v = mulshoup64_lazy(p[xi + t], W, Wp, q);
-                p[xi] = u + v;
-                p[xi + t] = u + q2 - v;
-            }
+    // the lazy Cooley-Tukey butterfly: u reduced below 2q, v times the twiddle (Shoup, < 2q)
+    auto bfly = [&](uint64_t& u, uint64_t& v, uint64_t W, uint64_t Wp) {
+        const uint64_t ur = u >= q2 ? u - q2 : u;
+        const uint64_t t = mulshoup64_lazy(v, W, Wp, q);
+        u = ur + t;
+        v = ur + q2 - t;
+    };
+    // blockDim.x is a multiple of N/4 (the kernels run N/2 threads): each thread keeps one group
+    // index and its twiddles for a pass and steps through the M polynomials
+    const int quarter = N >> 2, qshift = logN - 2;
+    const int gi = threadIdx.x & (quarter - 1), k0 = threadIdx.x >> qshift, kstep = blockDim.x >> qshift;
+    int s = 0;
+    // two stages per pass: each thread takes groups of four words (one per butterfly of both
+    // stages), the same butterflies in the same order as two radix-2 passes
+    for (; s + 1 < logN; s += 2) {
+        const int m = 1 << s, lt = logN - 1 - s, t = 1 << lt, t2 = t >> 1;
+        const int i = gi >> (lt - 1), j = gi & (t2 - 1);
+        const uint64_t Wa = w[m + i], Wap = wp[m + i];
+        const uint64_t Wb = w[2 * m + 2 * i], Wbp = wp[2 * m + 2 * i];
+        const uint64_t Wc = w[2 * m + 2 * i + 1], Wcp = wp[2 * m + 2 * i + 1];
+        for (int k = k0; k < M; k += kstep) {
+            uint64_t* p = sw + (size_t)k * N + (i << (lt + 1)) + j;
+            uint64_t x0 = p[0], x1 = p[t2], x2 = p[t], x3 = p[t + t2];
+            bfly(x0, x2, Wa, Wap);
+            bfly(x1, x3, Wa, Wap);
+            bfly(x0, x1, Wb, Wbp);
+            bfly(x2, x3, Wc, Wcp);
+            p[0] = x0;
+            p[t2] = x1;
+            p[t] = x2;
+            p[t + t2] = x3;
+        }
+        __syncthreads();
+    }
+    if (s < logN) {  // an odd stage count: the last stage (span 1) alone
+        const int m = 1 << s;
+        const int i = threadIdx.x & ((N >> 1) - 1);
+        const uint64_t W = w[m + i], Wp = wp[m + i];
+        for (int k = threadIdx.x >> (logN - 1); k < M; k += blockDim.x >> (logN - 1)) {
+            uint64_t* p = sw + (size_t)k * N + 2 * i;
+            uint64_t x0 = p[0], x1 = p[1];
+            bfly(x0, x1, W, Wp);
+            p[0] = x0;
+            p[1] = x1;
         }
         __syncthreads();
     }
@@ -478,19 +508,46 @@ __device__ void q_forward_batch(uint64_t* sw, int M, int N, int logN, const uint
 __device__ void q_inverse_batch(uint64_t* sw, int M, int N, int logN, const uint64_t* w, const uint64_t* wp,
                                 uint64_t q) {
     const uint64_t q2 = 2 * q;
-    for (int lt = 0; lt < logN; ++lt) {
+    // the lazy Gentleman-Sande butterfly
+    auto bfly = [&](uint64_t& u, uint64_t& v, uint64_t W, uint64_t Wp) {
+        const uint64_t sum = u + v;
+        const uint64_t d = u + q2 - v;
+        u = sum >= q2 ? sum - q2 : sum;
+        v = mulshoup64_lazy(d, W, Wp, q);
+    };
+    const int quarter = N >> 2, qshift = logN - 2;
+    const int gi = threadIdx.x & (quarter - 1), k0 = threadIdx.x >> qshift, kstep = blockDim.x >> qshift;
+    int lt = 0;
+    for (; lt + 1 < logN; lt += 2) {
         const int t = 1 << lt, h = N >> (lt + 1);
-        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-            const int i = b >> lt, j = b & (t - 1);
-            const int xi = (i << (lt + 1)) + j;
-            const uint64_t W = w[h + i], Wp = wp[h + i];
-            for (int k = 0; k < M; ++k) {
-                uint64_t* p = sw + (size_t)k * N;
-                const uint64_t u = p[xi], v = p[xi + t];
-                const uint64_t sum = u + v;
-                p[xi] = sum >= q2 ? sum - q2 : sum;
-                p[xi + t] = mulshoup64_lazy(u + q2 - v, W, Wp, q);
-            }
+        const int i = gi >> lt, j = gi & (t - 1);
+        const uint64_t Wa = w[h + 2 * i], Wap = wp[h + 2 * i];
+        const uint64_t Wb = w[h + 2 * i + 1], Wbp = wp[h + 2 * i + 1];
+        const uint64_t Wc = w[(h >> 1) + i], Wcp = wp[(h >> 1) + i];
+        for (int k = k0; k < M; k += kstep) {
+            uint64_t* p = sw + (size_t)k * N + (i << (lt + 2)) + j;
+            uint64_t x0 = p[0], x1 = p[t], x2 = p[2 * t], x3 = p[3 * t];
+            bfly(x0, x1, Wa, Wap);
+            bfly(x2, x3, Wb, Wbp);
+            bfly(x0, x2, Wc, Wcp);
+            bfly(x1, x3, Wc, Wcp);
+            p[0] = x0;
+            p[t] = x1;
+            p[2 * t] = x2;
+            p[3 * t] = x3;
+        }
+        __syncthreads();
+    }
+    if (lt < logN) {  // the last stage (span N/2) alone
+        const int t = 1 << lt;
+        const int j = threadIdx.x & ((N >> 1) - 1);
+        const uint64_t W = w[1], Wp = wp[1];
+        for (int k = threadIdx.x >> (logN - 1); k < M; k += blockDim.x >> (logN - 1)) {
+            uint64_t* p = sw + (size_t)k * N + j;
+            uint64_t x0 = p[0], x1 = p[t];
+            bfly(x0, x1, W, Wp);
+            p[0] = x0;
+            p[t] = x1;
         }
         __syncthreads();
     }
