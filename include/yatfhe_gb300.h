@@ -236,7 +236,7 @@ int yg_pbs_host(yg_ctx* ctx, const yg_key* key, const int32_t* h_in, int32_t* h_
  * process exits, instead of a per-call allocation.  At most yg_pbs_noalloc_max_count(ctx)
  * ciphertexts per call (4092 at N = 1024, 2046 at N = 2048); more is rejected with
  * YG_ERR_INVALID.  A call with count 0 (buffers may be NULL) only sets the device up: it
- * looks up the array's device address, which is when the driver commits the array's 16 MiB
+ * looks up the array's device address, which is when the CUDA driver commits the array's 16 MiB
  * on that device (it loads the library's device variables lazily), and loads the two
  * kernels a call launches.  Make that call at start-up, before any stream capture and
  * before the caller stops allowing allocations; otherwise the first call with count > 0 on

@@ -42,7 +42,7 @@ namespace {
 
 const YatfheParameters* g_param = nullptr;
 thread_local std::string g_err;
-int g_uploads = 0;  // GINX key uploads (the driver checks the adapter's key cache with it)
+int g_uploads = 0;  // GINX key uploads (adapter_run.cpp checks the adapter's key cache with it)
 int g_crt_uploads = 0;
 
 int fail(int rc, const std::string& what) {
@@ -54,7 +54,7 @@ int fail(int rc, const std::string& what) {
 
 extern "C" {
 
-// the process-wide parameters the reference functions run with (the driver's initYatfhe)
+// the process-wide parameters the reference functions run with (adapter_run.cpp's initYatfhe)
 void yg_test_use_params(const YatfheParameters* p) { g_param = p; }
 int yg_test_uploads(void) { return g_uploads; }
 int yg_test_crt_uploads(void) { return g_crt_uploads; }

@@ -339,7 +339,7 @@ int launch_keyswitch(const KsArgs& a, void* stream);
 // Bounded device-side waits on the current device that gave up since the library was loaded
 // (the kernels then read from global memory instead); 0 on success.
 int read_wait_timeouts(unsigned long long* out);
-// Loads the key-switching kernel on the current device (the driver loads kernels lazily, on
+// Loads the key-switching kernel on the current device (the CUDA driver loads kernels lazily, on
 // first use); 0 on success.
 int preload_keyswitch();
 int launch_lazy_blind_rotate(const LazyBrArgs& a, void* stream);
