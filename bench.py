@@ -1158,7 +1158,7 @@ def main():
         # one ciphertext per call in each layout that exists for these parameters (one
         # ciphertext per CTA), then the tuned shape back
         lone = {}
-        for name, lay in (("channel", 0), ("channel_row", 1), ("row_cluster", 2)):
+        for name, lay in (("channel", 0), ("channel_row", 1), ("row_cluster", 2), ("channel_cluster", 3)):
             if api.ctas_per_sm(run.ctx, 1, lay) < 1:
                 continue
             api.set_launch(run.ctx, 1, 0, lay)

@@ -294,11 +294,15 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
  * one inverse transform: twice the threads per ciphertext, about half the latency.
  * YG_LAYOUT_ROW_CLUSTER (T = 32, N = 1024, l_approx <= 4, per_cta 1): a cluster of two CTAs
  * per ciphertext, one per accumulator row, with one team per (channel, digit level), so the
- * levels' transforms run side by side: the shortest latency for lone ciphertexts (the
- * grid is always two CTAs per ciphertext; a persistent grid does not apply). */
+ * levels' transforms run side by side (the grid is always two CTAs per ciphertext; a
+ * persistent grid does not apply).  YG_LAYOUT_CHANNEL_CLUSTER (same limits): a cluster of
+ * six CTAs per ciphertext, one per (accumulator row, RNS channel), with one warp per digit
+ * level, so no SM scheduler runs more than one transform: the shortest latency for lone
+ * ciphertexts (six CTAs per ciphertext, no persistent grid). */
 #define YG_LAYOUT_CHANNEL 0
 #define YG_LAYOUT_CHANNEL_ROW 1
 #define YG_LAYOUT_ROW_CLUSTER 2
+#define YG_LAYOUT_CHANNEL_CLUSTER 3
 /* Launch shape for this plan: layout, per_cta ciphertexts per blind-rotation CTA (1, 2 or
  * 4; 0 = the context's setting, layout included) and grid CTAs (0 = enough for the batch;
  * fewer = persistent CTAs that loop over it). */

@@ -22,10 +22,11 @@ def _sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-@pytest.mark.parametrize("layout", [0, 1, 2])
+@pytest.mark.parametrize("layout", [0, 1, 2, 3])
 @pytest.mark.parametrize("name", ["t32_n1024_small40_seed7", "t32_n1024_seed5eed0001", "t56_n2048_seed5eed0003"])
 def test_gpu_reproduces_reference_golden(name, layout, built_lib):
-    """Every layout of the blind rotation (channel, channel-row, row-cluster where it exists)."""
+    """Every layout of the blind rotation (channel, channel-row, and the row- and
+    channel-cluster layouts where they exist)."""
     from yatfhe_gb300 import api
 
     g = np.load(GOLDEN / f"{name}.npz")
@@ -36,8 +37,8 @@ def test_gpu_reproduces_reference_golden(name, layout, built_lib):
     assert _sha(bsk) == str(g["sha_bsk"]) and _sha(ksk) == str(g["sha_ksk"])  # the reference's keys
     ctx = api.Context(p, 0)
     if api.ctas_per_sm(ctx, 1, layout) < 1:
-        assert layout == 2 and not (p.torus_bits == 32 and p.N == 1024)
-        pytest.skip("no row-cluster kernel for this parameter set")
+        assert layout in (2, 3) and not (p.torus_bits == 32 and p.N == 1024)
+        pytest.skip("no cluster kernel for this parameter set")
     api.set_launch(ctx, 1, 0, layout)
     key = api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk)
     d_in = torch.from_numpy(g["lwe_in"]).cuda()

@@ -109,12 +109,14 @@ def test_blind_rotate_acc_reference_semantics(t32_small, layout):
     api.set_launch(ctx, 1, 0, 0)
 
 
+@pytest.mark.parametrize("layout", [2, 3])
 @pytest.mark.parametrize("levels", [3, 4])
-def test_row_cluster_key_stage_with_skipped_steps(levels, built_lib):
-    """The row-cluster layout copies each active step's key rows into shared memory by TMA
-    (l <= 3; at l = 4 it reads them from global memory): with CMux steps skipped (a_i = 0) at
-    the start, in the middle and at the end, 40 ciphertexts give the oracle's bootstrap, no
-    bounded wait gave up, and the result equals the channel layout's."""
+def test_cluster_key_stage_with_skipped_steps(levels, layout, built_lib):
+    """The cluster layouts copy each active step's key rows into shared memory by TMA (the
+    row cluster for l <= 3, reading them from global memory at l = 4; the channel cluster at
+    every l): with CMux steps skipped (a_i = 0) at the start, in the middle and at the end,
+    40 ciphertexts give the oracle's bootstrap, no bounded wait gave up, and the result
+    equals the channel layout's."""
     import ctypes
     import dataclasses
 
@@ -128,7 +130,7 @@ def test_row_cluster_key_stage_with_skipped_steps(levels, built_lib):
     lut = lutmod.sign_lut(p.N, 32)
     api.set_launch(ctx, 1, 0, 0)
     want = _pbs_gpu(ctx, key, lwe, lut)
-    api.set_launch(ctx, 1, 0, 2)
+    api.set_launch(ctx, 1, 0, layout)
     got = _pbs_gpu(ctx, key, lwe, lut)
     api.set_launch(ctx, 1, 0, 0)
     np.testing.assert_array_equal(got, want)
@@ -150,6 +152,27 @@ def test_keyswitch_alone_t32(t32_small):
     got = api.switch_key_for_tlwe(ctx, key, torch.from_numpy(big).cuda()).cpu().numpy()
     for c in range(len(big)):
         np.testing.assert_array_equal(got[c], ora.keyswitch(big[c]))
+
+
+def test_keyswitch_split_matches_unsplit(t32_small):
+    """Small batches split the input coefficients across CTAs that add into the output; a
+    batch large enough to fill the GPU runs unsplit.  A ciphertext's key switch is the same in
+    batches of 1, 3, 9, 61 and 6,000 (extreme words included), and equals the oracle's."""
+    from yatfhe_gb300 import api
+
+    ora, ctx, key = t32_small
+    p = ctx.params
+    rng = np.random.default_rng(31)
+    big = rng.integers(-(1 << 31), 1 << 31, size=(6000, p.k * p.N + 1), dtype=np.int64).astype(np.int32)
+    big[0, :] = np.int32(-(1 << 31))
+    big[1, :] = np.int32((1 << 31) - 1)
+    d_big = torch.from_numpy(big).cuda()
+    full = api.switch_key_for_tlwe(ctx, key, d_big).cpu().numpy()
+    for count in (1, 3, 9, 61):
+        got = api.switch_key_for_tlwe(ctx, key, d_big[:count].contiguous()).cpu().numpy()
+        np.testing.assert_array_equal(got, full[:count], err_msg=f"batch of {count}")
+    for c in (0, 1, 2, 5999):
+        np.testing.assert_array_equal(full[c], ora.keyswitch(big[c]))
 
 
 def test_pbs_t56_small_bit_exact(t56_small):

@@ -18,6 +18,7 @@ YG_OK = 0
 LAYOUT_CHANNEL = 0      # YG_LAYOUT_CHANNEL
 LAYOUT_CHANNEL_ROW = 1  # YG_LAYOUT_CHANNEL_ROW
 LAYOUT_ROW_CLUSTER = 2  # YG_LAYOUT_ROW_CLUSTER
+LAYOUT_CHANNEL_CLUSTER = 3  # YG_LAYOUT_CHANNEL_CLUSTER
 _ERRORS = {-1: ValueError, -2: RuntimeError, -3: OSError, -4: MemoryError, -5: RuntimeError}
 
 

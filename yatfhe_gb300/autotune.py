@@ -3,9 +3,11 @@
 The knobs (yg_ctx_set_launch / yg_plan_set_launch):
   layout       work split of one ciphertext: a thread team per RNS channel (LAYOUT_CHANNEL),
                per channel and accumulator row (LAYOUT_CHANNEL_ROW: twice the threads,
-               about half the latency per ciphertext), or a two-CTA cluster per ciphertext
+               about half the latency per ciphertext), a two-CTA cluster per ciphertext
                with a team per channel and digit level in each (LAYOUT_ROW_CLUSTER, T32 at
-               N = 1024: the levels' transforms side by side, the shortest latency);
+               N = 1024: the levels' transforms side by side), or a six-CTA cluster with a
+               CTA per accumulator row and channel and a warp per digit level
+               (LAYOUT_CHANNEL_CLUSTER, same limits: the shortest latency);
   per_cta      ciphertexts per CTA, sharing its L1 (1, 2, 4 at N = 1024; 1, 2 at N = 2048):
                more share instruction-cache lines and key lines in L1, fewer keep more
                independent CTAs per SM;
@@ -55,7 +57,8 @@ def _store(table: dict) -> None:
 def candidates(ctx) -> list[tuple[int, int, int]]:
     """(layout, per_cta, ctas_per_sm) shapes that fit an SM."""
     out = []
-    for layout in (_lib.LAYOUT_CHANNEL, _lib.LAYOUT_CHANNEL_ROW, _lib.LAYOUT_ROW_CLUSTER):
+    clusters = (_lib.LAYOUT_ROW_CLUSTER, _lib.LAYOUT_CHANNEL_CLUSTER)
+    for layout in (_lib.LAYOUT_CHANNEL, _lib.LAYOUT_CHANNEL_ROW) + clusters:
         for per_cta in (1, 2, 4):
             try:
                 fit = api.ctas_per_sm(ctx, per_cta, layout)
@@ -64,7 +67,7 @@ def candidates(ctx) -> list[tuple[int, int, int]]:
             if fit < 1:
                 continue
             out.append((layout, per_cta, 0))
-            if layout != _lib.LAYOUT_ROW_CLUSTER:  # always two CTAs per ciphertext, never persistent
+            if layout not in clusters:  # a fixed cluster per ciphertext, never persistent
                 out.append((layout, per_cta, fit))
     return out
 

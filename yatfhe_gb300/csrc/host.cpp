@@ -1780,7 +1780,8 @@ int yg_plan_create(yg_ctx* ctx, const yg_key* const* keys, int num_keys, const i
 
 int yg_plan_set_launch(yg_plan* plan, int layout, int per_cta, int grid) {
     if (!plan || per_cta < 0 || grid < 0 ||
-        (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW && layout != YG_LAYOUT_ROW_CLUSTER))
+        (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW && layout != YG_LAYOUT_ROW_CLUSTER &&
+         layout != YG_LAYOUT_CHANNEL_CLUSTER))
         return set_err(YG_ERR_INVALID, "yg_plan_set_launch: bad arguments");
     if (per_cta > 0) {
         int fit = 0;
@@ -1848,7 +1849,8 @@ void yg_plan_destroy(yg_plan* plan) {
 
 int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out) {
     if (!ctx || !out) return set_err(YG_ERR_INVALID, "null argument");
-    if (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW && layout != YG_LAYOUT_ROW_CLUSTER)
+    if (layout != YG_LAYOUT_CHANNEL && layout != YG_LAYOUT_CHANNEL_ROW && layout != YG_LAYOUT_ROW_CLUSTER &&
+        layout != YG_LAYOUT_CHANNEL_CLUSTER)
         return set_err(YG_ERR_INVALID, "yg_ctas_per_sm: unknown layout");
     return guarded([&] {
         DeviceGuard g(ctx->device);

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <type_traits>
 
@@ -1494,7 +1495,7 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     } else {
         for (int j = tid; j < N; j += NT) acc[j] = 0;
     }
-    __syncthreads();
+    cluster.sync();  // the partner has started: its shared memory may be written from here on
 
     for (int i = 0; i < a.steps; ++i) {
         const int ai = (int)sa[i];
@@ -1651,15 +1652,301 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     cluster.sync();  // neither CTA leaves while the other may still write into its regions
 }
 
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// Channel-cluster layout (kLayoutChannelCluster), T = 32, N = 1024: one ciphertext per
+// cluster of six CTAs.  CTA (h, c), rank 3 h + c, owns accumulator row h in RNS channel c and
+// computes output h of every external product in that channel; its warp lvl < l runs the
+// forward transform of digit level lvl.  Per CMux step: (1) all threads rotate and decompose
+// row h into l digit rows (the three CTAs of a row compute the same digits); (2) each
+// transform warp runs its level's forward transform, writes it into the exchange region of
+// the same level in the partner CTA (the other row, the same channel), arrives at the cluster
+// barrier and multiplies its own transform with the key words K(lvl, h, h) while the barrier
+// completes; (3) then the partner's transform with K(lvl, 1-h, h): an exact 64-bit sum of two
+// products reduced once, into its partial region; (4) warp 0 adds the l partials, runs the
+// inverse transform and writes row h's residues in channel c into the three CTAs of row h;
+// after a second cluster barrier (5) each CTA of the row recombines the three channels (CRT)
+// and adds into its copy of row h.  An SM runs at most one transform warp per scheduler (the
+// row-cluster layout puts nine on four), so a step costs about one forward and one inverse
+// transform of a warp running alone.  The key rows of the next active step (output h of both
+// rows, every level, channel c: l x 2 x 4 KB) are copied into shared memory by TMA, as in the
+// row-cluster layout, with the same bounded wait and global-memory fallback.  Regions are
+// rewritten only after their readers are done: the partner writes an exchange region of step
+// i + 1 after the second barrier of step i, which follows this CTA's products of step i; a
+// row peer writes an inbox of step i + 1 after the first barrier of step i + 1, which this
+// CTA reaches only after its recombination of step i.
+template <int T>
+__global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster6_kernel(const BrArgs a) {
+    static_assert(T == 32, "the channel-cluster layout is built for the 32-bit torus");
+    namespace cg = cooperative_groups;
+    using Sh = TeamShape<10>;
+    constexpr int N = Sh::N, S = Sh::S;
+    constexpr int PS = prime_set_for(T);
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int h = rank / 3, c = rank - 3 * h;
+    const int L = a.L, n = a.n;
+    const int ct = (int)(blockIdx.x / 6);
+    const bool valid = ct < a.count;  // the grid is six CTAs per ciphertext: uniform per cluster
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const bool xform = warp < L;  // warp-uniform
+    const int lvl = xform ? warp : 0;
+    const Chan ch = pick_chan(a.ch, c);
+    const uint64_t keep = l2_evict_last_policy();
+    const uint32_t pinv = 0u - ch.pinv_neg;
+    const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
+
+    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);          // [L][TBUF] transposes, partials
+    uint32_t* exch = regions + (size_t)L * Sh::TBUF;                // [L][N] written by the partner
+    uint32_t* inbox = exch + (size_t)L * N;                         // [3][N] row h's residues by channel
+    int32_t* acc = reinterpret_cast<int32_t*>(inbox + 3 * N);       // [N] row h
+    int16_t* dig = reinterpret_cast<int16_t*>(acc + N);             // [L][N]
+    int16_t* sa = dig + (size_t)L * N;                              // [n+1]
+    uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
+    uint32_t* stage = reinterpret_cast<uint32_t*>(smem + brc6_stage_offset(n, L));  // [L][2][1024]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + brc6_smem_bytes(n, L) - 16);
+    volatile int* stage_ok = reinterpret_cast<volatile int*>(mbar + 1);
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
+    uint32_t* mine = regions + (size_t)lvl * Sh::TBUF;
+    uint32_t* my_exch = exch + (size_t)lvl * N;
+    uint32_t* their_exch = cluster.map_shared_rank(my_exch, 3 * (1 - h) + c);
+    uint32_t* peer_a = cluster.map_shared_rank(inbox + (size_t)c * N, 3 * h + (c == 2 ? 0 : c + 1));
+    uint32_t* peer_b = cluster.map_shared_rank(inbox + (size_t)c * N, 3 * h + (c == 0 ? 2 : c - 1));
+
+    const uint4* key = !valid ? nullptr : (a.key_of ? a.key_table[a.key_of[ct]] : a.key);
+    const int64_t* lut = !valid ? nullptr : (a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut);
+    bool tma = valid;  // uniform in the cluster
+    if (tma && tid == 0) {
+        mbar_init(mbar_a, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // thread 0: arms the barrier and copies the key rows of `step` (output h, channel c)
+    auto issue = [&](int step) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(mbar_a, (uint32_t)L * 2 * 4096);
+        for (int lv = 0; lv < L; ++lv)
+            for (int row = 0; row < 2; ++row) {
+                const size_t blk = (size_t)step * L + lv;
+                const uint4* src = key + ((blk * 2 + row) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+                bulk_copy_g2s((uint32_t)__cvta_generic_to_shared(stage + (lv * 2 + row) * 1024), src, 4096, mbar_a);
+            }
+    };
+    auto next_active = [&](int from) {
+        while (from < a.steps && sa[from] == 0) ++from;
+        return from;
+    };
+    uint32_t phase = 0;        // parity of the stage's next barrier phase
+    bool outstanding = false;  // thread 0: a copy issued and not yet waited for
+    const bool use_tab0 = a.radix_bits <= 7;
+    if (use_tab0) {
+        for (int idx = tid; idx < 129; idx += NT) {
+            const int d = idx - 64;
+            const int64_t v = (int64_t)c_tw_head[PS][0][c][0][1].x * d % ch.p;
+            tab0[64 + d] = (uint32_t)(v < 0 ? v + ch.p : v);
+        }
+    }
+    if (valid) {
+        if (a.scaled_in) {
+            for (int i = tid; i < n; i += NT) sa[i] = (int16_t)a.scaled_in[(size_t)ct * n + i];
+        } else {
+            const int32_t* in = a.lwe_in + (size_t)ct * (n + 1);
+            for (int i = tid; i <= n; i += NT) sa[i] = (int16_t)modswitch_down(in[i], 31 - 10, 11);
+        }
+    } else {
+        for (int i = tid; i <= n; i += NT) sa[i] = 0;
+    }
+    __syncthreads();
+    if (tma && tid == 0) {
+        const int f = next_active(0);
+        if (f < a.steps) {
+            issue(f);
+            outstanding = true;
+        }
+    }
+    if (valid && a.acc_in) {
+        for (int j = tid; j < N; j += NT) acc[j] = (int32_t)a.acc_in[(size_t)ct * 2 * N + h * N + j];
+    } else if (valid) {
+        // genNoiselessTrlweSample: acc = (0, X^-b v) (yatfhe/src/trlwe.cpp:175-182)
+        int t2 = -(int)sa[n];
+        t2 = ((t2 % (2 * N)) + 2 * N) % (2 * N);
+        const bool wrap = t2 >= N;
+        const int at = wrap ? t2 - N : t2;
+        for (int j = tid; j < N; j += NT) {
+            int32_t v = j < at ? tneg<T>((int32_t)lut[j - at + N]) : (int32_t)lut[j - at];
+            acc[j] = h == 0 ? 0 : (wrap ? tneg<T>(v) : v);
+        }
+    } else {
+        for (int j = tid; j < N; j += NT) acc[j] = 0;
+    }
+    cluster.sync();  // every CTA of the cluster has started: their shared memory may be written
+
+    for (int i = 0; i < a.steps; ++i) {
+        const int ai = (int)sa[i];
+        if (ai == 0) continue;  // the a_i = 0 skip (blind_rotate.cpp:1557), the same in every CTA
+        const int t2 = ai < 0 ? ai + 2 * N : ai;
+        const bool wrap = t2 >= N;
+        const int at = wrap ? t2 - N : t2;
+        // (1) X^{a_i} row - row, zero-mean digits (rotateTrlweMinusOne, gadgetDecomposeTrlwe)
+        auto decompose = [&](auto lc, auto rc) {
+            constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
+            const int levels = LC ? LC : L, radix = RC ? RC : a.radix_bits;
+#pragma unroll 1
+            for (int j = tid; j < N; j += NT) {
+                int32_t rot = j < at ? tneg<T>(acc[j - at + N]) : acc[j - at];
+                if (wrap) rot = tneg<T>(rot);
+                const int32_t tmp = tsub<T>(rot, acc[j]);
+                int16_t* d = dig + j;
+                zero_mean_digits<uint32_t, 32>((uint32_t)tmp, levels, radix, [&](int level, int v) { d[level * N] = (int16_t)v; });
+            }
+        };
+        if (L == 3 && a.radix_bits == 7)
+            decompose(std::integral_constant<int, 3>{}, std::integral_constant<int, 7>{});
+        else
+            decompose(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+        __syncthreads();
+        if (xform) {
+            // (2) this level's forward transform, written into the partner's exchange region
+            uint32_t x[32];
+            const int16_t* d = dig + (size_t)lvl * N;
+            if (use_tab0) {
+#pragma unroll
+                for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane];
+                ntt_forward<10, PS, 1>(x, mine, lane, c, 0, ch, tab0 + 64);
+            } else {
+                const uint32_t bias = fwd_bias_digits<10, PS>(ch.p);
+#pragma unroll
+                for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane] + bias;
+                ntt_forward<10, PS>(x, mine, lane, c, 0, ch);
+            }
+#pragma unroll
+            for (int r = 0; r < 32; ++r) their_exch[r * S + lane] = x[r];
+            cluster_arrive();
+            // own row with K(lvl, h, h) while the partner finishes: x < 46p and key words < p,
+            // so the sum of two products fits 64 bits
+            const size_t blk = (size_t)i * L + lvl;
+            const uint4* gown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+            const uint4* gpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+            bool from_stage = false;
+            if (tma) {
+                from_stage = mbar_wait_bounded(mbar_a, phase, kWaitCycles);
+                if (!from_stage) atomicAdd(&g_wait_timeouts, 1ull);
+                if (tid == 0) {
+                    if (from_stage) outstanding = false;
+                    *stage_ok = from_stage;
+                }
+            }
+            const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + h) * 1024) : nullptr;
+            const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + (1 - h)) * 1024) : nullptr;
+            uint64_t own[32];
+#pragma unroll
+            for (int rr = 0; rr < 8; ++rr) {
+                const uint4 ka = from_stage ? kown[rr * S + lane] : ldg_keep(gown + rr * S + lane, keep);
+                const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) own[rr * 4 + e] = (uint64_t)x[rr * 4 + e] * kav[e];
+            }
+            cluster_wait();  // both rows' transforms are in the partners' exchange regions
+            // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum
+#pragma unroll
+            for (int rr = 0; rr < 8; ++rr) {
+                const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
+                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int r = rr * 4 + e;
+                    const uint64_t s = own[r] + (uint64_t)my_exch[r * S + lane] * kbv[e];
+                    // s 2^-32 mod p (Montgomery) + p: in (0, 3.1p), reduced after the level sum
+                    mine[r * S + lane] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
+                }
+            }
+        } else {
+            cluster_arrive();
+            cluster_wait();
+        }
+        __syncthreads();  // every partial is written, and the stage has been read
+        if (tma) {
+            tma = *stage_ok;  // after thread 0 gave up the CTA reads the key from global memory
+            phase ^= 1;
+            if (tma && tid == 0) {
+                const int f = next_active(i + 1);
+                if (f < a.steps) {
+                    issue(f);
+                    outstanding = true;
+                }
+            }
+        }
+        // (4) warp 0: sum of the l partials, inverse transform, residues to the row's CTAs
+        if (warp == 0) {
+            uint32_t oa[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                uint32_t v = 0;
+#pragma unroll
+                for (int q = 0; q < kClusterMaxLevels; ++q)
+                    if (q < L) v += regions[(size_t)q * Sh::TBUF + r * S + lane];
+                oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
+            }
+            ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
+            uint32_t* own_box = inbox + (size_t)c * N;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                const uint32_t v = reduce_once(oa[r], ch.p);
+                own_box[r * S + lane] = v;
+                peer_a[r * S + lane] = v;
+                peer_b[r * S + lane] = v;
+            }
+        }
+        cluster_arrive();
+        cluster_wait();  // the row's three channels are in every inbox of the row
+        // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h
+#pragma unroll 1
+        for (int j = tid; j < N; j += NT) {
+            const int64_t v = crt_to_torus<T>(inbox[j], inbox[N + j], inbox[2 * N + j], a.crt);
+            acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
+        }
+        __syncthreads();
+    }
+
+    if (valid && a.acc_out && c == 0) {
+        int64_t* dst = a.acc_out + (size_t)ct * 2 * N + h * N;
+        for (int j = tid; j < N; j += NT) dst[j] = (int64_t)acc[j];
+    }
+    if (valid && a.big_out && c == 0) {
+        // extractTlweFromTrlwe(out, acc, 0): a'[j] = j ? -a[N-j] : a[0] from row 0, b' = b[0] from row 1
+        int32_t* dst = a.big_out + (size_t)ct * (N + 1);
+        if (h == 0) {
+            for (int j = tid; j < N; j += NT) dst[j] = j == 0 ? acc[0] : tneg<T>(acc[N - j]);
+        } else if (tid == 0) {
+            dst[N] = acc[0];
+        }
+    }
+    // a copy that timed out may still land: wait for it (bounded) before the CTA exits
+    if (outstanding && tid == 0 && !mbar_wait_bounded(mbar_a, phase ^ 1, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
+    cluster.sync();  // no CTA leaves while another may still write into its regions
+}
+
 constexpr int kKsTile = kKsTileCts;  // ciphertexts per block
 constexpr int kKsCols = 128;    // output columns per block (= threads)
 constexpr int kKsChunk = 32;    // input coefficients per digit refresh
 constexpr int kKsMaxT = 16;
+constexpr int kKsSplitCtasPerSm = 4;  // small batches: split the input until the grid has this many per SM
+constexpr int kKsMinSplitCoefs = 8;   // input coefficients of one split at least
 
+// Tiles of ciphertexts x output columns.  For small batches the input coefficients are also
+// split across gridDim.z CTAs (the grid would otherwise be a few CTAs, each streaming its
+// share of the whole key at one thread's memory parallelism): each adds its partial sum into
+// the zeroed output with atomic 32-bit adds, which wrap mod 2^32 like the sum itself, so the
+// result does not depend on their order.
 __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
     __shared__ int8_t sdig[kKsTile][kKsChunk][kKsMaxT];
     __shared__ int32_t sb[kKsTile];
     const int x = blockIdx.y * kKsCols + threadIdx.x;
+    const int splits = (int)gridDim.z;
+    const int per = (a.kN + splits - 1) / splits;
+    const int i_begin = (int)blockIdx.z * per, i_end = min(a.kN, i_begin + per);
     int c0, cnt;
     const int32_t* ksk;
     if (a.tiles) {
@@ -1680,18 +1967,18 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
         const int ct = c0 + threadIdx.x;
         sb[threadIdx.x] = (int)threadIdx.x < cnt ? a.big_in[(size_t)ct * (a.kN + 1) + a.kN] : 0;
     }
-    for (int i0 = 0; i0 < a.kN; i0 += kKsChunk) {
+    for (int i0 = i_begin; i0 < i_end; i0 += kKsChunk) {
         __syncthreads();
         for (int e = threadIdx.x; e < kKsTile * kKsChunk; e += kKsCols) {
             const int c = e / kKsChunk, ii = e % kKsChunk;
             const int ct = c0 + c, i = i0 + ii;
-            const int32_t v = (c < cnt && i < a.kN) ? a.big_in[(size_t)ct * (a.kN + 1) + i] : 0;
+            const int32_t v = (c < cnt && i < i_end) ? a.big_in[(size_t)ct * (a.kN + 1) + i] : 0;
             zero_mean_digits<uint32_t, 32>((uint32_t)v, a.t, a.ks_radix_bits,
                                            [&](int level, int d) { sdig[c][ii][level] = (int8_t)d; });
         }
         __syncthreads();
         if (x < nb) {
-            const int iend = min(kKsChunk, a.kN - i0);
+            const int iend = min(kKsChunk, i_end - i0);
             for (int ii = 0; ii < iend; ++ii) {
                 const int32_t* row = ksk + ((size_t)(i0 + ii) * a.t) * nb + x;
                 for (int j = 0; j < a.t; ++j) {
@@ -1706,7 +1993,10 @@ __global__ void __launch_bounds__(kKsCols) keyswitch_kernel(const KsArgs a) {
 #pragma unroll
         for (int c = 0; c < kKsTile; ++c) {
             const int ct = c0 + c;
-            if (c < cnt) a.out[(size_t)ct * nb + x] = (int32_t)((x == a.n ? (uint32_t)sb[c] : 0u) - acc[c]);
+            if (c >= cnt) continue;
+            const uint32_t v = (x == a.n && blockIdx.z == 0 ? (uint32_t)sb[c] : 0u) - acc[c];
+            if (splits == 1) a.out[(size_t)ct * nb + x] = (int32_t)v;
+            else atomicAdd(reinterpret_cast<unsigned int*>(a.out + (size_t)ct * nb + x), v);
         }
     }
 }
@@ -1803,7 +2093,7 @@ int launch_keyconv(int logN, int ps, const KeyConvArgs& a, void* stream) {
 
 namespace {
 
-// The row-cluster kernel exists for T = 32, N = 1024, one ciphertext per cluster, l <= 4.
+// The cluster kernels exist for T = 32, N = 1024, one ciphertext per cluster, l <= 4.
 bool cluster_variant(int logN, int torus_bits, int per_cta, int L) {
     return logN == 10 && torus_bits == 32 && per_cta <= 1 && L >= 1 && L <= kClusterMaxLevels;
 }
@@ -1814,6 +2104,8 @@ int prepare_brc() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
     if (!done[dev].load()) {
         if (cudaFuncSetAttribute(blind_rotate_cluster_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 227 * 1024) != cudaSuccess ||
+            cudaFuncSetAttribute(blind_rotate_cluster6_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  227 * 1024) != cudaSuccess)
             return -1;
         done[dev].store(true);
@@ -1832,6 +2124,13 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
         blind_rotate_cluster_kernel<32><<<2 * a.count, kChannels * a.L * 32, smem, (cudaStream_t)stream>>>(a);
         return cudaGetLastError() == cudaSuccess ? 0 : -1;
     }
+    if (a.layout == kLayoutChannelCluster) {
+        if (!cluster_variant(logN, torus_bits, a.per_cta, a.L)) return kNoVariant;
+        const size_t smem = brc6_smem_bytes(a.n, a.L);
+        if (smem > 227 * 1024 || prepare_brc() != 0) return -1;
+        blind_rotate_cluster6_kernel<32><<<6 * a.count, kCluster6Warps * 32, smem, (cudaStream_t)stream>>>(a);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
     return dispatch_br(logN, torus_bits, a.per_cta, a.layout, LaunchBr{a, stream});
 }
 
@@ -1846,6 +2145,21 @@ int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layo
                                                           smem) != cudaSuccess) {
             // the calculator may decline cluster kernels: its shared memory fits and 168
             // registers x 3 l warps (l <= 4) fit one SM's register file
+            (void)cudaGetLastError();
+            blocks = 1;
+        }
+        return blocks;
+    }
+    if (layout == kLayoutChannelCluster) {
+        if (!cluster_variant(logN, torus_bits, per_cta, L)) return 0;
+        const size_t smem = brc6_smem_bytes(n, L);
+        if (smem > 227 * 1024) return 0;
+        if (prepare_brc() != 0) return -1;
+        int blocks = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_cluster6_kernel<32>, kCluster6Warps * 32,
+                                                          smem) != cudaSuccess) {
+            // the calculator may decline cluster kernels: 168 registers x 256 threads and the
+            // shared memory fit one SM
             (void)cudaGetLastError();
             blocks = 1;
         }
@@ -1957,7 +2271,28 @@ int launch_keyswitch(const KsArgs& a, void* stream) {
     if (a.t > kKsMaxT) return -1;
     const int blocks = a.tiles ? a.num_tiles : (a.count + kKsTile - 1) / kKsTile;
     if (blocks <= 0) return 0;
-    dim3 grid(blocks, (a.n + 1 + kKsCols - 1) / kKsCols);
+    const int cols = (a.n + 1 + kKsCols - 1) / kKsCols;
+    // a grid of fewer than kKsSplitCtasPerSm CTAs per SM splits the input coefficients (at
+    // least kKsMinSplitCoefs each) across CTAs that add into the zeroed output
+    static std::atomic<int> sms[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    int sm_count = sms[dev].load(std::memory_order_relaxed);
+    if (sm_count == 0) {
+        if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+        sms[dev].store(sm_count, std::memory_order_relaxed);
+    }
+    const long long want = (long long)kKsSplitCtasPerSm * sm_count;
+    int splits = 1;
+    if ((long long)blocks * cols < want) {
+        const long long by_grid = (want + (long long)blocks * cols - 1) / ((long long)blocks * cols);
+        splits = (int)std::min<long long>(by_grid, std::max(1, a.kN / kKsMinSplitCoefs));
+        splits = (a.kN + (a.kN + splits - 1) / splits - 1) / ((a.kN + splits - 1) / splits);  // no empty split
+    }
+    if (splits > 1 &&
+        cudaMemsetAsync(a.out, 0, (size_t)a.count * (a.n + 1) * sizeof(int32_t), (cudaStream_t)stream) != cudaSuccess)
+        return -1;
+    dim3 grid(blocks, cols, splits);
     keyswitch_kernel<<<grid, kKsCols, 0, (cudaStream_t)stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -25,7 +25,7 @@ struct BrArgs {
     int count;
     int grid;                // CTAs to launch (0: enough for the batch; fewer: persistent CTAs)
     int per_cta;             // ciphertexts per CTA, sharing its L1 (1, 2 or 4; 0 means 1)
-    int layout;              // kLayoutChannel, kLayoutChannelRow or kLayoutRowCluster
+    int layout;              // kLayoutChannel, kLayoutChannelRow, kLayoutRowCluster or kLayoutChannelCluster
     int n;                   // LWE dimension
     int steps;               // CMux steps to run (n for a full blind rotation)
     int L;                   // gadget levels
@@ -310,6 +310,28 @@ __host__ __device__ inline size_t brc_stage_offset(int n, int L) {
 __host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
     const size_t stage = L <= kClusterStageLevels ? (size_t)L * 2 * kChannels * 1024 * 4 : 0;
     return brc_stage_offset(n, L) + stage + 16;
+}
+// A cluster of six CTAs per ciphertext, CTA (h, c) owning accumulator row h in RNS channel c,
+// one warp per digit level (T = 32, N = 1024, l <= 4): the latency shape with at most one
+// transform warp per scheduler.
+constexpr int kLayoutChannelCluster = 3;
+constexpr int kCluster6Warps = 8;  // warps 0..l-1 transform; all of them decompose and recombine
+// Shared memory of one CTA of the channel-cluster layout: per level a padded transpose region
+// (also its partial sum after the products) and an exchange region the partner CTA (the
+// other row, the same channel) writes into; the row's residues by channel after the inverse
+// transform (two of them written by the other channels' CTAs); the accumulator row, its
+// digits, the mod-2N input, the channel's first-stage digit table, and the stage the next
+// step's key rows are copied into by TMA ([l][2 rows][1024] words) with its mbarrier and
+// status word.
+__host__ __device__ inline size_t brc6_stage_offset(int n, int L) {
+    const size_t N = 1024, tbuf = N + N / 32;
+    size_t b = (size_t)L * tbuf * 4 + (size_t)L * N * 4 + 3 * N * 4;
+    b += N * 4 + (size_t)L * N * 2 + ((size_t)n + 1) * 2;
+    b = ((b + 3) & ~(size_t)3) + 132 * 4;
+    return (b + 127) & ~(size_t)127;
+}
+__host__ __device__ inline size_t brc6_smem_bytes(int n, int L) {
+    return brc6_stage_offset(n, L) + (size_t)L * 2 * 1024 * 4 + 16;
 }
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
