@@ -1652,30 +1652,62 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     cluster.sync();  // neither CTA leaves while the other may still write into its regions
 }
 
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
-__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+// Point-to-point signalling between the CTAs of a cluster: 16-byte stores into another CTA's
+// shared memory that complete bytes of the transaction count of an mbarrier there, so the
+// receiver waits for exactly the data it needs instead of a cluster-wide barrier.
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_async_v4(uint32_t addr, uint4 v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(addr),
+                 "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(bar)
+                 : "memory");
+}
+// Waits (at most `cycles` clocks) for a phase completed by other CTAs' stores.
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint32_t bar, uint32_t parity, long long cycles) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, "
+            "0, p;\n}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > cycles) return false;
+    }
+}
+// Word offset of lane l's 16-byte chunk k (its slots 4k..4k+3) in a [32 lanes][32 words]
+// region: the eight lanes of a quarter warp reach eight different bank quads.
+__device__ __forceinline__ int swz(int l, int k) { return l * 32 + 4 * (k ^ (l & 7)); }
 
 // Channel-cluster layout (kLayoutChannelCluster), T = 32, N = 1024: one ciphertext per
 // cluster of six CTAs.  CTA (h, c), rank 3 h + c, owns accumulator row h in RNS channel c and
 // computes output h of every external product in that channel; its warp lvl < l runs the
 // forward transform of digit level lvl.  Per CMux step: (1) all threads rotate and decompose
 // row h into l digit rows (the three CTAs of a row compute the same digits); (2) each
-// transform warp runs its level's forward transform, writes it into the exchange region of
-// the same level in the partner CTA (the other row, the same channel), arrives at the cluster
-// barrier and multiplies its own transform with the key words K(lvl, h, h) while the barrier
-// completes; (3) then the partner's transform with K(lvl, 1-h, h): an exact 64-bit sum of two
-// products reduced once, into its partial region; (4) warp 0 adds the l partials, runs the
-// inverse transform and writes row h's residues in channel c into the three CTAs of row h;
-// after a second cluster barrier (5) each CTA of the row recombines the three channels (CRT)
-// and adds into its copy of row h.  An SM runs at most one transform warp per scheduler (the
-// row-cluster layout puts nine on four), so a step costs about one forward and one inverse
-// transform of a warp running alone.  The key rows of the next active step (output h of both
-// rows, every level, channel c: l x 2 x 4 KB) are copied into shared memory by TMA, as in the
-// row-cluster layout, with the same bounded wait and global-memory fallback.  Regions are
-// rewritten only after their readers are done: the partner writes an exchange region of step
-// i + 1 after the second barrier of step i, which follows this CTA's products of step i; a
-// row peer writes an inbox of step i + 1 after the first barrier of step i + 1, which this
-// CTA reaches only after its recombination of step i.
+// transform warp runs its level's forward transform and stores it (st.async) into the
+// exchange region of the same level in the partner CTA (the other row, the same channel),
+// completing the partner's barrier for that level, then multiplies its own transform with the
+// key words K(lvl, h, h); (3) once the partner's transform is in, the partner's with
+// K(lvl, 1 - h, h): an exact 64-bit sum of two products reduced once; (4) warp 0 adds the l
+// partials, runs the inverse transform and stores row h's residues in channel c into its own
+// inbox and (st.async) the two other CTAs of row h; (5) once the two other channels' residues
+// are in, every thread recombines four coefficients (CRT) and adds them into the CTA's copy
+// of row h.  No scheduler runs more than one transform warp (the row-cluster layout puts nine
+// on an SM's four), so a step costs about one forward and one inverse transform of a warp
+// running alone, and no step waits at a cluster-wide barrier.  Exchange regions and inboxes
+// are double-buffered by the parity of the active step: another CTA's store for step u + 2
+// depends, through the chain of transforms and recombinations, on this CTA having finished
+// step u, so a buffer is rewritten only after it was read.  The key rows of the next active
+// step (output h of both rows, every level, channel c: l x 2 x 4 KB) are copied into shared
+// memory by TMA, issued by a warp that runs no transform, with the same bounded wait and
+// global-memory fallback as the row-cluster layout.  Every wait is bounded; a wait for
+// another CTA that gives up counts in g_wait_timeouts (the results are then wrong) and the
+// CTA stops waiting.
 template <int T>
 __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster6_kernel(const BrArgs a) {
     static_assert(T == 32, "the channel-cluster layout is built for the 32-bit torus");
@@ -1683,6 +1715,8 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     using Sh = TeamShape<10>;
     constexpr int N = Sh::N, S = Sh::S;
     constexpr int PS = prime_set_for(T);
+    constexpr int NT = kCluster6Warps * 32;  // the recombination gives each thread one 16-byte chunk
+    static_assert(kCluster6Warps == 8, "eight warps: one per chunk column of the swizzled regions");
     extern __shared__ __align__(16) unsigned char smem[];
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -1690,48 +1724,61 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     const int L = a.L, n = a.n;
     const int ct = (int)(blockIdx.x / 6);
     const bool valid = ct < a.count;  // the grid is six CTAs per ciphertext: uniform per cluster
-    const int tid = threadIdx.x, NT = blockDim.x;
+    const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const bool xform = warp < L;  // warp-uniform
     const int lvl = xform ? warp : 0;
+    const bool issuer = tid == NT - 32;  // lane 0 of the last warp, which runs no transform
     const Chan ch = pick_chan(a.ch, c);
     const uint64_t keep = l2_evict_last_policy();
     const uint32_t pinv = 0u - ch.pinv_neg;
     const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
 
     uint32_t* regions = reinterpret_cast<uint32_t*>(smem);          // [L][TBUF] transposes, partials
-    uint32_t* exch = regions + (size_t)L * Sh::TBUF;                // [L][N] written by the partner
-    uint32_t* inbox = exch + (size_t)L * N;                         // [3][N] row h's residues by channel
-    int32_t* acc = reinterpret_cast<int32_t*>(inbox + 3 * N);       // [N] row h
+    uint32_t* exch = regions + (size_t)L * Sh::TBUF;                // [2][L][N] written by the partner
+    uint32_t* inbox = exch + (size_t)2 * L * N;                     // [2][3][N] row h's residues by channel
+    int32_t* acc = reinterpret_cast<int32_t*>(inbox + 6 * N);       // [N] row h
     int16_t* dig = reinterpret_cast<int16_t*>(acc + N);             // [L][N]
     int16_t* sa = dig + (size_t)L * N;                              // [n+1]
     uint32_t* tab0 = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sa + n + 1) + 3) & ~(uintptr_t)3);
     uint32_t* stage = reinterpret_cast<uint32_t*>(smem + brc6_stage_offset(n, L));  // [L][2][1024]
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + brc6_smem_bytes(n, L) - 16);
-    volatile int* stage_ok = reinterpret_cast<volatile int*>(mbar + 1);
-    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + brc6_bars_offset(n, L));
+    volatile int* stage_ok = reinterpret_cast<volatile int*>(bars + kCluster6Bars);
+    const uint32_t bars_a = (uint32_t)__cvta_generic_to_shared(bars);
+    const uint32_t tma_bar = bars_a;                                  // the key stage
+    const uint32_t xbar0 = bars_a + 8u * (1 + lvl), xbar1 = xbar0 + 8u * kClusterMaxLevels;  // exchange, buffer 0/1
+    const uint32_t ibar0 = bars_a + 8u * (1 + 2 * kClusterMaxLevels), ibar1 = ibar0 + 8u;    // inbox, buffer 0/1
     uint32_t* mine = regions + (size_t)lvl * Sh::TBUF;
-    uint32_t* my_exch = exch + (size_t)lvl * N;
-    uint32_t* their_exch = cluster.map_shared_rank(my_exch, 3 * (1 - h) + c);
-    uint32_t* peer_a = cluster.map_shared_rank(inbox + (size_t)c * N, 3 * h + (c == 2 ? 0 : c + 1));
-    uint32_t* peer_b = cluster.map_shared_rank(inbox + (size_t)c * N, 3 * h + (c == 0 ? 2 : c - 1));
+    // the partner's exchange region of this level (buffer 0) and its barriers; the row peers'
+    // inbox of channel c (buffer 0) and theirs
+    const int partner = 3 * (1 - h) + c;
+    const int peer_a = 3 * h + (c == 2 ? 0 : c + 1), peer_b = 3 * h + (c == 0 ? 2 : c - 1);
+    const uint32_t x_dst = cluster_addr((uint32_t)__cvta_generic_to_shared(exch + (size_t)lvl * N), partner);
+    const uint32_t x_bar0 = cluster_addr(xbar0, partner);  // buffer 1: + 8 kClusterMaxLevels
+    const uint32_t box_local = (uint32_t)__cvta_generic_to_shared(inbox + (size_t)c * N);
+    const uint32_t a_dst = cluster_addr(box_local, peer_a), b_dst = cluster_addr(box_local, peer_b);
+    const uint32_t a_bar0 = cluster_addr(ibar0, peer_a), b_bar0 = cluster_addr(ibar0, peer_b);  // buffer 1: + 8
 
     const uint4* key = !valid ? nullptr : (a.key_of ? a.key_table[a.key_of[ct]] : a.key);
     const int64_t* lut = !valid ? nullptr : (a.lut_of ? a.lut_table[a.lut_of[ct]] : a.lut);
     bool tma = valid;  // uniform in the cluster
-    if (tma && tid == 0) {
-        mbar_init(mbar_a, 1);
+    if (tid == 0) {
+        mbar_init(tma_bar, 1);
+        for (int bb = 0; bb < 2; ++bb) {
+            for (int lv = 0; lv < L; ++lv) mbar_init(bars_a + 8u * (1 + bb * kClusterMaxLevels + lv), 1);
+            mbar_init(ibar0 + 8u * bb, 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // thread 0: arms the barrier and copies the key rows of `step` (output h, channel c)
+    // the issuer: arms the stage's barrier and copies the key rows of `step` (output h, channel c)
     auto issue = [&](int step) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(mbar_a, (uint32_t)L * 2 * 4096);
+        mbar_expect_tx(tma_bar, (uint32_t)L * 2 * 4096);
         for (int lv = 0; lv < L; ++lv)
             for (int row = 0; row < 2; ++row) {
                 const size_t blk = (size_t)step * L + lv;
                 const uint4* src = key + ((blk * 2 + row) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
-                bulk_copy_g2s((uint32_t)__cvta_generic_to_shared(stage + (lv * 2 + row) * 1024), src, 4096, mbar_a);
+                bulk_copy_g2s((uint32_t)__cvta_generic_to_shared(stage + (lv * 2 + row) * 1024), src, 4096, tma_bar);
             }
     };
     auto next_active = [&](int from) {
@@ -1739,7 +1786,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         return from;
     };
     uint32_t phase = 0;        // parity of the stage's next barrier phase
-    bool outstanding = false;  // thread 0: a copy issued and not yet waited for
+    bool outstanding = false;  // the issuer: a copy issued and not seen arrive
     const bool use_tab0 = a.radix_bits <= 7;
     if (use_tab0) {
         for (int idx = tid; idx < 129; idx += NT) {
@@ -1759,7 +1806,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         for (int i = tid; i <= n; i += NT) sa[i] = 0;
     }
     __syncthreads();
-    if (tma && tid == 0) {
+    if (tma && issuer) {
         const int f = next_active(0);
         if (f < a.steps) {
             issue(f);
@@ -1781,14 +1828,23 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     } else {
         for (int j = tid; j < N; j += NT) acc[j] = 0;
     }
-    cluster.sync();  // every CTA of the cluster has started: their shared memory may be written
+    cluster.sync();  // every CTA has started and initialised its barriers
 
+    int u = 0;          // active steps so far: buffer u & 1, barrier parity (u >> 1) & 1
+    bool lost = false;  // a wait for another CTA gave up: stop waiting (the results are wrong, counted)
     for (int i = 0; i < a.steps; ++i) {
         const int ai = (int)sa[i];
         if (ai == 0) continue;  // the a_i = 0 skip (blind_rotate.cpp:1557), the same in every CTA
         const int t2 = ai < 0 ? ai + 2 * N : ai;
         const bool wrap = t2 >= N;
         const int at = wrap ? t2 - N : t2;
+        const int b = u & 1;
+        const uint32_t par = (uint32_t)(u >> 1) & 1u;
+        ++u;
+        // arm this step's barriers (their previous phases completed two active steps ago):
+        // the partner's transform of each level, the row peers' residues
+        if (xform && lane == 0) mbar_expect_tx(b ? xbar1 : xbar0, 4096);
+        if (issuer) mbar_expect_tx(b ? ibar1 : ibar0, 2 * 4096);
         // (1) X^{a_i} row - row, zero-mean digits (rotateTrlweMinusOne, gadgetDecomposeTrlwe)
         auto decompose = [&](auto lc, auto rc) {
             constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
@@ -1808,7 +1864,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             decompose(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
         __syncthreads();
         if (xform) {
-            // (2) this level's forward transform, written into the partner's exchange region
+            // (2) this level's forward transform, stored into the partner's exchange region
             uint32_t x[32];
             const int16_t* d = dig + (size_t)lvl * N;
             if (use_tab0) {
@@ -1821,9 +1877,12 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane] + bias;
                 ntt_forward<10, PS>(x, mine, lane, c, 0, ch);
             }
+            {
+                const uint32_t dst = x_dst + 4u * (uint32_t)(b * L * N), bar = x_bar0 + 8u * kClusterMaxLevels * b;
 #pragma unroll
-            for (int r = 0; r < 32; ++r) their_exch[r * S + lane] = x[r];
-            cluster_arrive();
+                for (int k = 0; k < 8; ++k)
+                    st_async_v4(dst + 4u * swz(lane, k), make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]), bar);
+            }
             // own row with K(lvl, h, h) while the partner finishes: x < 46p and key words < p,
             // so the sum of two products fits 64 bits
             const size_t blk = (size_t)i * L + lvl;
@@ -1831,12 +1890,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             const uint4* gpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
             bool from_stage = false;
             if (tma) {
-                from_stage = mbar_wait_bounded(mbar_a, phase, kWaitCycles);
+                from_stage = mbar_wait_bounded(tma_bar, phase, kWaitCycles);
                 if (!from_stage) atomicAdd(&g_wait_timeouts, 1ull);
-                if (tid == 0) {
-                    if (from_stage) outstanding = false;
-                    *stage_ok = from_stage;
-                }
+                if (tid == 0) *stage_ok = from_stage;
             }
             const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + h) * 1024) : nullptr;
             const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + (1 - h)) * 1024) : nullptr;
@@ -1848,31 +1904,34 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
 #pragma unroll
                 for (int e = 0; e < 4; ++e) own[rr * 4 + e] = (uint64_t)x[rr * 4 + e] * kav[e];
             }
-            cluster_wait();  // both rows' transforms are in the partners' exchange regions
+            if (!lost && !mbar_wait_cluster_bounded(b ? xbar1 : xbar0, par, kWaitCycles)) {
+                lost = true;
+                atomicAdd(&g_wait_timeouts, 1ull);
+            }
             // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum
+            const uint32_t* theirs = exch + ((size_t)b * L + lvl) * N;
 #pragma unroll
             for (int rr = 0; rr < 8; ++rr) {
                 const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
-                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w};
+                const uint4 tb = *reinterpret_cast<const uint4*>(theirs + swz(lane, rr));
+                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w}, tv[4] = {tb.x, tb.y, tb.z, tb.w};
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int r = rr * 4 + e;
-                    const uint64_t s = own[r] + (uint64_t)my_exch[r * S + lane] * kbv[e];
+                    const uint64_t s = own[r] + (uint64_t)tv[e] * kbv[e];
                     // s 2^-32 mod p (Montgomery) + p: in (0, 3.1p), reduced after the level sum
                     mine[r * S + lane] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
                 }
             }
-        } else {
-            cluster_arrive();
-            cluster_wait();
         }
         __syncthreads();  // every partial is written, and the stage has been read
         if (tma) {
-            tma = *stage_ok;  // after thread 0 gave up the CTA reads the key from global memory
+            tma = *stage_ok;  // after a wait gave up the CTA reads the key from global memory
             phase ^= 1;
-            if (tma && tid == 0) {
+            if (issuer) {
+                if (tma) outstanding = false;  // the last copy arrived
                 const int f = next_active(i + 1);
-                if (f < a.steps) {
+                if (tma && f < a.steps) {
                     issue(f);
                     outstanding = true;
                 }
@@ -1890,22 +1949,37 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
             }
             ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
-            uint32_t* own_box = inbox + (size_t)c * N;
+            uint32_t* box = inbox + ((size_t)b * 3 + c) * N;
+            const uint32_t off = 4u * (uint32_t)(b * 3 * N);
+            const uint32_t abar = a_bar0 + 8u * b, bbar = b_bar0 + 8u * b;
 #pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                const uint32_t v = reduce_once(oa[r], ch.p);
-                own_box[r * S + lane] = v;
-                peer_a[r * S + lane] = v;
-                peer_b[r * S + lane] = v;
+            for (int k = 0; k < 8; ++k) {
+                const uint4 v = make_uint4(reduce_once(oa[4 * k], ch.p), reduce_once(oa[4 * k + 1], ch.p),
+                                           reduce_once(oa[4 * k + 2], ch.p), reduce_once(oa[4 * k + 3], ch.p));
+                *reinterpret_cast<uint4*>(box + swz(lane, k)) = v;
+                st_async_v4(a_dst + off + 4u * swz(lane, k), v, abar);
+                st_async_v4(b_dst + off + 4u * swz(lane, k), v, bbar);
             }
         }
-        cluster_arrive();
-        cluster_wait();  // the row's three channels are in every inbox of the row
-        // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h
-#pragma unroll 1
-        for (int j = tid; j < N; j += NT) {
-            const int64_t v = crt_to_torus<T>(inbox[j], inbox[N + j], inbox[2 * N + j], a.crt);
-            acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
+        __syncthreads();  // this channel's residues are in the inbox
+        if (!lost && !mbar_wait_cluster_bounded(b ? ibar1 : ibar0, par, kWaitCycles)) {
+            lost = true;
+            atomicAdd(&g_wait_timeouts, 1ull);
+        }
+        // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h: this
+        // thread's chunk (slots 4 warp .. 4 warp + 3 of lane `lane`, coefficients (4 warp + e) 32 + lane)
+        {
+            const uint32_t* box = inbox + (size_t)b * 3 * N + swz(lane, warp);
+            const uint4 r0 = *reinterpret_cast<const uint4*>(box);
+            const uint4 r1 = *reinterpret_cast<const uint4*>(box + N);
+            const uint4 r2 = *reinterpret_cast<const uint4*>(box + 2 * N);
+            const uint32_t v0[4] = {r0.x, r0.y, r0.z, r0.w}, v1[4] = {r1.x, r1.y, r1.z, r1.w}, v2[4] = {r2.x, r2.y, r2.z, r2.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int j = (4 * warp + e) * 32 + lane;
+                const int64_t v = crt_to_torus<T>(v0[e], v1[e], v2[e], a.crt);
+                acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
+            }
         }
         __syncthreads();
     }
@@ -1923,9 +1997,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             dst[N] = acc[0];
         }
     }
-    // a copy that timed out may still land: wait for it (bounded) before the CTA exits
-    if (outstanding && tid == 0 && !mbar_wait_bounded(mbar_a, phase ^ 1, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
-    cluster.sync();  // no CTA leaves while another may still write into its regions
+    // a copy whose wait gave up may still land: wait for it (bounded) before the CTA exits
+    if (outstanding && issuer && !mbar_wait_bounded(tma_bar, phase ^ 1, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
+    cluster.sync();  // no CTA leaves while another may still store into its regions
 }
 
 constexpr int kKsTile = kKsTileCts;  // ciphertexts per block

@@ -317,22 +317,23 @@ __host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
 constexpr int kLayoutChannelCluster = 3;
 constexpr int kCluster6Warps = 8;  // warps 0..l-1 transform; all of them decompose and recombine
 // Shared memory of one CTA of the channel-cluster layout: per level a padded transpose region
-// (also its partial sum after the products) and an exchange region the partner CTA (the
-// other row, the same channel) writes into; the row's residues by channel after the inverse
-// transform (two of them written by the other channels' CTAs); the accumulator row, its
-// digits, the mod-2N input, the channel's first-stage digit table, and the stage the next
-// step's key rows are copied into by TMA ([l][2 rows][1024] words) with its mbarrier and
-// status word.
+// (also its partial sum after the products); two buffers of per-level exchange regions the
+// partner CTA (the other row, the same channel) stores its transforms into; two buffers of
+// the row's residues by channel after the inverse transform (two channels stored by the other
+// CTAs of the row); the accumulator row, its digits, the mod-2N input, the channel's
+// first-stage digit table; the stage the next step's key rows are copied into by TMA
+// ([l][2 rows][1024] words); the mbarriers (the stage's, [2][kClusterMaxLevels] exchange
+// regions', [2] inboxes') and a status word.
+constexpr int kCluster6Bars = 1 + 2 * kClusterMaxLevels + 2;
 __host__ __device__ inline size_t brc6_stage_offset(int n, int L) {
     const size_t N = 1024, tbuf = N + N / 32;
-    size_t b = (size_t)L * tbuf * 4 + (size_t)L * N * 4 + 3 * N * 4;
+    size_t b = (size_t)L * tbuf * 4 + 2 * (size_t)L * N * 4 + 2 * 3 * N * 4;
     b += N * 4 + (size_t)L * N * 2 + ((size_t)n + 1) * 2;
     b = ((b + 3) & ~(size_t)3) + 132 * 4;
     return (b + 127) & ~(size_t)127;
 }
-__host__ __device__ inline size_t brc6_smem_bytes(int n, int L) {
-    return brc6_stage_offset(n, L) + (size_t)L * 2 * 1024 * 4 + 16;
-}
+__host__ __device__ inline size_t brc6_bars_offset(int n, int L) { return brc6_stage_offset(n, L) + (size_t)L * 2 * 1024 * 4; }
+__host__ __device__ inline size_t brc6_smem_bytes(int n, int L) { return brc6_bars_offset(n, L) + 8 * kCluster6Bars + 16; }
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
