@@ -221,6 +221,22 @@ void ctx_init_tables(yg_ctx* c) {
     }
     ck(cudaMalloc(&c->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
     ck(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
+    if (ct_inverse) {
+        // the 16-residue transforms of the latency layout: psi^brv(k) and psi^-e, natural order
+        std::vector<uint2> t16((size_t)yg::kChannels * 2 * N);
+        for (int ci = 0; ci < yg::kChannels; ci++) {
+            const uint32_t p = yg::kPrimeSet[c->ps][ci];
+            const u64 psi = minimal_root(N, p), psi_inv = invmod(psi, p);
+            for (int k = 0; k < N; k++) {
+                const uint32_t wf = (uint32_t)powmod(psi, brv(k, c->logN), p);
+                const uint32_t wi = (uint32_t)powmod(psi_inv, k, p);
+                t16[(size_t)ci * 2 * N + k] = make_uint2(wf, shoup32(wf, p));
+                t16[(size_t)ci * 2 * N + N + k] = make_uint2(wi, shoup32(wi, p));
+            }
+        }
+        ck(cudaMalloc(&c->d_tw16, t16.size() * sizeof(uint2)), "cudaMalloc twiddles");
+        ck(cudaMemcpy(c->d_tw16, t16.data(), t16.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
+    }
     if (yg::set_twiddle_heads(c->logN, c->ps, heads.data()) != 0) ck(cudaGetLastError(), "upload twiddle heads");
     for (int ci = 0; ci < yg::kChannels; ci++) {
         const uint32_t p = yg::kPrimeSet[c->ps][ci];
@@ -892,6 +908,7 @@ yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     a.radix_bits = c->p.radix_bits;
     for (int ci = 0; ci < yg::kChannels; ci++) a.ch[ci] = c->ch[ci];
     a.crt = c->crt;
+    a.tw16 = c->d_tw16;
     a.per_cta = c->per_cta;
     a.layout = c->layout;
     a.grid = c->ctas_per_sm > 0 ? c->ctas_per_sm * c->sm_count : 0;
@@ -1002,6 +1019,7 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
 void yg_ctx_destroy(yg_ctx* ctx) {
     if (!ctx) return;
     if (ctx->d_tw) cudaFree(ctx->d_tw);
+    if (ctx->d_tw16) cudaFree(ctx->d_tw16);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->d_qfwd) cudaFree(ctx->d_qfwd);
     delete ctx;

@@ -32,6 +32,8 @@ struct BrArgs {
     int radix_bits;
     Chan ch[kChannels];
     Crt crt;
+    const uint2* tw16;       // [3][fwd16 N | inv16 N]: the 16-residue transforms' tables (ntt.cuh),
+                             // or null (built for prime set 1, N = 1024)
 };
 
 // A run of at most kKsTileCts consecutive ciphertexts of a batch that share one KSK.
