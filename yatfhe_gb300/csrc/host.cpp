@@ -222,16 +222,14 @@ void ctx_init_tables(yg_ctx* c) {
     ck(cudaMalloc(&c->d_tw, tw.size() * sizeof(uint2)), "cudaMalloc twiddles");
     ck(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(uint2), cudaMemcpyHostToDevice), "upload twiddles");
     if (ct_inverse) {
-        // the 16-residue transforms of the latency layout: psi^brv(k) and psi^-e, natural order
-        std::vector<uint2> t16((size_t)yg::kChannels * 2 * N);
+        // the 16-residue inverse of the channel-cluster layout: psi^-e in natural order
+        std::vector<uint2> t16((size_t)yg::kChannels * N);
         for (int ci = 0; ci < yg::kChannels; ci++) {
             const uint32_t p = yg::kPrimeSet[c->ps][ci];
-            const u64 psi = minimal_root(N, p), psi_inv = invmod(psi, p);
+            const u64 psi_inv = invmod(minimal_root(N, p), p);
             for (int k = 0; k < N; k++) {
-                const uint32_t wf = (uint32_t)powmod(psi, brv(k, c->logN), p);
                 const uint32_t wi = (uint32_t)powmod(psi_inv, k, p);
-                t16[(size_t)ci * 2 * N + k] = make_uint2(wf, shoup32(wf, p));
-                t16[(size_t)ci * 2 * N + N + k] = make_uint2(wi, shoup32(wi, p));
+                t16[(size_t)ci * N + k] = make_uint2(wi, shoup32(wi, p));
             }
         }
         ck(cudaMalloc(&c->d_tw16, t16.size() * sizeof(uint2)), "cudaMalloc twiddles");

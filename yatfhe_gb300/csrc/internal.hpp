@@ -79,7 +79,7 @@ struct yg_ctx {
     int device = 0;
     uint64_t q = 0;
     uint2* d_tw = nullptr;  // [3][3N]: forward twiddles (N), then the inverse table (2N) per channel
-    uint2* d_tw16 = nullptr;  // [3][2N]: psi^brv(k) and psi^-e in natural order (16-residue transforms)
+    uint2* d_tw16 = nullptr;  // [3][N]: psi^-e in natural order (16-residue inverse, T = 32 at N = 1024)
     yg::Chan ch[yg::kChannels]{};
     yg::Crt crt{};
     uint32_t conv_scale[yg::kChannels]{}, conv_scale_s[yg::kChannels]{};

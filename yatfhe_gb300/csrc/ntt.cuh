@@ -306,20 +306,18 @@ __device__ __forceinline__ void ntt_inverse(uint32_t (&a)[32], uint32_t* tb, int
     }
 }
 
-// ---------------------------------------------------------------- 16-residue teams
+// ---------------------------------------------------------------- 16-residue inverse
 // N = 1024, prime set 1, a team of 64 threads (two warps) with 16 residues per thread: half
-// the per-thread chain of the 32-residue team, for the latency layout.  Index bits b9..b0 of
-// a slot or coefficient j, thread tt = (g, beta, gamma) = (tt >> 2, bit 1, bit 0):
-//   natural : register q holds j = q 64 + tt                      (b9..b6 in registers)
-//   middle  : register q holds j = g 64 + q 4 + (tt & 3)          (b5..b2 in registers)
-//   out     : slot16(tt, q) = g 64 + (8 beta + (q & 7)) 4 + gamma 2 + (q >> 3)
-// The forward transform runs 4 register stages (constant twiddles), a transpose, 4 register
-// stages (per-thread twiddles), then index bits 1 and 0 across lane pairs (tt ^ 2, tt ^ 1):
-// each lane sends 8 values and receives 8, and runs 8 whole butterflies; the inverse mirrors
-// it (bits 0 and 1 first, then 2..4 in registers, bit 5 across lanes, a transpose, bits
-// 6..9 and the psi^-j twist).  Twiddles come from plain tables: fwd16[k] = psi^brv(k) and
-// inv16[e] = psi^-e (with Shoup companions), both in natural order.  Same biased arithmetic
-// as the 32-residue transforms (rns.cuh: ct_bfly_b; outputs below 46p).
+// the per-thread chain of the 32-residue inverse, for the latency layout.  Index bits b9..b0
+// of a slot or coefficient j, thread tt = (g, beta, gamma) = (tt >> 2, bit 1, bit 0):
+//   in     : slot16(tt, q) = g 64 + (8 beta + (q & 7)) 4 + gamma 2 + (q >> 3)
+//   middle : register q holds j = g 64 + q 4 + (tt & 3)          (b5..b2 in registers)
+//   out    : register q holds j = q 64 + tt                      (b9..b6 in registers)
+// Index bits 0 and 1 first (bit 1 across lanes tt ^ 1: each lane sends 8 values, receives 8
+// and runs 8 whole butterflies), 2..4 in registers, bit 5 across lanes tt ^ 2, a transpose,
+// bits 6..9 in registers and the psi^-j twist.  Twiddles from a plain table inv16[e] =
+// psi^-e (with Shoup companions) in natural order.  Same biased arithmetic as the
+// 32-residue inverse (rns.cuh: ct_bfly_b).
 
 __device__ __forceinline__ int slot16(int tt, int q) {
     return (tt >> 2) * 64 + (8 * ((tt >> 1) & 1) + (q & 7)) * 4 + (tt & 1) * 2 + (q >> 3);
@@ -327,81 +325,6 @@ __device__ __forceinline__ int slot16(int tt, int q) {
 
 // barrier over the 64 threads of a 16-residue team: named barrier 1 + bar
 __device__ __forceinline__ void team16_sync(int bar) { asm volatile("bar.sync %0, 64;" ::"r"(1 + bar) : "memory"); }
-
-// TAB: a holds signed digits (|d| <= 64); the first stage reads psi^(N/2) d mod p from `tab`.
-template <bool TAB>
-__device__ __forceinline__ void ntt16_forward(uint32_t (&a)[16], uint32_t* tb, int tt, int bar, int chan,
-                                              const Chan& ch, const uint2* fwd16, const uint32_t* tab = nullptr) {
-    constexpr int PS = 1;
-    const uint32_t p = ch.p, neg_p = 0u - p;
-    const int g = tt >> 2;
-    int sp0 = 3;
-    if constexpr (TAB) {
-        const uint32_t bias = 2 * 10 * p;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int dx = (int)a[q], dy = (int)a[q + 8];
-            const uint32_t t = tab[dy];
-            a[q] = (uint32_t)dx + bias + t;
-            a[q + 8] = (uint32_t)dx + bias - t;
-        }
-        sp0 = 2;
-    }
-#pragma unroll
-    for (int sp = 3; sp >= 0; --sp) {
-        if (sp > sp0) continue;
-        const int h = 1 << sp;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            if (q & h) continue;
-            ct_bfly_b(a[q], a[q + h], c_tw_head[PS][0][chan][0][(8 >> sp) + (q >> (sp + 1))], neg_p);
-        }
-    }
-    team16_sync(bar);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) tb[tpad(q * 64 + tt)] = a[q];
-    team16_sync(bar);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) a[q] = tb[tpad(g * 64 + q * 4 + (tt & 3))];
-    const uint2* tw = pinned(fwd16);
-#pragma unroll
-    for (int sp = 3; sp >= 0; --sp) {
-        const int h = 1 << sp;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            if (q & h) continue;
-            ct_bfly_b(a[q], a[q + h], __ldg(&tw[(128 >> sp) + g * (8 >> sp) + (q >> (sp + 1))]), neg_p);
-        }
-    }
-    // index bit 1 (lanes tt, tt ^ 2): beta = 0 takes pairs q < 8, beta = 1 pairs 8..15
-    {
-        const bool hi = (tt >> 1) & 1;
-        const uint2* w1 = tw + 256 + g * 16 + (hi ? 8 : 0);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t recv = __shfl_xor_sync(0xffffffffu, hi ? a[k] : a[8 + k], 2);
-            uint32_t u = hi ? recv : a[k];
-            uint32_t v = hi ? a[8 + k] : recv;
-            ct_bfly_b(u, v, __ldg(&w1[k]), neg_p);
-            a[k] = u;
-            a[8 + k] = v;
-        }
-    }
-    // index bit 0 (lanes tt, tt ^ 1)
-    {
-        const bool hi = tt & 1;
-        const uint2* w0 = tw + 512 + g * 32 + 16 * ((tt >> 1) & 1) + (hi ? 1 : 0);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t recv = __shfl_xor_sync(0xffffffffu, hi ? a[k] : a[8 + k], 1);
-            uint32_t u = hi ? recv : a[k];
-            uint32_t v = hi ? a[8 + k] : recv;
-            ct_bfly_b(u, v, __ldg(&w0[2 * k]), neg_p);
-            a[k] = u;
-            a[8 + k] = v;
-        }
-    }
-}
 
 // Input residues in [0, 2p) at slot16; output N times the coefficients in [0, 2p), natural.
 __device__ __forceinline__ void ntt16_inverse(uint32_t (&a)[16], uint32_t* tb, int tt, int bar, const Chan& ch,

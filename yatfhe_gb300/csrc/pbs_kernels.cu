@@ -1701,12 +1701,13 @@ __device__ __forceinline__ int swz16(int tt, int k) { return tt * 16 + 4 * (k ^ 
 // are in, every thread recombines four coefficients (CRT) and adds them into the CTA's copy
 // of row h.  No scheduler runs more than one transform warp (the row-cluster layout puts nine
 // on an SM's four), so a step costs about one forward and one inverse transform of a warp
-// running alone, and no step waits at a cluster-wide barrier.  W2 (l <= 3): each level's
-// team is two warps with 16 residues per thread (ntt16_forward / ntt16_inverse), and so is
-// warp 0's inverse team (warps 0 and 1), which halves each transform's per-thread chain;
-// the regions then follow the 16-residue order (thread tt's chunk k holds its registers
-// 4k..4k+3, swz16), and thread (tt, k) of the recombination takes coefficients
-// (4k + e) 64 + tt.  Exchange regions and inboxes
+// running alone, and no step waits at a cluster-wide barrier.  The inverse transform runs on
+// warps 0 and 1 with 16 residues per thread (ntt16_inverse: half the per-thread chain on
+// schedulers no other warp uses then); they read the partials in its slot order (slot16),
+// store their residues in 16-byte chunks (thread tt's chunk k holds its coefficients
+// (4k + e) 64 + tt, swz16), and thread (tt, k) of the recombination takes those.  Two-warp
+// forward transforms measured slower: six transform warps on four schedulers put two on
+// two of them.  Exchange regions and inboxes
 // are double-buffered by the parity of the active step: another CTA's store for step u + 2
 // depends, through the chain of transforms and recombinations, on this CTA having finished
 // step u, so a buffer is rewritten only after it was read.  The key rows of the next active
@@ -1715,7 +1716,7 @@ __device__ __forceinline__ int swz16(int tt, int k) { return tt * 16 + 4 * (k ^ 
 // global-memory fallback as the row-cluster layout.  Every wait is bounded; a wait for
 // another CTA that gives up counts in g_wait_timeouts (the results are then wrong) and the
 // CTA stops waiting.
-template <int T, bool W2>
+template <int T>
 __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster6_kernel(const BrArgs a) {
     static_assert(T == 32, "the channel-cluster layout is built for the 32-bit torus");
     namespace cg = cooperative_groups;
@@ -1733,14 +1734,12 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     const bool valid = ct < a.count;  // the grid is six CTAs per ciphertext: uniform per cluster
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    constexpr int TW = W2 ? 2 : 1;               // warps per transform team
-    const bool xform = warp < TW * L;            // warp-uniform
-    const int lvl = xform ? warp / TW : 0;
-    const int tt = W2 ? (warp & 1) * 32 + lane : lane;  // thread in its team
+    const bool xform = warp < L;  // warp-uniform
+    const int lvl = xform ? warp : 0;
+    const int tt = (warp & 1) * 32 + lane;  // warps 0, 1: thread of the inverse team
     const bool issuer = tid == NT - 32;  // lane 0 of the last warp, which runs no transform
     const Chan ch = pick_chan(a.ch, c);
-    const uint2* fwd16 = W2 ? a.tw16 + (size_t)c * 2 * N : nullptr;
-    const uint2* inv16 = W2 ? fwd16 + N : nullptr;
+    const uint2* inv16 = a.tw16 + (size_t)c * N;
     const uint64_t keep = l2_evict_last_policy();
     const uint32_t pinv = 0u - ch.pinv_neg;
     const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
@@ -1854,7 +1853,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         ++u;
         // arm this step's barriers (their previous phases completed two active steps ago):
         // the partner's transform of each level, the row peers' residues
-        if (xform && tt == 0) mbar_expect_tx(b ? xbar1 : xbar0, 4096);  // one arrival per phase: the team's first thread
+        if (xform && lane == 0) mbar_expect_tx(b ? xbar1 : xbar0, 4096);  // one arrival per phase
         if (issuer) mbar_expect_tx(b ? ibar1 : ibar0, 2 * 4096);
         // (1) X^{a_i} row - row, zero-mean digits (rotateTrlweMinusOne, gadgetDecomposeTrlwe)
         auto decompose = [&](auto lc, auto rc) {
@@ -1876,21 +1875,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         __syncthreads();
         if (xform) {
             // (2) this level's forward transform, stored into the partner's exchange region
-            constexpr int R = W2 ? 16 : 32;  // residues per thread
-            uint32_t x[R];
+            uint32_t x[32];
             const int16_t* d = dig + (size_t)lvl * N;
-            if constexpr (W2) {
-                if (use_tab0) {
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) x[q] = (uint32_t)(int32_t)d[q * 64 + tt];
-                    ntt16_forward<true>(x, mine, tt, lvl, c, ch, fwd16, tab0 + 64);
-                } else {
-                    const uint32_t bias = fwd_bias_digits<10, PS>(ch.p);
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) x[q] = (uint32_t)(int32_t)d[q * 64 + tt] + bias;
-                    ntt16_forward<false>(x, mine, tt, lvl, c, ch, fwd16);
-                }
-            } else if (use_tab0) {
+            if (use_tab0) {
 #pragma unroll
                 for (int r = 0; r < 32; ++r) x[r] = (uint32_t)(int32_t)d[r * S + lane];
                 ntt_forward<10, PS, 1>(x, mine, lane, c, 0, ch, tab0 + 64);
@@ -1903,9 +1890,8 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             {
                 const uint32_t dst = x_dst + 4u * (uint32_t)(b * L * N), bar = x_bar0 + 8u * kClusterMaxLevels * b;
 #pragma unroll
-                for (int k = 0; k < R / 4; ++k)
-                    st_async_v4(dst + 4u * (W2 ? swz16(tt, k) : swz(lane, k)),
-                                make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]), bar);
+                for (int k = 0; k < 8; ++k)
+                    st_async_v4(dst + 4u * swz(lane, k), make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]), bar);
             }
             // own row with K(lvl, h, h) while the partner finishes: x < 46p and key words < p,
             // so the sum of two products fits 64 bits
@@ -1919,44 +1905,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 if (tid == 0) *stage_ok = from_stage;
             }
             const uint32_t* theirs = exch + ((size_t)b * L + lvl) * N;
-            if constexpr (W2) {
-                // the key block keeps the 32-residue order: registers q and q + 8 of thread tt
-                // (slots slot16(tt, q), slot16(tt, q + 8)) are words q 128 + 2 tt and + 1
-                const uint32_t* kown = from_stage ? stage + (lvl * 2 + h) * 1024 : reinterpret_cast<const uint32_t*>(gown);
-                const uint32_t* kpar =
-                    from_stage ? stage + (lvl * 2 + (1 - h)) * 1024 : reinterpret_cast<const uint32_t*>(gpar);
-                uint64_t own[16];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const uint2 ka = *reinterpret_cast<const uint2*>(kown + q * 128 + 2 * tt);
-                    own[q] = (uint64_t)x[q] * ka.x;
-                    own[q + 8] = (uint64_t)x[q + 8] * ka.y;
-                }
-                if (!lost && !mbar_wait_cluster_bounded(b ? xbar1 : xbar0, par, kWaitCycles)) {
-                    lost = true;
-                    atomicAdd(&g_wait_timeouts, 1ull);
-                }
-                // the team's other warp may still read the transpose region the partials go to
-                team16_sync(lvl);
-                // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum
-                uint32_t tv[16];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint4 tb = *reinterpret_cast<const uint4*>(theirs + swz16(tt, k));
-                    tv[4 * k] = tb.x;
-                    tv[4 * k + 1] = tb.y;
-                    tv[4 * k + 2] = tb.z;
-                    tv[4 * k + 3] = tb.w;
-                }
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const uint2 kb = *reinterpret_cast<const uint2*>(kpar + q * 128 + 2 * tt);
-                    const uint64_t s0 = own[q] + (uint64_t)tv[q] * kb.x;
-                    const uint64_t s1 = own[q + 8] + (uint64_t)tv[q + 8] * kb.y;
-                    mine[q * 64 + tt] = (uint32_t)(s0 >> 32) - __umulhi((uint32_t)s0 * pinv, ch.p) + ch.p;
-                    mine[(q + 8) * 64 + tt] = (uint32_t)(s1 >> 32) - __umulhi((uint32_t)s1 * pinv, ch.p) + ch.p;
-                }
-            } else {
+            {
                 const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + h) * 1024) : nullptr;
                 const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + (1 - h)) * 1024) : nullptr;
                 uint64_t own[32];
@@ -2001,19 +1950,20 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 }
             }
         }
-        // (4) warp 0 (W2: warps 0 and 1): sum of the l partials, inverse transform, residues
-        // to the row's CTAs
-        if (W2 && warp < 2) {
+        // (4) warps 0 and 1: sum of the l partials, inverse transform, residues to the row's CTAs
+        if (warp < 2) {
             uint32_t oa[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
+                // slot s of register q of thread tt; its partials sit at (s mod 32) 32 + s / 32
+                const int sl = slot16(tt, q), at_s = (sl & 31) * 32 + (sl >> 5);
                 uint32_t v = 0;
 #pragma unroll
                 for (int m = 0; m < kClusterMaxLevels; ++m)
-                    if (m < L) v += regions[(size_t)m * Sh::TBUF + q * 64 + tt];
+                    if (m < L) v += regions[(size_t)m * Sh::TBUF + at_s];
                 oa[q] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
             }
-            ntt16_inverse(oa, mine, tt, 0, ch, inv16);
+            ntt16_inverse(oa, regions, tt, 0, ch, inv16);  // transposes in warp 0's region, after every partial was read
             uint32_t* box = inbox + ((size_t)b * 3 + c) * N;
             const uint32_t off = 4u * (uint32_t)(b * 3 * N);
             const uint32_t abar = a_bar0 + 8u * b, bbar = b_bar0 + 8u * b;
@@ -2025,28 +1975,6 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 st_async_v4(a_dst + off + 4u * swz16(tt, k), v, abar);
                 st_async_v4(b_dst + off + 4u * swz16(tt, k), v, bbar);
             }
-        } else if (!W2 && warp == 0) {
-            uint32_t oa[32];
-#pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                uint32_t v = 0;
-#pragma unroll
-                for (int q = 0; q < kClusterMaxLevels; ++q)
-                    if (q < L) v += regions[(size_t)q * Sh::TBUF + r * S + lane];
-                oa[r] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
-            }
-            ntt_inverse<10, PS>(oa, mine, lane, c, 0, ch);
-            uint32_t* box = inbox + ((size_t)b * 3 + c) * N;
-            const uint32_t off = 4u * (uint32_t)(b * 3 * N);
-            const uint32_t abar = a_bar0 + 8u * b, bbar = b_bar0 + 8u * b;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint4 v = make_uint4(reduce_once(oa[4 * k], ch.p), reduce_once(oa[4 * k + 1], ch.p),
-                                           reduce_once(oa[4 * k + 2], ch.p), reduce_once(oa[4 * k + 3], ch.p));
-                *reinterpret_cast<uint4*>(box + swz(lane, k)) = v;
-                st_async_v4(a_dst + off + 4u * swz(lane, k), v, abar);
-                st_async_v4(b_dst + off + 4u * swz(lane, k), v, bbar);
-            }
         }
         __syncthreads();  // this channel's residues are in the inbox
         if (!lost && !mbar_wait_cluster_bounded(b ? ibar1 : ibar0, par, kWaitCycles)) {
@@ -2054,18 +1982,18 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             atomicAdd(&g_wait_timeouts, 1ull);
         }
         // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h: this
-        // thread's chunk (slots 4 warp .. 4 warp + 3 of lane `lane`, coefficients (4 warp + e) 32 + lane;
-        // W2: chunk tid >> 6 of team thread tid & 63, coefficients (4 (tid >> 6) + e) 64 + (tid & 63))
+        // thread's chunk, chunk tid >> 6 of inverse-team thread tid & 63, coefficients
+        // (4 (tid >> 6) + e) 64 + (tid & 63)
         {
-            const int ck = W2 ? tid >> 6 : warp, cl = W2 ? tid & 63 : lane;
-            const uint32_t* box = inbox + (size_t)b * 3 * N + (W2 ? swz16(cl, ck) : swz(cl, ck));
+            const int ck = tid >> 6, cl = tid & 63;
+            const uint32_t* box = inbox + (size_t)b * 3 * N + swz16(cl, ck);
             const uint4 r0 = *reinterpret_cast<const uint4*>(box);
             const uint4 r1 = *reinterpret_cast<const uint4*>(box + N);
             const uint4 r2 = *reinterpret_cast<const uint4*>(box + 2 * N);
             const uint32_t v0[4] = {r0.x, r0.y, r0.z, r0.w}, v1[4] = {r1.x, r1.y, r1.z, r1.w}, v2[4] = {r2.x, r2.y, r2.z, r2.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                const int j = W2 ? (4 * ck + e) * 64 + cl : (4 * ck + e) * 32 + cl;
+                const int j = (4 * ck + e) * 64 + cl;
                 const int64_t v = crt_to_torus<T>(v0[e], v1[e], v2[e], a.crt);
                 acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
             }
@@ -2268,9 +2196,7 @@ int prepare_brc() {
     if (!done[dev].load()) {
         if (cudaFuncSetAttribute(blind_rotate_cluster_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  227 * 1024) != cudaSuccess ||
-            cudaFuncSetAttribute(blind_rotate_cluster6_kernel<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 227 * 1024) != cudaSuccess ||
-            cudaFuncSetAttribute(blind_rotate_cluster6_kernel<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(blind_rotate_cluster6_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  227 * 1024) != cudaSuccess)
             return -1;
         done[dev].store(true);
@@ -2293,12 +2219,8 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
         if (!cluster_variant(logN, torus_bits, a.per_cta, a.L)) return kNoVariant;
         const size_t smem = brc6_smem_bytes(a.n, a.L);
         if (smem > 227 * 1024 || prepare_brc() != 0) return -1;
-        // two-warp teams when the context has the 16-residue tables and 2 l teams' warps leave
-        // the issuing warp free
-        if (a.tw16 && a.L <= 3)
-            blind_rotate_cluster6_kernel<32, true><<<6 * a.count, kCluster6Warps * 32, smem, (cudaStream_t)stream>>>(a);
-        else
-            blind_rotate_cluster6_kernel<32, false><<<6 * a.count, kCluster6Warps * 32, smem, (cudaStream_t)stream>>>(a);
+        if (!a.tw16) return -1;  // the 16-residue inverse's tables (built for every T = 32, N = 1024 context)
+        blind_rotate_cluster6_kernel<32><<<6 * a.count, kCluster6Warps * 32, smem, (cudaStream_t)stream>>>(a);
         return cudaGetLastError() == cudaSuccess ? 0 : -1;
     }
     return dispatch_br(logN, torus_bits, a.per_cta, a.layout, LaunchBr{a, stream});
@@ -2326,7 +2248,7 @@ int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layo
         if (smem > 227 * 1024) return 0;
         if (prepare_brc() != 0) return -1;
         int blocks = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_cluster6_kernel<32, false>, kCluster6Warps * 32,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, blind_rotate_cluster6_kernel<32>, kCluster6Warps * 32,
                                                           smem) != cudaSuccess) {
             // the calculator may decline cluster kernels: 168 registers x 256 threads and the
             // shared memory fit one SM

@@ -32,8 +32,7 @@ struct BrArgs {
     int radix_bits;
     Chan ch[kChannels];
     Crt crt;
-    const uint2* tw16;       // [3][fwd16 N | inv16 N]: the 16-residue transforms' tables (ntt.cuh),
-                             // or null (built for prime set 1, N = 1024)
+    const uint2* tw16;       // [3][N] psi^-e mod p_c with Shoup companions (ntt16_inverse), or null
 };
 
 // A run of at most kKsTileCts consecutive ciphertexts of a batch that share one KSK.
