@@ -1652,20 +1652,22 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     cluster.sync();  // neither CTA leaves while the other may still write into its regions
 }
 
-// Point-to-point signalling between the CTAs of a cluster: 16-byte stores into another CTA's
-// shared memory that complete bytes of the transaction count of an mbarrier there, so the
+// Point-to-point signalling between the CTAs of a cluster: a bulk copy (TMA) from this CTA's
+// shared memory into another CTA's that completes its bytes on an mbarrier there, so the
 // receiver waits for exactly the data it needs instead of a cluster-wide barrier.
 __device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int rank) {
     uint32_t r;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
     return r;
 }
-__device__ __forceinline__ void st_async_v4(uint32_t addr, uint4 v, uint32_t bar) {
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(addr),
-                 "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(bar)
+// `bytes` (a multiple of 16) from this CTA's shared memory at `src` to the cluster address
+// `dst`, completing them on the mbarrier at the cluster address `bar` (16-byte aligned both)
+__device__ __forceinline__ void bulk_s2c(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "r"(src), "r"(bytes), "r"(bar)
                  : "memory");
 }
-// Waits (at most `cycles` clocks) for a phase completed by other CTAs' stores.
+// Waits (at most `cycles` clocks) for a phase completed by other CTAs' copies.
 __device__ __forceinline__ bool mbar_wait_cluster_bounded(uint32_t bar, uint32_t parity, long long cycles) {
     const long long t0 = clock64();
     for (;;) {
@@ -1691,31 +1693,32 @@ __device__ __forceinline__ int swz16(int tt, int k) { return tt * 16 + 4 * (k ^ 
 // computes output h of every external product in that channel; its warp lvl < l runs the
 // forward transform of digit level lvl.  Per CMux step: (1) all threads rotate and decompose
 // row h into l digit rows (the three CTAs of a row compute the same digits); (2) each
-// transform warp runs its level's forward transform and stores it (st.async) into the
-// exchange region of the same level in the partner CTA (the other row, the same channel),
-// completing the partner's barrier for that level, then multiplies its own transform with the
-// key words K(lvl, h, h); (3) once the partner's transform is in, the partner's with
-// K(lvl, 1 - h, h): an exact 64-bit sum of two products reduced once; (4) warp 0 adds the l
-// partials, runs the inverse transform and stores row h's residues in channel c into its own
-// inbox and (st.async) the two other CTAs of row h; (5) once the two other channels' residues
-// are in, every thread recombines four coefficients (CRT) and adds them into the CTA's copy
-// of row h.  No scheduler runs more than one transform warp (the row-cluster layout puts nine
-// on an SM's four), so a step costs about one forward and one inverse transform of a warp
-// running alone, and no step waits at a cluster-wide barrier.  The inverse transform runs on
-// warps 0 and 1 with 16 residues per thread (ntt16_inverse: half the per-thread chain on
-// schedulers no other warp uses then); they read the partials in its slot order (slot16),
-// store their residues in 16-byte chunks (thread tt's chunk k holds its coefficients
-// (4k + e) 64 + tt, swz16), and thread (tt, k) of the recombination takes those.  Two-warp
-// forward transforms measured slower: six transform warps on four schedulers put two on
-// two of them.  Exchange regions and inboxes
-// are double-buffered by the parity of the active step: another CTA's store for step u + 2
+// transform warp runs its level's forward transform, writes it into its send buffer and one
+// lane copies that (cp.async.bulk, shared memory to shared memory) into the exchange region
+// of the same level in the partner CTA (the other row, the same channel), completing the
+// partner's barrier for that level; it then multiplies its own transform with the key words
+// K(lvl, h, h); (3) once the partner's transform is in, the partner's with K(lvl, 1 - h, h):
+// an exact 64-bit sum of two products reduced once; (4) warps 0 and 1 add the l partials,
+// run the inverse transform, write row h's residues in channel c into the CTA's inbox and
+// copy them into the inboxes of the two other CTAs of row h; (5) once the two other
+// channels' residues are in, every thread recombines four coefficients (CRT) and adds them
+// into the CTA's copy of row h.  No scheduler runs more than one transform warp (the
+// row-cluster layout puts nine on an SM's four), so a step costs about one forward and one
+// inverse transform of a warp running alone, and no step waits at a cluster-wide barrier.
+// The inverse runs with 16 residues per thread (ntt16_inverse: half the per-thread chain, on
+// schedulers no other warp uses then); warps 0 and 1 read the partials in its slot order
+// (slot16) and write their residues in 16-byte chunks (thread tt's chunk k holds its
+// coefficients (4k + e) 64 + tt, swz16), and thread (tt, k) of the recombination takes
+// those.  Two-warp forward transforms measured slower: six transform warps on four
+// schedulers put two on two of them.  Send buffers, exchange regions and inboxes are
+// double-buffered by the parity of the active step: another CTA's copy for step u + 2
 // depends, through the chain of transforms and recombinations, on this CTA having finished
-// step u, so a buffer is rewritten only after it was read.  The key rows of the next active
-// step (output h of both rows, every level, channel c: l x 2 x 4 KB) are copied into shared
-// memory by TMA, issued by a warp that runs no transform, with the same bounded wait and
-// global-memory fallback as the row-cluster layout.  Every wait is bounded; a wait for
-// another CTA that gives up counts in g_wait_timeouts (the results are then wrong) and the
-// CTA stops waiting.
+// step u, so a buffer is rewritten only after it was read (and a send buffer only after
+// its copy arrived).  The key rows of the next active step (output h of both rows, every
+// level, channel c: l x 2 x 4 KB) are copied into shared memory by TMA, issued by a warp
+// that runs no transform, with the same bounded wait and global-memory fallback as the
+// row-cluster layout.  Every wait is bounded; a wait for another CTA that gives up counts in
+// g_wait_timeouts (the results are then wrong) and the CTA stops waiting.
 template <int T>
 __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster6_kernel(const BrArgs a) {
     static_assert(T == 32, "the channel-cluster layout is built for the 32-bit torus");
@@ -1754,6 +1757,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     uint32_t* stage = reinterpret_cast<uint32_t*>(smem + brc6_stage_offset(n, L));  // [L][2][1024]
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + brc6_bars_offset(n, L));
     volatile int* stage_ok = reinterpret_cast<volatile int*>(bars + kCluster6Bars);
+    uint32_t* sendbuf = reinterpret_cast<uint32_t*>(smem + brc6_send_offset(n, L));  // [2][L][N]
     const uint32_t bars_a = (uint32_t)__cvta_generic_to_shared(bars);
     const uint32_t tma_bar = bars_a;                                  // the key stage
     const uint32_t xbar0 = bars_a + 8u * (1 + lvl), xbar1 = xbar0 + 8u * kClusterMaxLevels;  // exchange, buffer 0/1
@@ -1859,13 +1863,20 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         auto decompose = [&](auto lc, auto rc) {
             constexpr int LC = decltype(lc)::value, RC = decltype(rc)::value;
             const int levels = LC ? LC : L, radix = RC ? RC : a.radix_bits;
-#pragma unroll 1
-            for (int j = tid; j < N; j += NT) {
+            // coefficients tid + e NT: every accumulator word is loaded before any digit is stored
+            constexpr int E = N / NT;
+            int32_t tmp[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int j = tid + e * NT;
                 int32_t rot = j < at ? tneg<T>(acc[j - at + N]) : acc[j - at];
                 if (wrap) rot = tneg<T>(rot);
-                const int32_t tmp = tsub<T>(rot, acc[j]);
-                int16_t* d = dig + j;
-                zero_mean_digits<uint32_t, 32>((uint32_t)tmp, levels, radix, [&](int level, int v) { d[level * N] = (int16_t)v; });
+                tmp[e] = tsub<T>(rot, acc[j]);
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                int16_t* d = dig + tid + e * NT;
+                zero_mean_digits<uint32_t, 32>((uint32_t)tmp[e], levels, radix, [&](int level, int v) { d[level * N] = (int16_t)v; });
             }
         };
         if (L == 3 && a.radix_bits == 7)
@@ -1889,9 +1900,13 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             }
             {
                 const uint32_t dst = x_dst + 4u * (uint32_t)(b * L * N), bar = x_bar0 + 8u * kClusterMaxLevels * b;
+                uint32_t* sb = sendbuf + ((size_t)b * L + lvl) * N;
 #pragma unroll
                 for (int k = 0; k < 8; ++k)
-                    st_async_v4(dst + 4u * swz(lane, k), make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]), bar);
+                    *reinterpret_cast<uint4*>(sb + swz(lane, k)) = make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) bulk_s2c(dst, (uint32_t)__cvta_generic_to_shared(sb), 4096, bar);
             }
             // own row with K(lvl, h, h) while the partner finishes: x < 46p and key words < p,
             // so the sum of two products fits 64 bits
@@ -1920,8 +1935,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                     lost = true;
                     atomicAdd(&g_wait_timeouts, 1ull);
                 }
-                __syncwarp();  // the transpose reads of every lane precede the partials' writes
-                // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum
+                // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum;
+                // the partials are stored after every load, so the loads need not wait for them
+                uint32_t res[32];
 #pragma unroll
                 for (int rr = 0; rr < 8; ++rr) {
                     const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
@@ -1932,9 +1948,12 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                         const int r = rr * 4 + e;
                         const uint64_t s = own[r] + (uint64_t)tv[e] * kbv[e];
                         // s 2^-32 mod p (Montgomery) + p: in (0, 3.1p), reduced after the level sum
-                        mine[r * S + lane] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
+                        res[r] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
                     }
                 }
+                __syncwarp();  // the transpose reads of every lane precede the partials' writes
+#pragma unroll
+                for (int r = 0; r < 32; ++r) mine[r * S + lane] = res[r];
             }
         }
         __syncthreads();  // every partial is written, and the stage has been read
@@ -1972,8 +1991,13 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 const uint4 v = make_uint4(reduce_once(oa[4 * k], ch.p), reduce_once(oa[4 * k + 1], ch.p),
                                            reduce_once(oa[4 * k + 2], ch.p), reduce_once(oa[4 * k + 3], ch.p));
                 *reinterpret_cast<uint4*>(box + swz16(tt, k)) = v;
-                st_async_v4(a_dst + off + 4u * swz16(tt, k), v, abar);
-                st_async_v4(b_dst + off + 4u * swz16(tt, k), v, bbar);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            team16_sync(0);
+            if (tt == 0) {
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(box);
+                bulk_s2c(a_dst + off, src, 4096, abar);
+                bulk_s2c(b_dst + off, src, 4096, bbar);
             }
         }
         __syncthreads();  // this channel's residues are in the inbox
@@ -1991,11 +2015,13 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
             const uint4 r1 = *reinterpret_cast<const uint4*>(box + N);
             const uint4 r2 = *reinterpret_cast<const uint4*>(box + 2 * N);
             const uint32_t v0[4] = {r0.x, r0.y, r0.z, r0.w}, v1[4] = {r1.x, r1.y, r1.z, r1.w}, v2[4] = {r2.x, r2.y, r2.z, r2.w};
+            uint32_t old[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) old[e] = (uint32_t)acc[(4 * ck + e) * 64 + cl];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                const int j = (4 * ck + e) * 64 + cl;
                 const int64_t v = crt_to_torus<T>(v0[e], v1[e], v2[e], a.crt);
-                acc[j] = (int32_t)((uint32_t)acc[j] + (uint32_t)v);
+                acc[(4 * ck + e) * 64 + cl] = (int32_t)(old[e] + (uint32_t)v);
             }
         }
         __syncthreads();

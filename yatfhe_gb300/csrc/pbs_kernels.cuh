@@ -324,7 +324,8 @@ constexpr int kCluster6Warps = 8;  // warps 0..l-1 transform; all of them decomp
 // CTAs of the row); the accumulator row, its digits, the mod-2N input, the channel's
 // first-stage digit table; the stage the next step's key rows are copied into by TMA
 // ([l][2 rows][1024] words); the mbarriers (the stage's, [2][kClusterMaxLevels] exchange
-// regions', [2] inboxes') and a status word.
+// regions', [2] inboxes') and a status word in 128 bytes; two buffers of per-level send
+// buffers the transforms are copied to the partner from.
 constexpr int kCluster6Bars = 1 + 2 * kClusterMaxLevels + 2;
 __host__ __device__ inline size_t brc6_stage_offset(int n, int L) {
     const size_t N = 1024, tbuf = N + N / 32;
@@ -334,7 +335,9 @@ __host__ __device__ inline size_t brc6_stage_offset(int n, int L) {
     return (b + 127) & ~(size_t)127;
 }
 __host__ __device__ inline size_t brc6_bars_offset(int n, int L) { return brc6_stage_offset(n, L) + (size_t)L * 2 * 1024 * 4; }
-__host__ __device__ inline size_t brc6_smem_bytes(int n, int L) { return brc6_bars_offset(n, L) + 8 * kCluster6Bars + 16; }
+static_assert(8 * kCluster6Bars + 4 <= 128, "the barriers and the status word fit the 128 bytes before the send buffers");
+__host__ __device__ inline size_t brc6_send_offset(int n, int L) { return brc6_bars_offset(n, L) + 128; }
+__host__ __device__ inline size_t brc6_smem_bytes(int n, int L) { return brc6_send_offset(n, L) + (size_t)2 * L * 1024 * 4; }
 __host__ __device__ inline size_t br_smem_bytes(int logN, int torus_bits, int n, int L, int layout) {
     const size_t N = (size_t)1 << logN;
     const size_t tbuf = N + N / 32;
