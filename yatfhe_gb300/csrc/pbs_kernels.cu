@@ -1747,8 +1747,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     const uint32_t pinv = 0u - ch.pinv_neg;
     const uint32_t one_s = 0xFFFFFFFFu / ch.p;  // floor(2^32 / p): Shoup reduction by 1
 
-    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);          // [L][TBUF] transposes, partials
-    uint32_t* exch = regions + (size_t)L * Sh::TBUF;                // [2][L][N] written by the partner
+    uint32_t* regions = reinterpret_cast<uint32_t*>(smem);          // [L][TBUF] transposes
+    uint32_t* psum = regions + (size_t)L * Sh::TBUF;                // [N] the levels' partials, summed
+    uint32_t* exch = psum + N;                                      // [2][L][N] written by the partner
     uint32_t* inbox = exch + (size_t)2 * L * N;                     // [2][3][N] row h's residues by channel
     int32_t* acc = reinterpret_cast<int32_t*>(inbox + 6 * N);       // [N] row h
     int16_t* dig = reinterpret_cast<int16_t*>(acc + N);             // [L][N]
@@ -1799,8 +1800,8 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         while (from < a.steps && sa[from] == 0) ++from;
         return from;
     };
-    uint32_t phase = 0;        // parity of the stage's next barrier phase
-    bool outstanding = false;  // the issuer: a copy issued and not seen arrive
+    uint32_t phase = 0;        // the issuer: parity of the stage's next barrier phase
+    bool outstanding = false;  // the issuer: a copy whose wait gave up
     const bool use_tab0 = a.radix_bits <= 7;
     if (use_tab0) {
         for (int idx = tid; idx < 129; idx += NT) {
@@ -1819,13 +1820,27 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
     } else {
         for (int i = tid; i <= n; i += NT) sa[i] = 0;
     }
+    for (int j = tid; j < N; j += NT) psum[j] = 0;
     __syncthreads();
-    if (tma && issuer) {
-        const int f = next_active(0);
-        if (f < a.steps) {
-            issue(f);
+    // the issuer copies the key rows of the next active step and waits for them (bounded)
+    // while the transform warps work; stage_ok tells the step's readers whether they arrived
+    auto refill = [&](int from) {
+        const int f = next_active(from);
+        if (!tma || f >= a.steps) return;
+        issue(f);
+        if (mbar_wait_bounded(tma_bar, phase, kWaitCycles)) {
+            phase ^= 1;
+            *stage_ok = 1;
+        } else {
+            atomicAdd(&g_wait_timeouts, 1ull);
+            tma = false;  // read the key from global memory from here on
             outstanding = true;
+            *stage_ok = 0;
         }
+    };
+    if (issuer) {
+        *stage_ok = 0;
+        refill(0);
     }
     if (valid && a.acc_in) {
         for (int j = tid; j < N; j += NT) acc[j] = (int32_t)a.acc_in[(size_t)ct * 2 * N + h * N + j];
@@ -1908,24 +1923,21 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 __syncwarp();
                 if (lane == 0) bulk_s2c(dst, (uint32_t)__cvta_generic_to_shared(sb), 4096, bar);
             }
+            // the helper warp (4 + lvl) takes slots 16..31 of each lane: it may read the send buffer
+            asm volatile("bar.arrive %0, 64;" ::"r"(2 + lvl) : "memory");
             // own row with K(lvl, h, h) while the partner finishes: x < 46p and key words < p,
             // so the sum of two products fits 64 bits
             const size_t blk = (size_t)i * L + lvl;
             const uint4* gown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
             const uint4* gpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
-            bool from_stage = false;
-            if (tma) {
-                from_stage = mbar_wait_bounded(tma_bar, phase, kWaitCycles);
-                if (!from_stage) atomicAdd(&g_wait_timeouts, 1ull);
-                if (tid == 0) *stage_ok = from_stage;
-            }
+            const bool from_stage = *stage_ok;
             const uint32_t* theirs = exch + ((size_t)b * L + lvl) * N;
             {
                 const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + h) * 1024) : nullptr;
                 const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + (lvl * 2 + (1 - h)) * 1024) : nullptr;
-                uint64_t own[32];
+                uint64_t own[16];
 #pragma unroll
-                for (int rr = 0; rr < 8; ++rr) {
+                for (int rr = 0; rr < 4; ++rr) {
                     const uint4 ka = from_stage ? kown[rr * S + lane] : ldg_keep(gown + rr * S + lane, keep);
                     const uint32_t kav[4] = {ka.x, ka.y, ka.z, ka.w};
 #pragma unroll
@@ -1937,9 +1949,9 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                 }
                 // (3) the partner's row with K(lvl, 1 - h, h), one Montgomery reduction per sum;
                 // the partials are stored after every load, so the loads need not wait for them
-                uint32_t res[32];
+                uint32_t res[16];
 #pragma unroll
-                for (int rr = 0; rr < 8; ++rr) {
+                for (int rr = 0; rr < 4; ++rr) {
                     const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
                     const uint4 tb = *reinterpret_cast<const uint4*>(theirs + swz(lane, rr));
                     const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w}, tv[4] = {tb.x, tb.y, tb.z, tb.w};
@@ -1951,35 +1963,62 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
                         res[r] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
                     }
                 }
-                __syncwarp();  // the transpose reads of every lane precede the partials' writes
 #pragma unroll
-                for (int r = 0; r < 32; ++r) mine[r * S + lane] = res[r];
+                for (int r = 0; r < 16; ++r) atomicAdd(&psum[r * S + lane], res[r]);
             }
-        }
-        __syncthreads();  // every partial is written, and the stage has been read
-        if (tma) {
-            tma = *stage_ok;  // after a wait gave up the CTA reads the key from global memory
-            phase ^= 1;
-            if (issuer) {
-                if (tma) outstanding = false;  // the last copy arrived
-                const int f = next_active(i + 1);
-                if (tma && f < a.steps) {
-                    issue(f);
-                    outstanding = true;
+        } else if (warp >= 4 && warp - 4 < L) {
+            // helper of level hl: slots 16..31 of each lane, its transform read from the send buffer
+            const int hl = warp - 4;
+            asm volatile("bar.sync %0, 64;" ::"r"(2 + hl) : "memory");
+            const uint32_t* sb = sendbuf + ((size_t)b * L + hl) * N;
+            const size_t blk = (size_t)i * L + hl;
+            const uint4* gown = key + ((blk * 2 + h) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+            const uint4* gpar = key + ((blk * 2 + (1 - h)) * kChannels + c) * (key_block_words(N) / 4) + (h ? 8 : 0) * S;
+            const bool from_stage = *stage_ok;
+            const uint32_t* theirs = exch + ((size_t)b * L + hl) * N;
+            const uint4* kown = from_stage ? reinterpret_cast<const uint4*>(stage + (hl * 2 + h) * 1024) : nullptr;
+            const uint4* spar = from_stage ? reinterpret_cast<const uint4*>(stage + (hl * 2 + (1 - h)) * 1024) : nullptr;
+            uint64_t own[16];
+#pragma unroll
+            for (int rr = 4; rr < 8; ++rr) {
+                const uint4 xa = *reinterpret_cast<const uint4*>(sb + swz(lane, rr));
+                const uint4 ka = from_stage ? kown[rr * S + lane] : ldg_keep(gown + rr * S + lane, keep);
+                own[(rr - 4) * 4 + 0] = (uint64_t)xa.x * ka.x;
+                own[(rr - 4) * 4 + 1] = (uint64_t)xa.y * ka.y;
+                own[(rr - 4) * 4 + 2] = (uint64_t)xa.z * ka.z;
+                own[(rr - 4) * 4 + 3] = (uint64_t)xa.w * ka.w;
+            }
+            const uint32_t hbar = bars_a + 8u * (1 + b * kClusterMaxLevels + hl);
+            if (!lost && !mbar_wait_cluster_bounded(hbar, par, kWaitCycles)) {
+                lost = true;
+                atomicAdd(&g_wait_timeouts, 1ull);
+            }
+            uint32_t res[16];
+#pragma unroll
+            for (int rr = 4; rr < 8; ++rr) {
+                const uint4 kb = from_stage ? spar[rr * S + lane] : ldg_keep(gpar + rr * S + lane, keep);
+                const uint4 tb = *reinterpret_cast<const uint4*>(theirs + swz(lane, rr));
+                const uint32_t kbv[4] = {kb.x, kb.y, kb.z, kb.w}, tv[4] = {tb.x, tb.y, tb.z, tb.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int q = (rr - 4) * 4 + e;
+                    const uint64_t s = own[q] + (uint64_t)tv[e] * kbv[e];
+                    res[q] = (uint32_t)(s >> 32) - __umulhi((uint32_t)s * pinv, ch.p) + ch.p;
                 }
             }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) atomicAdd(&psum[(16 + q) * S + lane], res[q]);
         }
+        __syncthreads();  // every partial is in, and the stage has been read
+        if (issuer) refill(i + 1);
         // (4) warps 0 and 1: sum of the l partials, inverse transform, residues to the row's CTAs
         if (warp < 2) {
             uint32_t oa[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
-                // slot s of register q of thread tt; its partials sit at (s mod 32) 32 + s / 32
-                const int sl = slot16(tt, q), at_s = (sl & 31) * 32 + (sl >> 5);
-                uint32_t v = 0;
-#pragma unroll
-                for (int m = 0; m < kClusterMaxLevels; ++m)
-                    if (m < L) v += regions[(size_t)m * Sh::TBUF + at_s];
+                // slot s of register q of thread tt: its partial sum sits at (s mod 32) 32 + s / 32
+                const int sl = slot16(tt, q);
+                const uint32_t v = psum[(sl & 31) * 32 + (sl >> 5)];
                 oa[q] = v - __umulhi(v, one_s) * ch.p;  // l terms < 3.1p each: < 13p; reduced to [0, 2p)
             }
             ntt16_inverse(oa, regions, tt, 0, ch, inv16);  // transposes in warp 0's region, after every partial was read
@@ -2008,6 +2047,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         // (5) CRT -> applyIntt's centred mod-q value mod 2^32, accumulateTrlwe on row h: this
         // thread's chunk, chunk tid >> 6 of inverse-team thread tid & 63, coefficients
         // (4 (tid >> 6) + e) 64 + (tid & 63)
+        *reinterpret_cast<uint4*>(psum + 4 * tid) = make_uint4(0, 0, 0, 0);  // read before the inbox barrier
         {
             const int ck = tid >> 6, cl = tid & 63;
             const uint32_t* box = inbox + (size_t)b * 3 * N + swz16(cl, ck);
@@ -2041,7 +2081,7 @@ __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_c
         }
     }
     // a copy whose wait gave up may still land: wait for it (bounded) before the CTA exits
-    if (outstanding && issuer && !mbar_wait_bounded(tma_bar, phase ^ 1, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
+    if (outstanding && issuer && !mbar_wait_bounded(tma_bar, phase, kWaitCycles)) atomicAdd(&g_wait_timeouts, 1ull);
     cluster.sync();  // no CTA leaves while another may still store into its regions
 }
 

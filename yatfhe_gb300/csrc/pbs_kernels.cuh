@@ -317,8 +317,8 @@ __host__ __device__ inline size_t brc_smem_bytes(int n, int L) {
 // transform warp per scheduler.
 constexpr int kLayoutChannelCluster = 3;
 constexpr int kCluster6Warps = 8;  // warps 0..l-1 transform; all of them decompose and recombine
-// Shared memory of one CTA of the channel-cluster layout: per level a padded transpose region
-// (also its partial sum after the products); two buffers of per-level exchange regions the
+// Shared memory of one CTA of the channel-cluster layout: per level a padded transpose region;
+// the sum of the levels' partial products; two buffers of per-level exchange regions the
 // partner CTA (the other row, the same channel) stores its transforms into; two buffers of
 // the row's residues by channel after the inverse transform (two channels stored by the other
 // CTAs of the row); the accumulator row, its digits, the mod-2N input, the channel's
@@ -329,7 +329,7 @@ constexpr int kCluster6Warps = 8;  // warps 0..l-1 transform; all of them decomp
 constexpr int kCluster6Bars = 1 + 2 * kClusterMaxLevels + 2;
 __host__ __device__ inline size_t brc6_stage_offset(int n, int L) {
     const size_t N = 1024, tbuf = N + N / 32;
-    size_t b = (size_t)L * tbuf * 4 + 2 * (size_t)L * N * 4 + 2 * 3 * N * 4;
+    size_t b = (size_t)L * tbuf * 4 + N * 4 + 2 * (size_t)L * N * 4 + 2 * 3 * N * 4;
     b += N * 4 + (size_t)L * N * 2 + ((size_t)n + 1) * 2;
     b = ((b + 3) & ~(size_t)3) + 132 * 4;
     return (b + 127) & ~(size_t)127;
