@@ -827,12 +827,14 @@ def leg_multi_tenant(dev, steps=2, warmup=1, total=32768):
 
 
 def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), tenants=128, budget=4e9,
-                max_count=256, max_batch=304, max_inflight=2):
+                max_count=256, max_batch=304, max_inflight=2, latency_batch_max=0):
     """128 tenants on the TORUS=32 set, requests of 1..256 ciphertexts (log-uniform) arriving
     as a Poisson process, tenants Zipf(1.1)-popular, BSK/KSK in an HBM LRU cache capped at
     4 GB with refills from pinned host memory.  First the peak rate is measured with the
     offered load far above capacity, then each fraction of it is offered; every output is
-    compared with the same tenant's ciphertexts bootstrapped alone."""
+    compared with the same tenant's ciphertexts bootstrapped alone.  Batches of at most
+    latency_batch_max ciphertexts (0: the library's default, two waves of six-CTA clusters)
+    run in the channel-cluster latency layout."""
     import torch
 
     from yatfhe_gb300 import api, autotune, serving
@@ -852,7 +854,7 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
         if srv is None:
             tuning = autotune.tune(ctx, key, d_lut, objective="latency")
             srv = serving.Server(ctx, key_budget_bytes=budget, max_batch=max_batch, max_inflight=max_inflight,
-                                 max_tenants=tenants)
+                                 max_tenants=tenants, latency_batch_max=latency_batch_max)
         lwe = synthetic_lwe(p, max_count, 0x5EED3000 + t)
         pool[t] = torch.from_numpy(lwe)
         d_in = pool[t].to(f"cuda:{dev}")
@@ -877,6 +879,7 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
                        "p50_ms": r["sojourn"]["p50_ms"], "p99_ms": r["sojourn"]["p99_ms"],
                        "queue_p99_ms": r["queue"]["p99_ms"], "service_p50_ms": r["service"]["p50_ms"],
                        "hit_rate": r["hit_rate"], "key_misses": r["key_misses"], "batches": r["batches"],
+                       "latency_layout_batches": r["latency_batches"],
                        "slo_ms": r["slo_ms"], "slo_violation_rate": r["slo_violation_rate"],
                        "slo_violation_rate_100": r["slo_violation_rate_100"],
                        "slo_violation_rate_300": r["slo_violation_rate_300"],
@@ -889,7 +892,7 @@ def leg_serving(dev, requests=800, fractions=(0.5, 0.6, 0.7, 0.8, 0.9, 1.0), ten
     return {"workload": "serving_t32_128tenants_4GB", "tenants": tenants, "key_budget_bytes": int(budget),
             "key_slots": slots, "resident_fraction": slots / tenants, "max_batch": max_batch,
             "max_inflight": max_inflight, "request_sizes": f"floor(exp(U(0, ln {max_count + 1}))), 1..{max_count}",
-            "launch_shape": tuning["choice"],
+            "launch_shape": tuning["choice"], "latency_batch_max": latency_batch_max,
             "peak": {"requests_per_s": peak_rps, "bootstraps_per_s": peak["ciphertexts_per_s"],
                      "p50_ms": peak["sojourn"]["p50_ms"], "p99_ms": peak["sojourn"]["p99_ms"],
                      "hit_rate": peak["hit_rate"]},

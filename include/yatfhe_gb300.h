@@ -336,10 +336,16 @@ typedef struct yg_server_config {
     int max_batch;
     int max_inflight;
     int max_tenants;
+    /* Batches of at most this many ciphertexts run in YG_LAYOUT_CHANNEL_CLUSTER where the
+     * parameters have it (GINX keys, T = 32, N = 1024, l_approx <= 4): a lone ciphertext takes
+     * about a third of the time of the throughput layouts.  0: two waves of the six-CTA
+     * clusters the GPU holds at once; negative: never. */
+    int latency_batch_max;
 } yg_server_config;
 typedef struct yg_server_counters {
     uint64_t key_hits, key_misses, refill_bytes, batches, requests_done, ciphertexts_done;
     int key_slots;
+    uint64_t latency_batches; /* batches run in the latency layout (latency_batch_max) */
 } yg_server_counters;
 typedef struct yg_request_times {
     double t_submit, t_start, t_done; /* seconds on a monotonic clock */
@@ -401,6 +407,7 @@ typedef struct yg_trace_result {
     double tenant_fairness_jain;
     int peak_queue_depth, load_concurrency_peak;
     double load_concurrency_mean;
+    uint64_t latency_batches; /* of `batches`, those run in the latency layout */
 } yg_trace_result;
 int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_trace_result* out);
 

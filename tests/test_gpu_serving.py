@@ -81,6 +81,42 @@ def test_trace_with_evictions_is_bit_exact(served):
     tight = srv.run_trace(pool, expect, requests=60, warmup=0, rate=2000.0, zipf_s=1.1, max_count=16, seed=8,
                           slo_ms=1e-6)
     assert tight["slo_violation_rate"] == 1.0  # every sojourn exceeds a near-zero target
+    # small batches ran in the channel-cluster layout (the default: two waves of its clusters)
+    assert 0 < res["latency_batches"] <= res["batches"]
+
+
+def test_latency_layout_off_and_forced(built_lib):
+    """The same trace with the latency layout off (negative latency_batch_max) and forced for
+    every batch (a bound above max_batch) gives the same bit-exact outputs; only the
+    batches' layout differs."""
+    from yatfhe_gb300 import api, serving
+
+    p = small(T32_N1024, 24)
+    ctx = api.Context(p, 0)
+    tenants, max_count = 3, 16
+    keys = []
+    pool = torch.empty((tenants, max_count, p.n + 1), dtype=torch.int32).pin_memory()
+    expect = torch.empty_like(pool).pin_memory()
+    lut = lutmod.sign_lut(p.N, 32)
+    rng = np.random.default_rng(8)
+    for t in range(tenants):
+        o = Restatement(p)
+        o.keygen(2000 + t)
+        keys.append(api.BootstrapKey.from_ntt_words(ctx, o.bsk_ntt()).set_ksk(o.ksk()))
+        lwe = o.encrypt(rng.integers(-(1 << 31), 1 << 31, max_count))
+        pool[t] = torch.from_numpy(lwe)
+        expect[t] = api.functional_bootstrapping_mp_ntt(ctx, keys[t], torch.from_numpy(lwe).cuda(),
+                                                        torch.from_numpy(lut).cuda()).cpu()
+    for bound, want in ((-1, "none"), (1 << 20, "all")):
+        srv = serving.Server(ctx, key_budget_bytes=4 * keys[0].device_bytes, max_batch=48, max_inflight=2,
+                             latency_batch_max=bound)
+        for t in range(tenants):
+            srv.add_tenant(t, keys[t], lut)
+        srv.start()
+        res = srv.run_trace(pool, expect, requests=120, warmup=10, rate=3000.0, max_count=max_count, seed=9)
+        srv.close()
+        assert res["mismatched_requests"] == 0 and res["served"] == 120
+        assert res["latency_batches"] == (0 if want == "none" else res["batches"])
 
 
 def test_trace_sheds_beyond_queue_bound(served):

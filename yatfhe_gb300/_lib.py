@@ -33,12 +33,13 @@ class YgParams(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("key_budget_bytes", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
-                ("max_tenants", ctypes.c_int)]
+                ("max_tenants", ctypes.c_int), ("latency_batch_max", ctypes.c_int)]
 
 
 class ServerCounters(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in ("key_hits", "key_misses", "refill_bytes", "batches", "requests_done",
-                                               "ciphertexts_done")] + [("key_slots", ctypes.c_int)]
+                                               "ciphertexts_done")] + [("key_slots", ctypes.c_int),
+                                                                       ("latency_batches", ctypes.c_uint64)]
 
 
 class RequestTimes(ctypes.Structure):
@@ -67,7 +68,7 @@ class TraceResult(ctypes.Structure):
                 ("slo_violation_rate_100", ctypes.c_double), ("slo_violation_rate_300", ctypes.c_double),
                 ("slo_violation_rate_500", ctypes.c_double), ("tenant_fairness_jain", ctypes.c_double),
                 ("peak_queue_depth", ctypes.c_int), ("load_concurrency_peak", ctypes.c_int),
-                ("load_concurrency_mean", ctypes.c_double)]
+                ("load_concurrency_mean", ctypes.c_double), ("latency_batches", ctypes.c_uint64)]
 
 
 _vp = ctypes.c_void_p

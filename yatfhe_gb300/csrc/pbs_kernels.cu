@@ -2326,6 +2326,20 @@ int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layo
     return dispatch_br(logN, torus_bits, per_cta, layout, OccupancyBr{n, L});
 }
 
+int cluster6_max_clusters(int n, int L) {
+    if (L < 1 || L > kClusterMaxLevels || brc6_smem_bytes(n, L) > 227 * 1024 || prepare_brc() != 0) return 0;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(6);
+    cfg.blockDim = dim3(kCluster6Warps * 32);
+    cfg.dynamicSmemBytes = brc6_smem_bytes(n, L);
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, blind_rotate_cluster6_kernel<32>, &cfg) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    return clusters;
+}
+
 int launch_key_intt(const KeyInttArgs& a, void* stream) {
     if (a.polys <= 0) return 0;
     if (a.N != 1024 && a.N != 2048) return -1;

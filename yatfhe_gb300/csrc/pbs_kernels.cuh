@@ -362,6 +362,8 @@ int launch_blind_rotate(int logN, int torus_bits, const BrArgs& a, void* stream)
 // -1 on a CUDA error.
 constexpr int kNoVariant = -2;
 int br_ctas_per_sm(int logN, int torus_bits, int n, int L, int per_cta, int layout);
+// Six-CTA clusters of the channel-cluster layout the device runs at once (0: unknown).
+int cluster6_max_clusters(int n, int L);
 int launch_keyswitch(const KsArgs& a, void* stream);
 // Bounded device-side waits on the current device that gave up since the library was loaded
 // (the kernels then read from global memory instead); 0 on success.

@@ -141,6 +141,9 @@ struct yg_server {
 
     // statistics
     uint64_t hits = 0, misses = 0, refill_bytes = 0, batches_run = 0, ciphertexts_done = 0, requests_done = 0;
+    // GINX batches of at most latency_max ciphertexts run in the channel-cluster layout
+    int latency_max = 0;
+    uint64_t latency_batches_run = 0;
     // requests submitted and not yet started (the reference's queue depth, peak since the
     // last reset); key refills of batches not yet retired, sampled at every launch
     int waiting = 0, waiting_peak = 0;
@@ -312,6 +315,12 @@ bool launch_batch(yg_server* s, std::deque<Request*>& pending, Batch* b) {
     a.lwe_in = b->d_in;
     a.big_out = b->d_big;
     a.count = total;
+    if (total <= s->latency_max) {
+        a.layout = yg::kLayoutChannelCluster;
+        a.per_cta = 1;
+        a.grid = 0;
+        s->latency_batches_run++;
+    }
     yg::check_launch(yg::launch_blind_rotate(s->ctx->logN, p.torus_bits, a, b->stream), "blind rotate launch");
     }
     yg::KsArgs k{b->d_big, nullptr, b->d_out, total, kN, p.n, p.ks_level, p.ks_radix_bits, b->d_tiles, ntiles};
@@ -440,6 +449,13 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
         s->nslots = (int)(cfg->key_budget_bytes / (s->bsk_bytes + s->ksk_bytes));
         if (s->nslots < 1) s->nslots = 0;
         if (cfg->max_tenants < 1) throw std::invalid_argument("max_tenants must be positive");
+        // small batches in the latency layout where the parameters have it
+        if (cfg->latency_batch_max >= 0 && ctx->d_tw16 &&
+            yg::br_ctas_per_sm(ctx->logN, p.torus_bits, p.n, p.l_approx, 1, yg::kLayoutChannelCluster) >= 1) {
+            const int clusters = yg::cluster6_max_clusters(p.n, p.l_approx);
+            s->latency_max = cfg->latency_batch_max > 0 ? cfg->latency_batch_max
+                                                        : 2 * (clusters > 0 ? clusters : ctx->sm_count / 6);
+        }
         auto fail_clean = [&]() {
             for (auto* b : s->slot_bsk) cudaFree(b);
             for (auto* k : s->slot_ksk) cudaFree(k);
@@ -598,6 +614,7 @@ int yg_server_stats(yg_server* s, yg_server_counters* out) {
     out->requests_done = s->requests_done;
     out->ciphertexts_done = s->ciphertexts_done;
     out->key_slots = s->nslots;
+    out->latency_batches = s->latency_batches_run;
     return YG_OK;
 }
 
@@ -866,6 +883,7 @@ extern "C" int yg_server_run_trace(yg_server* s, const yg_trace_config* cfg, yg_
         out->key_misses = after.key_misses - before.key_misses;
         out->refill_bytes = after.refill_bytes - before.refill_bytes;
         out->batches = after.batches - before.batches;
+        out->latency_batches = after.latency_batches - before.latency_batches;
         const double lookups = (double)(out->key_hits + out->key_misses);
         out->hit_rate = lookups > 0 ? out->key_hits / lookups : 0;
         // the reference's SLO and fairness figures (blindrotate_serving.cpp:256-284, 324-336)

@@ -23,8 +23,8 @@ def _latency(l) -> dict:
 
 class Server:
     def __init__(self, ctx: Context, key_budget_bytes: float, max_batch: int = 4096, max_inflight: int = 2,
-                 max_tenants: int = 1024):
-        cfg = _lib.ServerConfig(int(key_budget_bytes), max_batch, max_inflight, max_tenants)
+                 max_tenants: int = 1024, latency_batch_max: int = 0):
+        cfg = _lib.ServerConfig(int(key_budget_bytes), max_batch, max_inflight, max_tenants, latency_batch_max)
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().yg_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.ctx, self._h, self.max_batch = ctx, h, max_batch
