@@ -16,7 +16,7 @@ carries the plain per-call form, a batch-size sweep and the other workloads unde
 in one CUDA graph, and the 128-tenant serving trace (p50/p99 at 50-100 % of peak).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--params t32_n1024|t56_n2048]
-                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving|serving_lazy|encrypt|crt]
+                  [--count C] [--impl ours|reference] [--workload batch|multi_tenant|serving|serving_lazy|encrypt|crt|lone]
 Multi-GPU: one process per GPU (torchrun); every rank bootstraps its own batch (weak
 scaling, no data-path collective).
 """
@@ -54,7 +54,7 @@ def parse_args():
     ap.add_argument("--count", type=int, default=0, help="ciphertexts per step (default 65536 / 16384)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "multi_tenant", "serving", "serving_lazy",
-                                                                  "encrypt", "crt"])
+                                                                  "encrypt", "crt", "lone"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-call / sweep legs and other workloads")
     ap.add_argument("--cpu-sample", type=int, default=0, help="ciphertexts in the CPU baseline sample")
     ap.add_argument("--per-cta", type=int, default=0, help="fix ciphertexts per CTA (skips the autotuner)")
@@ -663,6 +663,51 @@ def leg_crt(dev, count=2432, steps=3, warmup=1, cpu_sample=2):
             "sample_bit_exact": bool(same)}
 
 
+def leg_lone(dev, reps=20, warmup=3):
+    """One ciphertext per yg_pbs call (TORUS=32 set) in every layout the parameters have: the
+    latency of a lone bootstrap, CUDA events around `reps` back-to-back calls after `warmup`;
+    every layout's output must equal the channel-row layout's."""
+    import torch
+
+    from yatfhe_gb300 import _lib, api
+    from yatfhe_gb300.params import T32_N1024
+
+    p = T32_N1024
+    ctx = api.Context(p, dev)
+    bsk, ksk = synthetic_keys(p, 0x5EED4000)
+    key = api.BootstrapKey.from_ntt_words(ctx, bsk).set_ksk(ksk)
+    d_lut = torch.from_numpy(workload_lut(p)).to(f"cuda:{dev}")
+    d_in = torch.from_numpy(synthetic_lwe(p, 1, 0x5EED4001)).to(f"cuda:{dev}")
+    d_out = torch.empty_like(d_in)
+    s = torch.cuda.Stream(device=dev)
+    L = _lib.lib()
+    lat, outs = {}, {}
+    for name, lay in (("channel", 0), ("channel_row", 1), ("row_cluster", 2), ("channel_cluster", 3)):
+        if api.ctas_per_sm(ctx, 1, lay) < 1:
+            continue
+        api.set_launch(ctx, 1, 0, lay)
+
+        def call():
+            _lib.check(L.yg_pbs(ctx.handle, key.handle, ctypes.c_void_p(d_in.data_ptr()),
+                                ctypes.c_void_p(d_out.data_ptr()), 1, ctypes.c_void_p(d_lut.data_ptr()),
+                                ctypes.c_void_p(s.cuda_stream)))
+
+        for _ in range(warmup):
+            call()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            call()
+        b.record(s)
+        s.synchronize()
+        lat[name] = a.elapsed_time(b) / reps
+        outs[name] = d_out.cpu().numpy().copy()
+    key.close()
+    ref = outs["channel_row"]
+    return {"workload": "lone_t32_n1024", "latency_ms_by_layout": lat, "reps": reps,
+            "identical_across_layouts": all((o == ref).all() for o in outs.values())}
+
+
 def leg_encrypt(dev, count=1 << 20, steps=5, warmup=3, cpu_sample=20000):
     """symEncTlwe on the GPU for the TORUS=32 set (n=630): `count` messages per step encrypted
     by yg_encrypt_lwe (masks and TUniform(2^18) noise drawn by ChaCha20 in the kernel) and by
@@ -1052,6 +1097,14 @@ def main():
             line = {"metric": "approximate-CRT blind rotations per second", "value": r["rotations_per_s"],
                     "unit": "rotations/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
                     "vs_baseline": None, "dtype": "int8 residues / u32 mod 2^24-2^14+1", "data": "synthetic",
+                    "config": {"workload": r["workload"]}, "result": r}
+            print(json.dumps(line))
+            return
+        if args.workload == "lone":
+            r = leg_lone(dev)
+            line = {"metric": "lone-ciphertext bootstrap latency", "value": min(r["latency_ms_by_layout"].values()),
+                    "unit": "ms", "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "int32 torus / u32 RNS", "data": "synthetic",
                     "config": {"workload": r["workload"]}, "result": r}
             print(json.dumps(line))
             return
