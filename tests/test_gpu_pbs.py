@@ -156,22 +156,23 @@ def test_keyswitch_alone_t32(t32_small):
 
 def test_keyswitch_split_matches_unsplit(t32_small):
     """Small batches split the input coefficients across CTAs that add into the output; a
-    batch large enough to fill the GPU runs unsplit.  A ciphertext's key switch is the same in
-    batches of 1, 3, 9, 61 and 6,000 (extreme words included), and equals the oracle's."""
+    batch large enough to fill the GPU runs unsplit in tiles of 8 ciphertexts, a larger one
+    in tiles of 32.  A ciphertext's key switch is the same in batches of 1, 3, 9, 61, 6,000
+    and 20,000 (extreme words included), and equals the oracle's."""
     from yatfhe_gb300 import api
 
     ora, ctx, key = t32_small
     p = ctx.params
     rng = np.random.default_rng(31)
-    big = rng.integers(-(1 << 31), 1 << 31, size=(6000, p.k * p.N + 1), dtype=np.int64).astype(np.int32)
+    big = rng.integers(-(1 << 31), 1 << 31, size=(20000, p.k * p.N + 1), dtype=np.int64).astype(np.int32)
     big[0, :] = np.int32(-(1 << 31))
     big[1, :] = np.int32((1 << 31) - 1)
     d_big = torch.from_numpy(big).cuda()
     full = api.switch_key_for_tlwe(ctx, key, d_big).cpu().numpy()
-    for count in (1, 3, 9, 61):
+    for count in (1, 3, 9, 61, 6000):
         got = api.switch_key_for_tlwe(ctx, key, d_big[:count].contiguous()).cpu().numpy()
         np.testing.assert_array_equal(got, full[:count], err_msg=f"batch of {count}")
-    for c in (0, 1, 2, 5999):
+    for c in (0, 1, 2, 5999, 19999):
         np.testing.assert_array_equal(full[c], ora.keyswitch(big[c]))
 
 
