@@ -87,3 +87,54 @@ def test_product_does_not_import_the_oracle():
         if f.suffix in (".py", ".cu", ".cuh", ".cpp", ".h", ".hpp"):
             text = f.read_text()
             assert "oracle" not in re.sub(r"(#|//).*", "", text).lower() or f.name == "__init__.py", f
+
+
+STRUCTS = {  # ctypes mirror in yatfhe_gb300/_lib.py -> C struct in include/yatfhe_gb300.h
+    "YgParams": "yg_params",
+    "ServerConfig": "yg_server_config",
+    "ServerCounters": "yg_server_counters",
+    "RequestTimes": "yg_request_times",
+    "TraceConfig": "yg_trace_config",
+    "Latency": "yg_latency",
+    "TraceResult": "yg_trace_result",
+}
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every struct the Python binding passes through the C ABI has the header's size and
+    field offsets (a probe compiled with the host C compiler prints them)."""
+    import shutil
+    import subprocess
+
+    from yatfhe_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "yatfhe_gb300.h"', "int main(void) {"]
+    for py, c in STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for f, _ in getattr(_lib, py)._fields_:
+            lines.append(f'  printf("{py} {f} %zu\\n", offsetof({c}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for py in STRUCTS:
+        cls = getattr(_lib, py)
+        assert got[(py, "size")] == ctypes.sizeof(cls), py
+        for f, _ in cls._fields_:
+            assert got[(py, f)] == getattr(cls, f).offset, (py, f)
+
+
+def test_layout_constants_match_the_header():
+    from yatfhe_gb300 import _lib
+
+    text = (ROOT / "include" / "yatfhe_gb300.h").read_text()
+    defined = dict(re.findall(r"#define (YG_LAYOUT_[A-Z_]+) (\d+)", text))
+    assert defined, "no layout constants found"
+    for name, value in defined.items():
+        assert getattr(_lib, name[len("YG_"):]) == int(value), name
