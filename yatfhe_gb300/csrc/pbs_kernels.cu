@@ -1692,36 +1692,39 @@ __device__ __forceinline__ int swz(int l, int k) { return l * 32 + 4 * (k ^ (l &
 __device__ __forceinline__ int swz16(int tt, int k) { return tt * 16 + 4 * (k ^ ((tt >> 1) & 3)); }
 
 // Channel-cluster layout (kLayoutChannelCluster), T = 32, N = 1024: one ciphertext per
-// cluster of six CTAs.  CTA (h, c), rank 3 h + c, owns accumulator row h in RNS channel c and
-// computes output h of every external product in that channel; its warp lvl < l runs the
-// forward transform of digit level lvl.  Per CMux step: (1) all threads rotate and decompose
-// row h into l digit rows (the three CTAs of a row compute the same digits); (2) each
-// transform warp runs its level's forward transform, writes it into its send buffer and one
-// lane copies that (cp.async.bulk, shared memory to shared memory) into the exchange region
-// of the same level in the partner CTA (the other row, the same channel), completing the
-// partner's barrier for that level; it then multiplies its own transform with the key words
-// K(lvl, h, h); (3) once the partner's transform is in, the partner's with K(lvl, 1 - h, h):
-// an exact 64-bit sum of two products reduced once; (4) warps 0 and 1 add the l partials,
-// run the inverse transform, write row h's residues in channel c into the CTA's inbox and
-// copy them into the inboxes of the two other CTAs of row h; (5) once the two other
-// channels' residues are in, every thread recombines four coefficients (CRT) and adds them
-// into the CTA's copy of row h.  No scheduler runs more than one transform warp (the
-// row-cluster layout puts nine on an SM's four), so a step costs about one forward and one
-// inverse transform of a warp running alone, and no step waits at a cluster-wide barrier.
-// The inverse runs with 16 residues per thread (ntt16_inverse: half the per-thread chain, on
-// schedulers no other warp uses then); warps 0 and 1 read the partials in its slot order
-// (slot16) and write their residues in 16-byte chunks (thread tt's chunk k holds its
-// coefficients (4k + e) 64 + tt, swz16), and thread (tt, k) of the recombination takes
-// those.  Two-warp forward transforms measured slower: six transform warps on four
-// schedulers put two on two of them.  Send buffers, exchange regions and inboxes are
-// double-buffered by the parity of the active step: another CTA's copy for step u + 2
-// depends, through the chain of transforms and recombinations, on this CTA having finished
-// step u, so a buffer is rewritten only after it was read (and a send buffer only after
-// its copy arrived).  The key rows of the next active step (output h of both rows, every
-// level, channel c: l x 2 x 4 KB) are copied into shared memory by TMA, issued by a warp
-// that runs no transform, with the same bounded wait and global-memory fallback as the
-// row-cluster layout.  Every wait is bounded; a wait for another CTA that gives up counts in
-// g_wait_timeouts (the results are then wrong) and the CTA stops waiting.
+// cluster of six CTAs of eight warps.  CTA (h, c), rank 3 h + c, owns accumulator row h in RNS
+// channel c and computes output h of every external product in that channel.  Per CMux
+// step: (1) all threads rotate and decompose row h into l digit rows (the three CTAs of a
+// row compute the same digits); (2) warp lvl < l runs the forward transform of digit level
+// lvl, writes it into its send buffer and one lane copies that (cp.async.bulk, shared memory
+// to shared memory) into the exchange region of the same level in the partner CTA (the other
+// row, the same channel), completing the partner's barrier for that level; (3) warp lvl and
+// its helper warp 4 + lvl (which reads slots 16..31 of each lane from the send buffer) each
+// multiply their half of the transform with the key words K(lvl, h, h) and, once the
+// partner's transform is in, the partner's half with K(lvl, 1 - h, h): an exact 64-bit sum
+// of two products reduced once, added into the levels' partial sum with shared-memory atomic
+// adds; (4) warps 0 and 1 run the inverse transform on the partial sum, write row h's
+// residues in channel c into the CTA's inbox and copy them into the inboxes of the two other
+// CTAs of row h; (5) once the two other channels' residues are in, every thread recombines
+// four coefficients (CRT) and adds them into the CTA's copy of row h.  No scheduler runs more
+// than one transform warp (the row-cluster layout puts nine on an SM's four), so a step costs
+// about one forward and one inverse transform of a warp running alone, and no step waits at a
+// cluster-wide barrier.  The inverse runs with 16 residues per thread (ntt16_inverse: half
+// the per-thread chain, on schedulers no other warp uses then); warps 0 and 1 read the summed
+// partials in its slot order (slot16) and write their residues in 16-byte chunks (thread tt's
+// chunk k holds its coefficients (4k + e) 64 + tt, swz16), and thread (tt, k) of the
+// recombination takes those.  Two-warp forward transforms measured slower: six transform
+// warps on four schedulers put two on two of them.  Send buffers, exchange regions and
+// inboxes are double-buffered by the parity of the active step: another CTA's copy for step
+// u + 2 depends, through the chain of transforms and recombinations, on this CTA having
+// finished step u, so a buffer is rewritten only after it was read (and a send buffer only
+// after its copy arrived).  The key rows of the next active step (output h of both rows,
+// every level, channel c: l x 2 x 4 KB) are copied into shared memory by TMA from lane 0 of
+// warp 7, which runs no transform: it issues the copy once the step's products have read the
+// stage, waits for it (bounded) while the inverse runs, and publishes whether it arrived; the
+// products read the key from global memory after a wait gave up.  Every wait is bounded; a
+// wait for another CTA that gives up counts in g_wait_timeouts (the results are then wrong)
+// and the CTA stops waiting.
 template <int T>
 __global__ void __cluster_dims__(6, 1, 1) __maxnreg__(kBrMaxRegs) blind_rotate_cluster6_kernel(const BrArgs a) {
     static_assert(T == 32, "the channel-cluster layout is built for the 32-bit torus");
