@@ -315,7 +315,10 @@ int yg_ctas_per_sm(yg_ctx* ctx, int layout, int per_cta, int* out);
 /* Launch shape of every bootstrap on this context (the autotuner's choice): layout,
  * per_cta ciphertexts per CTA (sharing its L1); ctas_per_sm > 0 makes the grid persistent
  * with that many CTAs per SM, 0 launches one CTA per group of per_cta ciphertexts.
- * Default (YG_LAYOUT_CHANNEL, 1, 0). */
+ * Default (YG_LAYOUT_CHANNEL, 1, 0), except that until this is called a batch of at most
+ * two waves of six-CTA clusters (48 ciphertexts on a 152-SM GPU) runs in
+ * YG_LAYOUT_CHANNEL_CLUSTER where the parameters have it (one ciphertext alone: about a
+ * sixth of the channel layout's time); after a call the shape given applies to every batch. */
 int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm);
 
 /* Serving: a request loop over many tenants with continuous batching and an HBM key cache.

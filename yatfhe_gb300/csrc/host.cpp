@@ -913,6 +913,17 @@ yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key) {
     return a;
 }
 
+yg::BrArgs yg::br_args(const yg_ctx* c, const yg_key* key, int count) {
+    yg::BrArgs a = br_args(c, key);
+    a.count = count;
+    if (!c->launch_set && count <= c->latency_max) {
+        a.layout = yg::kLayoutChannelCluster;
+        a.per_cta = 1;
+        a.grid = 0;
+    }
+    return a;
+}
+
 int yg::check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bool lazy_ok) {
     if (!c || !k) return set_err(YG_ERR_INVALID, "null context or key");
     if (k->ctx != c) return set_err(YG_ERR_INVALID, "key belongs to another context");
@@ -954,11 +965,10 @@ int do_pbs(yg_ctx* c, const yg_key* key, const int32_t* d_in, int32_t* d_out, in
         a.count = count;
         rc = yg::launch_lazy_blind_rotate(a, s);
     } else {
-        yg::BrArgs a = br_args(c, key);
+        yg::BrArgs a = br_args(c, key, count);
         a.lwe_in = d_in;
         a.lut = d_lut;
         a.big_out = big;
-        a.count = count;
         rc = yg::launch_blind_rotate(c->logN, c->p.torus_bits, a, s);
     }
     if (rc == 0) {
@@ -1009,6 +1019,13 @@ int yg_ctx_create(const yg_params* params, int device, yg_ctx** out) {
         c->qtab = std::make_shared<QTables>(params->N, c->q);
         ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         ctx_init_tables(c.get());
+        // small batches run in the channel-cluster layout until yg_ctx_set_launch is called:
+        // up to two waves of its six-CTA clusters
+        if (c->d_tw16 && yg::br_ctas_per_sm(c->logN, c->p.torus_bits, c->p.n, c->p.l_approx, 1,
+                                            yg::kLayoutChannelCluster) >= 1) {
+            const int clusters = yg::cluster6_max_clusters(c->p.n, c->p.l_approx);
+            c->latency_max = 2 * (clusters > 0 ? clusters : c->sm_count / 6);
+        }
         *out = c.release();
         return YG_OK;
     });
@@ -1572,11 +1589,10 @@ int yg_blind_rotate(yg_ctx* ctx, const yg_key* key, const int32_t* d_in, const i
     }
     return guarded([&] {
         DeviceGuard g(ctx->device);
-        yg::BrArgs a = br_args(ctx, key);
+        yg::BrArgs a = br_args(ctx, key, count);
         a.lwe_in = d_in;
         a.lut = d_lut;
         a.acc_out = d_acc;
-        a.count = count;
         a.steps = steps;
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
@@ -1615,11 +1631,10 @@ int yg_blind_rotate_extract(yg_ctx* ctx, const yg_key* key, const int32_t* d_in,
     }
     return guarded([&] {
         DeviceGuard g(ctx->device);
-        yg::BrArgs a = br_args(ctx, key);
+        yg::BrArgs a = br_args(ctx, key, count);
         a.lwe_in = d_in;
         a.lut = d_lut;
         a.big_out = d_big;
-        a.count = count;
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
     });
@@ -1645,11 +1660,10 @@ int yg_blind_rotate_acc(yg_ctx* ctx, const yg_key* key, const int32_t* d_scaled,
     }
     return guarded([&] {
         DeviceGuard g(ctx->device);
-        yg::BrArgs a = br_args(ctx, key);
+        yg::BrArgs a = br_args(ctx, key, count);
         a.scaled_in = d_scaled;
         a.acc_in = d_acc;
         a.acc_out = d_acc;
-        a.count = count;
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         return YG_OK;
     });
@@ -1843,6 +1857,11 @@ int yg_plan_run(yg_plan* plan, const int32_t* d_in, int32_t* d_out, void* stream
         a.lut_of = plan->d_lut_of;
         a.big_out = plan->d_big;
         a.count = plan->count;
+        if (plan->per_cta == 0 && !ctx->launch_set && plan->count <= ctx->latency_max) {
+            a.layout = yg::kLayoutChannelCluster;  // the context's default for a small batch
+            a.per_cta = 1;
+            a.grid = 0;
+        }
         if (plan->per_cta > 0) {
             a.per_cta = plan->per_cta;
             a.layout = plan->layout;
@@ -1900,6 +1919,7 @@ int yg_ctx_set_launch(yg_ctx* ctx, int layout, int per_cta, int ctas_per_sm) {
     ctx->layout = layout;
     ctx->per_cta = per_cta;
     ctx->ctas_per_sm = ctas_per_sm;
+    ctx->launch_set = true;
     return YG_OK;
 }
 

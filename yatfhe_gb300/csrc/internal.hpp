@@ -88,6 +88,9 @@ struct yg_ctx {
     int layout = 0;        // YG_LAYOUT_* of the blind rotation (yg_ctx_set_launch)
     int per_cta = 1;       // ciphertexts per blind-rotation CTA (yg_ctx_set_launch)
     int ctas_per_sm = 0;   // persistent CTAs per SM, 0 = one CTA per ciphertext group
+    bool launch_set = false;  // yg_ctx_set_launch was called: its shape applies to every batch
+    int latency_max = 0;      // batches of at most this many run in the channel-cluster layout
+                              // while launch_set is false (0: that layout does not exist here)
     cudaStream_t side = nullptr;  // second stream of the pipelined host-buffer bootstrap
     std::mutex side_mu;           // creates `side` once
     uint64_t* d_qfwd = nullptr;   // [wf | wfp] (N each): mod-q forward twiddles, made by the first RLWE encryption
@@ -120,6 +123,9 @@ int check_key(const yg_ctx* c, const yg_key* k, bool need_bsk, bool need_ksk, bo
 
 // Blind-rotation launch arguments of a context and key (buffers and count left empty).
 BrArgs br_args(const yg_ctx* c, const yg_key* key);
+// br_args for a batch of `count` GINX ciphertexts: the context's launch shape, or for a small
+// batch on a context whose shape was never set the channel-cluster layout.
+BrArgs br_args(const yg_ctx* c, const yg_key* key, int count);
 // The same for a lazy key (the lazy blind rotation).
 LazyBrArgs lazy_launch_args(const yg_ctx* c, const yg_key* key);
 // A lazy key's device parts: the half rows (bytes), the table block of [wi | wip | wf | wfp]

@@ -59,6 +59,9 @@ void setup(const yg_ctx* ctx) {
     const int rc = yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, ctx->per_cta,
                                       ctx->layout);
     if (rc == -1) yg::ck(cudaGetLastError(), "loading the blind-rotation kernel");
+    if (!ctx->launch_set && ctx->latency_max > 0 &&
+        yg::br_ctas_per_sm(ctx->logN, ctx->p.torus_bits, ctx->p.n, ctx->p.l_approx, 1, yg::kLayoutChannelCluster) == -1)
+        yg::ck(cudaGetLastError(), "loading the blind-rotation kernel");  // a small batch's layout
     if (yg::preload_keyswitch() != 0) yg::ck(cudaGetLastError(), "loading the key-switching kernel");
 }
 
@@ -89,11 +92,10 @@ extern "C" int yg_pbs_noalloc(yg_ctx* ctx, const yg_key* key, const int32_t* d_i
         yg::DeviceGuard g(ctx->device);
         int32_t* big = scratch_on(ctx->device);
         const int kN = ctx->p.k * ctx->p.N;
-        yg::BrArgs a = yg::br_args(ctx, key);
+        yg::BrArgs a = yg::br_args(ctx, key, count);
         a.lwe_in = d_in;
         a.lut = d_lut;
         a.big_out = big;
-        a.count = count;
         yg::check_launch(yg::launch_blind_rotate(ctx->logN, ctx->p.torus_bits, a, stream), "blind rotate launch");
         yg::KsArgs k{big, key->d_ksk, d_out, count, kN, ctx->p.n, ctx->p.ks_level, ctx->p.ks_radix_bits};
         yg::check_launch(yg::launch_keyswitch(k, stream), "keyswitch launch");

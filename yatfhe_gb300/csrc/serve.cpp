@@ -450,12 +450,8 @@ int yg_server_create(yg_ctx* ctx, const yg_server_config* cfg, yg_server** out) 
         if (s->nslots < 1) s->nslots = 0;
         if (cfg->max_tenants < 1) throw std::invalid_argument("max_tenants must be positive");
         // small batches in the latency layout where the parameters have it
-        if (cfg->latency_batch_max >= 0 && ctx->d_tw16 &&
-            yg::br_ctas_per_sm(ctx->logN, p.torus_bits, p.n, p.l_approx, 1, yg::kLayoutChannelCluster) >= 1) {
-            const int clusters = yg::cluster6_max_clusters(p.n, p.l_approx);
-            s->latency_max = cfg->latency_batch_max > 0 ? cfg->latency_batch_max
-                                                        : 2 * (clusters > 0 ? clusters : ctx->sm_count / 6);
-        }
+        if (cfg->latency_batch_max >= 0 && ctx->latency_max > 0)
+            s->latency_max = cfg->latency_batch_max > 0 ? cfg->latency_batch_max : ctx->latency_max;
         auto fail_clean = [&]() {
             for (auto* b : s->slot_bsk) cudaFree(b);
             for (auto* k : s->slot_ksk) cudaFree(k);
